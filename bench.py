@@ -1,0 +1,334 @@
+"""Benchmark of the null-collision Monte Carlo step on GB300.
+
+Workload (the 16 M-particle point of the mixed avalanche): relativistic
+runaway electrons in air (N2/O2 0.79/0.21, 1 atm, 293 K) at E = 0.5 MV/m,
+electrons / photons / positrons tracked through Moller, Seltzer-Berger,
+screened Coulomb, Compton, photoelectric, Bethe-Heitler, Bhabha and
+annihilation with continuum losses below 10 keV (photon cut 5 keV),
+dt = 1 ps.  The population starts from 2^24 electrons at 1 MeV with isotropic
+directions (Philox seed 0); warm-up steps let secondaries appear, then K
+steps are timed.  A "step" is one advance! + droplow! over every particle.
+
+Metric: particle-steps/s (live particles at step start x steps / time).
+`value` times the device-resident step (CUDA events on the library's
+stream); `e2e` times the same steps through the C ABI with the population
+copied in from and out to pinned host buffers every step.
+Inputs (16 M x 48 B = 805 MB) are far larger than L2 (129 MB).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s on 1 GB300 (plain GPU step, mixed e-/gamma/e+ avalanche at 2^24 particles)"
+UNIT = "particle-steps/s"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    return ws, rank
+
+
+def _barrier_max(value: float, ws: int) -> float:
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0"))) if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class Clocks:
+    """Sample SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self._stop = threading.Event()
+        self._th = None
+
+    def __enter__(self):
+        def run():
+            q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap")
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.samples.append([v.strip() for v in out.split(",")])
+                except Exception:
+                    break
+                self._stop.wait(0.2)
+        self._th = threading.Thread(target=run, daemon=True)
+        self._th.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        if self._th:
+            self._th.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def _peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def _profile_traffic():
+    """DRAM bytes per k_step launch from the committed ncu summary, scaled
+    to the bench workload (see profiles/k_step_rrea.md), or None."""
+    path = os.path.join(ROOT, "profiles", "k_step_rrea.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("traffic_bytes_per_slot:"):
+                return float(line.split(":", 1)[1].strip())
+    return None
+
+
+def build_workload(pcl, n_seed: int, seed: int, device: int, steps_per_launch: int = 1):
+    co = pcl.co
+    comp = pcl.workloads.air_composition()
+    dt = 1e-12
+    efield = 5e5
+    et, gt, pt = pcl.workloads.beam_tables(comp, efield, dt)
+    cl = pcl.workloads.air_continuum_loss(comp)
+    pusher = pcl.workloads.pusher((0.0, 0.0, -efield), cl=cl)
+    rng = np.random.Generator(np.random.Philox(seed))
+    p = pcl.workloads.isotropic(n_seed, 1e6 * co.eV, rng)
+    arr = pcl.ParticleArrays(np.zeros((n_seed, 3)), p, np.ones(n_seed), np.zeros(n_seed))
+    cap_e = int(n_seed * 1.25) + (1 << 16)
+    cap_g = max(1 << 20, n_seed // 4)
+    cap_p = max(1 << 16, n_seed // 64)
+    mp = pcl.MultiPopulation(
+        ("electron", pcl.Population(cap_e, arr, et, 1e4 * co.eV, particle=pcl.Electron)),
+        ("photon", pcl.Population(cap_g, [], gt, 5e3 * co.eV, particle=pcl.Photon)),
+        ("positron", pcl.Population(cap_p, [], pt, 1e4 * co.eV, particle=pcl.Positron)),
+        seed=seed, device=device, steps_per_launch=steps_per_launch)
+    mp.set_pusher(pusher)
+    return mp, pusher, dt, dict(tables=(et, gt, pt), cl=cl, comp=comp)
+
+
+def cpu_reference(pcl, n_sample: int, steps: int, threads: int, seed: int = 0):
+    """The oracle (C++ Float64 restatement of the reference step) on a bounded
+    sample of the workload: n_sample electrons, `steps` steps of 1 ps."""
+    from oracle.harness import Arrays, OracleWorld
+    co = pcl.co
+    comp = pcl.workloads.air_composition()
+    dt = 1e-12
+    et, gt, pt = pcl.workloads.beam_tables(comp, 5e5, dt)
+    cl = pcl.workloads.air_continuum_loss(comp)
+    pusher = pcl.workloads.pusher((0.0, 0.0, -5e5), cl=cl)
+    cuts = {pcl.Electron: 1e4 * co.eV, pcl.Photon: 5e3 * co.eV, pcl.Positron: 1e4 * co.eV}
+    W = OracleWorld(seed, {pcl.Electron: et, pcl.Photon: gt, pcl.Positron: pt}, cuts, pusher)
+    rng = np.random.Generator(np.random.Philox(seed))
+    p = pcl.workloads.isotropic(n_sample, 1e6 * co.eV, rng)
+    s = -np.log(rng.random(n_sample))
+    W.upload(pcl.Electron, Arrays(np.zeros((n_sample, 3)), p, np.ones(n_sample), np.zeros(n_sample), s,
+                                  np.arange(n_sample, dtype=np.uint64), np.zeros(n_sample, np.uint32)))
+    W.advance(dt, threads)  # warm-up step
+    psteps = 0
+    t0 = time.perf_counter()
+    for k in range(steps):
+        live = sum(len(W.download(sp).w) for sp in (0, 1, 2))
+        W.advance((k + 2) * dt, threads)
+        psteps += live
+    el = time.perf_counter() - t0
+    return psteps / el, el, psteps
+
+
+def run_reference(args):
+    ws, rank = _dist()
+    if rank != 0:
+        return 0
+    import __graft_entry__ as graft
+    graft.build()
+    pcl = graft.load_package()
+    threads = os.cpu_count() or 1
+    n_sample = args.cpu_sample
+    values = []
+    for k in range(args.warmup + args.steps):
+        v, el, ps = cpu_reference(pcl, n_sample, 2, threads, seed=k)
+        if k >= args.warmup:
+            values.append((v, el, ps))
+    tot_ps = sum(v[2] for v in values)
+    tot_t = sum(v[1] for v in values)
+    val = tot_ps / tot_t
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "rrea-air-0.5MVm-16M", "sample": f"{n_sample} e- at 1 MeV isotropic, 2 steps of 1 ps per bench step"},
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{n_sample} electrons x 2 steps per bench step, C++ Float64 oracle"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300")
+    ap.add_argument("--n", type=int, default=1 << 24, help="seed electrons")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 17)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--steps-per-launch", type=int, default=1)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank = _dist()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    import __graft_entry__ as graft
+    graft.build()
+    pcl = graft.load_package()
+    L = pcl.lib()
+    mp, pusher, dt, extra = build_workload(pcl, args.n, seed=rank, device=local,
+                                           steps_per_launch=args.steps_per_launch)
+    ctx = mp.ctx
+    K = args.steps_per_launch
+    # ---- warm-up
+    t = 0.0
+    for _ in range(args.warmup):
+        t += dt * K
+        pcl.run(mp, pusher, t, dt) if K > 1 else pcl.advance(mp, pusher, t)
+    L.pcl_sync(ctx)
+    tal0 = mp.tallies()
+    L.pcl_kernel_stats(ctx, None, None, None, None, 1)
+    # ---- timed region: device-resident steps
+    _barrier(ws)
+    with Clocks(local) as clk:
+        L.pcl_timer_start(ctx)
+        for _ in range(args.steps):
+            t += dt * K
+            pcl.run(mp, pusher, t, dt) if K > 1 else pcl.advance(mp, pusher, t)
+        ms = C.c_double()
+        L.pcl_timer_stop(ctx, C.byref(ms))
+    tal1 = mp.tallies()
+    kms = C.c_double(); kl = C.c_int64(); nl = C.c_int64(); kb = C.c_double()
+    L.pcl_kernel_stats(ctx, C.byref(kms), C.byref(kl), C.byref(nl), C.byref(kb), 1)
+    psteps = tal1.particle_steps - tal0.particle_steps
+    elapsed = _barrier_max(ms.value / 1e3, ws)
+    total_psteps = psteps * ws
+    value = total_psteps / elapsed
+    peak, peak_kind = _peaks()
+    achieved = (kb.value / max(kl.value, 1)) / (kms.value / max(kl.value, 1) / 1e3) / 1e9
+    slots_per_launch = (kb.value / max(kl.value, 1)) / 96.0
+    tps = _profile_traffic()
+    traffic = tps * slots_per_launch if tps else None
+    # ---- end to end through the C ABI with pinned host buffers
+    e2e = None
+    try:
+        import torch
+        caps = [mp.get(s).max_particles for s in (0, 1, 2)]
+        host = []
+        for s in (0, 1, 2):
+            xw = torch.empty((caps[s], 4), dtype=torch.float32).pin_memory()
+            ps = torch.empty((caps[s], 4), dtype=torch.float32).pin_memory()
+            meta = torch.empty((caps[s], 4), dtype=torch.int32).pin_memory()
+            pk = pcl._lib.Packed(C.cast(xw.data_ptr(), C.POINTER(C.c_float)),
+                                 C.cast(ps.data_ptr(), C.POINTER(C.c_float)),
+                                 C.cast(meta.data_ptr(), C.POINTER(C.c_uint32)))
+            host.append((xw, ps, meta, pk))
+        ns = []
+        for s in (0, 1, 2):
+            n = C.c_int64(caps[s])
+            pcl._lib.check(L.pcl_download_packed(ctx, s, C.byref(n), C.byref(host[s][3])), ctx)
+            ns.append(n.value)
+        tal_a = mp.tallies()
+        h2d = d2h = 0
+        L.pcl_timer_start(ctx)
+        for _ in range(args.e2e_steps):
+            for s in (0, 1, 2):
+                pcl._lib.check(L.pcl_upload_packed(ctx, s, ns[s], C.byref(host[s][3])), ctx)
+                h2d += 48 * ns[s]
+            t += dt
+            pcl.advance(mp, pusher, t)
+            for s in (0, 1, 2):
+                n = C.c_int64(caps[s])
+                pcl._lib.check(L.pcl_download_packed(ctx, s, C.byref(n), C.byref(host[s][3])), ctx)
+                ns[s] = n.value
+                d2h += 48 * n.value
+        ms2 = C.c_double()
+        L.pcl_timer_stop(ctx, C.byref(ms2))
+        tal_b = mp.tallies()
+        e_el = _barrier_max(ms2.value / 1e3, ws)
+        e2e = {"value": (tal_b.particle_steps - tal_a.particle_steps) * ws / e_el, "unit": UNIT,
+               "h2d_bytes_per_step": int(h2d / args.e2e_steps), "d2h_bytes_per_step": int(d2h / args.e2e_steps)}
+    except Exception as ex:  # pragma: no cover
+        e2e = {"value": None, "unit": UNIT, "error": str(ex)[:200], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    # ---- CPU baseline (rank 0, N = 1)
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        v, el, ps = cpu_reference(pcl, args.cpu_sample, 8, threads)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{args.cpu_sample} e- at 1 MeV isotropic, 8 steps of 1 ps after 1 warm-up "
+                         f"({ps} particle-steps, {el:.1f} s), C++ Float64 oracle"}
+    errs = {pcl._lib.ERROR_NAMES[q]: int(tal1.errors[q]) for q in range(8) if tal1.errors[q]}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": "rrea-air-0.5MVm-16M", "seed_electrons": args.n, "dt_s": dt,
+                           "steps_per_launch": K, "live_at_end": list(tal1.live),
+                           "l2": "inputs larger than L2 (population > 800 MB)", "parallelism": f"replicas{ws}"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_kind": peak_kind,
+                             "traffic": traffic, "kernel": "k_step"},
+                "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(nl.value), "clocks": clk.summary(),
+                "errors": errs}
+        print(json.dumps(line))
+    mp.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

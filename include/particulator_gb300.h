@@ -1,0 +1,290 @@
+/*
+ * particulator_gb300.h — C ABI of the GB300 null-collision Monte Carlo step.
+ *
+ * This is the drop-in boundary for the hot path of Particulator.jl: a Julia
+ * host keeps building its populations, collision tables and pusher with the
+ * package API and calls these entry points through `ccall` instead of running
+ * `advance!` / `run!` on the CPU.  Every entry point takes plain pointers and
+ * sizes, returns PCL_OK (0) or a negative PCL_ERR_* status, never throws and
+ * never traps.  The library copies host buffers it is given; it owns all
+ * device memory.  A context is externally single-threaded; all parallelism is
+ * on the GPU.  There is no CPU fallback: without a CUDA device every call that
+ * needs one returns PCL_ERR_CUDA.
+ *
+ * Units at this boundary are the reference's SI units in FP64 (m, kg m/s, J,
+ * s, 1/s, m^2) unless a name says otherwise; the library converts to its FP32
+ * device units on upload (momentum in m_e c, energy in m_e c^2, time in ns).
+ *
+ * Reference interfaces each entry point replaces are cited as file:line in the
+ * Particulator.jl source tree.
+ */
+#ifndef PARTICULATOR_GB300_H
+#define PARTICULATOR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PCL_OK               0
+#define PCL_ERR_INVALID     -1  /* bad argument or size                              */
+#define PCL_ERR_CUDA        -2  /* CUDA runtime error or no device                   */
+#define PCL_ERR_CAPACITY    -3  /* a population outgrew its capacity (population.jl:107) */
+#define PCL_ERR_UNSUPPORTED -4  /* process kind or option with no device implementation */
+#define PCL_ERR_STATE       -5  /* call order (e.g. advance before a species is set)  */
+#define PCL_ERR_TIMEOUT     -6  /* a bounded device wait gave up                      */
+#define PCL_ERR_NUMERIC     -7  /* numeric guard tripped (see pcl_tallies.errors)     */
+
+/* ---- species (MultiPopulation(:electron, :photon, :positron), mixed_population.jl:4-12) */
+#define PCL_ELECTRON  0
+#define PCL_PHOTON    1
+#define PCL_POSITRON  2
+#define PCL_NSPECIES  3
+
+/* species flags */
+#define PCL_SPECIES_TRACKED     0  /* a normal Population (population.jl:7-21)            */
+#define PCL_SPECIES_TALLY_ONLY  1  /* secondaries are counted and binned, never stored    */
+
+/* ---- collision process kinds (closed set; arbitrary Julia `collide` methods
+ * are rejected with PCL_ERR_UNSUPPORTED) --------------------------------- */
+#define PCL_PROC_MOLLER          1  /* moller.jl:8-87                 */
+#define PCL_PROC_RBEB            2  /* rbeb.jl:5-196                  */
+#define PCL_PROC_SELTZER_BERGER  3  /* seltzer.jl:9-231               */
+#define PCL_PROC_REL_COULOMB     4  /* relativistic_coulomb.jl:5-75   */
+#define PCL_PROC_COMPTON         5  /* compton.jl:1-3, 59-144         */
+#define PCL_PROC_KN_COMPTON      6  /* compton.jl:5-7, 34-47          */
+#define PCL_PROC_PHOTOELECTRIC   7  /* photo_electric.jl:7-99         */
+#define PCL_PROC_BETHE_HEITLER   8  /* bethe_heitler.jl:1-193         */
+#define PCL_PROC_BHABHA          9  /* bhaba.jl:4-91                  */
+#define PCL_PROC_ANNIHILATION   10  /* anihilation.jl:1-67            */
+
+#define PCL_MAX_PROC      16   /* processes per species table              */
+#define PCL_MAX_ORDER      4   /* Chebyshev terms per interval             */
+#define PCL_MAX_INTERVALS 63   /* binary intervals (k); k+1 fits are kept  */
+#define PCL_MAX_SB         4   /* distinct Seltzer-Berger tables (one per Z) */
+#define PCL_NERR           8   /* error counters in pcl_tallies            */
+
+/* error counter slots (pcl_tallies.errors[]) */
+#define PCL_E_RATEBOUND   0  /* xi < 0 after all processes (collisions.jl:186 @assert)      */
+#define PCL_E_TABLE_RANGE 1  /* energy outside a table's fitted range (extrapolated)         */
+#define PCL_E_REJECT_CAP  2  /* a rejection loop hit its iteration cap                       */
+#define PCL_E_SUBSTEP_CAP 3  /* a particle hit the sub-step cap inside one step              */
+#define PCL_E_SPILL       4  /* warp child-stack overflow (children handled by a spill pass) */
+#define PCL_E_CAPACITY    5  /* particles dropped because a population was full             */
+#define PCL_E_KINEMATICS  6  /* sampler precondition failed (seltzer.jl:73, rbeb.jl:63, ...) */
+#define PCL_E_NEG_RATE    7  /* rate bound <= 0 above the cut (treated as 0)                 */
+
+/* ---- process descriptor ---------------------------------------------------
+ * One entry of the reference's `processes` list `(coef, proc)`
+ * (collision_table.jl:115-133).  `param` meaning per kind, SI units:
+ *   MOLLER, BHABHA : param[0] = tcut (J)                       (moller.jl:8-11, bhaba.jl:4-7)
+ *   RBEB           : param[0] = B (J), param[1] = U (J), param[2] = N  (rbeb.jl:5-14)
+ *   REL_COULOMB    : Z (may be fractional via param[0] when Z == 0)     (relativistic_coulomb.jl:5-8)
+ *   ANNIHILATION   : Z (may be fractional via param[0] when Z == 0)     (anihilation.jl:1-4)
+ *   PHOTOELECTRIC  : param[0..nparam) = shell binding energies (J) in the order of
+ *                    binding_energies(Z) (atomic_shells.jl:481-486), at most 8;
+ *                    aux0/aux1 = SANDIA left energies (J) and coefficients [naux][4]
+ *                    (SI: m^2 J^i per atom) used only for the cross section
+ *   SELTZER_BERGER : aux0 = log primary energy (log J) [naux], aux1 = total
+ *                    cross section (m^2) [naux], aux2 = inverse-CDF table
+ *                    log(k/T) [naux2 = ncum][naux] column-major (pcum fastest),
+ *                    exactly the fields of SeltzerBerger (seltzer.jl:9-21)
+ *   COMPTON, KN_COMPTON, BETHE_HEITLER : Z only
+ */
+typedef struct pcl_process {
+    int32_t kind;
+    int32_t Z;
+    double  coef;        /* scatterer density (1/m^3) multiplying speed * totalcs */
+    double  param[8];
+    int32_t nparam;
+    int32_t naux;
+    const double* aux0;
+    const double* aux1;
+    const double* aux2;
+    int32_t naux2;
+    int32_t reserved;
+} pcl_process;
+
+/* ---- context configuration --------------------------------------------- */
+typedef struct pcl_config {
+    uint64_t seed;             /* Philox4x32-10 key for every particle stream        */
+    int32_t  device;           /* CUDA device ordinal                                 */
+    int32_t  block_size;       /* threads per block of the step kernel (0 = 256)      */
+    int32_t  grid_blocks;      /* persistent grid size (0 = 2 x SM count)             */
+    int32_t  steps_per_launch; /* time steps fused into one launch (0/1 = one)        */
+    int32_t  compaction_period;/* compact dead slots every this many steps (0 = 1)    */
+    int32_t  use_graph;        /* capture the step sequence of pcl_run in a CUDA graph */
+    int32_t  reserved[4];
+} pcl_config;
+
+/* ---- per-context tallies (FP64 / int64 on the device) -------------------- */
+typedef struct pcl_tallies {
+    double  t;                                   /* simulated time (s)                     */
+    int64_t steps;                               /* time steps completed                   */
+    int64_t n[PCL_NSPECIES];                     /* slots in use (live + dead)              */
+    int64_t live[PCL_NSPECIES];                  /* live particles after the last step      */
+    int64_t particle_steps;                      /* sum over steps of live particles at step start */
+    int64_t collisions[PCL_NSPECIES][PCL_MAX_PROC]; /* real collisions, table order (callback.jl:118-141) */
+    int64_t nulls[PCL_NSPECIES];                 /* null collisions                          */
+    int64_t spawned[PCL_NSPECIES];               /* secondaries stored (above the cut)      */
+    int64_t tally_count[PCL_NSPECIES];           /* tally-only species: secondaries counted */
+    double  tally_w[PCL_NSPECIES];               /* ... their summed weight                  */
+    double  tally_wE[PCL_NSPECIES];              /* ... and weight x kinetic energy (J)       */
+    int64_t errors[PCL_NERR];                    /* PCL_E_* counters                          */
+} pcl_tallies;
+
+/* ---- run options (run!, run.jl:1-29, with the device-side callbacks) ---- */
+typedef struct pcl_run_opts {
+    int32_t target_species;  /* PopulationTargetCallback{S} (callback.jl:253-267); -1 = none */
+    int32_t target_ismax;    /* 1: stop when live >= target_n; 0: stop when live <= target_n */
+    int64_t target_n;
+    int64_t max_steps;       /* 0 = no limit besides tfinal */
+} pcl_run_opts;
+
+/* ---- packed device layout (FP32 device units), used for zero-conversion
+ * host<->device transfers: three arrays of 16-byte records per species.
+ *   xw[i]   = {x, y, z (m), w}
+ *   ps[i]   = {px, py, pz (m_e c), s}
+ *   meta[i] = {sid_lo, sid_hi, ctr (0xFFFFFFFF = dead slot), bits of t_off (ns, float)}
+ * t_off is the particle's time relative to the context's simulated time. */
+typedef struct pcl_packed {
+    float*    xw;
+    float*    ps;
+    uint32_t* meta;
+} pcl_packed;
+
+/* ======================================================================= */
+/* Host-side table builders (FP64).  They restate the reference's init path so
+ * that a caller without Julia can produce the tables the step consumes.     */
+
+/* Seltzer-Berger sampling table from a G4Physics2DVector (RawG4Physics2DVector,
+ * util.jl:165-190): x = k/T fractions [nx], y = ln(T/MeV) [ny], value[ny][nx]
+ * row-major (row = primary energy).  Replaces SeltzerBerger(d, Z; ncum, pcum,
+ * gamma_min, gamma_max, energy_scale) (seltzer.jl:23-64) with pcum = LinRange(0,1,ncum).
+ * Outputs: log_energy[ny], totalcs[ny], data[ncum*ny] (column-major, pcum fastest). */
+int pcl_sb_build(int Z, int nx, int ny, const double* x, const double* y, const double* value,
+                 int ncum, double gamma_min, double gamma_max, double energy_scale,
+                 double* log_energy, double* totalcs, double* data);
+
+/* Total cross section (m^2 per target) of one process at n kinetic energies (J):
+ * totalcs(proc, E) of the process files above. */
+int pcl_totalcs(const pcl_process* proc, int64_t n, const double* energy, double* out);
+
+/* collision_table_from_processes(processes, particle, Fdt; safety, nintervals,
+ * order, max_energy) (collision_table.jl:115-149) with compratebound (152-167).
+ * rate is written in the reference's column-major a[k, j, i] layout:
+ *   rate[k + order*(j + nproc*i)], k < order, j < nproc (table order), i <= nintervals;
+ * ratebound[k + order*i]; perm[j] = index into procs of table position j. */
+int pcl_build_collision_table(int species, int nproc, const pcl_process* procs, double Fdt,
+                              double safety, int nintervals, int order, double max_energy,
+                              double* rate, double* ratebound, int32_t* perm);
+
+/* ChebContinuumLoss(ContinuumLoss(nel, I, Tcut), Tmax, n) (continuum.jl:36-43,
+ * 63-139).  Writes k (number of binary intervals), xmax = 2^k Tcut, and the
+ * electron / positron coefficient matrices ec, pc [n][k+1] column-major
+ * (term fastest).  cap = capacity of ec/pc in doubles. */
+int pcl_build_continuum_loss(double nel, double I, double Tcut, double Tmax, int n,
+                             int* k, double* xmax, double* ec, double* pc, int cap);
+
+/* ======================================================================= */
+/* Context and device state                                                 */
+
+int  pcl_create(const pcl_config* cfg, void** ctx);
+void pcl_destroy(void* ctx);
+const char* pcl_last_error(void* ctx);
+const char* pcl_version(void);
+int  pcl_device_count(void);
+
+/* Population(max_particles, inparticles, collisions, energy_cut) (population.jl:34-44),
+ * the capacity / cut half: allocates the double-buffered device SoA. */
+int pcl_set_species(void* ctx, int species, double energy_cut, int64_t capacity, int flags);
+
+/* The table half of Population: a ChebyshevCollisionTable (collision_table.jl:63-106)
+ * in the layout written by pcl_build_collision_table; procs are in table order.
+ * nproc = 0 gives a species with no processes (rate bound 0). */
+int pcl_set_collision_table(void* ctx, int species, int order, int nproc, int nintervals,
+                            double xmax, const double* rate, const double* ratebound,
+                            const pcl_process* procs);
+
+/* RK2Pusher(CombinedForcing(ElectromagneticField(HomogeneousField(E), HomogeneousField(B)),
+ *           ChebContinuumLoss(...)))  (pusher.jl:37-63, field.jl:4-8,54-70, continuum.jl:25-57).
+ * cl_order = 0 disables continuum losses. */
+int pcl_set_forcing(void* ctx, const double E[3], const double B[3], int cl_order, int cl_k,
+                    double cl_xmax, const double* cl_ec, const double* cl_pc);
+
+/* Replace the species' population with n particles (SI, FP64): x[3n], p[3n]
+ * (interleaved xyz), w[n], t[n] (absolute, s).  s[n] = normalised time to the
+ * next collision or NULL to draw s = -log U from each particle's stream, as the
+ * state constructors do (electron.jl:30-33).  sid[n] = stream ids or NULL for
+ * sid = sid_base + i.  Mirrors filling Population + init! (mixed_population.jl:20-35). */
+int pcl_upload(void* ctx, int species, int64_t n, const double* x, const double* p,
+               const double* w, const double* t, const double* s, const uint64_t* sid,
+               uint64_t sid_base);
+
+/* Copy the live particles of a species out (SI, FP64).  *n in: capacity of the
+ * arrays, out: live particles written.  ctr = draws consumed per particle. */
+int pcl_download(void* ctx, int species, int64_t* n, double* x, double* p, double* w,
+                 double* t, double* s, uint64_t* sid, uint32_t* ctr);
+
+/* Zero-conversion transfers of the packed layout (dead slots included on
+ * download; *n in: capacity, out: slots).  Host buffers should be pinned. */
+int pcl_upload_packed(void* ctx, int species, int64_t n, const pcl_packed* host);
+int pcl_download_packed(void* ctx, int species, int64_t* n, pcl_packed* host);
+
+/* advance!(mpopl, pusher, tfinal) followed by foreach(droplow!, mpopl)
+ * (mixed_population.jl:38-47, population.jl:273-284, run.jl:7-8): advance every
+ * live particle and every secondary born in the step to tfinal, drop particles
+ * below their cut.  tfinal must be > the context time. */
+int pcl_advance(void* ctx, double tfinal);
+
+/* run!(mpopl, pusher, tfinal, dt, callback) (run.jl:1-29) with the device-side
+ * PopulationTargetCallback / CollisionCounter.  Steps of dt until tfinal, the
+ * target or max_steps; fills *out. */
+int pcl_run(void* ctx, double tfinal, double dt, const pcl_run_opts* opts, pcl_tallies* out);
+
+/* Counters, population statistics and maintenance. */
+int pcl_get_tallies(void* ctx, pcl_tallies* out);
+int pcl_reset_tallies(void* ctx);
+/* FP64 weighted moments of the live particles of a species:
+ * out = {sum w, sum w*E (J), sum w*x, y, z (m), sum w*x^2, y^2, z^2, max E (J), live count}
+ * (weight, meanenergy, spread, posvar, maxenergy, nactives: population.jl:89-223). */
+int pcl_moments(void* ctx, int species, double out[10]);
+/* repack! (population.jl:229-259): compact dead slots (order-preserving). */
+int pcl_compact(void* ctx);
+/* Energy histogram of a tally-only species' secondaries: nbins log bins over
+ * [emin, emax] J, set once; read returns counts (int64) and summed weights. */
+int pcl_set_tally_histogram(void* ctx, int species, int nbins, double emin, double emax);
+int pcl_get_tally_histogram(void* ctx, int species, int nbins, int64_t* counts, double* weights);
+
+/* Synchronise the context stream and report the first sticky error. */
+int pcl_sync(void* ctx);
+
+/* ---- measurement (no reference counterpart: instrumentation) -------------
+ * pcl_timer_start / pcl_timer_stop record CUDA events on the context's own
+ * stream and return the elapsed device time in ms.  pcl_kernel_stats returns,
+ * since the last reset, the summed event time (ms) of the step kernel's
+ * main-pass launches, how many there were, the number of kernels the library
+ * launched in total, and the step kernel's algorithmic HBM bytes
+ * (48 B per slot read + 48 B per particle written + 4 B per slot marked dead). */
+int pcl_timer_start(void* ctx);
+int pcl_timer_stop(void* ctx, double* ms);
+int pcl_kernel_stats(void* ctx, double* step_kernel_ms, int64_t* step_launches, int64_t* launches,
+                     double* step_bytes, int reset);
+
+/* ---- test hook: run one process sampler on the device --------------------
+ * For each of n primaries (species of the table, energies via p[3n] in SI,
+ * stream ids sid[n], counter 0), performs do_one_collision! forced onto table
+ * position `proc_index` (collisions.jl:168-176, without the selection draw) and
+ * writes the outcome: out_p[3*(3n)] momenta (primary, child 1, child 2; SI),
+ * out_s[3n], out_kind[3n] (species of each slot, -1 = none / removed),
+ * out_ctr[n] = draws consumed. */
+int pcl_test_sampler(void* ctx, int species, int proc_index, int64_t n, const double* p,
+                     const uint64_t* sid, double* out_p, double* out_s, int32_t* out_kind,
+                     uint32_t* out_ctr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PARTICULATOR_GB300_H */

@@ -1,0 +1,1006 @@
+// Host side of the C ABI: context, device memory, table packing, the step
+// driver (advance! / run!) and the maintenance calls.  Every entry point
+// returns a PCL_* status and records a message for pcl_last_error.
+#include <cuda_runtime.h>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "device.cuh"
+#include "physconst.h"
+#include "../../include/particulator_gb300.h"
+
+namespace pcl {
+__global__ void k_step(StepArgs A);
+__global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long cap2);
+__global__ void k_begin_spill(Control* ctl, unsigned long long* in_n, unsigned long long* out_n);
+
+__global__ void k_compact_count(CompactArgs C);
+__global__ void k_compact_scan(CompactArgs C);
+__global__ void k_compact_scatter(CompactArgs C);
+__global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta, long long n, int species,
+                          double* out);
+__global__ void k_test_sampler(StepArgs A, int species, int j, long long n, const float* p_in,
+                               const uint32_t* sid, float* out_p, float* out_s, int* out_kind,
+                               uint32_t* out_ctr);
+size_t step_smem_bytes(int blob_bytes, int threads);
+constexpr int kTile = 2048;
+
+// Host Philox4x32-10 (same function as the device one; used to draw initial s).
+static void philox_host(uint32_t c[4], uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        uint64_t m0 = uint64_t(0xD2511F53u) * c[0];
+        uint64_t m1 = uint64_t(0xCD9E8D57u) * c[2];
+        uint32_t hi0 = uint32_t(m0 >> 32), lo0 = uint32_t(m0);
+        uint32_t hi1 = uint32_t(m1 >> 32), lo1 = uint32_t(m1);
+        uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0; c[1] = lo1; c[2] = n2; c[3] = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+}
+
+struct SpeciesState {
+    bool set = false;
+    double cut = INFINITY;   // J
+    long long cap = 0;
+    int flags = 0;
+    float4* xw[2] = {nullptr, nullptr};
+    float4* ps[2] = {nullptr, nullptr};
+    uint4* meta[2] = {nullptr, nullptr};
+    int cur = 0;
+    // collision table (host copy, SI)
+    int order = 1, nproc = 0, nint = 1;
+    double xmax = 1.0;
+    std::vector<double> rate, rb;
+    std::vector<pcl_process> procs;
+    std::vector<int> sb_index;
+    // tally-only histogram
+    int hist_bins = 0;
+    double hist_emin = 0, hist_emax = 0;
+    unsigned long long* hist_n = nullptr;
+    double* hist_w = nullptr;
+};
+
+struct SBTable {
+    int Z, ne, ncum;
+    std::vector<double> log_energy;  // log J
+    const double* key_ptr;           // caller's aux2 (identity)
+    float* d_data = nullptr;         // [ne][ncum]
+};
+
+struct Ctx {
+    pcl_config cfg;
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+    SpeciesState sp[3];
+    std::vector<SBTable> sb;
+    // forcing
+    double E[3] = {0, 0, 0}, B[3] = {0, 0, 0};
+    int cl_order = 0, cl_k = 0;
+    double cl_xmax = 0;
+    std::vector<double> cl_ec, cl_pc;
+    // blob
+    bool blob_dirty = true;
+    std::vector<unsigned char> blob;
+    float4* d_blob = nullptr;
+    size_t d_blob_cap = 0;
+    // device control and scratch
+    Control* d_ctl = nullptr;
+    Control* h_ctl = nullptr;   // pinned mirror
+    float4* sp_xw[2] = {nullptr, nullptr};
+    float4* sp_ps[2] = {nullptr, nullptr};
+    uint4* sp_meta[2] = {nullptr, nullptr};
+    unsigned long long* d_spn = nullptr;  // [2]
+    long long sp_cap = 0;
+    unsigned int* d_tile_cnt = nullptr;
+    unsigned long long* d_tile_off = nullptr;
+    unsigned long long* d_nnew = nullptr;
+    long long tiles_cap = 0;
+    double* d_mom = nullptr;
+    // accumulated host state
+    double t = 0.0;
+    long long steps = 0;
+    long long particle_steps = 0;
+    long long live[3] = {0, 0, 0};
+    long long steps_since_compact = 0;
+    int sticky = PCL_OK;
+    // instrumentation
+    cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
+    double k_ms = 0.0, k_bytes = 0.0;
+    long long k_launches = 0, launches = 0;
+};
+
+static int fail(Ctx* c, int code, const std::string& msg) {
+    if (c) c->last_error = msg;
+    return code;
+}
+
+
+// Stream-ordered copies: every transfer goes through the context stream and
+// waits for it, so kernels on the (non-blocking) stream never race a copy.
+static cudaError_t h2d(Ctx* c, void* dst, const void* src, size_t bytes) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(c->stream);
+}
+static cudaError_t d2h(Ctx* c, void* dst, const void* src, size_t bytes) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, c->stream);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(c->stream);
+}
+
+#define CK(call)                                                                          \
+    do {                                                                                  \
+        cudaError_t _e = (call);                                                          \
+        if (_e != cudaSuccess)                                                            \
+            return fail(c, PCL_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+static void free_species_buffers(SpeciesState& s) {
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(s.xw[b]); cudaFree(s.ps[b]); cudaFree(s.meta[b]);
+        s.xw[b] = nullptr; s.ps[b] = nullptr; s.meta[b] = nullptr;
+    }
+    cudaFree(s.hist_n); cudaFree(s.hist_w);
+    s.hist_n = nullptr; s.hist_w = nullptr;
+}
+
+static int ensure_tiles(Ctx* c) {
+    long long capmax = 0;
+    for (auto& s : c->sp) capmax = std::max(capmax, s.cap);
+    long long nt = (capmax + kTile - 1) / kTile;
+    if (nt < 1) nt = 1;
+    if (nt <= c->tiles_cap) return PCL_OK;
+    cudaFree(c->d_tile_cnt); cudaFree(c->d_tile_off);
+    CK(cudaMalloc(&c->d_tile_cnt, sizeof(unsigned int) * 3 * nt));
+    CK(cudaMalloc(&c->d_tile_off, sizeof(unsigned long long) * 3 * nt));
+    c->tiles_cap = nt;
+    return PCL_OK;
+}
+
+static int ensure_spill(Ctx* c) {
+    long long capmax = 0;
+    for (auto& s : c->sp) capmax = std::max(capmax, s.cap);
+    long long want = std::max<long long>(1 << 16, capmax / 16);
+    if (want <= c->sp_cap) return PCL_OK;
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(c->sp_xw[b]); cudaFree(c->sp_ps[b]); cudaFree(c->sp_meta[b]);
+        CK(cudaMalloc(&c->sp_xw[b], sizeof(float4) * want));
+        CK(cudaMalloc(&c->sp_ps[b], sizeof(float4) * want));
+        CK(cudaMalloc(&c->sp_meta[b], sizeof(uint4) * want));
+    }
+    c->sp_cap = want;
+    return PCL_OK;
+}
+
+// ------------------------------------------------------------ blob pack --
+static void pack_proc(const pcl_process& P, int sbi, DevProc& D) {
+    std::memset(&D, 0, sizeof(D));
+    D.kind = P.kind;
+    D.sb = -1;
+    using namespace si;
+    switch (P.kind) {
+        case PCL_PROC_MOLLER:
+        case PCL_PROC_BHABHA:
+            D.p[0] = float(P.param[0] / mc2);
+            break;
+        case PCL_PROC_RBEB:
+            D.p[0] = float(P.param[0] / mc2);
+            D.p[1] = float(P.param[1] / mc2);
+            D.p[2] = float(P.param[2]);
+            break;
+        case PCL_PROC_REL_COULOMB: {
+            double Z = (P.Z == 0) ? P.param[0] : double(P.Z);
+            double a = 1.3413 * std::pow(Z, -1.0 / 3.0) * a_0;     // relativistic_coulomb.jl:14
+            double lam = hbar / (m_e * c * a);
+            D.p[0] = float(lam * lam / 4.0);                       // alpha = p[0] / p^2
+            break;
+        }
+        case PCL_PROC_SELTZER_BERGER:
+            D.sb = sbi;
+            D.p[0] = float(P.Z);
+            break;
+        case PCL_PROC_PHOTOELECTRIC:
+            D.nbind = std::min(P.nparam, 8);
+            for (int m = 0; m < D.nbind; ++m) D.p[m] = float(P.param[m] / mc2);
+            break;
+        case PCL_PROC_BETHE_HEITLER: {
+            double Z = P.Z;
+            double aZ = alpha, aZ2 = aZ * aZ, aZ4 = aZ2 * aZ2, aZ6 = aZ4 * aZ2;  // _fc (bethe_heitler.jl:153-161)
+            double fc = (1 / (1 + aZ2) + 0.20206 - 0.0369 * aZ2 + 0.0083 * aZ4 - 0.0020 * aZ6) * aZ2;
+            double FZ = 8 * std::log(Z) / 3;
+            D.p[0] = float(Z);
+            D.p[1] = float(std::pow(Z, 1.0 / 3.0));
+            D.p[2] = float(FZ);
+            D.p[3] = float(FZ + 8 * fc);
+            D.p[4] = float(2e6 * eV / mc2);
+            D.p[5] = float(50e6 * eV / mc2);
+            break;
+        }
+        default:
+            break;
+    }
+}
+
+static int build_blob(Ctx* c) {
+    if (!c->blob_dirty) return PCL_OK;
+    using si::mc2;
+    using si::e;
+    using si::m_e;
+    std::vector<float> data;
+    auto off = [&]() { return int((sizeof(BlobHdr) / 4) + data.size()); };
+    BlobHdr H;
+    std::memset(&H, 0, sizeof(H));
+    const float charge[3] = {-1.0f, 0.0f, 1.0f};
+    for (int s = 0; s < 3; ++s) {
+        SpeciesState& S = c->sp[s];
+        SpeciesHdr& h = H.sp[s];
+        h.nproc = S.nproc;
+        h.order = S.order;
+        h.k = S.nint;
+        h.tally_only = (S.flags & PCL_SPECIES_TALLY_ONLY) ? 1 : 0;
+        h.xscale = float(1.0 / (S.xmax / mc2));
+        h.cut = S.set ? float(S.cut / mc2) : INFINITY;
+        h.charge = charge[s];
+        const int nI = S.nint + 1;
+        h.rate_off = off();
+        for (int i = 0; i < nI; ++i)
+            for (int j = 0; j < S.nproc; ++j)
+                for (int k = 0; k < S.order; ++k)
+                    data.push_back(float(rate_to_dev(S.rate[k + S.order * (j + S.nproc * i)])));
+        h.rb_off = off();
+        for (int i = 0; i < nI; ++i)
+            for (int k = 0; k < S.order; ++k)
+                data.push_back(S.rb.empty() ? 0.0f : float(rate_to_dev(S.rb[k + S.order * i])));
+        h.cl_off = -1;
+        if (c->cl_order > 0 && s != PCL_PHOTON) {
+            const std::vector<double>& cf = (s == PCL_ELECTRON) ? c->cl_ec : c->cl_pc;
+            h.cl_off = off();
+            h.cl_k = c->cl_k;
+            h.cl_order = c->cl_order;
+            h.cl_xscale = float(1.0 / (c->cl_xmax / mc2));
+            for (int i = 0; i <= c->cl_k; ++i)
+                for (int k = 0; k < c->cl_order; ++k) data.push_back(float(force_to_dev(cf[k + c->cl_order * i])));
+        }
+        for (int j = 0; j < S.nproc; ++j) pack_proc(S.procs[j], S.sb_index[j], h.proc[j]);
+        if (S.hist_bins > 0) {
+            h.hist_bins = S.hist_bins;
+            double lmin = std::log(S.hist_emin / mc2), lmax = std::log(S.hist_emax / mc2);
+            h.hist_lmin = float(lmin);
+            h.hist_linv = float(S.hist_bins / (lmax - lmin));
+        }
+    }
+    H.nsb = int(c->sb.size());
+    for (size_t b = 0; b < c->sb.size(); ++b) {
+        SBHdr& h = H.sb[b];
+        h.ne = c->sb[b].ne;
+        h.ncum = c->sb[b].ncum;
+        h.inv_dp = float(c->sb[b].ncum - 1);
+        h.le_off = off();
+        for (int j = 0; j < h.ne; ++j) data.push_back(float(c->sb[b].log_energy[j] - std::log(mc2)));
+    }
+    for (int a = 0; a < 3; ++a) {
+        H.E[a] = float(force_to_dev(e * c->E[a]));            // per unit charge
+        H.B[a] = float(e * c->B[a] / m_e * NS);
+    }
+    while (data.size() % 4) data.push_back(0.0f);
+    size_t bytes = sizeof(BlobHdr) + data.size() * 4;
+    bytes = (bytes + 15) & ~size_t(15);
+    H.bytes = int(bytes);
+    c->blob.assign(bytes, 0);
+    std::memcpy(c->blob.data(), &H, sizeof(H));
+    std::memcpy(c->blob.data() + sizeof(H), data.data(), data.size() * 4);
+    if (bytes > c->d_blob_cap) {
+        cudaFree(c->d_blob);
+        CK(cudaMalloc(&c->d_blob, bytes));
+        c->d_blob_cap = bytes;
+    }
+    CK(cudaMemcpyAsync(c->d_blob, c->blob.data(), bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->blob_dirty = false;
+    return PCL_OK;
+}
+
+static StepArgs make_args(Ctx* c, float dt, int nsteps, int spill_mode, int sp_in) {
+    StepArgs A;
+    std::memset(&A, 0, sizeof(A));
+    for (int s = 0; s < 3; ++s) {
+        SpeciesState& S = c->sp[s];
+        A.xw[s] = S.xw[S.cur];
+        A.ps[s] = S.ps[S.cur];
+        A.meta[s] = S.meta[S.cur];
+        A.cap[s] = S.cap;
+        A.hist_n[s] = S.hist_n;
+        A.hist_w[s] = S.hist_w;
+    }
+    int sp_out = 1 - sp_in;
+    A.sp_in_xw = c->sp_xw[sp_in]; A.sp_in_ps = c->sp_ps[sp_in]; A.sp_in_meta = c->sp_meta[sp_in];
+    A.sp_out_xw = c->sp_xw[sp_out]; A.sp_out_ps = c->sp_ps[sp_out]; A.sp_out_meta = c->sp_meta[sp_out];
+    A.sp_cap = c->sp_cap;
+    A.sp_in_n = c->d_spn + sp_in;
+    A.sp_out_n = c->d_spn + sp_out;
+    A.ctl = c->d_ctl;
+    A.blob = c->d_blob;
+    for (size_t b = 0; b < c->sb.size(); ++b) A.sb_data[b] = c->sb[b].d_data;
+    A.key0 = uint32_t(c->cfg.seed);
+    A.key1 = uint32_t(c->cfg.seed >> 32);
+    A.dt = dt;
+    A.nsteps = nsteps;
+    A.spill_mode = spill_mode;
+    A.blob_bytes = int(c->blob.size());
+    return A;
+}
+
+static int grid_blocks(Ctx* c) {
+    if (c->cfg.grid_blocks > 0) return c->cfg.grid_blocks;
+    return 2 * c->sm_count;
+}
+
+static int block_threads(Ctx* c) {
+    int b = c->cfg.block_size > 0 ? c->cfg.block_size : 256;
+    return std::min(256, std::max(32, (b / 32) * 32));
+}
+
+static int readback(Ctx* c) {
+    CK(cudaMemcpyAsync(c->h_ctl, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return PCL_OK;
+}
+
+static int compact_all(Ctx* c) {
+    int rc = ensure_tiles(c);
+    if (rc) return rc;
+    CompactArgs C;
+    std::memset(&C, 0, sizeof(C));
+    long long capmax = 0;
+    for (int s = 0; s < 3; ++s) {
+        SpeciesState& S = c->sp[s];
+        int o = 1 - S.cur;
+        C.sxw[s] = S.xw[S.cur]; C.sps[s] = S.ps[S.cur]; C.smeta[s] = S.meta[S.cur];
+        C.dxw[s] = S.xw[o]; C.dps[s] = S.ps[o]; C.dmeta[s] = S.meta[o];
+        C.tile_cnt[s] = c->d_tile_cnt + s * c->tiles_cap;
+        C.tile_off[s] = c->d_tile_off + s * c->tiles_cap;
+        capmax = std::max(capmax, S.cap);
+    }
+    C.n = c->d_ctl->n;
+    C.n_out = c->d_nnew;
+    int nt = int(std::max<long long>(1, (capmax + kTile - 1) / kTile));
+    C.ntiles_max = nt;
+    dim3 g(nt, 3);
+    k_compact_count<<<g, 256, 0, c->stream>>>(C);
+    k_compact_scan<<<3, 1024, 0, c->stream>>>(C);
+    k_compact_scatter<<<g, 256, 0, c->stream>>>(C);
+    CK(cudaGetLastError());
+    c->launches += 3;
+    CK(cudaMemcpyAsync(c->d_ctl->n, c->d_nnew, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToDevice,
+                       c->stream));
+    for (int s = 0; s < 3; ++s)
+        if (c->sp[s].cap > 0) c->sp[s].cur = 1 - c->sp[s].cur;
+    c->steps_since_compact = 0;
+    return PCL_OK;
+}
+
+// One launch of `nsteps` steps of length dt (seconds), plus spill passes.
+static int launch_steps(Ctx* c, double dt_si, int nsteps) {
+    int rc = build_blob(c);
+    if (rc) return rc;
+    if ((rc = ensure_spill(c))) return rc;
+    const float dt = float(t_to_dev(dt_si));
+    const int threads = block_threads(c);
+    const size_t smem = step_smem_bytes(int(c->blob.size()), threads);
+    CK(cudaFuncSetAttribute(k_step, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    k_begin<<<1, 64, 0, c->stream>>>(c->d_ctl, c->sp[0].cap, c->sp[1].cap, c->sp[2].cap);
+    CK(cudaMemsetAsync(c->d_spn, 0, 2 * sizeof(unsigned long long), c->stream));
+    StepArgs A = make_args(c, dt, nsteps, 0, 0);
+    CK(cudaEventRecord(c->ev_k0, c->stream));
+    k_step<<<grid_blocks(c), threads, smem, c->stream>>>(A);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(c->ev_k1, c->stream));
+    c->launches += 2;
+    if ((rc = readback(c))) return rc;
+    {
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, c->ev_k0, c->ev_k1));
+        c->k_ms += ms;
+        c->k_launches += 1;
+        double nstart = 0, nout = 0, ndead = 0;
+        for (int s = 0; s < 3; ++s) {
+            nstart += double(c->h_ctl->n_start[s]);
+            nout += double(c->h_ctl->live_end[nsteps - 1][s]);
+            ndead += double(c->h_ctl->dead[s]);
+        }
+        c->k_bytes += 48.0 * nstart + 48.0 * nout + 4.0 * ndead;
+    }
+    // spill passes: queue written by the previous pass is the next pass's input
+    int in = 1;  // main pass wrote spill queue index 1 (sp_out = 1 - sp_in(0))
+    for (int pass = 0; pass < 64; ++pass) {
+        unsigned long long pending = 0;
+        CK(d2h(c, &pending, c->d_spn + in, sizeof(pending)));
+        if (pending == 0) break;
+        if ((long long)pending > c->sp_cap) pending = (unsigned long long)c->sp_cap;
+        CK(h2d(c, c->d_spn + in, &pending, sizeof(pending)));
+        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + in, c->d_spn + (1 - in));
+        StepArgs S = make_args(c, dt, nsteps, 1, in);
+        k_step<<<grid_blocks(c), threads, smem, c->stream>>>(S);
+        CK(cudaGetLastError());
+        c->launches += 2;
+        in = 1 - in;
+        if (pass == 63) return fail(c, PCL_ERR_TIMEOUT, "spill passes did not drain");
+    }
+    if ((rc = readback(c))) return rc;
+    if (c->h_ctl->timeout) return fail(c, PCL_ERR_TIMEOUT, "table staging wait timed out");
+    c->t += dt_si * nsteps;
+    c->steps += nsteps;
+    for (int k = 0; k < nsteps; ++k) c->particle_steps += (long long)c->h_ctl->live_start[k];
+    for (int s = 0; s < 3; ++s) c->live[s] = (long long)c->h_ctl->live_end[nsteps - 1][s];
+    c->steps_since_compact += nsteps;
+    int period = c->cfg.compaction_period > 0 ? c->cfg.compaction_period : 1;
+    if (c->steps_since_compact >= period) {
+        if ((rc = compact_all(c))) return rc;
+    }
+    if (c->h_ctl->err[PCL_E_CAPACITY] > 0) return fail(c, PCL_ERR_CAPACITY, "population capacity exceeded");
+    return PCL_OK;
+}
+
+static int check_species(Ctx* c, int s) {
+    if (s < 0 || s >= 3) return fail(c, PCL_ERR_INVALID, "species out of range");
+    return PCL_OK;
+}
+
+}  // namespace pcl
+
+using namespace pcl;
+
+// =============================================================== C ABI ===
+extern "C" {
+
+const char* pcl_version(void) { return "particulator_gb300 0.1 (sm_103a)"; }
+
+int pcl_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+    return n;
+}
+
+const char* pcl_last_error(void* ctx) {
+    if (!ctx) return "null context";
+    return static_cast<Ctx*>(ctx)->last_error.c_str();
+}
+
+int pcl_create(const pcl_config* cfg, void** out) {
+    if (!cfg || !out) return PCL_ERR_INVALID;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PCL_ERR_CUDA;
+    if (cfg->device < 0 || cfg->device >= ndev) return PCL_ERR_INVALID;
+    if (cfg->steps_per_launch > PCL_MAX_STEPS_PER_LAUNCH) return PCL_ERR_INVALID;
+    Ctx* c = new Ctx();
+    c->cfg = *cfg;
+    c->device = cfg->device;
+    if (cudaSetDevice(c->device) != cudaSuccess) { delete c; return PCL_ERR_CUDA; }
+    cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, c->device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&c->d_ctl, sizeof(Control)) != cudaSuccess ||
+        cudaMallocHost(&c->h_ctl, sizeof(Control)) != cudaSuccess ||
+        cudaMalloc(&c->d_spn, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&c->d_nnew, 3 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&c->d_mom, 16 * sizeof(double)) != cudaSuccess ||
+        cudaEventCreate(&c->ev_k0) != cudaSuccess || cudaEventCreate(&c->ev_k1) != cudaSuccess ||
+        cudaEventCreate(&c->ev_t0) != cudaSuccess || cudaEventCreate(&c->ev_t1) != cudaSuccess) {
+        pcl_destroy(c);
+        return PCL_ERR_CUDA;
+    }
+    cudaMemset(c->d_ctl, 0, sizeof(Control));
+    cudaMemset(c->d_spn, 0, 2 * sizeof(unsigned long long));
+    std::memset(c->h_ctl, 0, sizeof(Control));
+    cudaDeviceSynchronize();
+    *out = c;
+    return PCL_OK;
+}
+
+void pcl_destroy(void* ctx) {
+    if (!ctx) return;
+    Ctx* c = static_cast<Ctx*>(ctx);
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& s : c->sp) free_species_buffers(s);
+    for (auto& t : c->sb) cudaFree(t.d_data);
+    for (int b = 0; b < 2; ++b) { cudaFree(c->sp_xw[b]); cudaFree(c->sp_ps[b]); cudaFree(c->sp_meta[b]); }
+    cudaFree(c->d_spn); cudaFree(c->d_blob); cudaFree(c->d_ctl); cudaFree(c->d_tile_cnt);
+    cudaFree(c->d_tile_off); cudaFree(c->d_nnew); cudaFree(c->d_mom);
+    if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    for (cudaEvent_t ev : {c->ev_k0, c->ev_k1, c->ev_t0, c->ev_t1})
+        if (ev) cudaEventDestroy(ev);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int pcl_set_species(void* ctx, int species, double energy_cut, int64_t capacity, int flags) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (capacity < 0 || capacity >= (1ll << 31)) return fail(c, PCL_ERR_INVALID, "capacity out of range");
+    if (!(energy_cut >= 0)) return fail(c, PCL_ERR_INVALID, "energy cut must be >= 0");
+    CK(cudaSetDevice(c->device));
+    SpeciesState& S = c->sp[species];
+    CK(cudaStreamSynchronize(c->stream));
+    free_species_buffers(S);
+    S.set = true;
+    S.cut = energy_cut;
+    S.flags = flags;
+    S.cap = (flags & PCL_SPECIES_TALLY_ONLY) ? 0 : capacity;
+    S.cur = 0;
+    if (S.cap > 0) {
+        for (int b = 0; b < 2; ++b) {
+            CK(cudaMalloc(&S.xw[b], sizeof(float4) * S.cap));
+            CK(cudaMalloc(&S.ps[b], sizeof(float4) * S.cap));
+            CK(cudaMalloc(&S.meta[b], sizeof(uint4) * S.cap));
+        }
+    }
+    unsigned long long zero = 0;
+    CK(h2d(c, &c->d_ctl->n[species], &zero, sizeof(zero)));
+    c->live[species] = 0;
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
+int pcl_set_collision_table(void* ctx, int species, int order, int nproc, int nintervals, double xmax,
+                            const double* rate, const double* ratebound, const pcl_process* procs) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (order < 1 || order > PCL_MAX_ORDER || nproc < 0 || nproc > PCL_MAX_PROC || nintervals < 1 ||
+        nintervals > PCL_MAX_INTERVALS || !(xmax > 0) || !ratebound || (nproc > 0 && (!rate || !procs)))
+        return fail(c, PCL_ERR_INVALID, "bad collision table");
+    SpeciesState& S = c->sp[species];
+    const int nI = nintervals + 1;
+    S.order = order; S.nproc = nproc; S.nint = nintervals; S.xmax = xmax;
+    S.rate.assign(rate, rate + size_t(order) * nproc * nI);
+    if (nproc == 0) S.rate.clear();
+    S.rb.assign(ratebound, ratebound + size_t(order) * nI);
+    S.procs.assign(procs, procs + nproc);
+    S.sb_index.assign(nproc, -1);
+    CK(cudaSetDevice(c->device));
+    for (int j = 0; j < nproc; ++j) {
+        const pcl_process& P = procs[j];
+        if (P.kind < PCL_PROC_MOLLER || P.kind > PCL_PROC_ANNIHILATION)
+            return fail(c, PCL_ERR_UNSUPPORTED, "unsupported process kind");
+        if (P.kind == PCL_PROC_SELTZER_BERGER) {
+            if (!P.aux0 || !P.aux2 || P.naux < 2 || P.naux2 < 2)
+                return fail(c, PCL_ERR_INVALID, "Seltzer-Berger process needs log_energy and data");
+            int found = -1;
+            for (size_t b = 0; b < c->sb.size(); ++b)
+                if (c->sb[b].Z == P.Z && c->sb[b].ne == P.naux && c->sb[b].ncum == P.naux2 &&
+                    c->sb[b].log_energy == std::vector<double>(P.aux0, P.aux0 + P.naux))
+                    found = int(b);
+            if (found < 0) {
+                if (c->sb.size() >= PCL_MAX_SB) return fail(c, PCL_ERR_UNSUPPORTED, "too many SB tables");
+                SBTable T;
+                T.Z = P.Z; T.ne = P.naux; T.ncum = P.naux2;
+                T.log_energy.assign(P.aux0, P.aux0 + P.naux);
+                T.key_ptr = P.aux2;
+                std::vector<float> f(size_t(T.ne) * T.ncum);
+                for (size_t q = 0; q < f.size(); ++q) f[q] = float(P.aux2[q]);
+                CK(cudaMalloc(&T.d_data, f.size() * sizeof(float)));
+                CK(h2d(c, T.d_data, f.data(), f.size() * sizeof(float)));
+                c->sb.push_back(T);
+                found = int(c->sb.size()) - 1;
+            }
+            S.sb_index[j] = found;
+        }
+        if (P.kind == PCL_PROC_PHOTOELECTRIC && P.nparam < 1)
+            return fail(c, PCL_ERR_INVALID, "photoelectric process needs binding energies");
+    }
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
+int pcl_set_forcing(void* ctx, const double E[3], const double B[3], int cl_order, int cl_k, double cl_xmax,
+                    const double* cl_ec, const double* cl_pc) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !E || !B) return PCL_ERR_INVALID;
+    if (cl_order < 0 || cl_order > PCL_MAX_ORDER) return fail(c, PCL_ERR_INVALID, "bad continuum order");
+    for (int a = 0; a < 3; ++a) { c->E[a] = E[a]; c->B[a] = B[a]; }
+    c->cl_order = cl_order;
+    if (cl_order > 0) {
+        if (cl_k < 1 || cl_k > PCL_MAX_INTERVALS || !(cl_xmax > 0) || !cl_ec || !cl_pc)
+            return fail(c, PCL_ERR_INVALID, "bad continuum-loss table");
+        c->cl_k = cl_k;
+        c->cl_xmax = cl_xmax;
+        c->cl_ec.assign(cl_ec, cl_ec + size_t(cl_order) * (cl_k + 1));
+        c->cl_pc.assign(cl_pc, cl_pc + size_t(cl_order) * (cl_k + 1));
+    }
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
+int pcl_upload(void* ctx, int species, int64_t n, const double* x, const double* p, const double* w,
+               const double* t, const double* s, const uint64_t* sid, uint64_t sid_base) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    if (!S.set || S.cap == 0) return fail(c, PCL_ERR_STATE, "species not set or tally-only");
+    if (n < 0 || n > S.cap) return fail(c, PCL_ERR_CAPACITY, "upload exceeds capacity");
+    if (n > 0 && (!x || !p || !w || !t)) return fail(c, PCL_ERR_INVALID, "null particle arrays");
+    std::vector<float4> hx(n), hp(n);
+    std::vector<uint4> hm(n);
+    const uint32_t k0 = uint32_t(c->cfg.seed), k1 = uint32_t(c->cfg.seed >> 32);
+    for (int64_t i = 0; i < n; ++i) {
+        uint64_t id = sid ? sid[i] : sid_base + uint64_t(i);
+        uint32_t ctr = 0;
+        double sv;
+        if (s) {
+            sv = s[i];
+        } else {  // s = nextcoll() drawn from the particle's own stream (electron.jl:30-33)
+            uint32_t cc[4] = {0u, uint32_t(id), uint32_t(id >> 32), 0u};
+            philox_host(cc, k0, k1);
+            double u = double(((cc[0] >> 9) << 1) | 1u) * 5.9604644775390625e-8;
+            sv = -std::log(u);
+            ctr = 1;
+        }
+        hx[i] = make_float4(float(x[3 * i]), float(x[3 * i + 1]), float(x[3 * i + 2]), float(w[i]));
+        hp[i] = make_float4(float(p_to_dev(p[3 * i])), float(p_to_dev(p[3 * i + 1])),
+                            float(p_to_dev(p[3 * i + 2])), float(sv));
+        float toff = float(t_to_dev(t[i] - c->t));
+        uint32_t tb;
+        std::memcpy(&tb, &toff, 4);
+        hm[i] = make_uint4(uint32_t(id), uint32_t(id >> 32), ctr, tb);
+    }
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (n > 0) {
+        CK(h2d(c, S.xw[S.cur], hx.data(), sizeof(float4) * n));
+        CK(h2d(c, S.ps[S.cur], hp.data(), sizeof(float4) * n));
+        CK(h2d(c, S.meta[S.cur], hm.data(), sizeof(uint4) * n));
+    }
+    unsigned long long nn = (unsigned long long)n;
+    CK(h2d(c, &c->d_ctl->n[species], &nn, sizeof(nn)));
+    c->live[species] = n;
+    return PCL_OK;
+}
+
+static int get_n(Ctx* c, int species, long long& n) {
+    unsigned long long nn = 0;
+    CK(d2h(c, &nn, &c->d_ctl->n[species], sizeof(nn)));
+    n = std::min<long long>((long long)nn, c->sp[species].cap);
+    return PCL_OK;
+}
+
+int pcl_download(void* ctx, int species, int64_t* n, double* x, double* p, double* w, double* t, double* s,
+                 uint64_t* sid, uint32_t* ctr) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !n) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    CK(cudaSetDevice(c->device));
+    long long slots = 0;
+    if (S.cap > 0 && (rc = get_n(c, species, slots))) return rc;
+    std::vector<float4> hx(slots), hp(slots);
+    std::vector<uint4> hm(slots);
+    if (slots > 0) {
+        CK(d2h(c, hx.data(), S.xw[S.cur], sizeof(float4) * slots));
+        CK(d2h(c, hp.data(), S.ps[S.cur], sizeof(float4) * slots));
+        CK(d2h(c, hm.data(), S.meta[S.cur], sizeof(uint4) * slots));
+    }
+    int64_t capn = *n, m = 0;
+    for (long long i = 0; i < slots; ++i) {
+        if (hm[i].z == PCL_DEAD_CTR) continue;
+        if (m >= capn) return fail(c, PCL_ERR_CAPACITY, "download arrays too small");
+        if (x) { x[3 * m] = hx[i].x; x[3 * m + 1] = hx[i].y; x[3 * m + 2] = hx[i].z; }
+        if (p) {
+            p[3 * m] = p_to_si(hp[i].x); p[3 * m + 1] = p_to_si(hp[i].y); p[3 * m + 2] = p_to_si(hp[i].z);
+        }
+        if (w) w[m] = hx[i].w;
+        if (s) s[m] = hp[i].w;
+        float toff;
+        std::memcpy(&toff, &hm[i].w, 4);
+        if (t) t[m] = c->t + t_to_si(toff);
+        if (sid) sid[m] = uint64_t(hm[i].x) | (uint64_t(hm[i].y) << 32);
+        if (ctr) ctr[m] = hm[i].z;
+        ++m;
+    }
+    *n = m;
+    return PCL_OK;
+}
+
+int pcl_upload_packed(void* ctx, int species, int64_t n, const pcl_packed* host) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !host) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    if (!S.set || S.cap == 0) return fail(c, PCL_ERR_STATE, "species not set or tally-only");
+    if (n < 0 || n > S.cap) return fail(c, PCL_ERR_CAPACITY, "upload exceeds capacity");
+    CK(cudaSetDevice(c->device));
+    if (n > 0) {
+        CK(cudaMemcpyAsync(S.xw[S.cur], host->xw, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(S.ps[S.cur], host->ps, sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemcpyAsync(S.meta[S.cur], host->meta, sizeof(uint4) * n, cudaMemcpyHostToDevice, c->stream));
+    }
+    unsigned long long nn = (unsigned long long)n;
+    CK(cudaMemcpyAsync(&c->d_ctl->n[species], &nn, sizeof(nn), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->live[species] = n;
+    return PCL_OK;
+}
+
+int pcl_download_packed(void* ctx, int species, int64_t* n, pcl_packed* host) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !host || !n) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    CK(cudaSetDevice(c->device));
+    long long slots = 0;
+    if (S.cap > 0 && (rc = get_n(c, species, slots))) return rc;
+    if (slots > *n) return fail(c, PCL_ERR_CAPACITY, "download arrays too small");
+    if (slots > 0) {
+        CK(cudaMemcpyAsync(host->xw, S.xw[S.cur], sizeof(float4) * slots, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(host->ps, S.ps[S.cur], sizeof(float4) * slots, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(host->meta, S.meta[S.cur], sizeof(uint4) * slots, cudaMemcpyDeviceToHost, c->stream));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    *n = slots;
+    return PCL_OK;
+}
+
+int pcl_advance(void* ctx, double tfinal) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    if (!(tfinal > c->t)) return fail(c, PCL_ERR_INVALID, "tfinal must exceed the current time");
+    bool any = false;
+    for (auto& s : c->sp) any = any || s.set;
+    if (!any) return fail(c, PCL_ERR_STATE, "no species set");
+    CK(cudaSetDevice(c->device));
+    return launch_steps(c, tfinal - c->t, 1);
+}
+
+int pcl_run(void* ctx, double tfinal, double dt, const pcl_run_opts* opts, pcl_tallies* out) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    if (!(dt > 0)) return fail(c, PCL_ERR_INVALID, "dt must be > 0");
+    CK(cudaSetDevice(c->device));
+    const int K = std::max(1, c->cfg.steps_per_launch);
+    long long done = 0;
+    while (c->t < tfinal) {
+        // run.jl:6-27: advance!, droplow!, onstep (population target)
+        long long left = (long long)std::ceil((tfinal - c->t) / dt - 1e-9);
+        int ns = int(std::min<long long>(K, std::max<long long>(1, left)));
+        if (opts && opts->max_steps > 0) ns = int(std::min<long long>(ns, opts->max_steps - done));
+        if (ns <= 0) break;
+        int rc = launch_steps(c, dt, ns);
+        if (rc) return rc;
+        done += ns;
+        if (opts && opts->target_species >= 0 && opts->target_species < 3) {
+            long long live = c->live[opts->target_species];
+            bool cont = opts->target_ismax ? (live < opts->target_n) : (live > opts->target_n);
+            if (!cont) break;
+        }
+        if (opts && opts->max_steps > 0 && done >= opts->max_steps) break;
+    }
+    if (out) return pcl_get_tallies(ctx, out);
+    return PCL_OK;
+}
+
+int pcl_get_tallies(void* ctx, pcl_tallies* out) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !out) return PCL_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    int rc = readback(c);
+    if (rc) return rc;
+    std::memset(out, 0, sizeof(*out));
+    const Control& C = *c->h_ctl;
+    out->t = c->t;
+    out->steps = c->steps;
+    out->particle_steps = c->particle_steps;
+    for (int s = 0; s < 3; ++s) {
+        out->n[s] = std::min<long long>((long long)C.n[s], c->sp[s].cap);
+        out->live[s] = c->live[s];
+        for (int j = 0; j < PCL_MAX_PROC; ++j) out->collisions[s][j] = (long long)C.coll[s][j];
+        out->nulls[s] = (long long)C.nulls[s];
+        out->spawned[s] = (long long)C.spawned[s];
+        out->tally_count[s] = (long long)C.tally_count[s];
+        out->tally_w[s] = C.tally_w[s];
+        out->tally_wE[s] = e_to_si(C.tally_wE[s]);
+    }
+    for (int e = 0; e < PCL_NERR; ++e) out->errors[e] = (long long)C.err[e];
+    return PCL_OK;
+}
+
+int pcl_reset_tallies(void* ctx) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    int rc = readback(c);
+    if (rc) return rc;
+    Control keep = *c->h_ctl;
+    Control z;
+    std::memset(&z, 0, sizeof(z));
+    for (int s = 0; s < 3; ++s) z.n[s] = keep.n[s];
+    CK(h2d(c, c->d_ctl, &z, sizeof(z)));
+    c->particle_steps = 0;
+    for (auto& S : c->sp) {
+        if (S.hist_bins > 0) {
+            CK(cudaMemsetAsync(S.hist_n, 0, sizeof(unsigned long long) * S.hist_bins, c->stream));
+            CK(cudaMemsetAsync(S.hist_w, 0, sizeof(double) * S.hist_bins, c->stream));
+            CK(cudaStreamSynchronize(c->stream));
+        }
+    }
+    return PCL_OK;
+}
+
+int pcl_moments(void* ctx, int species, double out[10]) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !out) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    CK(cudaSetDevice(c->device));
+    long long slots = 0;
+    if (S.cap > 0 && (rc = get_n(c, species, slots))) return rc;
+    CK(cudaMemsetAsync(c->d_mom, 0, 10 * sizeof(double), c->stream));
+    if (slots > 0) {
+        int blocks = int(std::min<long long>(4 * c->sm_count, (slots + 255) / 256));
+        k_moments<<<blocks, 256, 0, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], slots, species,
+                                                   c->d_mom);
+        CK(cudaGetLastError());
+    }
+    double h[10];
+    CK(cudaMemcpyAsync(h, c->d_mom, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int q = 0; q < 8; ++q) out[q] = h[q];
+    out[1] = e_to_si(h[1]);
+    out[8] = e_to_si(h[8]);
+    unsigned long long live;
+    std::memcpy(&live, &h[9], 8);
+    out[9] = double(live);
+    return PCL_OK;
+}
+
+int pcl_compact(void* ctx) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    int rc = compact_all(c);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return PCL_OK;
+}
+
+int pcl_set_tally_histogram(void* ctx, int species, int nbins, double emin, double emax) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (nbins < 0 || nbins > (1 << 16) || (nbins > 0 && !(emin > 0 && emax > emin)))
+        return fail(c, PCL_ERR_INVALID, "bad histogram");
+    SpeciesState& S = c->sp[species];
+    CK(cudaSetDevice(c->device));
+    cudaFree(S.hist_n); cudaFree(S.hist_w);
+    S.hist_n = nullptr; S.hist_w = nullptr;
+    S.hist_bins = nbins; S.hist_emin = emin; S.hist_emax = emax;
+    if (nbins > 0) {
+        CK(cudaMalloc(&S.hist_n, sizeof(unsigned long long) * nbins));
+        CK(cudaMalloc(&S.hist_w, sizeof(double) * nbins));
+        CK(cudaMemsetAsync(S.hist_n, 0, sizeof(unsigned long long) * nbins, c->stream));
+        CK(cudaMemsetAsync(S.hist_w, 0, sizeof(double) * nbins, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
+int pcl_get_tally_histogram(void* ctx, int species, int nbins, int64_t* counts, double* weights) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    if (nbins != S.hist_bins) return fail(c, PCL_ERR_INVALID, "bin count mismatch");
+    if (nbins == 0) return PCL_OK;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (counts) CK(d2h(c, counts, S.hist_n, sizeof(int64_t) * nbins));
+    if (weights) CK(d2h(c, weights, S.hist_w, sizeof(double) * nbins));
+    return PCL_OK;
+}
+
+int pcl_sync(void* ctx) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    return PCL_OK;
+}
+
+int pcl_timer_start(void* ctx) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    CK(cudaEventRecord(c->ev_t0, c->stream));
+    return PCL_OK;
+}
+
+int pcl_timer_stop(void* ctx, double* ms) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !ms) return PCL_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    CK(cudaEventRecord(c->ev_t1, c->stream));
+    CK(cudaEventSynchronize(c->ev_t1));
+    float f = 0.0f;
+    CK(cudaEventElapsedTime(&f, c->ev_t0, c->ev_t1));
+    *ms = f;
+    return PCL_OK;
+}
+
+int pcl_kernel_stats(void* ctx, double* step_kernel_ms, int64_t* step_launches, int64_t* launches,
+                     double* step_bytes, int reset) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    if (step_kernel_ms) *step_kernel_ms = c->k_ms;
+    if (step_launches) *step_launches = c->k_launches;
+    if (launches) *launches = c->launches;
+    if (step_bytes) *step_bytes = c->k_bytes;
+    if (reset) { c->k_ms = 0; c->k_launches = 0; c->launches = 0; c->k_bytes = 0; }
+    return PCL_OK;
+}
+
+int pcl_test_sampler(void* ctx, int species, int proc_index, int64_t n, const double* p, const uint64_t* sid,
+                     double* out_p, double* out_s, int32_t* out_kind, uint32_t* out_ctr) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    if (proc_index < 0 || proc_index >= S.nproc) return fail(c, PCL_ERR_INVALID, "process index");
+    if (n <= 0 || !p || !sid || !out_p || !out_s || !out_kind || !out_ctr) return PCL_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    if ((rc = build_blob(c))) return rc;
+    std::vector<float> hp(3 * n);
+    std::vector<uint32_t> hs(2 * n);
+    for (int64_t i = 0; i < 3 * n; ++i) hp[i] = float(p_to_dev(p[i]));
+    for (int64_t i = 0; i < n; ++i) { hs[2 * i] = uint32_t(sid[i]); hs[2 * i + 1] = uint32_t(sid[i] >> 32); }
+    float *dp = nullptr, *dop = nullptr, *dos = nullptr;
+    uint32_t *dsid = nullptr, *dctr = nullptr;
+    int* dkind = nullptr;
+    CK(cudaMalloc(&dp, sizeof(float) * 3 * n));
+    CK(cudaMalloc(&dsid, sizeof(uint32_t) * 2 * n));
+    CK(cudaMalloc(&dop, sizeof(float) * 9 * n));
+    CK(cudaMalloc(&dos, sizeof(float) * 3 * n));
+    CK(cudaMalloc(&dkind, sizeof(int) * 3 * n));
+    CK(cudaMalloc(&dctr, sizeof(uint32_t) * n));
+    CK(h2d(c, dp, hp.data(), sizeof(float) * 3 * n));
+    CK(h2d(c, dsid, hs.data(), sizeof(uint32_t) * 2 * n));
+    CK(cudaMemsetAsync(dop, 0, sizeof(float) * 9 * n, c->stream));
+    CK(cudaMemsetAsync(dos, 0, sizeof(float) * 3 * n, c->stream));
+    StepArgs A = make_args(c, 0.0f, 1, 0, 0);
+    size_t smem = c->blob.size() + 16;
+    CK(cudaFuncSetAttribute(k_test_sampler, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    int blocks = int((n + 127) / 128);
+    k_test_sampler<<<blocks, 128, smem, c->stream>>>(A, species, proc_index, n, dp, dsid, dop, dos, dkind, dctr);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    std::vector<float> hop(9 * n), hos(3 * n);
+    CK(d2h(c, hop.data(), dop, sizeof(float) * 9 * n));
+    CK(d2h(c, hos.data(), dos, sizeof(float) * 3 * n));
+    CK(d2h(c, out_kind, dkind, sizeof(int) * 3 * n));
+    CK(d2h(c, out_ctr, dctr, sizeof(uint32_t) * n));
+    for (int64_t i = 0; i < 9 * n; ++i) out_p[i] = p_to_si(hop[i]);
+    for (int64_t i = 0; i < 3 * n; ++i) out_s[i] = hos[i];
+    cudaFree(dp); cudaFree(dsid); cudaFree(dop); cudaFree(dos); cudaFree(dkind); cudaFree(dctr);
+    return PCL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,127 @@
+// Types shared by the host context code and the device step kernels.
+//
+// HBM layout of a population (one per species, double-buffered for
+// compaction): three arrays of 16-byte records, slot i of each holding
+//   xw[i]   = {x, y, z (m), w}
+//   ps[i]   = {px, py, pz (m_e c), s}
+//   meta[i] = {sid_lo, sid_hi, ctr, t_off bits}
+// 48 B per particle, one 128-bit load per record (float4-vectorised, fully
+// coalesced when consecutive lanes hold consecutive slots).  A slot whose ctr
+// is DEAD_CTR is a removed particle (remove_particle!, population.jl:120-122);
+// the step updates particles in place and appends secondaries, and the
+// compaction kernels (repack!, population.jl:229-259) squeeze dead slots out.
+//
+// The per-species collision tables, continuum-loss fits and process
+// parameters are packed on the host into one "table blob" that every block
+// copies into shared memory with one cp.async.bulk at kernel start.
+#pragma once
+#include <stdint.h>
+
+#define PCL_DEAD_CTR 0xFFFFFFFFu
+#define PCL_MAX_STEPS_PER_LAUNCH 64
+
+namespace pcl {
+
+// Device view of one process (normalised units).
+struct DevProc {
+    int32_t kind;
+    int32_t sb;       // Seltzer-Berger table index, -1 otherwise
+    int32_t nbind;    // photoelectric: number of binding energies
+    int32_t pad;
+    float   p[8];     // kind-specific, see ctx.cu:pack_proc
+};
+
+struct SpeciesHdr {
+    int32_t nproc;
+    int32_t order;
+    int32_t k;            // binary intervals of the collision table
+    int32_t tally_only;
+    float   xscale;       // 1 / xmax (normalised energy)
+    float   cut;          // energy cut (m_e c^2)
+    int32_t rate_off;     // float offset of rate[i][j][order] in the blob
+    int32_t rb_off;       // float offset of ratebound[i][order]
+    int32_t cl_off;       // float offset of the continuum-loss fit [i][order], -1 = none
+    int32_t cl_k;
+    int32_t cl_order;
+    float   cl_xscale;
+    float   charge;       // -1, 0, +1
+    int32_t hist_bins;    // tally-only: histogram bins (0 = none)
+    float   hist_lmin;    // log(Emin) (device energy units)
+    float   hist_linv;    // bins / (log Emax - log Emin)
+    DevProc proc[16];
+};
+
+struct SBHdr {
+    int32_t ne;        // primary energies
+    int32_t ncum;      // cumulative-probability points (pcum = LinRange(0, 1, ncum))
+    int32_t le_off;    // float offset of log(T / m_e c^2) [ne] in the blob
+    float   inv_dp;    // ncum - 1
+};
+
+struct BlobHdr {
+    SpeciesHdr sp[3];
+    SBHdr sb[4];
+    float E[3];        // e E / (m_e c) per ns   (force per unit charge)
+    float B[3];        // e B / m_e per ns       (times beta x B)
+    int32_t nsb;
+    int32_t bytes;     // total blob size (multiple of 16)
+    int32_t pad[2];
+};
+
+// Device-side counters of one context (global memory, zeroed per launch
+// where noted by the host).
+struct Control {
+    unsigned long long n[3];          // slots in use (live + dead); appends add here
+    unsigned long long n_start[3];    // slots present at launch start (work space)
+    unsigned long long head;          // work-fetch cursor over the concatenated work space
+    unsigned long long spill_n;       // children written to the spill queue by this launch
+    unsigned long long coll[3][16];   // real collisions per table position
+    unsigned long long nulls[3];
+    unsigned long long spawned[3];
+    unsigned long long tally_count[3];
+    double             tally_w[3];
+    double             tally_wE[3];   // device energy units
+    unsigned long long err[8];
+    unsigned long long live_end[PCL_MAX_STEPS_PER_LAUNCH][3];  // live at the end of step k
+    unsigned long long live_start[PCL_MAX_STEPS_PER_LAUNCH];   // particle-steps of step k
+    unsigned long long dead[3];       // slots marked dead by this launch
+    int                timeout;
+    int                pad;
+};
+
+// Arguments of the step kernel (passed by value).
+struct StepArgs {
+    float4* xw[3];
+    float4* ps[3];
+    uint4*  meta[3];
+    long long cap[3];
+    // spill queues: the kernel reads `sp_in` (spill mode) and writes `sp_out`
+    float4* sp_in_xw; float4* sp_in_ps; uint4* sp_in_meta;
+    float4* sp_out_xw; float4* sp_out_ps; uint4* sp_out_meta;
+    long long sp_cap;
+    const unsigned long long* sp_in_n;   // spill-mode input count (device)
+    unsigned long long* sp_out_n;        // spill output count (device)
+    Control* ctl;
+    const float4* blob;                  // table blob (global), staged to shared
+    const float* sb_data[4];             // Seltzer-Berger tables [ne][ncum] (energy-major)
+    double* hist_w[3];                   // tally-only histogram weights (device)
+    unsigned long long* hist_n[3];       // tally-only histogram counts (device)
+    uint32_t key0, key1;                 // Philox key
+    float dt;                            // step length (ns)
+    int nsteps;                          // steps in this launch
+    int spill_mode;                      // 0: populations, 1: spill queue
+    int blob_bytes;
+};
+
+// Arguments of the compaction kernels (repack!, population.jl:229-259).
+struct CompactArgs {
+    const float4* sxw[3]; const float4* sps[3]; const uint4* smeta[3];
+    float4* dxw[3]; float4* dps[3]; uint4* dmeta[3];
+    const unsigned long long* n;   // slots per species (ctl->n)
+    unsigned int* tile_cnt[3];
+    unsigned long long* tile_off[3];
+    unsigned long long* n_out;     // live counts per species (copied to ctl->n after the scatter)
+    int ntiles_max;
+};
+
+}  // namespace pcl

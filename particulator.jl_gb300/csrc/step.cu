@@ -1,0 +1,1220 @@
+// GB300 (sm_103a) kernels of the null-collision Monte Carlo step.
+//
+// One thread owns one particle at a time and runs the reference's per-particle
+// sub-step loop (advance1!, mixed_population.jl:56-93): null-collision clock
+// s / r, Ralston RK2 push (pusher.jl:41-63) with the homogeneous field and the
+// Chebyshev continuum loss (field.jl:54-70, continuum.jl:45-57), and, at the
+// end of a sub-step that reaches the clock, do_one_collision!
+// (collisions.jl:142-199): Chebyshev rates on binary intervals (cheby.jl:127-143,
+// collision_table.jl:82-106), linear scan of xi = U r, then one of the
+// process samplers.  Lanes are refilled after every sub-step, so a warp never
+// idles on lanes whose particle finished early: an idle lane first pops a
+// secondary from its warp's child stack in shared memory (secondaries are
+// advanced from their birth time to the end of the step, as the reference's
+// repeated advance1! passes do, mixed_population.jl:43-46), then takes the
+// next input slot from a warp-private chunk of the work space.
+//
+// Every random number comes from the particle's own Philox4x32-10 stream
+// (Salmon et al., SC'11): key = context seed, counter = (draw / 4, sid_lo,
+// sid_hi, 0).  A secondary's stream id is drawn from the parent's stream in a
+// separate counter domain, so results do not depend on thread scheduling.
+// Each uniform is u = (2 floor(x / 2^9) + 1) 2^-24, exactly representable in
+// FP32 and FP64, in (0, 1).
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+
+#include "device.cuh"
+#include "../../include/particulator_gb300.h"
+
+namespace pcl {
+
+constexpr int   kWarpStack   = 64;          // child-stack entries per warp
+constexpr int   kRejectCap   = 10000;       // rejection-loop iteration cap
+constexpr int   kSubstepCap  = 1 << 20;     // sub-steps per particle per step
+constexpr float kEpsT        = 2.220446049250313e-7f;  // eps(Float64) s in ns (mixed_population.jl:66)
+constexpr float kCns         = 0.299792458f;           // c in m/ns
+
+// block-tally word offsets (uint32 in shared memory)
+constexpr int T_COLL = 0;              // [3][16]
+constexpr int T_NULL = 48;             // [3]
+constexpr int T_SPAWN = 51;            // [3]
+constexpr int T_DEAD = 54;             // [3]
+constexpr int T_ERR = 57;              // [8]
+constexpr int T_LEND = 65;             // [64][3]
+constexpr int T_LSTART = T_LEND + 3 * PCL_MAX_STEPS_PER_LAUNCH;  // [64]
+constexpr int T_WORDS = T_LSTART + PCL_MAX_STEPS_PER_LAUNCH;     // 321
+
+// ------------------------------------------------------------ Philox ----
+__device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3,
+                                              uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+}
+
+// ----------------------------------------------------------- lane state --
+struct Lane {
+    float x, y, z, w;
+    float px, py, pz, s;
+    float r, tl;
+    uint32_t sid_lo, sid_hi, ctr;
+    uint32_t c0, c1, c2, c3;   // Philox words not yet consumed (front = c0)
+    int slot;                  // input slot, or -1 for a secondary (appended on finish)
+    int species;
+    int k;                     // time step within this launch
+    int nsub;
+    bool alive, rvalid;
+};
+
+struct KCtx {
+    const BlobHdr* H;
+    const float* blob;
+    float4* stk;       // this warp's child stack: entry e = stk[3e .. 3e+2]
+    int* top;          // this warp's stack top
+    uint32_t* tal;     // block tallies
+    const StepArgs* A;
+    // test-hook capture of secondaries (pcl_test_sampler): when non-null,
+    // secondaries go to cap[0..1] instead of the stack
+    float* cap;
+    int* ncap;
+};
+
+__device__ __forceinline__ uint32_t next_bits(Lane& L, uint32_t k0, uint32_t k1) {
+    uint32_t sh = L.ctr & 3u;
+    if (!L.rvalid || sh == 0u) {
+        uint32_t a = L.ctr >> 2, b = L.sid_lo, c = L.sid_hi, d = 0u;
+        philox4x32_10(a, b, c, d, k0, k1);
+        if (sh == 0u) { L.c0 = a; L.c1 = b; L.c2 = c; L.c3 = d; }
+        else if (sh == 1u) { L.c0 = b; L.c1 = c; L.c2 = d; }
+        else if (sh == 2u) { L.c0 = c; L.c1 = d; }
+        else { L.c0 = d; }
+        L.rvalid = true;
+    }
+    uint32_t v = L.c0;
+    L.c0 = L.c1; L.c1 = L.c2; L.c2 = L.c3;
+    L.ctr += 1u;
+    return v;
+}
+
+__device__ __forceinline__ float bits_to_u(uint32_t v) {
+    return __uint2float_rn(((v >> 9) << 1) | 1u) * 5.9604644775390625e-8f;  // 2^-24
+}
+
+__device__ __forceinline__ float U(Lane& L, const KCtx& K) {
+    return bits_to_u(next_bits(L, K.A->key0, K.A->key1));
+}
+
+// nextcoll() = -log(rand()) (util.jl:17)
+__device__ __forceinline__ float nextcoll(Lane& L, const KCtx& K) { return -logf(U(L, K)); }
+
+__device__ __forceinline__ void err(const KCtx& K, int e) { atomicAdd(&K.tal[T_ERR + e], 1u); }
+
+// ------------------------------------------------------------ kinematics --
+// kinenergy (electron.jl:53, positron.jl:40, photon.jl:50) with the
+// cancellation-free form p^2 / (gamma + 1) for leptons (device units).
+__device__ __forceinline__ float kin_energy(int species, float px, float py, float pz) {
+    float p2 = px * px + py * py + pz * pz;
+    if (species == PCL_PHOTON) return sqrtf(p2);
+    return p2 / (sqrtf(1.0f + p2) + 1.0f);
+}
+
+// precheb (cheby.jl:127-143).  Energies beyond the table (x >= xmax, where the
+// reference indexes past its array) extrapolate the last interval.
+__device__ __forceinline__ int precheb(float x, int k, float xscale, float t[4], bool& oor) {
+    float x1 = x * xscale;
+    uint32_t bits = __float_as_uint(x1);
+    int e = int((bits >> 23) & 0xffu);
+    int i;
+    float xi;
+    float two_k1 = __uint_as_float(uint32_t(127 + k + 1) << 23);
+    if (!(x1 > 0.0f) || e == 0) {
+        i = 0;
+        xi = two_k1 * x1 - 1.0f;
+    } else {
+        i = (e - 126) + k;
+        if (i > 0) {
+            float s = __uint_as_float((bits & 0x807fffffu) | 0x3f000000u);
+            xi = 4.0f * s - 3.0f;
+            if (i > k) {
+                oor = true;
+                i = k;
+                xi = 4.0f * x1 - 3.0f;
+            }
+        } else {
+            i = 0;
+            xi = two_k1 * x1 - 1.0f;
+        }
+    }
+    t[0] = 1.0f;
+    t[1] = xi;
+    t[2] = 2.0f * xi * t[1] - t[0];
+    t[3] = 2.0f * xi * t[2] - t[1];
+    return i;
+}
+
+__device__ __forceinline__ float cheb_dot(const float* a, const float t[4], int order) {
+    float s = a[0] * t[0];
+    if (order > 1) s += a[1] * t[1];
+    if (order > 2) s += a[2] * t[2];
+    if (order > 3) s += a[3] * t[3];
+    return s;
+}
+
+// setr! (collisions.jl:63-74): r = ratebound(E) above the cut, else 0.
+__device__ __forceinline__ float setr(const SpeciesHdr& S, const KCtx& K, float E) {
+    if (E < S.cut) return 0.0f;
+    float t[4];
+    bool oor = false;
+    int i = precheb(E, S.k, S.xscale, t, oor);
+    if (oor) err(K, PCL_E_TABLE_RANGE);
+    float rb = cheb_dot(K.blob + S.rb_off + i * S.order, t, S.order);
+    if (!(rb > 0.0f)) {
+        if (S.nproc > 0) err(K, PCL_E_NEG_RATE);
+        return 0.0f;
+    }
+    return rb;
+}
+
+// ChebContinuumLoss.force magnitude (continuum.jl:45-57), device force units.
+__device__ __forceinline__ float cl_mag(const SpeciesHdr& S, const KCtx& K, float E) {
+    if (S.cl_off < 0) return 0.0f;
+    float t[4];
+    bool oor = false;
+    int i = precheb(E, S.cl_k, S.cl_xscale, t, oor);
+    if (oor) err(K, PCL_E_TABLE_RANGE);
+    return cheb_dot(K.blob + S.cl_off + i * S.cl_order, t, S.cl_order);
+}
+
+// force(CombinedForcing(ElectromagneticField, ChebContinuumLoss), lepton)
+// (pusher.jl:14-23, field.jl:54-70, continuum.jl:45-57).  Returns beta too.
+__device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K, float px, float py,
+                                             float pz, float& bx, float& by, float& bz, float& fx,
+                                             float& fy, float& fz) {
+    float p2 = px * px + py * py + pz * pz;
+    float g = sqrtf(1.0f + p2);
+    float ig = 1.0f / g;
+    bx = px * ig; by = py * ig; bz = pz * ig;
+    const float q = S.charge;
+    const float* E = K.H->E;
+    const float* B = K.H->B;
+    fx = q * (E[0] + (by * B[2] - bz * B[1]));
+    fy = q * (E[1] + (bz * B[0] - bx * B[2]));
+    fz = q * (E[2] + (bx * B[1] - by * B[0]));
+    float f = cl_mag(S, K, p2 / (g + 1.0f));
+    if (f != 0.0f) {
+        float pn = sqrtf(p2);
+        if (pn > 0.0f) {
+            float c = f / pn;
+            fx -= c * px; fy -= c * py; fz -= c * pz;
+        }
+    }
+}
+
+// advance_particle(RK2Pusher, y, dt) (pusher.jl:41-63); photons move in a
+// straight line (photon.jl:46-52; both forcings vanish on photons).
+__device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K, float h) {
+    if (L.species == PCL_PHOTON) {
+        float pn = sqrtf(L.px * L.px + L.py * L.py + L.pz * L.pz);
+        float v = h * kCns / pn;
+        L.x += v * L.px; L.y += v * L.py; L.z += v * L.pz;
+        return;
+    }
+    float b1x, b1y, b1z, f1x, f1y, f1z;
+    lepton_force(S, K, L.px, L.py, L.pz, b1x, b1y, b1z, f1x, f1y, f1z);
+    const float h23 = h * (2.0f / 3.0f);
+    float qx = L.px + h23 * f1x, qy = L.py + h23 * f1y, qz = L.pz + h23 * f1z;
+    float b2x, b2y, b2z, f2x, f2y, f2z;
+    lepton_force(S, K, qx, qy, qz, b2x, b2y, b2z, f2x, f2y, f2z);
+    const float hc = h * kCns;
+    L.x += hc * (0.25f * b1x + 0.75f * b2x);
+    L.y += hc * (0.25f * b1y + 0.75f * b2y);
+    L.z += hc * (0.25f * b1z + 0.75f * b2z);
+    L.px += h * (0.25f * f1x + 0.75f * f2x);
+    L.py += h * (0.25f * f1y + 0.75f * f2y);
+    L.pz += h * (0.25f * f1z + 0.75f * f2z);
+}
+
+// turn(u, cos theta, phi, n) (util.jl:40-57).  s = hypot(mu_x, mu_y) replaces
+// sqrt(1 - mu_z^2) (identical for a unit vector, but free of the singularity
+// at mu_z = +-1); at s = 0 the azimuth reference is the x axis.  sin theta is
+// passed in, computed by each sampler without cancellation.
+__device__ __forceinline__ void turn(float ux, float uy, float uz, float cth, float sth, float cph,
+                                     float sph, float n, float& ox, float& oy, float& oz) {
+    float un = sqrtf(ux * ux + uy * uy + uz * uz);
+    float iu = 1.0f / un;
+    float mx = ux * iu, my = uy * iu, mz = uz * iu;
+    float s = sqrtf(mx * mx + my * my);
+    float ca = 1.0f, sa = 0.0f;
+    if (s > 0.0f) { float is = 1.0f / s; ca = mx * is; sa = my * is; }
+    float ax = sth * (ca * mz * cph - sa * sph) + mx * cth;
+    float ay = sth * (sa * mz * cph + ca * sph) + my * cth;
+    float az = -s * sth * cph + mz * cth;
+    ox = n * ax; oy = n * ay; oz = n * az;
+}
+
+// sample_modified_tsai_cos_theta(T) (util.jl:143-159); returns x = u^2/umax^2,
+// cos theta = 1 - 2x.
+__device__ __forceinline__ float tsai_x(Lane& L, const KCtx& K, float T) {
+    const float umax = 2.0f * (1.0f + T);
+    float u = 0.0f;
+    int it = 0;
+    for (;;) {
+        float r1 = U(L, K);
+        float r2 = U(L, K);
+        float uu = -logf(r1 * r2);
+        float r3 = U(L, K);
+        u = (0.25f > r3) ? uu * 1.6f : uu * (1.6f / 3.0f);
+        if (u <= umax) break;
+        if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); u = umax; break; }
+    }
+    float q = u / umax;
+    return q * q;
+}
+
+__device__ __forceinline__ void sincos_2pi(float u, float& s, float& c) { sincospif(2.0f * u, &s, &c); }
+
+// Lehtinen angles for a binary collision (moller.jl:26-28): energies E0
+// (primary before), Ei (outgoing), d = E0 - Ei.  sin^2 = 2 d / (E0 (Ei + 2)).
+__device__ __forceinline__ void lehtinen(float E0, float Ei, float d, float& c, float& s) {
+    float den = E0 * (Ei + 2.0f);
+    c = sqrtf(Ei * (E0 + 2.0f) / den);
+    s = sqrtf(2.0f * d / den);
+}
+
+// add_particle! (population.jl:103-113) of a secondary born in a collision.
+// The secondary's stream id comes from the parent's stream in domain 1 at the
+// parent's counter at the start of the collision; child index 0 / 1 takes
+// words (0,1) / (2,3).
+__device__ void emit(Lane& L, const KCtx& K, int sp, float cpx, float cpy, float cpz, float cs,
+                     int cidx, uint32_t ctr0) {
+    const SpeciesHdr& S = K.H->sp[sp];
+    float E = kin_energy(sp, cpx, cpy, cpz);
+    if (K.cap) {  // test hook: record every outcome, cut applied by the caller
+        int n = *K.ncap;
+        float* o = K.cap + 4 * n;
+        o[0] = cpx; o[1] = cpy; o[2] = cpz; o[3] = cs;
+        *K.ncap = n + 1;
+        return;
+    }
+    if (!(E > S.cut)) return;
+    if (S.tally_only) {
+        atomicAdd(&K.A->ctl->tally_count[sp], 1ull);
+        atomicAdd(&K.A->ctl->tally_w[sp], double(L.w));
+        atomicAdd(&K.A->ctl->tally_wE[sp], double(L.w) * double(E));
+        if (S.hist_bins > 0 && K.A->hist_n[sp]) {
+            int b = int(floorf((logf(E) - S.hist_lmin) * S.hist_linv));
+            if (b >= 0 && b < S.hist_bins) {
+                atomicAdd(&K.A->hist_n[sp][b], 1ull);
+                atomicAdd(&K.A->hist_w[sp][b], double(L.w));
+            }
+        }
+        return;
+    }
+    uint32_t a = ctr0, b = L.sid_lo, c = L.sid_hi, d = 1u;
+    philox4x32_10(a, b, c, d, K.A->key0, K.A->key1);
+    uint32_t slo = cidx ? c : a, shi = cidx ? d : b;
+    atomicAdd(&K.tal[T_SPAWN + sp], 1u);
+    float4 e0 = make_float4(L.x, L.y, L.z, L.w);
+    float4 e1 = make_float4(cpx, cpy, cpz, cs);
+    uint4 e2 = make_uint4(slo, shi, uint32_t(sp) | (uint32_t(L.k) << 2), __float_as_uint(L.tl));
+    int pos = atomicAdd(K.top, 1);
+    if (pos < kWarpStack) {
+        K.stk[3 * pos + 0] = e0;
+        K.stk[3 * pos + 1] = e1;
+        K.stk[3 * pos + 2] = make_float4(__uint_as_float(e2.x), __uint_as_float(e2.y),
+                                         __uint_as_float(e2.z), __uint_as_float(e2.w));
+    } else {
+        err(K, PCL_E_SPILL);
+        unsigned long long q = atomicAdd(K.A->sp_out_n, 1ull);
+        if ((long long)q < K.A->sp_cap) {
+            K.A->sp_out_xw[q] = e0;
+            K.A->sp_out_ps[q] = e1;
+            K.A->sp_out_meta[q] = e2;
+        } else {
+            err(K, PCL_E_CAPACITY);
+        }
+    }
+}
+
+// ----------------------------------------------------------- samplers ----
+// relativistic_coulomb.jl:10-51
+__device__ void s_coulomb(Lane& L, const KCtx& K, const DevProc& P) {
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float p2 = L.px * L.px + L.py * L.py + L.pz * L.pz;
+    float pn = sqrtf(p2);
+    float b2 = p2 / (1.0f + p2);
+    float al = P.p[0] / p2;
+    float x = 0.0f;
+    int it = 0;
+    for (;;) {
+        float u = U(L, K);
+        x = al * u / (al + (1.0f - u));
+        float z = U(L, K);
+        if (z < 1.0f - b2 * x) break;
+        if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
+    }
+    float cth = 1.0f - 2.0f * x, sth = 2.0f * sqrtf(x * (1.0f - x));
+    turn(L.px, L.py, L.pz, cth, sth, cph, sph, pn, L.px, L.py, L.pz);
+    L.s = nextcoll(L, K);
+}
+
+// moller.jl:13-37, 64-87
+__device__ void s_moller(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+    const float e0 = P.p[0] / E;
+    const float g = 1.0f + E;
+    const float nrm = 4.0f / (9.0f * g * g - 10.0f * g + 5.0f);
+    const float c2 = 2.0f * g * g + 2.0f * g - 1.0f;
+    const float g2 = g * g, em2 = E * E;
+    float eps = 0.5f;
+    int it = 0;
+    for (;;) {
+        float r = U(L, K);
+        eps = e0 / (1.0f - r + 2.0f * e0 * r);
+        float om = 1.0f - eps;
+        float gg = nrm * (em2 * eps * eps - c2 * (eps / om) + g2 / (om * om));
+        if (U(L, K) < gg) break;
+        if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
+    }
+    float E2 = eps * E, E1 = E - E2;
+    float p1 = sqrtf(E1 * (E1 + 2.0f)), p2 = sqrtf(E2 * (E2 + 2.0f));
+    float c1, s1, cc2, s2;
+    lehtinen(E, E1, E2, c1, s1);
+    lehtinen(E, E2, E1, cc2, s2);
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float ax, ay, az, bx, by, bz;
+    turn(L.px, L.py, L.pz, c1, s1, cph, sph, p1, ax, ay, az);
+    turn(L.px, L.py, L.pz, cc2, s2, cph, -sph, p2, bx, by, bz);
+    L.px = ax; L.py = ay; L.pz = az;
+    L.s = nextcoll(L, K);
+    float cs = nextcoll(L, K);
+    emit(L, K, PCL_ELECTRON, bx, by, bz, cs, 0, ctr0);
+}
+
+// rbeb.jl:54-80, 156-196
+__device__ void s_rbeb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+    const float B = P.p[0];
+    if (!(E > B)) {  // below threshold: the reference asserts; count it and treat as null
+        err(K, PCL_E_KINEMATICS);
+        L.s = nextcoll(L, K);
+        return;
+    }
+    const float t1 = E, b1 = B;
+    const float op = 1.0f + t1;
+    const float bt2 = t1 * (t1 + 2.0f) / (op * op);
+    const float t = E / B;
+    const float A = -(1.0f + 2.0f * t1) / (t + 1.0f) / (op * op);
+    const float C = logf(t1 * (t1 + 2.0f)) - bt2 - logf(2.0f * b1);
+    const float M = b1 * b1 / (op * op);
+    const float ratio = (t + 1.0f) / (t - 1.0f);
+    const float pbn = 2.0f + 2.0f * C + (t + 1.0f) * (t + 1.0f) * M / 4.0f;
+    float w = 0.0f;
+    int it = 0;
+    for (;;) {
+        float u = U(L, K);
+        w = u / (ratio - u);
+        float a1 = 1.0f / (w + 1.0f), a2 = 1.0f / (t - w);
+        float pb = pbn * a1 * a1;
+        float p0 = A * (a1 + a2) + ((a1 * a1 + a2 * a2) + M) + C * (a1 * a1 * a1 + a2 * a2 * a2);
+        if (U(L, K) * pb < p0) break;
+        if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
+    }
+    float E2 = B * w, E1 = E - E2 - B;
+    if (!(E2 < E1)) err(K, PCL_E_KINEMATICS);
+    float p1 = sqrtf(E1 * (E1 + 2.0f)), p2 = sqrtf(E2 * (E2 + 2.0f));
+    float c1, s1, cc2, s2;
+    lehtinen(E, E1, E2 + B, c1, s1);
+    lehtinen(E, E2, E1 + B, cc2, s2);
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float ax, ay, az, bx, by, bz;
+    turn(L.px, L.py, L.pz, c1, s1, cph, sph, p1, ax, ay, az);
+    turn(L.px, L.py, L.pz, cc2, s2, cph, -sph, p2, bx, by, bz);
+    L.px = ax; L.py = ay; L.pz = az;
+    L.s = nextcoll(L, K);
+    float cs = nextcoll(L, K);
+    emit(L, K, PCL_ELECTRON, bx, by, bz, cs, 0, ctr0);
+}
+
+// seltzer.jl:67-122 with the photon angle of util.jl:143-159.  The inverse-CDF
+// lookup reproduces the reference's interpolation weights as written
+// (seltzer.jl:278-284, off-diagonal corners included).
+__device__ void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+    const SBHdr& T = K.H->sb[P.sb];
+    const float* data = K.A->sb_data[P.sb];
+    uint32_t bits = next_bits(L, K.A->key0, K.A->key1);
+    float x = bits_to_u(bits);
+    // i1 = searchsortedfirst(pcum, x) - 1 = floor(x (ncum - 1)), exact in integers
+    unsigned long long prod = (((unsigned long long)(bits >> 9) << 1) | 1ull) * (unsigned long long)(T.ncum - 1);
+    int i1 = int(prod >> 24);
+    if (i1 > T.ncum - 2) i1 = T.ncum - 2;
+    int i2 = i1 + 1;
+    float xa = float(i1) / T.inv_dp, xb = float(i2) / T.inv_dp;
+    float y = logf(E);
+    const float* le = K.blob + T.le_off;
+    // j2 = searchsortedfirst(log_energy, y)
+    int lo = 0, hi = T.ne;
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (le[mid] < y) lo = mid + 1; else hi = mid; }
+    int j1 = lo - 1;
+    if (j1 < 0) { j1 = 0; err(K, PCL_E_TABLE_RANGE); }
+    if (j1 > T.ne - 2) { j1 = T.ne - 2; err(K, PCL_E_TABLE_RANGE); }
+    int j2 = j1 + 1;
+    float y1 = le[j1], y2 = le[j2];
+    const float* d1 = data + (size_t)j1 * T.ncum;
+    const float* d2 = data + (size_t)j2 * T.ncum;
+    float u11 = __ldg(d1 + i1), u21 = __ldg(d1 + i2), u12 = __ldg(d2 + i1), u22 = __ldg(d2 + i2);
+    float A = (xb - xa) * (y2 - y1);
+    float S = u11 * (xb - x) * (y2 - y) + u12 * (x - xa) * (y2 - y) + u21 * (xb - x) * (y - y1) +
+              u22 * (x - xa) * (y - y1);
+    float k = E * expf(S / A);
+    if (!(k < E)) err(K, PCL_E_KINEMATICS);
+    float xt = tsai_x(L, K, E);
+    float cth = 1.0f - 2.0f * xt, sth = 2.0f * sqrtf(xt * (1.0f - xt));
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float gx, gy, gz;
+    turn(L.px, L.py, L.pz, cth, sth, cph, sph, k, gx, gy, gz);
+    L.px -= gx; L.py -= gy; L.pz -= gz;
+    L.s = nextcoll(L, K);
+    float cs = nextcoll(L, K);
+    emit(L, K, PCL_PHOTON, gx, gy, gz, cs, 0, ctr0);
+}
+
+// compton.jl:9-28, 119-144 (Compton and KleinNishinaCompton share the sampler)
+__device__ void s_compton(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
+    const float e0 = 1.0f / (1.0f + 2.0f * E);
+    const float a1 = log1pf(2.0f * E);
+    const float a2 = (1.0f - e0 * e0) * 0.5f;
+    const float pa = a1 / (a1 + a2);
+    float eps = 1.0f, t = 0.0f;
+    int it = 0;
+    for (;;) {
+        if (U(L, K) < pa) eps = expf(-U(L, K) * a1);
+        else eps = sqrtf(e0 * e0 + (1.0f - e0 * e0) * U(L, K));
+        t = (1.0f - eps) / (eps * E);
+        float g = 1.0f - eps / (1.0f + eps * eps) * t * (2.0f - t);
+        if (U(L, K) < g) break;
+        if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
+    }
+    float cth = 1.0f - t, sth = sqrtf(fmaxf(0.0f, t * (2.0f - t)));
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float gx, gy, gz;
+    turn(L.px, L.py, L.pz, cth, sth, cph, sph, eps * E, gx, gy, gz);
+    float ex = L.px - gx, ey = L.py - gy, ez = L.pz - gz;
+    L.px = gx; L.py = gy; L.pz = gz;
+    L.s = nextcoll(L, K);
+    float cs = nextcoll(L, K);
+    emit(L, K, PCL_ELECTRON, ex, ey, ez, cs, 0, ctr0);
+}
+
+// photo_electric.jl:38-52, 60-99
+__device__ void s_photoelectric(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+    float b = P.p[0];
+    for (int m = 0; m < P.nbind; ++m) { b = P.p[m]; if (E > b) break; }
+    if (!(E > b)) err(K, PCL_E_KINEMATICS);
+    float Ee = E - b;
+    float g = 1.0f + Ee;
+    float beta = sqrtf(Ee * (Ee + 2.0f)) / g;
+    float A = 1.0f / beta - 1.0f;
+    float k2 = beta * g * Ee * (Ee - 1.0f) * 0.5f;   // beta gamma (gamma-1)(gamma-2) / 2
+    float g0 = 2.0f * (1.0f / A + k2);
+    float nu = 0.0f;
+    int it = 0;
+    for (;;) {
+        float xi = U(L, K);
+        nu = 2.0f * A / ((A + 2.0f) * (A + 2.0f) - 4.0f * xi) * (2.0f * xi + (A + 2.0f) * sqrtf(xi));
+        float xi1 = U(L, K);
+        float gn = (2.0f - nu) * (1.0f / (A + nu) + k2);
+        if (xi1 * g0 < gn) break;
+        if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
+    }
+    float cth = 1.0f - nu, sth = sqrtf(fmaxf(0.0f, nu * (2.0f - nu)));
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float ex, ey, ez;
+    turn(L.px, L.py, L.pz, cth, sth, cph, sph, sqrtf(Ee * (Ee + 2.0f)), ex, ey, ez);
+    float cs = nextcoll(L, K);
+    L.alive = false;
+    emit(L, K, PCL_ELECTRON, ex, ey, ez, cs, 0, ctr0);
+}
+
+// _screen_function1/2 (bethe_heitler.jl:163-193)
+__device__ __forceinline__ float screen1(float d) {
+    return d > 1.4f ? 42.038f - 8.29f * logf(d + 0.958f) : 42.184f - d * (7.444f - 1.623f * d);
+}
+__device__ __forceinline__ float screen2(float d) {
+    return d > 1.4f ? 42.038f - 8.29f * logf(d + 0.958f) : 41.326f - d * (5.848f - 0.902f * d);
+}
+
+// bethe_heitler.jl:5-25, 85-146
+__device__ void s_bethe_heitler(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+    const float e0 = 1.0f / E;
+    if (!(e0 < 0.5f)) err(K, PCL_E_KINEMATICS);
+    float eps;
+    if (E < P.p[4]) {  // 2 MeV
+        eps = e0 + (0.5f - e0) * U(L, K);
+    } else {
+        const float d0 = 136.0f * e0 / P.p[1];
+        const float FZ = (E > P.p[5]) ? P.p[3] : P.p[2];  // 50 MeV
+        const float dmin = 4.0f * d0;
+        const float dmax = expf((42.24f - FZ) / 8.368f) - 0.952f;
+        const float ep = (1.0f - sqrtf(1.0f - dmin / dmax)) * 0.5f;
+        const float emin = fmaxf(e0, ep);
+        const float er = 0.5f - emin;
+        const float F10 = screen1(dmin) - FZ, F20 = screen2(dmin) - FZ;
+        const float NF1 = fmaxf(F10 * er * er, 0.0f), NF2 = fmaxf(1.5f * F20, 0.0f);
+        const float NC = NF1 / (NF1 + NF2);
+        int it = 0;
+        for (;;) {
+            bool acc;
+            if (NC > U(L, K)) {
+                eps = 0.5f - er * cbrtf(U(L, K));
+                float d = d0 / (eps * (1.0f - eps));
+                acc = U(L, K) < (screen1(d) - FZ) / F10;
+            } else {
+                eps = emin + er * U(L, K);
+                float d = d0 / (eps * (1.0f - eps));
+                acc = U(L, K) < (screen2(d) - FZ) / F20;
+            }
+            if (acc) break;
+            if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
+        }
+    }
+    float etot, ptot;
+    if (U(L, K) < 0.5f) { etot = (1.0f - eps) * E; ptot = eps * E; }   // rand(Bool)
+    else { ptot = (1.0f - eps) * E; etot = eps * E; }
+    // the sampler returns (ekin, pkin); collide binds them as (pkin, ekin)
+    const float first = fmaxf(0.0f, etot - 1.0f), second = fmaxf(0.0f, ptot - 1.0f);
+    const float ekin_c = second, pkin_c = first;
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float xe = tsai_x(L, K, ekin_c);
+    float ex, ey, ez;
+    turn(L.px, L.py, L.pz, 1.0f - 2.0f * xe, 2.0f * sqrtf(xe * (1.0f - xe)), cph, sph,
+         sqrtf(ekin_c * (ekin_c + 2.0f)), ex, ey, ez);
+    float xp = tsai_x(L, K, pkin_c);
+    float qx, qy, qz;
+    turn(L.px, L.py, L.pz, 1.0f - 2.0f * xp, 2.0f * sqrtf(xp * (1.0f - xp)), cph, sph,
+         sqrtf(pkin_c * (pkin_c + 2.0f)), qx, qy, qz);
+    float se = nextcoll(L, K);
+    float sp = nextcoll(L, K);
+    L.alive = false;
+    emit(L, K, PCL_ELECTRON, ex, ey, ez, se, 0, ctr0);
+    emit(L, K, PCL_POSITRON, qx, qy, qz, sp, 1, ctr0);
+}
+
+// bhaba.jl:9-33, 55-91
+__device__ void s_bhabha(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+    const float e0 = P.p[0] / E;
+    const float g = 1.0f + E;
+    const float y = 1.0f / (g + 1.0f);
+    const float B0 = g * g / (E * (E + 2.0f));
+    const float uu = 1.0f - 2.0f * y;
+    const float B1 = 2.0f - y * y, B2 = uu * (3.0f + y * y), B3 = uu * uu + uu * uu * uu,
+                B4 = uu * uu * uu;
+    const float g2 = B0 + B1 * e0 + B2 * e0 * e0 + B3 * e0 * e0 * e0 + B4 * e0 * e0 * e0 * e0;
+    float eps = e0;
+    int it = 0;
+    for (;;) {
+        float r = U(L, K);
+        eps = e0 / (1.0f - r + e0 * r);
+        float g1 = B0 + B1 * eps + B2 * eps * eps + B3 * eps * eps * eps + B4 * eps * eps * eps * eps;
+        if (U(L, K) < g1 / g2) break;
+        if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
+    }
+    float E2 = eps * E, E1 = E - E2;
+    float p1 = sqrtf(E1 * (E1 + 2.0f)), p2 = sqrtf(E2 * (E2 + 2.0f));
+    float c1, s1, cc2, s2;
+    lehtinen(E, E1, E2, c1, s1);
+    lehtinen(E, E2, E1, cc2, s2);
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float ax, ay, az, bx, by, bz;
+    turn(L.px, L.py, L.pz, c1, s1, cph, sph, p1, ax, ay, az);
+    turn(L.px, L.py, L.pz, cc2, s2, cph, -sph, p2, bx, by, bz);
+    L.px = ax; L.py = ay; L.pz = az;
+    L.s = nextcoll(L, K);
+    float cs = nextcoll(L, K);
+    emit(L, K, PCL_ELECTRON, bx, by, bz, cs, 0, ctr0);
+}
+
+// anihilation.jl:6-23, 39-67
+__device__ void s_annihilation(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
+    const float g = 1.0f + E;
+    const float q = sqrtf(E / (E + 2.0f));
+    const float emax = 0.5f * (1.0f + q), emin = 0.5f * (1.0f - q);
+    const float ratio = emax / emin;
+    float eps = 0.5f;
+    int it = 0;
+    for (;;) {
+        eps = emin * powf(ratio, U(L, K));
+        float gg = 1.0f - eps + (2.0f * g * eps - 1.0f) / (eps * (g + 1.0f) * (g + 1.0f));
+        if (U(L, K) < gg) break;
+        if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
+    }
+    float cth = (eps * (g + 1.0f) - 1.0f) / (eps * sqrtf(E * (E + 2.0f)));
+    float sth = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float ax, ay, az;
+    turn(L.px, L.py, L.pz, cth, sth, cph, sph, eps * (E + 2.0f), ax, ay, az);
+    float bx = L.px - ax, by = L.py - ay, bz = L.pz - az;
+    float sa = nextcoll(L, K);
+    float sb = nextcoll(L, K);
+    L.alive = false;
+    emit(L, K, PCL_PHOTON, ax, ay, az, sa, 0, ctr0);
+    emit(L, K, PCL_PHOTON, bx, by, bz, sb, 1, ctr0);
+}
+
+// Dispatch one real collision with table position j; updates the primary
+// (state change + setr!) or removes it, and emits secondaries (apply!,
+// collisions.jl:83-133).
+__device__ void sample_process(Lane& L, const KCtx& K, const SpeciesHdr& S, const DevProc& P, float E,
+                               uint32_t ctr0) {
+    switch (P.kind) {
+        case PCL_PROC_REL_COULOMB: s_coulomb(L, K, P); break;
+        case PCL_PROC_MOLLER: s_moller(L, K, P, E, ctr0); break;
+        case PCL_PROC_RBEB: s_rbeb(L, K, P, E, ctr0); break;
+        case PCL_PROC_SELTZER_BERGER: s_sb(L, K, P, E, ctr0); break;
+        case PCL_PROC_COMPTON:
+        case PCL_PROC_KN_COMPTON: s_compton(L, K, E, ctr0); break;
+        case PCL_PROC_PHOTOELECTRIC: s_photoelectric(L, K, P, E, ctr0); break;
+        case PCL_PROC_BETHE_HEITLER: s_bethe_heitler(L, K, P, E, ctr0); break;
+        case PCL_PROC_BHABHA: s_bhabha(L, K, P, E, ctr0); break;
+        case PCL_PROC_ANNIHILATION: s_annihilation(L, K, E, ctr0); break;
+        default: err(K, PCL_E_KINEMATICS); break;
+    }
+    if (L.alive) L.r = setr(S, K, kin_energy(L.species, L.px, L.py, L.pz));
+}
+
+// do_one_collision! (collisions.jl:142-199)
+__device__ void collide(Lane& L, const KCtx& K, const SpeciesHdr& S) {
+    if (L.r == 0.0f) return;
+    float E = kin_energy(L.species, L.px, L.py, L.pz);
+    if (!(E >= S.cut)) return;
+    float t[4];
+    bool oor = false;
+    int i = precheb(E, S.k, S.xscale, t, oor);
+    if (oor) err(K, PCL_E_TABLE_RANGE);
+    const uint32_t ctr0 = L.ctr;
+    float xi = U(L, K) * L.r;
+    const float* a = K.blob + S.rate_off + i * S.nproc * S.order;
+    int j = 0;
+    for (; j < S.nproc; ++j) {
+        float nu = cheb_dot(a + j * S.order, t, S.order);
+        if (nu > xi) break;
+        xi -= nu;
+    }
+    if (j == S.nproc) {  // NullOutcome (collisions.jl:83-88)
+        atomicAdd(&K.tal[T_NULL + L.species], 1u);
+        L.r = setr(S, K, E);
+        L.s = nextcoll(L, K);
+        return;
+    }
+    atomicAdd(&K.tal[T_COLL + 16 * L.species + j], 1u);
+    sample_process(L, K, S, S.proc[j], E, ctr0);
+}
+
+// ---------------------------------------------------------- TMA staging --
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Copy the table blob into shared memory with one bulk asynchronous copy
+// (cp.async.bulk, completion on an mbarrier).  Bounded wait; false on timeout.
+__device__ bool stage_blob(void* dst, const void* src, int bytes, unsigned long long* mbar) {
+    uint32_t bar = smem_u32(mbar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_u32(dst)),
+            "l"(src), "r"(bytes), "r"(bar)
+            : "memory");
+    }
+    uint32_t done = 0;
+    for (int it = 0; it < (1 << 22) && !done; ++it) {
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar), "r"(0u)
+            : "memory");
+        if (!done) __nanosleep(64);
+    }
+    return done != 0;
+}
+
+// Load particle data of an input slot.
+__device__ __forceinline__ void load_slot(Lane& L, const float4* xw, const float4* ps, const uint4* meta,
+                                          long long slot) {
+    float4 a = xw[slot];
+    float4 b = ps[slot];
+    uint4 m = meta[slot];
+    L.x = a.x; L.y = a.y; L.z = a.z; L.w = a.w;
+    L.px = b.x; L.py = b.y; L.pz = b.z; L.s = b.w;
+    L.sid_lo = m.x; L.sid_hi = m.y; L.ctr = m.z; L.tl = __uint_as_float(m.w);
+}
+
+// ------------------------------------------------------------ the step ---
+__global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int nwarps = blockDim.x >> 5;
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const unsigned FULL = 0xffffffffu;
+    const unsigned lt = (1u << lane) - 1u;
+
+    const BlobHdr* H = reinterpret_cast<const BlobHdr*>(smem);
+    float4* stk_all = reinterpret_cast<float4*>(smem + A.blob_bytes);
+    int* tops = reinterpret_cast<int*>(stk_all + size_t(nwarps) * kWarpStack * 3);
+    uint32_t* tal = reinterpret_cast<uint32_t*>(tops + nwarps);
+    unsigned long long* mbar =
+        reinterpret_cast<unsigned long long*>(reinterpret_cast<uintptr_t>(tal + T_WORDS + 8) & ~uintptr_t(7));
+
+    for (int i = threadIdx.x; i < T_WORDS; i += blockDim.x) tal[i] = 0u;
+    if (lane == 0) tops[warp] = 0;
+    bool ok = stage_blob(smem, A.blob, A.blob_bytes, mbar);
+    if (__syncthreads_or(!ok)) {
+        if (threadIdx.x == 0) atomicExch(&A.ctl->timeout, 1);
+        return;
+    }
+
+    KCtx K;
+    K.H = H;
+    K.blob = reinterpret_cast<const float*>(smem);
+    K.stk = stk_all + size_t(warp) * kWarpStack * 3;
+    K.top = tops + warp;
+    K.tal = tal;
+    K.A = &A;
+    K.cap = nullptr;
+    K.ncap = nullptr;
+
+    Control* ctl = A.ctl;
+    const float dt = A.dt;
+    const int nsteps = A.nsteps;
+
+    // work space: concatenated species ranges, or the spill queue
+    long long nsp0, nsp1, total;
+    if (A.spill_mode) {
+        nsp0 = 0; nsp1 = 0;
+        total = (long long)(*A.sp_in_n);
+    } else {
+        nsp0 = (long long)ctl->n_start[0];
+        nsp1 = (long long)ctl->n_start[1];
+        total = nsp0 + nsp1 + (long long)ctl->n_start[2];
+    }
+    const long long nwarps_grid = (long long)gridDim.x * nwarps;
+
+    long long cur = 0, end = 0;  // warp-private chunk (uniform)
+    bool input_done = false;
+    Lane L;
+    L.slot = -1; L.alive = false; L.rvalid = false;
+    bool has = false;
+
+    for (;;) {
+        // ---------------- refill idle lanes: children first, then input
+        unsigned need = __ballot_sync(FULL, !has);
+        if (need) {
+            __syncwarp();
+            int top = *K.top;
+            if (top > kWarpStack) top = kWarpStack;
+            int take = min(__popc(need), top);
+            int rank = __popc(need & lt);
+            if (!has && rank < take) {
+                int e = top - 1 - rank;
+                float4 a = K.stk[3 * e + 0], b = K.stk[3 * e + 1], c = K.stk[3 * e + 2];
+                L.x = a.x; L.y = a.y; L.z = a.z; L.w = a.w;
+                L.px = b.x; L.py = b.y; L.pz = b.z; L.s = b.w;
+                L.sid_lo = __float_as_uint(c.x); L.sid_hi = __float_as_uint(c.y);
+                uint32_t sk = __float_as_uint(c.z);
+                L.species = int(sk & 3u); L.k = int(sk >> 2);
+                L.tl = c.w;
+                L.ctr = 0u; L.rvalid = false; L.slot = -1; L.alive = true; L.nsub = 0;
+                L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz));
+                has = true;
+            }
+            __syncwarp();
+            if (lane == 0) *K.top = top - take;
+            __syncwarp();
+            need = __ballot_sync(FULL, !has);
+            while (need && !input_done) {
+                if (cur >= end) {
+                    long long base = 0, len = 0;
+                    if (lane == 0) {
+                        long long done_est = (long long)(*(volatile unsigned long long*)&ctl->head);
+                        long long rem = total - done_est;
+                        long long chunk = rem / (4 * nwarps_grid);
+                        chunk = chunk < 32 ? 32 : (chunk > 1024 ? 1024 : chunk);
+                        base = (long long)atomicAdd(&ctl->head, (unsigned long long)chunk);
+                        len = (base < total) ? min(chunk, total - base) : 0;
+                    }
+                    base = __shfl_sync(FULL, base, 0);
+                    len = __shfl_sync(FULL, len, 0);
+                    if (len <= 0) { input_done = true; break; }
+                    cur = base; end = base + len;
+                }
+                int avail = int(min(end - cur, 32ll));
+                int nn = __popc(need);
+                int tk = min(avail, nn);
+                int rk = __popc(need & lt);
+                if (!has && rk < tk) {
+                    long long v = cur + rk;
+                    if (A.spill_mode) {
+                        float4 a = A.sp_in_xw[v], b = A.sp_in_ps[v];
+                        uint4 m = A.sp_in_meta[v];
+                        L.x = a.x; L.y = a.y; L.z = a.z; L.w = a.w;
+                        L.px = b.x; L.py = b.y; L.pz = b.z; L.s = b.w;
+                        L.sid_lo = m.x; L.sid_hi = m.y;
+                        L.species = int(m.z & 3u); L.k = int(m.z >> 2);
+                        L.tl = __uint_as_float(m.w);
+                        L.ctr = 0u; L.slot = -1;
+                        has = true;
+                    } else {
+                        int sp; long long sl;
+                        if (v < nsp0) { sp = 0; sl = v; }
+                        else if (v < nsp0 + nsp1) { sp = 1; sl = v - nsp0; }
+                        else { sp = 2; sl = v - nsp0 - nsp1; }
+                        L.species = sp;
+                        load_slot(L, A.xw[sp], A.ps[sp], A.meta[sp], sl);
+                        L.slot = int(sl);
+                        L.k = 0;
+                        has = (L.ctr != PCL_DEAD_CTR);
+                        if (has) atomicAdd(&tal[T_LSTART + 0], 1u);
+                    }
+                    if (has) {
+                        L.rvalid = false; L.alive = true; L.nsub = 0;
+                        L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz));
+                    }
+                }
+                cur += tk;
+                need = __ballot_sync(FULL, !has);
+            }
+        }
+        if (__ballot_sync(FULL, has) == 0u) {
+            // no work in this warp; the stack is empty because it is drained first
+            if (input_done) break;
+            continue;
+        }
+
+        // ---------------- one sub-step (or a step boundary) per busy lane
+        int fin = 0;  // 1: survives the launch, 2: removed
+        if (has) {
+            const SpeciesHdr& S = H->sp[L.species];
+            const float tb = float(L.k + 1) * dt;
+            const float trem = tb - L.tl;
+            if (L.alive && trem > kEpsT && L.nsub < kSubstepCap) {
+                float tnext = L.s / L.r;
+                bool coll = trem > tnext;
+                float h = coll ? tnext : trem;
+                if (!coll) L.s -= h * L.r;
+                push(L, S, K, h);
+                L.tl = coll ? (L.tl + h) : tb;
+                L.nsub += 1;
+                if (coll) collide(L, K, S);
+                if (!L.alive) fin = 2;
+            } else {
+                if (L.nsub >= kSubstepCap) { err(K, PCL_E_SUBSTEP_CAP); L.tl = tb; }
+                if (!L.alive) {
+                    fin = 2;
+                } else {
+                    float E = kin_energy(L.species, L.px, L.py, L.pz);
+                    if (E < S.cut) {  // droplow! (population.jl:273-284)
+                        fin = 2;
+                    } else {
+                        atomicAdd(&tal[T_LEND + 3 * L.k + L.species], 1u);
+                        if (L.k + 1 >= nsteps) {
+                            fin = 1;
+                        } else {
+                            L.k += 1;
+                            L.nsub = 0;
+                            L.r = setr(S, K, E);  // advance_init! of the next step
+                            atomicAdd(&tal[T_LSTART + L.k], 1u);
+                        }
+                    }
+                }
+            }
+        }
+
+        // ---------------- finish: appended secondaries reserve slots per species
+        unsigned am = __ballot_sync(FULL, fin == 1 && L.slot < 0);
+        while (am) {
+            int leader = __ffs(am) - 1;
+            int lsp = __shfl_sync(FULL, L.species, leader);
+            unsigned grp = __ballot_sync(FULL, fin == 1 && L.slot < 0 && L.species == lsp);
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(&ctl->n[lsp], (unsigned long long)__popc(grp));
+            base = __shfl_sync(FULL, base, leader);
+            if (grp & (1u << lane)) {
+                long long slot = (long long)base + __popc(grp & lt);
+                if (slot < A.cap[lsp]) {
+                    float tb = float(L.k + 1) * dt;
+                    A.xw[lsp][slot] = make_float4(L.x, L.y, L.z, L.w);
+                    A.ps[lsp][slot] = make_float4(L.px, L.py, L.pz, L.s);
+                    A.meta[lsp][slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(L.tl - tb));
+                } else {
+                    err(K, PCL_E_CAPACITY);
+                }
+            }
+            am &= ~grp;
+        }
+        if (fin == 1 && L.slot >= 0) {
+            float tb = float(L.k + 1) * dt;
+            const int sp = L.species;
+            A.xw[sp][L.slot] = make_float4(L.x, L.y, L.z, L.w);
+            A.ps[sp][L.slot] = make_float4(L.px, L.py, L.pz, L.s);
+            A.meta[sp][L.slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(L.tl - tb));
+        } else if (fin == 2 && L.slot >= 0) {
+            A.meta[L.species][L.slot].z = PCL_DEAD_CTR;
+            atomicAdd(&tal[T_DEAD + L.species], 1u);
+        }
+        if (fin) has = false;
+    }
+
+    // ---------------- flush block tallies
+    __syncthreads();
+    for (int i = threadIdx.x; i < T_WORDS; i += blockDim.x) {
+        uint32_t v = tal[i];
+        if (!v) continue;
+        unsigned long long vv = v;
+        if (i < T_NULL) atomicAdd(&ctl->coll[i / 16][i % 16], vv);
+        else if (i < T_SPAWN) atomicAdd(&ctl->nulls[i - T_NULL], vv);
+        else if (i < T_DEAD) atomicAdd(&ctl->spawned[i - T_SPAWN], vv);
+        else if (i < T_ERR) atomicAdd(&ctl->dead[i - T_DEAD], vv);
+        else if (i < T_LEND) atomicAdd(&ctl->err[i - T_ERR], vv);
+        else if (i < T_LSTART) atomicAdd(&ctl->live_end[(i - T_LEND) / 3][(i - T_LEND) % 3], vv);
+        else atomicAdd(&ctl->live_start[i - T_LSTART], vv);
+    }
+}
+
+// Launch prologue: snapshot the work space and clear per-launch counters.
+__global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long cap2) {
+    int t = threadIdx.x;
+    const long long cap[3] = {cap0, cap1, cap2};
+    if (t < 3) {
+        unsigned long long n = ctl->n[t];
+        if ((long long)n > cap[t]) n = (unsigned long long)cap[t];
+        ctl->n[t] = n;
+        ctl->n_start[t] = n;
+        ctl->dead[t] = 0;
+    }
+    if (t == 0) { ctl->head = 0; ctl->spill_n = 0; ctl->timeout = 0; }
+    for (int i = t; i < PCL_MAX_STEPS_PER_LAUNCH * 3; i += blockDim.x) ctl->live_end[i / 3][i % 3] = 0;
+    for (int i = t; i < PCL_MAX_STEPS_PER_LAUNCH; i += blockDim.x) ctl->live_start[i] = 0;
+}
+
+// Spill-pass prologue: the spill queue written by the previous pass becomes
+// the input of the next.
+__global__ void k_begin_spill(Control* ctl, unsigned long long* in_n, unsigned long long* out_n) {
+    if (threadIdx.x == 0) { *out_n = 0; ctl->head = 0; }
+    (void)in_n;
+}
+
+// ------------------------------------------------------------ compaction -
+// repack! (population.jl:229-259) as an order-preserving stream compaction
+// into the other buffer: count live slots per tile, scan the tile counts,
+// scatter.  gridDim.y = species.
+constexpr int kTile = 2048;
+
+
+
+__global__ void k_compact_count(CompactArgs C) {
+    const int sp = blockIdx.y;
+    const long long n = (long long)C.n[sp];
+    const long long t0 = (long long)blockIdx.x * kTile;
+    if (t0 >= n) return;
+    unsigned int cnt = 0;
+    for (long long i = t0 + threadIdx.x; i < min(n, t0 + kTile); i += blockDim.x)
+        cnt += (C.smeta[sp][i].z != PCL_DEAD_CTR) ? 1u : 0u;
+    for (int o = 16; o; o >>= 1) cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    __shared__ unsigned int ws[32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int s = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += ws[w];
+        C.tile_cnt[sp][blockIdx.x] = s;
+    }
+}
+
+__global__ void k_compact_scan(CompactArgs C) {
+    const int sp = blockIdx.x;
+    const long long n = (long long)C.n[sp];
+    const int nt = int((n + kTile - 1) / kTile);
+    __shared__ unsigned long long carry;
+    __shared__ unsigned long long wsum[32];
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < nt; base += blockDim.x) {
+        int i = base + threadIdx.x;
+        unsigned long long v = (i < nt) ? C.tile_cnt[sp][i] : 0ull;
+        // block exclusive scan
+        unsigned long long x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xffffffffu, x, o);
+            if ((threadIdx.x & 31) >= o) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) wsum[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            unsigned long long w = (threadIdx.x < (blockDim.x >> 5)) ? wsum[threadIdx.x] : 0ull;
+            for (int o = 1; o < 32; o <<= 1) {
+                unsigned long long y = __shfl_up_sync(0xffffffffu, w, o);
+                if (threadIdx.x >= o) w += y;
+            }
+            wsum[threadIdx.x] = w;
+        }
+        __syncthreads();
+        unsigned long long wpre = (threadIdx.x >= 32) ? wsum[(threadIdx.x >> 5) - 1] : 0ull;
+        unsigned long long incl = x + wpre;
+        if (i < nt) C.tile_off[sp][i] = carry + incl - v;
+        __syncthreads();
+        if (threadIdx.x == blockDim.x - 1) carry += incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) C.n_out[sp] = carry;
+}
+
+__global__ void k_compact_scatter(CompactArgs C) {
+    const int sp = blockIdx.y;
+    const long long n = (long long)C.n[sp];
+    const long long t0 = (long long)blockIdx.x * kTile;
+    if (t0 >= n) return;
+    __shared__ unsigned int wcnt[32];
+    __shared__ unsigned long long run;
+    if (threadIdx.x == 0) run = C.tile_off[sp][blockIdx.x];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (long long b = t0; b < min(n, t0 + kTile); b += blockDim.x) {
+        long long i = b + threadIdx.x;
+        bool live = false;
+        uint4 m;
+        if (i < n && i < t0 + kTile) { m = C.smeta[sp][i]; live = (m.z != PCL_DEAD_CTR); }
+        unsigned bal = __ballot_sync(0xffffffffu, live);
+        if (lane == 0) wcnt[w] = __popc(bal);
+        __syncthreads();
+        unsigned int pre = 0, tot = 0;
+        for (int q = 0; q < nw; ++q) { if (q < w) pre += wcnt[q]; tot += wcnt[q]; }
+        if (live) {
+            unsigned long long d = run + pre + __popc(bal & ((1u << lane) - 1u));
+            C.dxw[sp][d] = C.sxw[sp][i];
+            C.dps[sp][d] = C.sps[sp][i];
+            C.dmeta[sp][d] = m;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) run += tot;
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------- moments ---
+// FP64 weighted moments of the live particles (weight, meanenergy, spread,
+// posvar, maxenergy, nactives; population.jl:89-223).
+__global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta, long long n, int species,
+                          double* out) {
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double emax = 0.0;
+    unsigned long long live = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        uint4 m = meta[i];
+        if (m.z == PCL_DEAD_CTR) continue;
+        float4 a = xw[i], b = ps[i];
+        double p2 = double(b.x) * b.x + double(b.y) * b.y + double(b.z) * b.z;
+        double E = (species == PCL_PHOTON) ? sqrt(p2) : p2 / (sqrt(1.0 + p2) + 1.0);
+        double w = a.w;
+        acc[0] += w; acc[1] += w * E;
+        acc[2] += w * a.x; acc[3] += w * a.y; acc[4] += w * a.z;
+        acc[5] += w * double(a.x) * a.x; acc[6] += w * double(a.y) * a.y; acc[7] += w * double(a.z) * a.z;
+        emax = fmax(emax, E);
+        live += 1;
+    }
+    for (int o = 16; o; o >>= 1) {
+        for (int q = 0; q < 8; ++q) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
+        emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        live += __shfl_xor_sync(0xffffffffu, live, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        for (int q = 0; q < 8; ++q) atomicAdd(&out[q], acc[q]);
+        atomicMax(reinterpret_cast<unsigned long long*>(&out[8]), (unsigned long long)__double_as_longlong(emax));
+        atomicAdd(reinterpret_cast<unsigned long long*>(&out[9]), live);
+    }
+}
+
+// ------------------------------------------------------- sampler test ----
+// Test hook behind pcl_test_sampler: force table position j for n primaries.
+__global__ void k_test_sampler(StepArgs A, int species, int j, long long n, const float* p_in,
+                               const uint32_t* sid, float* out_p, float* out_s, int* out_kind,
+                               uint32_t* out_ctr) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(smem + A.blob_bytes);
+    __shared__ uint32_t tal[T_WORDS];
+    for (int i = threadIdx.x; i < T_WORDS; i += blockDim.x) tal[i] = 0u;
+    bool ok = stage_blob(smem, A.blob, A.blob_bytes, mbar);
+    if (__syncthreads_or(!ok)) return;
+    const BlobHdr* H = reinterpret_cast<const BlobHdr*>(smem);
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float capbuf[8];
+    int ncap = 0;
+    KCtx K;
+    K.H = H; K.blob = reinterpret_cast<const float*>(smem); K.stk = nullptr; K.top = nullptr; K.tal = tal;
+    K.A = &A; K.cap = capbuf; K.ncap = &ncap;
+    Lane L;
+    L.x = L.y = L.z = 0.0f; L.w = 1.0f; L.tl = 0.0f; L.k = 0; L.s = 0.0f;
+    L.px = p_in[3 * i]; L.py = p_in[3 * i + 1]; L.pz = p_in[3 * i + 2];
+    L.sid_lo = sid[2 * i]; L.sid_hi = sid[2 * i + 1]; L.ctr = 0u; L.rvalid = false;
+    L.species = species; L.alive = true; L.slot = -1; L.nsub = 0;
+    const SpeciesHdr& S = H->sp[species];
+    float E = kin_energy(species, L.px, L.py, L.pz);
+    L.r = setr(S, K, E);
+    const DevProc& P = S.proc[j];
+    sample_process(L, K, S, P, E, 0u);
+    for (int q = 0; q < 3; ++q) out_kind[3 * i + q] = -1;
+    if (L.alive) {
+        out_p[9 * i + 0] = L.px; out_p[9 * i + 1] = L.py; out_p[9 * i + 2] = L.pz;
+        out_s[3 * i] = L.s; out_kind[3 * i] = species;
+    }
+    // secondaries: species per process kind
+    int ks[2] = {-1, -1};
+    switch (P.kind) {
+        case PCL_PROC_MOLLER: case PCL_PROC_RBEB: case PCL_PROC_COMPTON: case PCL_PROC_KN_COMPTON:
+        case PCL_PROC_PHOTOELECTRIC: case PCL_PROC_BHABHA: ks[0] = PCL_ELECTRON; break;
+        case PCL_PROC_SELTZER_BERGER: ks[0] = PCL_PHOTON; break;
+        case PCL_PROC_BETHE_HEITLER: ks[0] = PCL_ELECTRON; ks[1] = PCL_POSITRON; break;
+        case PCL_PROC_ANNIHILATION: ks[0] = PCL_PHOTON; ks[1] = PCL_PHOTON; break;
+        default: break;
+    }
+    for (int c = 0; c < ncap && c < 2; ++c) {
+        out_p[9 * i + 3 * (c + 1) + 0] = capbuf[4 * c + 0];
+        out_p[9 * i + 3 * (c + 1) + 1] = capbuf[4 * c + 1];
+        out_p[9 * i + 3 * (c + 1) + 2] = capbuf[4 * c + 2];
+        out_s[3 * i + c + 1] = capbuf[4 * c + 3];
+        out_kind[3 * i + c + 1] = ks[c];
+    }
+    out_ctr[i] = L.ctr;
+}
+
+// Shared-memory bytes of k_step for a block of `threads`.
+size_t step_smem_bytes(int blob_bytes, int threads) {
+    int nw = threads / 32;
+    size_t b = size_t(blob_bytes) + size_t(nw) * kWarpStack * 3 * 16 + size_t(nw) * 4 + T_WORDS * 4 + 64;
+    return (b + 15) & ~size_t(15);
+}
+
+}  // namespace pcl

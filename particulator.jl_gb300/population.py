@@ -1,0 +1,444 @@
+"""Populations and the step/run API (population.jl, mixed_population.jl,
+run.jl, callback.jl), backed by the device context of the C ABI.
+
+Names follow the reference; Julia's `!` suffix is dropped (``advance`` is
+``advance!``, ``run`` is ``run!``, ``init`` is ``init!``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from . import constants as co
+from .forcing import RK2Pusher
+from .tables import Electron, Photon, Positron, PARTICLE_NAMES, ChebyshevCollisionTable
+
+SPECIES_BY_NAME = {"electron": Electron, "photon": Photon, "positron": Positron}
+
+
+@dataclass
+class _State:
+    x: tuple
+    p: tuple
+    w: float = 1.0
+    t: float = 0.0
+    s: float | None = None   # None: s = nextcoll() drawn from the particle's stream
+
+
+class ElectronState(_State):
+    """ElectronState(x, p, w=1, t=0) (electron.jl:13-34)."""
+    particle = Electron
+
+
+class PhotonState(_State):
+    """PhotonState(x, p, w=1, t=0) (photon.jl:6-33)."""
+    particle = Photon
+
+
+class PositronState(_State):
+    """PositronState(x, p, w=1, t=0) (positron.jl:3-22)."""
+    particle = Positron
+
+
+@dataclass
+class ParticleArrays:
+    """A structure-of-arrays batch of particle states (SI units)."""
+    x: np.ndarray
+    p: np.ndarray
+    w: np.ndarray
+    t: np.ndarray
+    s: np.ndarray | None = None
+    sid: np.ndarray | None = None
+    ctr: np.ndarray | None = None
+
+    def __len__(self):
+        return len(self.w)
+
+    @classmethod
+    def from_states(cls, states):
+        n = len(states)
+        x = np.array([st.x for st in states], dtype=np.float64).reshape(n, 3)
+        p = np.array([st.p for st in states], dtype=np.float64).reshape(n, 3)
+        w = np.array([st.w for st in states], dtype=np.float64)
+        t = np.array([st.t for st in states], dtype=np.float64)
+        s = None
+        if n and all(st.s is not None for st in states):
+            s = np.array([st.s for st in states], dtype=np.float64)
+        return cls(x, p, w, t, s)
+
+    @classmethod
+    def empty(cls):
+        return cls(np.zeros((0, 3)), np.zeros((0, 3)), np.zeros(0), np.zeros(0))
+
+
+def kinenergy(particle: int, p) -> np.ndarray:
+    """kinenergy for an (n, 3) array of SI momenta (electron.jl:53, photon.jl:50)."""
+    p = np.asarray(p, dtype=np.float64)
+    p2 = np.sum(p * p, axis=-1)
+    if particle == Photon:
+        return np.sqrt(p2) * co.c
+    q = p2 / co.electron_mc ** 2
+    return co.electron_mc2 * q / (np.sqrt(1 + q) + 1)
+
+
+class Population:
+    """Population(max_particles, inparticles, collisions, energy_cut)
+    (population.jl:7-44).  ``inparticles`` is a list of states or a
+    ``ParticleArrays``.  ``tally_only=True`` makes a population whose
+    secondaries are counted and binned but not stored."""
+
+    def __init__(self, max_particles: int, inparticles, collisions: ChebyshevCollisionTable | None,
+                 energy_cut: float = 0.0, *, particle: int | None = None, tally_only: bool = False,
+                 sid_base: int | None = None):
+        if isinstance(inparticles, ParticleArrays):
+            arr = inparticles
+        else:
+            inparticles = list(inparticles)
+            arr = ParticleArrays.from_states(inparticles) if inparticles else ParticleArrays.empty()
+            if particle is None and inparticles:
+                particle = inparticles[0].particle
+        if particle is None:
+            particle = collisions.particle if collisions is not None else Electron
+        if len(arr) > max_particles:
+            raise ValueError("more initial particles than max_particles")
+        self.particle = particle
+        self.max_particles = int(max_particles)
+        self.collisions = collisions
+        self.energy_cut = float(energy_cut)
+        self.tally_only = tally_only
+        self.sid_base = sid_base
+        self._init = arr
+        self._mp: MultiPopulation | None = None
+
+    @property
+    def ctx(self):
+        if self._mp is None:
+            raise RuntimeError("population is not part of a MultiPopulation")
+        return self._mp.ctx
+
+    def moments(self) -> np.ndarray:
+        out = np.zeros(10)
+        _lib.check(_lib.lib().pcl_moments(self.ctx, self.particle, _lib.dptr(out)), self.ctx, "pcl_moments")
+        return out
+
+    def particles(self) -> ParticleArrays:
+        """Download the live particles (SI)."""
+        L = _lib.lib()
+        n = C.c_int64(self.max_particles)
+        x = np.zeros((self.max_particles, 3)); p = np.zeros((self.max_particles, 3))
+        w = np.zeros(self.max_particles); t = np.zeros(self.max_particles); s = np.zeros(self.max_particles)
+        sid = np.zeros(self.max_particles, np.uint64); ctr = np.zeros(self.max_particles, np.uint32)
+        if self.max_particles and not self.tally_only:
+            _lib.check(L.pcl_download(self.ctx, self.particle, C.byref(n), _lib.dptr(x), _lib.dptr(p), _lib.dptr(w),
+                                      _lib.dptr(t), _lib.dptr(s), _lib.u64ptr(sid), _lib.u32ptr(ctr)),
+                       self.ctx, "pcl_download")
+        else:
+            n.value = 0
+        m = n.value
+        return ParticleArrays(x[:m], p[:m], w[:m], t[:m], s[:m], sid[:m], ctr[:m])
+
+
+class MultiPopulation:
+    """MultiPopulation(:electron => ..., :photon => ..., :positron => ...)
+    (mixed_population.jl:4-12).  Owns one device context; configuration
+    keywords select the device, the Philox seed and the launch shape."""
+
+    def __init__(self, *pairs, seed: int = 0, device: int = 0, steps_per_launch: int = 1,
+                 compaction_period: int = 1, block_size: int = 0, grid_blocks: int = 0, **named):
+        index = {}
+        for name, pop in list(pairs) + list(named.items()):
+            key = SPECIES_BY_NAME[name] if isinstance(name, str) else int(name)
+            index[key] = pop
+        self.index = index
+        cfg = _lib.Config()
+        cfg.seed = seed
+        cfg.device = device
+        cfg.steps_per_launch = steps_per_launch
+        cfg.compaction_period = compaction_period
+        cfg.block_size = block_size
+        cfg.grid_blocks = grid_blocks
+        self.config = cfg
+        h = C.c_void_p()
+        rc = _lib.lib().pcl_create(C.byref(cfg), C.byref(h))
+        if rc != _lib.PCL_OK:
+            raise _lib.PCLError(rc, "pcl_create failed (is a CUDA device available?)")
+        self.ctx = h
+        self._pusher_key = None
+        self._keep = []
+        sid_base = 0
+        for key in sorted(index):
+            pop = index[key]
+            pop._mp = self
+            self._configure(key, pop, sid_base)
+            sid_base += pop.max_particles
+        self.t = 0.0
+
+    def _configure(self, key, pop: Population, sid_base: int):
+        L = _lib.lib()
+        flags = _lib.SPECIES_TALLY_ONLY if pop.tally_only else _lib.SPECIES_TRACKED
+        _lib.check(L.pcl_set_species(self.ctx, key, pop.energy_cut, pop.max_particles, flags), self.ctx,
+                   "pcl_set_species")
+        tab = pop.collisions
+        if tab is not None:
+            procs = tab.c_procs()
+            self._keep.append((procs, tab))
+            rate = np.ascontiguousarray(tab.rate) if tab.nproc else np.zeros(1)
+            rb = np.ascontiguousarray(tab.ratebound)
+            _lib.check(L.pcl_set_collision_table(self.ctx, key, tab.order, tab.nproc, tab.b.k, tab.b.xmax,
+                                                 _lib.dptr(rate), _lib.dptr(rb), procs), self.ctx,
+                       "pcl_set_collision_table")
+        arr = pop._init
+        if not pop.tally_only and len(arr):
+            base = pop.sid_base if pop.sid_base is not None else sid_base
+            x = np.ascontiguousarray(arr.x, dtype=np.float64).reshape(-1)
+            p = np.ascontiguousarray(arr.p, dtype=np.float64).reshape(-1)
+            w = np.ascontiguousarray(arr.w, dtype=np.float64)
+            t = np.ascontiguousarray(arr.t, dtype=np.float64)
+            s = None if arr.s is None else np.ascontiguousarray(arr.s, dtype=np.float64)
+            sid = None if arr.sid is None else np.ascontiguousarray(arr.sid, dtype=np.uint64)
+            _lib.check(L.pcl_upload(self.ctx, key, len(arr), _lib.dptr(x), _lib.dptr(p), _lib.dptr(w), _lib.dptr(t),
+                                    _lib.dptr(s), _lib.u64ptr(sid), int(base)), self.ctx, "pcl_upload")
+
+    def get(self, particle):
+        key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        return self.index[key]
+
+    def __getitem__(self, particle):
+        return self.get(particle)
+
+    def pairs(self):
+        return [(PARTICLE_NAMES[k], v) for k, v in sorted(self.index.items())]
+
+    def set_pusher(self, pusher: RK2Pusher):
+        E, B, cl = pusher.device_forcing()
+        key = (tuple(E), tuple(B), id(cl))
+        if key == self._pusher_key:
+            return
+        L = _lib.lib()
+        E = np.ascontiguousarray(E); B = np.ascontiguousarray(B)
+        if cl is None:
+            rc = L.pcl_set_forcing(self.ctx, _lib.dptr(E), _lib.dptr(B), 0, 0, 0.0, None, None)
+        else:
+            self._keep.append(cl)
+            rc = L.pcl_set_forcing(self.ctx, _lib.dptr(E), _lib.dptr(B), cl.n, cl.bints.k, cl.bints.xmax,
+                                   _lib.dptr(cl.ec), _lib.dptr(cl.pc))
+        _lib.check(rc, self.ctx, "pcl_set_forcing")
+        self._pusher_key = key
+
+    def tallies(self) -> _lib.Tallies:
+        t = _lib.Tallies()
+        _lib.check(_lib.lib().pcl_get_tallies(self.ctx, C.byref(t)), self.ctx, "pcl_get_tallies")
+        return t
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            _lib.lib().pcl_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------ callbacks --
+class AbstractCallback:
+    """Hook protocol (callback.jl:15-35).  Device-side callbacks only: the
+    built-ins below; arbitrary Python hooks run on the host between steps."""
+
+    def onstep(self, mpopl, t):
+        return True
+
+    def onoutput(self, mpopl, t, i):
+        return None
+
+
+class VoidCallback(AbstractCallback):
+    pass
+
+
+class CombinedCallback(AbstractCallback):
+    """CombinedCallback((a, b, ...)) (callback.jl:41-108)."""
+
+    def __init__(self, tpl):
+        self.tpl = tuple(tpl)
+
+    def onstep(self, mpopl, t):
+        ok = True
+        for c in self.tpl:
+            ok = c.onstep(mpopl, t) and ok
+        return ok
+
+    def onoutput(self, mpopl, t, i):
+        for c in self.tpl:
+            c.onoutput(mpopl, t, i)
+
+
+class CollisionCounter(AbstractCallback):
+    """CollisionCounter (callback.jl:118-141): per-process collision counts,
+    tallied on the device; ``counts(mpopl)`` maps (species, process) -> count."""
+
+    def counts(self, mpopl):
+        t = mpopl.tallies()
+        out = {}
+        for key, pop in mpopl.index.items():
+            if pop.collisions is None:
+                continue
+            for j, proc in enumerate(pop.collisions.proc):
+                out[(PARTICLE_NAMES[key], j, type(proc).__name__)] = t.collisions[key][j]
+            out[(PARTICLE_NAMES[key], -1, "NullCollision")] = t.nulls[key]
+        return out
+
+
+class PopulationTargetCallback(AbstractCallback):
+    """PopulationTargetCallback{S}(n, ismax) (callback.jl:253-267)."""
+
+    def __init__(self, particle, n: int, ismax: bool = True):
+        self.particle = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        self.n = int(n)
+        self.ismax = ismax
+
+    def onstep(self, mpopl, t):
+        live = mpopl.tallies().live[self.particle]
+        return live < self.n if self.ismax else live > self.n
+
+
+class ParticleCountCallback(AbstractCallback):
+    """ParticleCountCallback(particles) (callback.jl:190-204): total weight of
+    each listed species at every output time."""
+
+    def __init__(self, particles):
+        self.p = [SPECIES_BY_NAME[s] if isinstance(s, str) else int(s) for s in particles]
+        self.counts = []
+
+    def onoutput(self, mpopl, t, i):
+        self.counts.append([t] + [weight(mpopl.get(s)) for s in self.p])
+
+
+# ---------------------------------------------------------------- stepping --
+def init(mpopl: MultiPopulation):
+    """init! (mixed_population.jl:20-35): the rate bounds are set on the
+    device at the start of every step, so there is nothing to do here."""
+    return None
+
+
+def advance(mpopl: MultiPopulation, pusher: RK2Pusher, tfinal: float, callback=None):
+    """advance!(mpopl, pusher, tfinal, callback) followed by droplow! on every
+    population (mixed_population.jl:38-47, run.jl:7): one device step."""
+    mpopl.set_pusher(pusher)
+    _lib.check(_lib.lib().pcl_advance(mpopl.ctx, float(tfinal)), mpopl.ctx, "pcl_advance")
+    mpopl.t = float(tfinal)
+
+
+def run(mpopl: MultiPopulation, pusher: RK2Pusher, tfinal: float, dt: float, callback=None, *,
+        output_dt: float | None = None, verbosity: int = 0):
+    """run!(mpopl, pusher, tfinal, dt, callback; output_dt, verbosity)
+    (run.jl:1-29).  Steps run on the device in launches of
+    ``steps_per_launch``; host callbacks are evaluated after each launch."""
+    callback = callback or VoidCallback()
+    mpopl.set_pusher(pusher)
+    L = _lib.lib()
+    opts = _lib.RunOpts()
+    opts.target_species = -1
+    cbs = callback.tpl if isinstance(callback, CombinedCallback) else (callback,)
+    host_step = [c for c in cbs if type(c).onstep is not AbstractCallback.onstep
+                 and not isinstance(c, PopulationTargetCallback)]
+    for c in cbs:
+        if isinstance(c, PopulationTargetCallback):
+            opts.target_species = c.particle
+            opts.target_ismax = 1 if c.ismax else 0
+            opts.target_n = c.n
+    t = mpopl.t
+    nxt = t
+    isave = 0
+    tallies = _lib.Tallies()
+    while t < tfinal * (1 - 1e-15):
+        chunk_end = tfinal
+        if output_dt is not None:
+            chunk_end = min(tfinal, max(nxt, t + dt))
+        if host_step:
+            chunk_end = min(chunk_end, t + dt)
+        _lib.check(L.pcl_run(mpopl.ctx, float(chunk_end), float(dt), C.byref(opts), C.byref(tallies)), mpopl.ctx,
+                   "pcl_run")
+        t = tallies.t
+        mpopl.t = t
+        cont = all(c.onstep(mpopl, t) for c in host_step) if host_step else True
+        if opts.target_species >= 0:
+            live = tallies.live[opts.target_species]
+            hit = live >= opts.target_n if opts.target_ismax else live <= opts.target_n
+            cont = cont and not hit
+        if output_dt is not None and t >= nxt * (1 - 1e-12):
+            nxt += output_dt
+            isave += 1
+            if verbosity > 0:
+                print(f"{100 * t / tfinal:.2f}% complete, time = {t / 1e-9:.3f} ns, "
+                      + ", ".join(f"{n} => {tallies.live[k]}" for k, n in PARTICLE_NAMES.items()))
+            callback.onoutput(mpopl, t, isave)
+        if not cont:
+            if verbosity > 0:
+                print("Early stop due to onstep() callback")
+            break
+    return tallies
+
+
+# -------------------------------------------------------------- statistics --
+def nparticles(pop: Population) -> int:
+    """nparticles (population.jl:78): slots in use, live or not."""
+    return int(mpop_tallies(pop).n[pop.particle])
+
+
+def mpop_tallies(pop: Population):
+    return pop._mp.tallies()
+
+
+def nactives(pop: Population) -> int:
+    """nactives (population.jl:89-97)."""
+    return int(pop.moments()[9])
+
+
+def weight(pop: Population) -> float:
+    """weight (population.jl:130-140)."""
+    return float(pop.moments()[0])
+
+
+def meanenergy(pop: Population) -> float:
+    """meanenergy (population.jl:152-166)."""
+    m = pop.moments()
+    return float(m[1] / m[0]) if m[0] else math.nan
+
+
+def maxenergy(pop: Population) -> float:
+    """maxenergy (population.jl:172-174)."""
+    return float(pop.moments()[8])
+
+
+def spread(pop: Population):
+    """spread (population.jl:180-198): centroid and rms distance from it."""
+    m = pop.moments()
+    tot = m[0]
+    xm = m[2:5] / tot
+    x2 = (m[5] + m[6] + m[7]) / tot
+    return xm, math.sqrt(abs(x2 - float(np.dot(xm, xm))))
+
+
+def posvar(pop: Population) -> np.ndarray:
+    """posvar (population.jl:204-223)."""
+    m = pop.moments()
+    tot = m[0]
+    return m[5:8] / tot - (m[2:5] / tot) ** 2
+
+
+def repack(pop: Population):
+    """repack! (population.jl:229-259): compact dead slots (all species)."""
+    _lib.check(_lib.lib().pcl_compact(pop.ctx), pop.ctx, "pcl_compact")
+
+
+def droplow(pop: Population):
+    """droplow! (population.jl:273-284): the device step already drops
+    particles below the cut; this compacts the population."""
+    repack(pop)

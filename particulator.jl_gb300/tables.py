@@ -1,0 +1,161 @@
+"""Collision tables and continuum losses: thin wrappers over the library's
+FP64 host builders, with the reference's names and keyword defaults."""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from . import constants as co
+
+Electron, Photon, Positron = _lib.ELECTRON, _lib.PHOTON, _lib.POSITRON
+PARTICLE_NAMES = {Electron: "electron", Photon: "photon", Positron: "positron"}
+
+
+def speed(particle: int, eng):
+    """speed(::Type{P}, eng) (electron.jl:47, positron.jl:34, photon.jl:46)."""
+    if particle == Photon:
+        return co.c * np.ones_like(np.asarray(eng, dtype=float))
+    return co.c * np.sqrt(1 - (co.electron_mc2 / (co.electron_mc2 + np.asarray(eng))) ** 2)
+
+
+def momentum_norm_from_kin(particle: int, kin):
+    """momentum_norm_from_kin (electron.jl:51, photon.jl:47)."""
+    kin = np.asarray(kin, dtype=float)
+    if particle == Photon:
+        return kin / co.c
+    return np.sqrt((kin + co.electron_mc2) ** 2 - co.electron_mc2 ** 2) / co.c
+
+
+@dataclass
+class BinaryIntervals:
+    """BinaryIntervals(k, xmax) (cheby.jl:15-21)."""
+    k: int
+    xmax: float
+
+    def interval(self, i: int):
+        if i == 0:
+            l, _ = self.interval(1)
+            return 0.0, l
+        l = 2.0 ** (i - self.k - 1)
+        return l * self.xmax, 2 * l * self.xmax
+
+
+def precheb(x, b: BinaryIntervals, n: int):
+    """precheb (cheby.jl:127-143) for scalar x: (interval, (T_0..T_{n-1}))."""
+    x1 = x / b.xmax
+    s, l = np.frexp(x1)
+    i = 0 if x1 == 0 else int(l) + b.k
+    if i > 0:
+        xi = 4 * s - 3
+    else:
+        xi = 2.0 ** (b.k + 1) * x1 - 1
+        i = 0
+    t = [1.0, xi][:n]
+    while len(t) < n:
+        t.append(2 * xi * t[-1] - t[-2])
+    return i, tuple(t)
+
+
+@dataclass
+class ChebyshevCollisionTable:
+    """ChebyshevCollisionTable (collision_table.jl:63-106): processes in table
+    order, binary intervals, rate a[k, j, i] and ratebound[k, i] (SI, 1/s)."""
+    proc: tuple
+    coef: np.ndarray
+    b: BinaryIntervals
+    order: int
+    rate: np.ndarray          # flat, a[k + order*(j + nproc*i)]
+    ratebound: np.ndarray     # flat, rb[k + order*i]
+    perm: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    particle: int = Electron
+
+    def __len__(self):
+        return len(self.proc)
+
+    @property
+    def nproc(self):
+        return len(self.proc)
+
+    def rate_array(self) -> np.ndarray:
+        """a as an array indexed [k, j, i]."""
+        return self.rate.reshape(self.b.k + 1, self.nproc, self.order).transpose(2, 1, 0)
+
+    def rate_at(self, j: int, eng: float) -> float:
+        i, t = precheb(eng, self.b, self.order)
+        a = self.rate_array()
+        return float(sum(a[q, j, i] * t[q] for q in range(self.order)))
+
+    def ratebound_at(self, eng: float) -> float:
+        i, t = precheb(eng, self.b, self.order)
+        rb = self.ratebound.reshape(self.b.k + 1, self.order)
+        return float(sum(rb[i, q] * t[q] for q in range(self.order)))
+
+    def c_procs(self):
+        arr = (_lib.Process * max(1, self.nproc))()
+        for j, (cf, p) in enumerate(zip(self.coef, self.proc)):
+            arr[j] = p.to_c(float(cf))
+        return arr
+
+
+def collision_table_from_processes(processes, particle: int, Fdt: float, *, safety: float = 1.1,
+                                   nintervals: int = 32, order: int = 3,
+                                   max_energy: float = 1e3 * co.eV * 2 ** 18) -> ChebyshevCollisionTable:
+    """collision_table_from_processes(processes, particle, Fdt; safety,
+    nintervals, order, max_energy) (collision_table.jl:115-149).
+    ``processes`` is a list of ``(coef, process)``."""
+    n = len(processes)
+    procs = (_lib.Process * max(1, n))()
+    for j, (cf, p) in enumerate(processes):
+        procs[j] = p.to_c(float(cf))
+    rate = np.zeros(order * max(1, n) * (nintervals + 1))
+    rb = np.zeros(order * (nintervals + 1))
+    perm = np.zeros(max(1, n), dtype=np.int32)
+    rc = _lib.lib().pcl_build_collision_table(int(particle), n, procs, float(Fdt), float(safety), int(nintervals),
+                                              int(order), float(max_energy), _lib.dptr(rate), _lib.dptr(rb),
+                                              _lib.i32ptr(perm))
+    _lib.check(rc, None, "pcl_build_collision_table")
+    perm = perm[:n]
+    return ChebyshevCollisionTable(proc=tuple(processes[p][1] for p in perm),
+                                   coef=np.array([processes[p][0] for p in perm], dtype=np.float64),
+                                   b=BinaryIntervals(nintervals, float(max_energy)), order=order,
+                                   rate=rate[:order * n * (nintervals + 1)] if n else np.zeros(0), ratebound=rb,
+                                   perm=perm, particle=particle)
+
+
+@dataclass
+class ContinuumLoss:
+    """ContinuumLoss(nel, I, Tcut) (continuum.jl:6-15)."""
+    nel: float
+    I: float
+    Tcut: float
+
+
+@dataclass
+class ChebContinuumLoss:
+    """ChebContinuumLoss(cl, Tmax, n) (continuum.jl:25-43): Chebyshev fits of the
+    restricted stopping power of electrons (ec) and positrons (pc), [n][k+1]."""
+    bints: BinaryIntervals
+    ec: np.ndarray
+    pc: np.ndarray
+    n: int
+
+    @classmethod
+    def build(cls, cl: ContinuumLoss, Tmax: float, n: int) -> "ChebContinuumLoss":
+        cap = n * 64
+        ec = np.zeros(cap)
+        pc = np.zeros(cap)
+        k = C.c_int(0)
+        xmax = C.c_double(0)
+        rc = _lib.lib().pcl_build_continuum_loss(float(cl.nel), float(cl.I), float(cl.Tcut), float(Tmax), int(n),
+                                                 C.byref(k), C.byref(xmax), _lib.dptr(ec), _lib.dptr(pc), cap)
+        _lib.check(rc, None, "pcl_build_continuum_loss")
+        m = n * (k.value + 1)
+        return cls(BinaryIntervals(k.value, xmax.value), ec[:m].copy(), pc[:m].copy(), n)
+
+    def force_magnitude(self, particle: int, eng: float) -> float:
+        a = (self.ec if particle == Electron else self.pc).reshape(self.bints.k + 1, self.n)
+        i, t = precheb(eng, self.bints, self.n)
+        return float(sum(a[i, q] * t[q] for q in range(self.n)))

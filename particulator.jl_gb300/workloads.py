@@ -1,0 +1,142 @@
+"""Air, its process lists and the benchmark workloads.
+
+The process lists follow the reference's beam script (scripts/beam.jl:94-129)
+with Moller ionisation in place of the RBEB orbitals for electrons; the
+coefficient of every atomic process is the atom density 2 n_X2.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import constants as co
+from .forcing import CombinedForcing, ElectromagneticField, HomogeneousField, RK2Pusher
+from .population import MultiPopulation, ParticleArrays, Population
+from .processes import (BetheHeitler, Bhaba, Compton, Moller, ORBITALS, PhotoElectric, PositronAnihilation,
+                        RelativisticCoulomb, SeltzerBerger)
+from .tables import (ChebContinuumLoss, ContinuumLoss, Electron, Photon, Positron,
+                     collision_table_from_processes, momentum_norm_from_kin)
+
+KEV = 1e3 * co.eV
+MEV = 1e6 * co.eV
+
+
+def air_composition(T: float = 293.0, p: float = co.atm, f_n2: float = 0.79, f_o2: float = 0.21):
+    """Molecule densities (1/m^3) of N2/O2 air at pressure p and temperature T."""
+    n = p / (co.Boltzmann * T)
+    return {"N2": f_n2 * n, "O2": f_o2 * n}
+
+
+_SB_CACHE = {}
+
+
+def seltzer_berger(Z: int) -> SeltzerBerger:
+    if Z not in _SB_CACHE:
+        _SB_CACHE[Z] = SeltzerBerger(Z)
+    return _SB_CACHE[Z]
+
+
+def electron_processes(comp, tcut: float = 10 * KEV, ionization: str = "moller"):
+    procs = [(2 * comp["N2"], RelativisticCoulomb(7)), (2 * comp["O2"], RelativisticCoulomb(8)),
+             (2 * comp["N2"], seltzer_berger(7)), (2 * comp["O2"], seltzer_berger(8))]
+    if ionization == "moller":
+        procs += [(2 * comp["N2"], Moller(7, tcut)), (2 * comp["O2"], Moller(8, tcut))]
+    elif ionization == "rbeb":
+        procs += [(comp["N2"], orb) for orb in ORBITALS["N2"]] + [(comp["O2"], orb) for orb in ORBITALS["O2"]]
+    return procs
+
+
+def positron_processes(comp, tcut: float = 10 * KEV):
+    return [(2 * comp["N2"], RelativisticCoulomb(7)), (2 * comp["O2"], RelativisticCoulomb(8)),
+            (2 * comp["N2"], Bhaba(7, tcut)), (2 * comp["O2"], Bhaba(8, tcut)),
+            (2 * comp["N2"], PositronAnihilation(7)), (2 * comp["O2"], PositronAnihilation(8))]
+
+
+def photon_processes(comp):
+    return [(2 * comp["N2"], PhotoElectric(7)), (2 * comp["O2"], PhotoElectric(8)),
+            (2 * comp["N2"], BetheHeitler(7)), (2 * comp["O2"], BetheHeitler(8)),
+            (2 * comp["N2"], Compton(7)), (2 * comp["O2"], Compton(8))]
+
+
+def air_continuum_loss(comp, I: float = 85.7 * co.eV, Tcut: float = 10 * KEV, Tmax: float = 1e3 * co.eV * 2 ** 18,
+                       n: int = 3) -> ChebContinuumLoss:
+    """ChebContinuumLoss(ContinuumLoss(nel, I, Tcut), Tmax, n) of air; nel counts
+    14 electrons per N2 and 16 per O2."""
+    nel = 14 * comp["N2"] + 16 * comp["O2"]
+    return ChebContinuumLoss.build(ContinuumLoss(nel, I, Tcut), Tmax, n)
+
+
+def pusher(efield, bfield=(0.0, 0.0, 0.0), cl: ChebContinuumLoss | None = None) -> RK2Pusher:
+    em = ElectromagneticField(HomogeneousField(efield), HomogeneousField(bfield))
+    return RK2Pusher(CombinedForcing(em, cl) if cl is not None else CombinedForcing(em))
+
+
+def isotropic(n: int, kin: float, rng: np.random.Generator, particle: int = Electron) -> np.ndarray:
+    """n momenta of kinetic energy `kin` with isotropic directions (SI)."""
+    u = 2 * rng.random(n) - 1
+    phi = 2 * np.pi * rng.random(n)
+    s = np.sqrt(1 - u * u)
+    d = np.stack([s * np.cos(phi), s * np.sin(phi), u], axis=1)
+    return d * float(momentum_norm_from_kin(particle, kin))
+
+
+@dataclass
+class Workload:
+    mpopl: MultiPopulation
+    pusher: RK2Pusher
+    dt: float
+    tfinal: float
+    name: str
+
+
+def beam_tables(comp, efield: float, dt: float, safety: float = 1.15, cut_e: float = 10 * KEV,
+                cut_p: float = 10 * KEV, ionization: str = "moller"):
+    Fdt = co.elementary_charge * abs(efield) * dt
+    et = collision_table_from_processes(electron_processes(comp, cut_e, ionization), Electron, Fdt, safety=safety)
+    pt = collision_table_from_processes(positron_processes(comp, cut_p), Positron, Fdt, safety=safety)
+    gt = collision_table_from_processes(photon_processes(comp), Photon, 0.0, safety=safety)
+    return et, gt, pt
+
+
+def plain_electrons(n: int = 1000, kin: float = 1 * MEV, efield: float = 1e6, dt: float = 1e-12,
+                    tfinal: float = 50e-9, cut: float = 10 * KEV, seed: int = 1, capacity: int | None = None,
+                    **cfg) -> Workload:
+    """Electrons only in air, E along -z, n e- at the origin with momentum along
+    +z (a 1e-6 y component avoids the pole of `turn`, as scripts/beam.jl:56
+    does); Moller, Seltzer-Berger, screened Coulomb, continuum loss below the
+    cut; bremsstrahlung photons tallied, not tracked."""
+    comp = air_composition()
+    Fdt = co.elementary_charge * efield * dt
+    et = collision_table_from_processes(electron_processes(comp, cut), Electron, Fdt, safety=1.15)
+    pn = float(momentum_norm_from_kin(Electron, kin))
+    x = np.zeros((n, 3))
+    p = np.tile([0.0, 1e-6 * pn, pn], (n, 1))
+    arr = ParticleArrays(x, p, np.ones(n), np.zeros(n))
+    cap = capacity or max(4 * n, 4096)
+    electrons = Population(cap, arr, et, cut, particle=Electron)
+    photons = Population(0, ParticleArrays.empty(), None, 0.0, particle=Photon, tally_only=True)
+    mp = MultiPopulation(("electron", electrons), ("photon", photons), seed=seed, **cfg)
+    cl = air_continuum_loss(comp, Tcut=cut)
+    return Workload(mp, pusher((0.0, 0.0, -efield), cl=cl), dt, tfinal, "electrons-air-1MVm")
+
+
+def avalanche(n: int = 10000, kin: float = 1 * MEV, efield: float = 5e5, dt: float = 1e-12,
+              cut_e: float = 10 * KEV, cut_g: float = 5 * KEV, cut_p: float = 10 * KEV, seed: int = 0,
+              capacity: int = 1 << 22, capacity_p: int | None = None, **cfg) -> Workload:
+    """Mixed e-/gamma/e+ relativistic runaway avalanche in air: n e- at the
+    origin, isotropic, E along -z; photons tracked through Compton,
+    photoelectric and Bethe-Heitler; positrons through Bhabha, annihilation
+    and Coulomb."""
+    comp = air_composition()
+    et, gt, pt = beam_tables(comp, efield, dt, cut_e=cut_e, cut_p=cut_p)
+    rng = np.random.Generator(np.random.Philox(seed))
+    p = isotropic(n, kin, rng)
+    arr = ParticleArrays(np.zeros((n, 3)), p, np.ones(n), np.zeros(n))
+    capp = capacity_p or max(capacity // 8, 4096)
+    electrons = Population(capacity, arr, et, cut_e, particle=Electron)
+    photons = Population(capacity, ParticleArrays.empty(), gt, cut_g, particle=Photon)
+    positrons = Population(capp, ParticleArrays.empty(), pt, cut_p, particle=Positron)
+    mp = MultiPopulation(("electron", electrons), ("photon", photons), ("positron", positrons), seed=seed, **cfg)
+    cl = air_continuum_loss(comp, Tcut=cut_e)
+    return Workload(mp, pusher((0.0, 0.0, -efield), cl=cl), dt, 1.0, "rrea-air-0.5MVm")

@@ -1,0 +1,147 @@
+"""GPU parity: the device step against the CPU oracle on identical inputs.
+
+Both sides consume the same per-particle Philox streams, so for every particle
+whose decisions are not within FP32 rounding of a threshold (the oracle's
+tie flag) the draw counters, surviving stream ids and collision choices must
+be identical, and momenta, s and positions must agree within 1e-5 relative
+(FP32 device vs Float64 oracle).
+"""
+import numpy as np
+import pytest
+
+from conftest import random_population
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5   # relative tolerance on momenta (FP32 device vs Float64 oracle)
+
+
+def _mixed(pcl, air, n=(4096, 2048, 1024), seed=3, **cfg):
+    rng = np.random.default_rng(seed)
+    pops = {pcl.Electron: random_population(pcl, pcl.Electron, n[0], 1e4, 3e7, rng),
+            pcl.Photon: random_population(pcl, pcl.Photon, n[1], 5e3, 3e7, rng),
+            pcl.Positron: random_population(pcl, pcl.Positron, n[2], 1e4, 3e7, rng)}
+    cap = 1 << 16
+    mp = pcl.MultiPopulation(*[(k, pcl.Population(cap, pops[k], air["tabs"][k], air["cuts"][k], particle=k))
+                               for k in pops], seed=seed, **cfg)
+    return mp
+
+
+def _oracle_from(oracle, pcl, mp, air, pusher, tally_only=()):
+    W = oracle.OracleWorld(int(mp.config.seed), air["tabs"], air["cuts"], pusher, tally_only=tally_only)
+    for k in mp.index:
+        if not mp.get(k).tally_only:
+            W.upload(k, mp.get(k).particles())
+    return W
+
+
+def _check(pcl, oracle, mp, W, species=(0, 1, 2), rtol=RTOL):
+    reports = []
+    for k in species:
+        rep = oracle.compare_populations(mp.get(k).particles(), W.download(k), k, rtol=rtol)
+        reports.append(rep)
+        assert rep["ok"], rep
+    return reports
+
+
+def _pusher(pcl, air, E=5e5):
+    return pcl.workloads.pusher((0.0, 0.0, -E), cl=air["cl"])
+
+
+@pytest.mark.parametrize("dt", [1e-12, 25e-12])
+def test_one_step_mixed(pcl, oracle, gpu, air, dt):
+    mp = _mixed(pcl, air, seed=3 if dt < 1e-11 else 4)
+    pusher = _pusher(pcl, air)
+    W = _oracle_from(oracle, pcl, mp, air, pusher)
+    pcl.advance(mp, pusher, dt)
+    W.advance(dt, 4)
+    _check(pcl, oracle, mp, W)
+    t = mp.tallies()
+    c = W.counters()
+    # per-process collision counts agree up to tie-affected lineages
+    diff = np.abs(np.array([list(t.collisions[s]) for s in range(3)]) - c["coll"]).sum()
+    assert diff <= 4 * (c["ties"] + 1), (diff, c["ties"])
+    assert sum(t.errors[q] for q in (2, 3, 5)) == 0, list(t.errors)
+    mp.close()
+
+
+def test_several_steps_then_compare(pcl, oracle, gpu, air):
+    """Ten plain steps of 1 ps: state, secondaries and removals all carry over."""
+    mp = _mixed(pcl, air, n=(2048, 1024, 512), seed=5)
+    pusher = _pusher(pcl, air)
+    W = _oracle_from(oracle, pcl, mp, air, pusher)
+    for k in range(10):
+        pcl.advance(mp, pusher, (k + 1) * 1e-12)
+        W.advance((k + 1) * 1e-12, 4)
+    _check(pcl, oracle, mp, W, rtol=3 * RTOL)
+    mp.close()
+
+
+def test_multistep_launch_matches_plain(pcl, oracle, gpu, air):
+    """Eight steps fused into one launch equal eight oracle steps."""
+    mp = _mixed(pcl, air, n=(2048, 1024, 512), seed=6, steps_per_launch=8)
+    pusher = _pusher(pcl, air)
+    W = _oracle_from(oracle, pcl, mp, air, pusher)
+    opts_dt = 1e-12
+    pcl.run(mp, pusher, 8 * opts_dt, opts_dt)
+    for k in range(8):
+        W.advance((k + 1) * opts_dt, 4)
+    assert mp.tallies().steps == 8
+    _check(pcl, oracle, mp, W, rtol=3 * RTOL)
+    mp.close()
+
+
+def test_electrons_tally_photons(pcl, oracle, gpu):
+    """Electrons-only workload with bremsstrahlung photons tallied."""
+    wl = pcl.workloads.plain_electrons(n=1000, tfinal=20e-12, seed=1)
+    mp, pusher = wl.mpopl, wl.pusher
+    e = mp.get(pcl.Electron)
+    tabs = {pcl.Electron: e.collisions}
+    cuts = {pcl.Electron: e.energy_cut, pcl.Photon: 0.0}
+    W = oracle.OracleWorld(1, tabs, cuts, pusher, tally_only=(pcl.Photon,))
+    W.upload(pcl.Electron, e.particles())
+    for k in range(20):
+        pcl.advance(mp, pusher, (k + 1) * wl.dt)
+        W.advance((k + 1) * wl.dt, 4)
+    rep = oracle.compare_populations(e.particles(), W.download(pcl.Electron), pcl.Electron, rtol=3 * RTOL)
+    assert rep["ok"], rep
+    t = mp.tallies()
+    c = W.counters()
+    assert abs(t.tally_count[1] - c["tally_count"][1]) <= c["ties"] + 1
+    mp.close()
+
+
+def test_compaction_preserves_particles(pcl, gpu, air):
+    mp = _mixed(pcl, air, n=(2048, 1024, 512), seed=8, compaction_period=1000)
+    pusher = _pusher(pcl, air)
+    for k in range(5):
+        pcl.advance(mp, pusher, (k + 1) * 5e-12)
+    before = {k: mp.get(k).particles() for k in mp.index}
+    t = mp.tallies()
+    assert t.n[0] >= t.live[0]
+    pcl.repack(mp.get(0))
+    t2 = mp.tallies()
+    for k in mp.index:
+        after = mp.get(k).particles()
+        assert t2.n[k] == len(after.w) == len(before[k].w)
+        assert np.array_equal(np.sort(after.sid), np.sort(before[k].sid))
+        # order preserving
+        assert np.array_equal(after.sid, before[k].sid)
+    mp.close()
+
+
+def test_moments_match_download(pcl, gpu, air):
+    mp = _mixed(pcl, air, n=(2048, 1024, 512), seed=9)
+    pusher = _pusher(pcl, air)
+    pcl.advance(mp, pusher, 3e-12)
+    for k in mp.index:
+        pop = mp.get(k)
+        a = pop.particles()
+        m = pop.moments()
+        E = pcl.kinenergy(k, a.p)
+        assert m[9] == len(a.w)
+        np.testing.assert_allclose(m[0], a.w.sum(), rtol=1e-12)
+        np.testing.assert_allclose(m[1], (a.w * E).sum(), rtol=1e-5)
+        np.testing.assert_allclose(m[2:5], (a.w[:, None] * a.x).sum(0), rtol=1e-5, atol=1e-12)
+        assert abs(pcl.meanenergy(pop) - (a.w * E).sum() / a.w.sum()) <= 1e-5 * pcl.meanenergy(pop)
+    mp.close()

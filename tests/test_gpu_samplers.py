@@ -1,0 +1,67 @@
+"""Per-process sampler parity: the device sampler (pcl_test_sampler) against
+the oracle's restatement, same stream ids, every process of the three air
+tables.  Draw counts must be identical (same rejection-loop trip counts) and
+all outgoing momenta and s values equal within FP32 tolerance."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-5
+
+# energy windows (eV) where each process is sampled in practice
+WINDOWS = {"RelativisticCoulomb": (1e4, 1e8), "Moller": (2.1e4, 1e8), "SeltzerBerger": (1.1e4, 1e8),
+           "Compton": (5e3, 1e8), "PhotoElectric": (5e3, 1e6), "BetheHeitler": (1.1e6, 1e8),
+           "Bhaba": (2.1e4, 1e8), "PositronAnihilation": (1e4, 1e8), "RBEB": (1e3, 1e7)}
+
+
+def _cases(pcl, air):
+    out = []
+    for sp, tab in air["tabs"].items():
+        for j, proc in enumerate(tab.proc):
+            out.append((sp, j, type(proc).__name__))
+    return out
+
+
+@pytest.fixture(scope="module")
+def ctx(pcl, air, gpu):
+    mp = pcl.MultiPopulation(*[(k, pcl.Population(1024, [], air["tabs"][k], air["cuts"][k], particle=k))
+                               for k in air["tabs"]], seed=2024)
+    mp.set_pusher(pcl.workloads.pusher((0.0, 0.0, -5e5), cl=air["cl"]))
+    yield mp
+    mp.close()
+
+
+def test_all_processes(pcl, oracle, air, ctx):
+    import ctypes as C
+    L = pcl.lib()
+    W = oracle.OracleWorld(2024, air["tabs"], air["cuts"], pcl.workloads.pusher((0.0, 0.0, -5e5), cl=air["cl"]))
+    rng = np.random.default_rng(12)
+    n = 4096
+    for sp, j, name in _cases(pcl, air):
+        lo, hi = WINDOWS[name]
+        E = np.exp(rng.uniform(np.log(lo), np.log(hi), n)) * pcl.co.eV
+        d = pcl.workloads.isotropic(n, 1.0, rng, sp)
+        p = d * (pcl.momentum_norm_from_kin(sp, E) / np.linalg.norm(d, axis=1))[:, None]
+        # the device works in FP32: hand both sides the same FP32-representable input
+        p = (p / pcl.co.electron_mc).astype(np.float32).astype(np.float64) * pcl.co.electron_mc
+        sid = rng.integers(0, 2 ** 63, n, dtype=np.uint64)
+        p = np.ascontiguousarray(p)
+        gp = np.zeros(9 * n); gs = np.zeros(3 * n); gk = np.zeros(3 * n, np.int32); gc = np.zeros(n, np.uint32)
+        rc = L.pcl_test_sampler(ctx.ctx, sp, j, n, pcl._lib.dptr(p.reshape(-1)), pcl._lib.u64ptr(sid),
+                                pcl._lib.dptr(gp), pcl._lib.dptr(gs), pcl._lib.i32ptr(gk), pcl._lib.u32ptr(gc))
+        assert rc == 0, pcl.lib().pcl_last_error(ctx.ctx)
+        op, os_, ok, oc, ot = W.sample(sp, j, p, sid)
+        gp = gp.reshape(n, 3, 3); gs = gs.reshape(n, 3); gk = gk.reshape(n, 3)
+        clean = ot == 0
+        assert clean.mean() > 0.98, (name, clean.mean())
+        assert np.array_equal(gc[clean], oc[clean]), (name, np.nonzero(gc[clean] != oc[clean])[0][:5])
+        assert np.array_equal(gk[clean], ok[clean]), name
+        pn = np.linalg.norm(p, axis=1)[clean]
+        for q in range(3):
+            live = ok[clean][:, q] >= 0
+            dp = np.linalg.norm(gp[clean][:, q] - op[clean][:, q], axis=1)[live] / pn[live]
+            if live.any():
+                assert dp.max() <= RTOL, (name, q, dp.max(), np.argmax(dp))
+                ds = np.abs(gs[clean][:, q] - os_[clean][:, q])[live] / np.maximum(1, os_[clean][:, q][live])
+                assert ds.max() <= 2 * RTOL, (name, q, ds.max())

@@ -1,0 +1,114 @@
+"""The CPU oracle: its random streams pinned by published known answers, its
+samplers checked against conservation laws, and its step independent of the
+thread count (every particle owns its stream)."""
+import numpy as np
+import pytest
+
+from conftest import random_population
+
+
+def test_philox_known_answers(oracle):
+    """Philox4x32-10 known-answer vectors of the Random123 distribution
+    (Salmon et al., SC'11)."""
+    assert oracle.philox([0, 0, 0, 0], [0, 0]) == [0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8]
+    assert oracle.philox([0xffffffff] * 4, [0xffffffff] * 2) == [0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd]
+    assert oracle.philox([0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344], [0xa4093822, 0x299f31d0]) == \
+        [0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1]
+
+
+@pytest.fixture(scope="module")
+def world(pcl, oracle, air):
+    pusher = pcl.workloads.pusher((0.0, 0.0, -5e5), cl=air["cl"])
+    return oracle.OracleWorld(99, air["tabs"], air["cuts"], pusher), pusher
+
+
+def _sample(pcl, world, sp, j, lo, hi, n=2000, seed=0):
+    W, _ = world
+    rng = np.random.default_rng(seed)
+    E = np.exp(rng.uniform(np.log(lo), np.log(hi), n)) * pcl.co.eV
+    d = pcl.workloads.isotropic(n, 1.0, rng, sp)
+    p = d * (pcl.momentum_norm_from_kin(sp, E) / np.linalg.norm(d, axis=1))[:, None]
+    sid = np.arange(n, dtype=np.uint64) + 1000 * j
+    return p, E, W.sample(sp, j, p, sid)
+
+
+def _energy(pcl, sp, p):
+    return pcl.kinenergy(sp, p)
+
+
+def test_moller_conserves_energy(pcl, world, air):
+    tab = air["tabs"][pcl.Electron]
+    j = [type(q).__name__ for q in tab.proc].index("Moller")
+    p, E, (op, os_, ok, oc, ot) = _sample(pcl, world, pcl.Electron, j, 3e4, 1e8)
+    e1 = _energy(pcl, pcl.Electron, op[:, 0])
+    e2 = _energy(pcl, pcl.Electron, op[:, 1])
+    np.testing.assert_allclose(e1 + e2, E, rtol=1e-9)
+    assert np.all(e2 <= 0.5 * E * (1 + 1e-12)) and np.all(e2 >= tab.proc[j].tcut * (1 - 1e-12))
+    assert np.all(ok[:, 0] == pcl.Electron) and np.all(ok[:, 1] == pcl.Electron)
+
+
+def test_bremsstrahlung_conserves_momentum(pcl, world, air):
+    tab = air["tabs"][pcl.Electron]
+    j = [type(q).__name__ for q in tab.proc].index("SeltzerBerger")
+    p, E, (op, os_, ok, oc, ot) = _sample(pcl, world, pcl.Electron, j, 2e4, 1e8)
+    np.testing.assert_allclose(op[:, 0] + op[:, 1], p, rtol=1e-9, atol=1e-12 * np.abs(p).max())
+    k = np.linalg.norm(op[:, 1], axis=1) * pcl.co.c
+    assert np.all(k < E)
+    assert np.all(ok[:, 1] == pcl.Photon)
+
+
+def test_coulomb_keeps_momentum_norm(pcl, world, air):
+    tab = air["tabs"][pcl.Electron]
+    j = [type(q).__name__ for q in tab.proc].index("RelativisticCoulomb")
+    p, E, (op, os_, ok, oc, ot) = _sample(pcl, world, pcl.Electron, j, 1e4, 1e8)
+    np.testing.assert_allclose(np.linalg.norm(op[:, 0], axis=1), np.linalg.norm(p, axis=1), rtol=1e-12)
+    # 1 (phi) + 2 per rejection iteration + 1 (s): odd, >= 4
+    assert np.all(oc >= 4) and np.all(oc % 2 == 0)
+
+
+def test_compton_and_annihilation_conserve_momentum(pcl, world, air):
+    gt = air["tabs"][pcl.Photon]
+    j = [type(q).__name__ for q in gt.proc].index("Compton")
+    p, E, (op, os_, ok, oc, ot) = _sample(pcl, world, pcl.Photon, j, 5e3, 1e8)
+    np.testing.assert_allclose(op[:, 0] + op[:, 1], p, rtol=1e-9, atol=1e-12 * np.abs(p).max())
+    pt = air["tabs"][pcl.Positron]
+    j = [type(q).__name__ for q in pt.proc].index("PositronAnihilation")
+    p, E, (op, os_, ok, oc, ot) = _sample(pcl, world, pcl.Positron, j, 1e4, 1e8)
+    np.testing.assert_allclose(op[:, 1] + op[:, 2], p, rtol=1e-9, atol=1e-12 * np.abs(p).max())
+    assert np.all(ok[:, 0] == -1) and np.all(ok[:, 1:] == pcl.Photon)
+    # total energy E + 2 m c^2 is shared by the two photons
+    eg = (np.linalg.norm(op[:, 1], axis=1) + np.linalg.norm(op[:, 2], axis=1)) * pcl.co.c
+    np.testing.assert_allclose(eg, E + 2 * pcl.co.electron_mc2, rtol=1e-6)
+
+
+def test_pair_production_energy(pcl, world, air):
+    gt = air["tabs"][pcl.Photon]
+    j = [type(q).__name__ for q in gt.proc].index("BetheHeitler")
+    p, E, (op, os_, ok, oc, ot) = _sample(pcl, world, pcl.Photon, j, 1.2e6, 1e8)
+    ee = _energy(pcl, pcl.Electron, op[:, 1]) + _energy(pcl, pcl.Positron, op[:, 2])
+    np.testing.assert_allclose(ee, E - 2 * pcl.co.electron_mc2, rtol=1e-9, atol=1e-22)
+    assert np.all(ok[:, 1] == pcl.Electron) and np.all(ok[:, 2] == pcl.Positron)
+
+
+def test_step_is_thread_count_independent(pcl, oracle, air):
+    pusher = pcl.workloads.pusher((0.0, 0.0, -5e5), cl=air["cl"])
+    rng = np.random.default_rng(4)
+    res = []
+    for nt in (1, 3, 8):
+        W = oracle.OracleWorld(5, air["tabs"], air["cuts"], pusher)
+        for sp, n, lo, hi in ((0, 3000, 1e4, 1e7), (1, 500, 5e3, 1e7), (2, 200, 1e4, 1e7)):
+            a = random_population(pcl, sp, n, lo, hi, np.random.default_rng(10 + sp))
+            W.upload(sp, oracle.Arrays(a.x, a.p, a.w, a.t, np.full(n, 0.7), np.arange(n, dtype=np.uint64) + 10 ** 6 * sp,
+                                       np.zeros(n, np.uint32)))
+        for k in range(5):
+            W.advance((k + 1) * 5e-12, nt)
+        out = []
+        for sp in range(3):
+            d = W.download(sp)
+            o = np.argsort(d.sid)
+            out.append((d.sid[o], d.ctr[o], d.p[o], d.x[o]))
+        res.append(out)
+    for r in res[1:]:
+        for a, b in zip(res[0], r):
+            for u, v in zip(a, b):
+                assert np.array_equal(u, v)

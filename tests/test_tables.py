@@ -1,0 +1,111 @@
+"""Host table builders (C++ in the library) against the independent numpy
+restatement in oracle/tables_ref.py, plus properties the reference relies on."""
+import numpy as np
+import pytest
+
+from oracle import tables_ref as ref
+
+
+@pytest.fixture(scope="module")
+def comp(pcl):
+    return pcl.workloads.air_composition()
+
+
+def _grid():
+    return np.exp(np.linspace(np.log(1.5e3), np.log(2.5e8), 400)) * ref.eV
+
+
+def test_totalcs_every_process(pcl, comp):
+    E = _grid()
+    procs = (pcl.workloads.electron_processes(comp) + pcl.workloads.photon_processes(comp)
+             + pcl.workloads.positron_processes(comp))
+    for _, p in procs:
+        got = pcl.totalcs(p, E)
+        want = ref.totalcs(p, E)
+        both = np.isfinite(want)
+        assert np.array_equal(np.isfinite(got), both), type(p).__name__
+        np.testing.assert_allclose(got[both], want[both], rtol=1e-11, atol=1e-40, err_msg=type(p).__name__)
+
+
+def test_known_cross_section_values(pcl):
+    """Published values the formulas must reproduce: Klein-Nishina per electron at
+    1 MeV is 0.2112 b (L&L 86); BH vanishes below 2 m c^2."""
+    kn = pcl.KleinNishinaCompton(1)
+    assert abs(pcl.totalcs(kn, 1e6 * ref.eV) / 1e-28 - 0.2112) < 5e-4
+    assert pcl.totalcs(pcl.BetheHeitler(7), 1.0e6 * ref.eV) == 0.0
+    assert pcl.totalcs(pcl.Moller(7, 1e4 * ref.eV), 1.5e4 * ref.eV) == 0.0  # x = tcut/E > 1/2 -> max(0, <0)
+
+
+def test_sb_table_matches_restatement(pcl):
+    sb = pcl.SeltzerBerger(7)
+    _, x, y, value = pcl.data.read_g4_2dvector(pcl.data.sb_path(7))
+    le, tcs, data = ref.sb_build(7, x, y, value)
+    np.testing.assert_allclose(sb.log_energy, le, rtol=1e-15)
+    np.testing.assert_allclose(sb.totalcs, tcs, rtol=1e-12)
+    np.testing.assert_allclose(sb.table(), data, rtol=1e-9, atol=1e-9)
+    # inverse CDF: monotone in pcum, ends at the integration limits
+    t = sb.table()
+    assert np.all(np.diff(t, axis=0) >= -1e-12)
+    # pcum = 1 -> upper limit min(log(gamma_max / T), log 1) (seltzer.jl:184)
+    T = np.exp(sb.log_energy)
+    np.testing.assert_allclose(t[-1], np.minimum(np.log(5e7 * ref.eV / T), 0.0), atol=1e-9)
+
+
+@pytest.mark.parametrize("which", ["electron", "photon", "positron"])
+def test_collision_table_matches_restatement(pcl, comp, which):
+    co = pcl.co
+    Fdt = co.elementary_charge * 5e5 * 1e-12
+    procs = {"electron": pcl.workloads.electron_processes(comp),
+             "photon": pcl.workloads.photon_processes(comp),
+             "positron": pcl.workloads.positron_processes(comp)}[which]
+    sp = {"electron": pcl.Electron, "photon": pcl.Photon, "positron": pcl.Positron}[which]
+    F = 0.0 if sp == pcl.Photon else Fdt
+    tab = pcl.collision_table_from_processes(procs, sp, F, safety=1.15)
+    a, rb, perm = ref.collision_table(procs, sp == pcl.Photon, sp != pcl.Photon, F, safety=1.15)
+    assert list(tab.perm) == list(perm)
+    got = tab.rate_array()
+    np.testing.assert_allclose(got, a[:, perm, :], rtol=1e-9, atol=1e-6 * np.abs(a).max())
+    np.testing.assert_allclose(tab.ratebound.reshape(-1, tab.order).T, rb, rtol=1e-9, atol=1e-6 * np.abs(rb).max())
+
+
+def test_positron_table_order_reference_quirk(pcl, comp):
+    """Bhabha and annihilation cross sections are NaN at E = 0; Julia's
+    sortperm(rev=true) puts NaN keys first (collision_table.jl:141-145)."""
+    tab = pcl.collision_table_from_processes(pcl.workloads.positron_processes(comp), pcl.Positron, 0.0)
+    names = [type(p).__name__ for p in tab.proc]
+    assert names == ["Bhaba", "Bhaba", "PositronAnihilation", "PositronAnihilation", "RelativisticCoulomb",
+                     "RelativisticCoulomb"]
+
+
+def test_ratebound_bounds_rates(pcl, comp):
+    """ratebound >= sum of rates on a dense grid above the cut (the null-collision
+    method's requirement, collisions.jl:156-161)."""
+    co = pcl.co
+    Fdt = co.elementary_charge * 5e5 * 1e-12
+    tab = pcl.collision_table_from_processes(pcl.workloads.electron_processes(comp), pcl.Electron, Fdt, safety=1.15)
+    for E in np.exp(np.linspace(np.log(1e4), np.log(2e8), 600)) * co.eV:
+        s = sum(tab.rate_at(j, E) for j in range(tab.nproc))
+        assert tab.ratebound_at(E) >= s * (1 - 1e-12), E / co.eV
+
+
+def test_chebfit_exact_on_polynomials(pcl):
+    """An order-n fit reproduces polynomials of degree < n to rounding."""
+    k, xmax, n = 10, 1.0, 3
+    a = ref.chebfit(lambda x: 3 * x * x - 2 * x + 0.5, k, xmax, n)
+    x = np.linspace(1e-6, 0.999, 200)
+    np.testing.assert_allclose(ref.chebeval(x, k, xmax, a), 3 * x * x - 2 * x + 0.5, rtol=1e-12, atol=1e-12)
+
+
+def test_continuum_loss_matches_restatement(pcl, comp):
+    co = pcl.co
+    nel = 14 * comp["N2"] + 16 * comp["O2"]
+    cl = pcl.ChebContinuumLoss.build(pcl.ContinuumLoss(nel, 85.7 * co.eV, 1e4 * co.eV), 2.6e8 * co.eV, 3)
+    k, xmax = cl.bints.k, cl.bints.xmax
+    assert abs(xmax - 2 ** k * 1e4 * co.eV) < 1e-30
+    ec = ref.chebfit(lambda E: ref.energy_loss(nel, 85.7 * co.eV, 1e4 * co.eV, False, E), k, xmax, 3)
+    pc = ref.chebfit(lambda E: ref.energy_loss(nel, 85.7 * co.eV, 1e4 * co.eV, True, E), k, xmax, 3)
+    np.testing.assert_allclose(cl.ec.reshape(k + 1, 3).T, ec, rtol=1e-10)
+    np.testing.assert_allclose(cl.pc.reshape(k + 1, 3).T, pc, rtol=1e-10)
+    # restricted stopping power of 1 MeV electrons in air: ~0.16 MeV/m (below the 0.2 MeV/m total)
+    f = cl.force_magnitude(pcl.Electron, 1e6 * co.eV) / (1e6 * co.eV)
+    assert 0.12 < f < 0.2
