@@ -216,7 +216,9 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--n", type=int, default=1 << 24, help="seed electrons")
     ap.add_argument("--e2e-steps", type=int, default=5)
-    ap.add_argument("--cpu-sample", type=int, default=1 << 17)
+    ap.add_argument("--cpu-sample", type=int, default=1 << 21)
+    ap.add_argument("--cpu-steps", type=int, default=48)
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--steps-per-launch", type=int, default=1)
     args = ap.parse_args()
@@ -266,6 +268,8 @@ def main():
     # ---- end to end through the C ABI with pinned host buffers
     e2e = None
     try:
+        if args.no_e2e:
+            raise RuntimeError("skipped (--no-e2e)")
         import torch
         caps = [mp.get(s).max_particles for s in (0, 1, 2)]
         host = []
@@ -308,9 +312,9 @@ def main():
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, el, ps = cpu_reference(pcl, args.cpu_sample, 8, threads)
+        v, el, ps = cpu_reference(pcl, args.cpu_sample, args.cpu_steps, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_sample} e- at 1 MeV isotropic, 8 steps of 1 ps after 1 warm-up "
+               "sample": f"{args.cpu_sample} e- at 1 MeV isotropic, {args.cpu_steps} steps of 1 ps after 1 warm-up "
                          f"({ps} particle-steps, {el:.1f} s), C++ Float64 oracle"}
     errs = {pcl._lib.ERROR_NAMES[q]: int(tal1.errors[q]) for q in range(8) if tal1.errors[q]}
     if rank == 0:

@@ -174,7 +174,7 @@ def philox(ctr, key):
     return list(o)
 
 
-def compare_populations(gpu, orc, species, rtol=1e-5, xtol=None, max_unmatched_frac=0.01):
+def compare_populations(gpu, orc, species, rtol=1e-5, xtol=None, max_unmatched_frac=0.01, stol=None):
     """Match GPU and oracle particles by stream id.  Oracle particles not in a
     tie lineage must exist on the GPU with the same draw counter, and
     momenta / s / positions within tolerance.  Returns a report dict."""
@@ -215,6 +215,7 @@ def compare_populations(gpu, orc, species, rtol=1e-5, xtol=None, max_unmatched_f
     extra = len(gpu.w) - len(ig)
     rep["gpu_unmatched"] = int(extra)
     tie_budget = int(orc.tie.sum()) + max(2, int(max_unmatched_frac * max(1, len(orc.w))))
-    rep["ok"] = (missing == 0 and bad_ctr == 0 and rep["max_dp_rel"] <= rtol and rep["max_ds"] <= 2 * rtol
+    stol = 2 * rtol if stol is None else stol
+    rep["ok"] = (missing == 0 and bad_ctr == 0 and rep["max_dp_rel"] <= rtol and rep["max_ds"] <= stol
                  and rep["max_dx_rel"] <= 10 * rtol and rep["w_equal"] and extra <= tie_budget)
     return rep

@@ -209,8 +209,10 @@ static inline double kinenergy(int species, const double* p) {
 }
 
 // ---- Chebyshev on binary intervals ----
-// precheb (cheby.jl:127-143); x >= xmax extrapolates the last interval
-static inline int precheb(double x, int k, double xmax, int n, double* t, bool& oor) {
+// precheb (cheby.jl:127-143); x >= xmax extrapolates the last interval.
+// *edge = relative distance of x to the nearest interval boundary (the
+// piecewise fits are discontinuous there at the level of the fit error).
+static inline int precheb(double x, int k, double xmax, int n, double* t, bool& oor, double* edge = nullptr) {
     double x1 = x / xmax;
     int l = 0;
     double s = std::frexp(x1, &l);
@@ -218,9 +220,11 @@ static inline int precheb(double x, int k, double xmax, int n, double* t, bool& 
     double xi;
     if (i > 0) {
         xi = 4 * s - 3;
+        if (edge) *edge = std::min((s - 0.5) / 0.5, (1.0 - s));
         if (i > k) { oor = true; i = k; xi = 4 * x1 - 3; }
     } else {
         xi = std::ldexp(1.0, k + 1) * x1 - 1;
+        if (edge) *edge = (1.0 - xi) / 2;
         i = 0;
     }
     t[0] = 1.0;
@@ -238,8 +242,10 @@ static double setr(Walker& Wk, int species) {
     const Table& T = S.tab;
     double t[4];
     bool oor = false;
-    int i = precheb(eng, T.k, T.xmax, T.order, t, oor);
+    double edge = 1.0;
+    int i = precheb(eng, T.k, T.xmax, T.order, t, oor, &edge);
     if (oor) Wk.err(E_TABLE_RANGE);
+    if (T.nproc > 0) Wk.near(edge, 0.0, 1.0);
     double r = 0.0;
     for (int q = 0; q < T.order; ++q) r += T.rb[q + T.order * i] * t[q];
     if (!(r > 0)) {
@@ -743,8 +749,10 @@ static void do_one_collision(Walker& Wk, int species, SpawnBuf& out) {
     const Table& T = S.tab;
     double t[4];
     bool oor = false;
-    int i = precheb(eng, T.k, T.xmax, T.order, t, oor);
+    double edge = 1.0;
+    int i = precheb(eng, T.k, T.xmax, T.order, t, oor, &edge);
     if (oor) Wk.err(E_TABLE_RANGE);
+    Wk.near(edge, 0.0, 1.0);
     uint32_t ctr0 = L.ctr;
     double xi = Wk.rand() * L.r;
     int j = 0;

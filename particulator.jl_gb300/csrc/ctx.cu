@@ -67,7 +67,7 @@ struct SpeciesState {
 struct SBTable {
     int Z, ne, ncum;
     std::vector<double> log_energy;  // log J
-    const double* key_ptr;           // caller's aux2 (identity)
+    std::vector<double> data;        // host copy of the inverse-CDF table (identity)
     float* d_data = nullptr;         // [ne][ncum]
 };
 
@@ -306,7 +306,7 @@ static int build_blob(Ctx* c) {
     return PCL_OK;
 }
 
-static StepArgs make_args(Ctx* c, float dt, int nsteps, int spill_mode, int sp_in) {
+static StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, int sp_in) {
     StepArgs A;
     std::memset(&A, 0, sizeof(A));
     for (int s = 0; s < 3; ++s) {
@@ -390,7 +390,7 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
     int rc = build_blob(c);
     if (rc) return rc;
     if ((rc = ensure_spill(c))) return rc;
-    const float dt = float(t_to_dev(dt_si));
+    const double dt = t_to_dev(dt_si);
     const int threads = block_threads(c);
     const size_t smem = step_smem_bytes(int(c->blob.size()), threads);
     CK(cudaFuncSetAttribute(k_step, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
@@ -576,16 +576,19 @@ int pcl_set_collision_table(void* ctx, int species, int order, int nproc, int ni
             if (!P.aux0 || !P.aux2 || P.naux < 2 || P.naux2 < 2)
                 return fail(c, PCL_ERR_INVALID, "Seltzer-Berger process needs log_energy and data");
             int found = -1;
+            // one device table per distinct inverse-CDF content (the reference's
+            // SeltzerBerger struct carries no Z, and every Z shares one energy grid)
             for (size_t b = 0; b < c->sb.size(); ++b)
-                if (c->sb[b].Z == P.Z && c->sb[b].ne == P.naux && c->sb[b].ncum == P.naux2 &&
-                    c->sb[b].log_energy == std::vector<double>(P.aux0, P.aux0 + P.naux))
+                if (c->sb[b].ne == P.naux && c->sb[b].ncum == P.naux2 &&
+                    c->sb[b].log_energy == std::vector<double>(P.aux0, P.aux0 + P.naux) &&
+                    c->sb[b].data == std::vector<double>(P.aux2, P.aux2 + size_t(P.naux) * P.naux2))
                     found = int(b);
             if (found < 0) {
                 if (c->sb.size() >= PCL_MAX_SB) return fail(c, PCL_ERR_UNSUPPORTED, "too many SB tables");
                 SBTable T;
                 T.Z = P.Z; T.ne = P.naux; T.ncum = P.naux2;
                 T.log_energy.assign(P.aux0, P.aux0 + P.naux);
-                T.key_ptr = P.aux2;
+                T.data.assign(P.aux2, P.aux2 + size_t(P.naux) * P.naux2);
                 std::vector<float> f(size_t(T.ne) * T.ncum);
                 for (size_t q = 0; q < f.size(); ++q) f[q] = float(P.aux2[q]);
                 CK(cudaMalloc(&T.d_data, f.size() * sizeof(float)));
@@ -985,7 +988,7 @@ int pcl_test_sampler(void* ctx, int species, int proc_index, int64_t n, const do
     CK(h2d(c, dsid, hs.data(), sizeof(uint32_t) * 2 * n));
     CK(cudaMemsetAsync(dop, 0, sizeof(float) * 9 * n, c->stream));
     CK(cudaMemsetAsync(dos, 0, sizeof(float) * 3 * n, c->stream));
-    StepArgs A = make_args(c, 0.0f, 1, 0, 0);
+    StepArgs A = make_args(c, 0.0, 1, 0, 0);
     size_t smem = c->blob.size() + 16;
     CK(cudaFuncSetAttribute(k_test_sampler, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     int blocks = int((n + 127) / 128);

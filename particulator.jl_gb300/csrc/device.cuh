@@ -107,7 +107,7 @@ struct StepArgs {
     double* hist_w[3];                   // tally-only histogram weights (device)
     unsigned long long* hist_n[3];       // tally-only histogram counts (device)
     uint32_t key0, key1;                 // Philox key
-    float dt;                            // step length (ns)
+    double dt;                           // step length (ns)
     int nsteps;                          // steps in this launch
     int spill_mode;                      // 0: populations, 1: spill queue
     int blob_bytes;

@@ -63,7 +63,8 @@ __device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32
 struct Lane {
     float x, y, z, w;
     float px, py, pz, s;
-    float r, tl;
+    float r;
+    double trem;               // time left in the current step (ns, FP64 bookkeeping)
     uint32_t sid_lo, sid_hi, ctr;
     uint32_t c0, c1, c2, c3;   // Philox words not yet consumed (front = c0)
     int slot;                  // input slot, or -1 for a secondary (appended on finish)
@@ -323,7 +324,7 @@ __device__ void emit(Lane& L, const KCtx& K, int sp, float cpx, float cpy, float
     atomicAdd(&K.tal[T_SPAWN + sp], 1u);
     float4 e0 = make_float4(L.x, L.y, L.z, L.w);
     float4 e1 = make_float4(cpx, cpy, cpz, cs);
-    uint4 e2 = make_uint4(slo, shi, uint32_t(sp) | (uint32_t(L.k) << 2), __float_as_uint(L.tl));
+    uint4 e2 = make_uint4(slo, shi, uint32_t(sp) | (uint32_t(L.k) << 2), __float_as_uint(float(L.trem)));
     int pos = atomicAdd(K.top, 1);
     if (pos < kWarpStack) {
         K.stk[3 * pos + 0] = e0;
@@ -489,17 +490,29 @@ __device__ void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t
 }
 
 // compton.jl:9-28, 119-144 (Compton and KleinNishinaCompton share the sampler)
+// 1 - eps is carried explicitly (-expm1 in the first branch,
+// (1 - e0^2)(1 - U)/(1 + eps) in the second): eps -> 1 for low-energy photons
+// and the direct difference would lose most of its FP32 bits.
 __device__ void s_compton(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
     const float e0 = 1.0f / (1.0f + 2.0f * E);
     const float a1 = log1pf(2.0f * E);
-    const float a2 = (1.0f - e0 * e0) * 0.5f;
+    const float ome0sq = (2.0f * E * e0) * (1.0f + e0);   // 1 - e0^2
+    const float a2 = ome0sq * 0.5f;
     const float pa = a1 / (a1 + a2);
     float eps = 1.0f, t = 0.0f;
     int it = 0;
     for (;;) {
-        if (U(L, K) < pa) eps = expf(-U(L, K) * a1);
-        else eps = sqrtf(e0 * e0 + (1.0f - e0 * e0) * U(L, K));
-        t = (1.0f - eps) / (eps * E);
+        float om;
+        if (U(L, K) < pa) {
+            float q = -U(L, K) * a1;
+            eps = expf(q);
+            om = -expm1f(q);
+        } else {
+            float u = U(L, K);
+            eps = sqrtf(e0 * e0 + ome0sq * u);
+            om = ome0sq * (1.0f - u) / (1.0f + eps);
+        }
+        t = om / (eps * E);
         float g = 1.0f - eps / (1.0f + eps * eps) * t * (2.0f - t);
         if (U(L, K) < g) break;
         if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
@@ -768,7 +781,8 @@ __device__ __forceinline__ void load_slot(Lane& L, const float4* xw, const float
     uint4 m = meta[slot];
     L.x = a.x; L.y = a.y; L.z = a.z; L.w = a.w;
     L.px = b.x; L.py = b.y; L.pz = b.z; L.s = b.w;
-    L.sid_lo = m.x; L.sid_hi = m.y; L.ctr = m.z; L.tl = __uint_as_float(m.w);
+    L.sid_lo = m.x; L.sid_hi = m.y; L.ctr = m.z;
+    L.trem = -double(__uint_as_float(m.w));  // + dt by the caller (t_off <= 0 is time still owed)
 }
 
 // ------------------------------------------------------------ the step ---
@@ -806,7 +820,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
     K.ncap = nullptr;
 
     Control* ctl = A.ctl;
-    const float dt = A.dt;
+    const double dt = A.dt;
     const int nsteps = A.nsteps;
 
     // work space: concatenated species ranges, or the spill queue
@@ -844,7 +858,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
                 L.sid_lo = __float_as_uint(c.x); L.sid_hi = __float_as_uint(c.y);
                 uint32_t sk = __float_as_uint(c.z);
                 L.species = int(sk & 3u); L.k = int(sk >> 2);
-                L.tl = c.w;
+                L.trem = double(c.w);
                 L.ctr = 0u; L.rvalid = false; L.slot = -1; L.alive = true; L.nsub = 0;
                 L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz));
                 has = true;
@@ -882,7 +896,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
                         L.px = b.x; L.py = b.y; L.pz = b.z; L.s = b.w;
                         L.sid_lo = m.x; L.sid_hi = m.y;
                         L.species = int(m.z & 3u); L.k = int(m.z >> 2);
-                        L.tl = __uint_as_float(m.w);
+                        L.trem = double(__uint_as_float(m.w));
                         L.ctr = 0u; L.slot = -1;
                         has = true;
                     } else {
@@ -892,6 +906,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
                         else { sp = 2; sl = v - nsp0 - nsp1; }
                         L.species = sp;
                         load_slot(L, A.xw[sp], A.ps[sp], A.meta[sp], sl);
+                        L.trem += dt;
                         L.slot = int(sl);
                         L.k = 0;
                         has = (L.ctr != PCL_DEAD_CTR);
@@ -916,20 +931,18 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
         int fin = 0;  // 1: survives the launch, 2: removed
         if (has) {
             const SpeciesHdr& S = H->sp[L.species];
-            const float tb = float(L.k + 1) * dt;
-            const float trem = tb - L.tl;
-            if (L.alive && trem > kEpsT && L.nsub < kSubstepCap) {
+            if (L.alive && L.trem > double(kEpsT) && L.nsub < kSubstepCap) {
                 float tnext = L.s / L.r;
-                bool coll = trem > tnext;
-                float h = coll ? tnext : trem;
+                bool coll = L.trem > double(tnext);
+                float h = coll ? tnext : float(L.trem);
                 if (!coll) L.s -= h * L.r;
                 push(L, S, K, h);
-                L.tl = coll ? (L.tl + h) : tb;
+                L.trem = coll ? (L.trem - double(tnext)) : 0.0;
                 L.nsub += 1;
                 if (coll) collide(L, K, S);
                 if (!L.alive) fin = 2;
             } else {
-                if (L.nsub >= kSubstepCap) { err(K, PCL_E_SUBSTEP_CAP); L.tl = tb; }
+                if (L.nsub >= kSubstepCap) { err(K, PCL_E_SUBSTEP_CAP); L.trem = 0.0; }
                 if (!L.alive) {
                     fin = 2;
                 } else {
@@ -943,6 +956,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
                         } else {
                             L.k += 1;
                             L.nsub = 0;
+                            L.trem += dt;  // remainder below eps(Float64) carries over (mixed_population.jl:65)
                             L.r = setr(S, K, E);  // advance_init! of the next step
                             atomicAdd(&tal[T_LSTART + L.k], 1u);
                         }
@@ -963,10 +977,9 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
             if (grp & (1u << lane)) {
                 long long slot = (long long)base + __popc(grp & lt);
                 if (slot < A.cap[lsp]) {
-                    float tb = float(L.k + 1) * dt;
                     A.xw[lsp][slot] = make_float4(L.x, L.y, L.z, L.w);
                     A.ps[lsp][slot] = make_float4(L.px, L.py, L.pz, L.s);
-                    A.meta[lsp][slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(L.tl - tb));
+                    A.meta[lsp][slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-float(L.trem)));
                 } else {
                     err(K, PCL_E_CAPACITY);
                 }
@@ -974,11 +987,10 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
             am &= ~grp;
         }
         if (fin == 1 && L.slot >= 0) {
-            float tb = float(L.k + 1) * dt;
             const int sp = L.species;
             A.xw[sp][L.slot] = make_float4(L.x, L.y, L.z, L.w);
             A.ps[sp][L.slot] = make_float4(L.px, L.py, L.pz, L.s);
-            A.meta[sp][L.slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(L.tl - tb));
+            A.meta[sp][L.slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-float(L.trem)));
         } else if (fin == 2 && L.slot >= 0) {
             A.meta[L.species][L.slot].z = PCL_DEAD_CTR;
             atomicAdd(&tal[T_DEAD + L.species], 1u);
@@ -1176,7 +1188,7 @@ __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, cons
     K.H = H; K.blob = reinterpret_cast<const float*>(smem); K.stk = nullptr; K.top = nullptr; K.tal = tal;
     K.A = &A; K.cap = capbuf; K.ncap = &ncap;
     Lane L;
-    L.x = L.y = L.z = 0.0f; L.w = 1.0f; L.tl = 0.0f; L.k = 0; L.s = 0.0f;
+    L.x = L.y = L.z = 0.0f; L.w = 1.0f; L.trem = 0.0; L.k = 0; L.s = 0.0f;
     L.px = p_in[3 * i]; L.py = p_in[3 * i + 1]; L.pz = p_in[3 * i + 2];
     L.sid_lo = sid[2 * i]; L.sid_hi = sid[2 * i + 1]; L.ctr = 0u; L.rvalid = false;
     L.species = species; L.alive = true; L.slot = -1; L.nsub = 0;

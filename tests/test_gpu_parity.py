@@ -35,12 +35,12 @@ def _oracle_from(oracle, pcl, mp, air, pusher, tally_only=()):
     return W
 
 
-def _check(pcl, oracle, mp, W, species=(0, 1, 2), rtol=RTOL):
+def _check(pcl, oracle, mp, W, species=(0, 1, 2), rtol=RTOL, stol=None):
     reports = []
     for k in species:
-        rep = oracle.compare_populations(mp.get(k).particles(), W.download(k), k, rtol=rtol)
+        rep = oracle.compare_populations(mp.get(k).particles(), W.download(k), k, rtol=rtol, stol=stol)
         reports.append(rep)
-        assert rep["ok"], rep
+        assert rep["ok"], str(rep)
     return reports
 
 
@@ -55,7 +55,9 @@ def test_one_step_mixed(pcl, oracle, gpu, air, dt):
     W = _oracle_from(oracle, pcl, mp, air, pusher)
     pcl.advance(mp, pusher, dt)
     W.advance(dt, 4)
-    _check(pcl, oracle, mp, W)
+    # s after a step carries the FP32 rate-bound error (~1e-6 relative) once per
+    # collision: ~r dt collisions per step, ~75 at 25 ps
+    _check(pcl, oracle, mp, W, stol=2 * RTOL * max(1.0, dt / 1e-12 / 3))
     t = mp.tallies()
     c = W.counters()
     # per-process collision counts agree up to tie-affected lineages
@@ -104,7 +106,7 @@ def test_electrons_tally_photons(pcl, oracle, gpu):
         pcl.advance(mp, pusher, (k + 1) * wl.dt)
         W.advance((k + 1) * wl.dt, 4)
     rep = oracle.compare_populations(e.particles(), W.download(pcl.Electron), pcl.Electron, rtol=3 * RTOL)
-    assert rep["ok"], rep
+    assert rep["ok"], str(rep)
     t = mp.tallies()
     c = W.counters()
     assert abs(t.tally_count[1] - c["tally_count"][1]) <= c["ties"] + 1

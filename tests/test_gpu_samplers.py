@@ -38,6 +38,7 @@ def test_all_processes(pcl, oracle, air, ctx):
     W = oracle.OracleWorld(2024, air["tabs"], air["cuts"], pcl.workloads.pusher((0.0, 0.0, -5e5), cl=air["cl"]))
     rng = np.random.default_rng(12)
     n = 4096
+    failures = []
     for sp, j, name in _cases(pcl, air):
         lo, hi = WINDOWS[name]
         E = np.exp(rng.uniform(np.log(lo), np.log(hi), n)) * pcl.co.eV
@@ -54,14 +55,23 @@ def test_all_processes(pcl, oracle, air, ctx):
         op, os_, ok, oc, ot = W.sample(sp, j, p, sid)
         gp = gp.reshape(n, 3, 3); gs = gs.reshape(n, 3); gk = gk.reshape(n, 3)
         clean = ot == 0
-        assert clean.mean() > 0.98, (name, clean.mean())
-        assert np.array_equal(gc[clean], oc[clean]), (name, np.nonzero(gc[clean] != oc[clean])[0][:5])
-        assert np.array_equal(gk[clean], ok[clean]), name
+        if clean.mean() <= 0.98:
+            failures.append((name, "ties", clean.mean()))
+        if not np.array_equal(gc[clean], oc[clean]):
+            failures.append((name, "draws", np.nonzero(gc[clean] != oc[clean])[0][:5]))
+            continue
+        if not np.array_equal(gk[clean], ok[clean]):
+            failures.append((name, "kinds"))
+            continue
         pn = np.linalg.norm(p, axis=1)[clean]
         for q in range(3):
             live = ok[clean][:, q] >= 0
             dp = np.linalg.norm(gp[clean][:, q] - op[clean][:, q], axis=1)[live] / pn[live]
             if live.any():
-                assert dp.max() <= RTOL, (name, q, dp.max(), np.argmax(dp))
+                if dp.max() > RTOL:
+                    i = np.argmax(dp)
+                    failures.append((name, q, "dp", float(dp.max()), float(E[clean][live][i] / pcl.co.eV)))
                 ds = np.abs(gs[clean][:, q] - os_[clean][:, q])[live] / np.maximum(1, os_[clean][:, q][live])
-                assert ds.max() <= 2 * RTOL, (name, q, ds.max())
+                if ds.max() > 2 * RTOL:
+                    failures.append((name, q, "ds", float(ds.max())))
+    assert not failures, failures
