@@ -116,7 +116,8 @@ typedef struct pcl_config {
     int32_t  steps_per_launch; /* time steps fused into one launch (0/1 = one)        */
     int32_t  compaction_period;/* compact dead slots every this many steps (0 = 1)    */
     int32_t  use_graph;        /* capture the step sequence of pcl_run in a CUDA graph */
-    int32_t  reserved[4];
+    int32_t  blocks_per_sm;    /* resident step-kernel blocks per SM: 2, 3 or 4 (0 = 4) */
+    int32_t  reserved[3];
 } pcl_config;
 
 /* ---- per-context tallies (FP64 / int64 on the device) -------------------- */

@@ -670,6 +670,13 @@ static void s_ann(Walker& Wk, double eng) {
         if (it + 1 >= REJECT_CAP) { Wk.err(E_REJECT_CAP); break; }
     }
     double cth = (eps * (g + 1) - 1) / (eps * std::sqrt(g * g - 1));
+    // Near the kinematic limits eps -> eps_min/max, sin(theta) ~ sqrt(q - 2|eps - 1/2|)
+    // has an infinite derivative: the FP32 rounding of E alone moves the photon
+    // directions there, so that window (1e-3 of q) is an ill-conditioned tie.
+    {
+        double q = std::sqrt((g - 1) / (g + 1));
+        Wk.near(2 * std::fabs(eps - 0.5), q, 50.0 * q);
+    }
     double phi = 2 * pi * Wk.rand();
     double Etot = eng + 2 * mc2;
     double pa[3];

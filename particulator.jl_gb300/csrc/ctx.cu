@@ -14,7 +14,7 @@
 #include "../../include/particulator_gb300.h"
 
 namespace pcl {
-__global__ void k_step(StepArgs A);
+cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A);
 __global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long cap2);
 __global__ void k_begin_spill(Control* ctl, unsigned long long* in_n, unsigned long long* out_n);
 
@@ -336,9 +336,14 @@ static StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, int sp_
     return A;
 }
 
+static int blocks_per_sm(Ctx* c) {
+    int b = c->cfg.blocks_per_sm;
+    return (b >= 2 && b <= 4) ? b : 4;
+}
+
 static int grid_blocks(Ctx* c) {
     if (c->cfg.grid_blocks > 0) return c->cfg.grid_blocks;
-    return 2 * c->sm_count;
+    return blocks_per_sm(c) * c->sm_count;
 }
 
 static int block_threads(Ctx* c) {
@@ -393,13 +398,11 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
     const double dt = t_to_dev(dt_si);
     const int threads = block_threads(c);
     const size_t smem = step_smem_bytes(int(c->blob.size()), threads);
-    CK(cudaFuncSetAttribute(k_step, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     k_begin<<<1, 64, 0, c->stream>>>(c->d_ctl, c->sp[0].cap, c->sp[1].cap, c->sp[2].cap);
     CK(cudaMemsetAsync(c->d_spn, 0, 2 * sizeof(unsigned long long), c->stream));
     StepArgs A = make_args(c, dt, nsteps, 0, 0);
     CK(cudaEventRecord(c->ev_k0, c->stream));
-    k_step<<<grid_blocks(c), threads, smem, c->stream>>>(A);
-    CK(cudaGetLastError());
+    CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, A));
     CK(cudaEventRecord(c->ev_k1, c->stream));
     c->launches += 2;
     if ((rc = readback(c))) return rc;
@@ -426,8 +429,7 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
         CK(h2d(c, c->d_spn + in, &pending, sizeof(pending)));
         k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + in, c->d_spn + (1 - in));
         StepArgs S = make_args(c, dt, nsteps, 1, in);
-        k_step<<<grid_blocks(c), threads, smem, c->stream>>>(S);
-        CK(cudaGetLastError());
+        CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, S));
         c->launches += 2;
         in = 1 - in;
         if (pass == 63) return fail(c, PCL_ERR_TIMEOUT, "spill passes did not drain");

@@ -29,7 +29,7 @@
 
 namespace pcl {
 
-constexpr int   kWarpStack   = 64;          // child-stack entries per warp
+constexpr int   kWarpStack   = 32;          // child-stack entries per warp
 constexpr int   kRejectCap   = 10000;       // rejection-loop iteration cap
 constexpr int   kSubstepCap  = 1 << 20;     // sub-steps per particle per step
 constexpr float kEpsT        = 2.220446049250313e-7f;  // eps(Float64) s in ns (mixed_population.jl:66)
@@ -64,7 +64,8 @@ struct Lane {
     float x, y, z, w;
     float px, py, pz, s;
     float r;
-    double trem;               // time left in the current step (ns, FP64 bookkeeping)
+    float th, tlo;             // time left in the current step (ns), as an unevaluated
+                               // sum th + tlo (double-float: ~48-bit precision on FP32 pipes)
     uint32_t sid_lo, sid_hi, ctr;
     uint32_t c0, c1, c2, c3;   // Philox words not yet consumed (front = c0)
     int slot;                  // input slot, or -1 for a secondary (appended on finish)
@@ -73,6 +74,27 @@ struct Lane {
     int nsub;
     bool alive, rvalid;
 };
+
+
+// Double-float arithmetic for the per-particle step clock (Knuth's TwoSum and
+// Dekker's Fast2Sum; only additions, so no contraction can break them).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+// (th, tlo) += (ah, al)
+__device__ __forceinline__ void dd_add(float& th, float& tlo, float ah, float al) {
+    float s, e;
+    two_sum(th, ah, s, e);
+    e = __fadd_rn(e, __fadd_rn(tlo, al));
+    fast_two_sum(s, e, th, tlo);
+}
+__device__ __forceinline__ float dd_val(float th, float tlo) { return __fadd_rn(th, tlo); }
 
 struct KCtx {
     const BlobHdr* H;
@@ -123,7 +145,9 @@ __device__ __forceinline__ void err(const KCtx& K, int e) { atomicAdd(&K.tal[T_E
 __device__ __forceinline__ float kin_energy(int species, float px, float py, float pz) {
     float p2 = px * px + py * py + pz * pz;
     if (species == PCL_PHOTON) return sqrtf(p2);
-    return p2 / (sqrtf(1.0f + p2) + 1.0f);
+    // p^2/(gamma + 1) = p^2 (1/gamma) / (1 + 1/gamma)
+    float ig = rsqrtf(1.0f + p2);
+    return __fdividef(p2 * ig, 1.0f + ig);
 }
 
 // precheb (cheby.jl:127-143).  Energies beyond the table (x >= xmax, where the
@@ -199,8 +223,7 @@ __device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K,
                                              float pz, float& bx, float& by, float& bz, float& fx,
                                              float& fy, float& fz) {
     float p2 = px * px + py * py + pz * pz;
-    float g = sqrtf(1.0f + p2);
-    float ig = 1.0f / g;
+    float ig = rsqrtf(1.0f + p2);   // 1 / gamma
     bx = px * ig; by = py * ig; bz = pz * ig;
     const float q = S.charge;
     const float* E = K.H->E;
@@ -208,13 +231,10 @@ __device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K,
     fx = q * (E[0] + (by * B[2] - bz * B[1]));
     fy = q * (E[1] + (bz * B[0] - bx * B[2]));
     fz = q * (E[2] + (bx * B[1] - by * B[0]));
-    float f = cl_mag(S, K, p2 / (g + 1.0f));
-    if (f != 0.0f) {
-        float pn = sqrtf(p2);
-        if (pn > 0.0f) {
-            float c = f / pn;
-            fx -= c * px; fy -= c * py; fz -= c * pz;
-        }
+    float f = cl_mag(S, K, __fdividef(p2 * ig, 1.0f + ig));
+    if (f != 0.0f && p2 > 0.0f) {
+        float c = f * rsqrtf(p2);
+        fx -= c * px; fy -= c * py; fz -= c * pz;
     }
 }
 
@@ -222,8 +242,7 @@ __device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K,
 // straight line (photon.jl:46-52; both forcings vanish on photons).
 __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K, float h) {
     if (L.species == PCL_PHOTON) {
-        float pn = sqrtf(L.px * L.px + L.py * L.py + L.pz * L.pz);
-        float v = h * kCns / pn;
+        float v = h * kCns * rsqrtf(L.px * L.px + L.py * L.py + L.pz * L.pz);
         L.x += v * L.px; L.y += v * L.py; L.z += v * L.pz;
         return;
     }
@@ -248,12 +267,11 @@ __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K
 // passed in, computed by each sampler without cancellation.
 __device__ __forceinline__ void turn(float ux, float uy, float uz, float cth, float sth, float cph,
                                      float sph, float n, float& ox, float& oy, float& oz) {
-    float un = sqrtf(ux * ux + uy * uy + uz * uz);
-    float iu = 1.0f / un;
+    float iu = rsqrtf(ux * ux + uy * uy + uz * uz);
     float mx = ux * iu, my = uy * iu, mz = uz * iu;
-    float s = sqrtf(mx * mx + my * my);
-    float ca = 1.0f, sa = 0.0f;
-    if (s > 0.0f) { float is = 1.0f / s; ca = mx * is; sa = my * is; }
+    float s2 = mx * mx + my * my;
+    float s = 0.0f, ca = 1.0f, sa = 0.0f;
+    if (s2 > 0.0f) { float is = rsqrtf(s2); s = s2 * is; ca = mx * is; sa = my * is; }
     float ax = sth * (ca * mz * cph - sa * sph) + mx * cth;
     float ay = sth * (sa * mz * cph + ca * sph) + my * cth;
     float az = -s * sth * cph + mz * cth;
@@ -324,7 +342,7 @@ __device__ void emit(Lane& L, const KCtx& K, int sp, float cpx, float cpy, float
     atomicAdd(&K.tal[T_SPAWN + sp], 1u);
     float4 e0 = make_float4(L.x, L.y, L.z, L.w);
     float4 e1 = make_float4(cpx, cpy, cpz, cs);
-    uint4 e2 = make_uint4(slo, shi, uint32_t(sp) | (uint32_t(L.k) << 2), __float_as_uint(float(L.trem)));
+    uint4 e2 = make_uint4(slo, shi, uint32_t(sp) | (uint32_t(L.k) << 2), __float_as_uint(dd_val(L.th, L.tlo)));
     int pos = atomicAdd(K.top, 1);
     if (pos < kWarpStack) {
         K.stk[3 * pos + 0] = e0;
@@ -674,8 +692,13 @@ __device__ void s_annihilation(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
         if (U(L, K) < gg) break;
         if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
     }
-    float cth = (eps * (g + 1.0f) - 1.0f) / (eps * sqrtf(E * (E + 2.0f)));
-    float sth = sqrtf(fmaxf(0.0f, 1.0f - cth * cth));
+    // with d = eps - 1/2 (exact): eps (gamma + 1) - 1 = E/2 + d (E + 2) and
+    // 1 - cos^2 = (E + 2)(q - 2d)(q + 2d) / (2 eps^2 P^2), P^2 = E (E + 2)
+    const float d = eps - 0.5f;
+    const float P2 = E * (E + 2.0f);
+    const float iP = rsqrtf(P2);
+    float cth = (0.5f * E + d * (E + 2.0f)) * iP / eps;
+    float sth = sqrtf(fmaxf(0.0f, (E + 2.0f) * (q - 2.0f * d) * (q + 2.0f * d) * 0.5f)) * iP / eps;
     float sph, cph;
     sincos_2pi(U(L, K), sph, cph);
     float ax, ay, az;
@@ -782,11 +805,13 @@ __device__ __forceinline__ void load_slot(Lane& L, const float4* xw, const float
     L.x = a.x; L.y = a.y; L.z = a.z; L.w = a.w;
     L.px = b.x; L.py = b.y; L.pz = b.z; L.s = b.w;
     L.sid_lo = m.x; L.sid_hi = m.y; L.ctr = m.z;
-    L.trem = -double(__uint_as_float(m.w));  // + dt by the caller (t_off <= 0 is time still owed)
+    L.th = -__uint_as_float(m.w);  // + dt by the caller (t_off <= 0 is time still owed)
+    L.tlo = 0.0f;
 }
 
 // ------------------------------------------------------------ the step ---
-__global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwarps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5;
@@ -820,7 +845,8 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
     K.ncap = nullptr;
 
     Control* ctl = A.ctl;
-    const double dt = A.dt;
+    const float dt_hi = float(A.dt);
+    const float dt_lo = float(A.dt - double(dt_hi));
     const int nsteps = A.nsteps;
 
     // work space: concatenated species ranges, or the spill queue
@@ -858,7 +884,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
                 L.sid_lo = __float_as_uint(c.x); L.sid_hi = __float_as_uint(c.y);
                 uint32_t sk = __float_as_uint(c.z);
                 L.species = int(sk & 3u); L.k = int(sk >> 2);
-                L.trem = double(c.w);
+                L.th = c.w; L.tlo = 0.0f;
                 L.ctr = 0u; L.rvalid = false; L.slot = -1; L.alive = true; L.nsub = 0;
                 L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz));
                 has = true;
@@ -896,7 +922,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
                         L.px = b.x; L.py = b.y; L.pz = b.z; L.s = b.w;
                         L.sid_lo = m.x; L.sid_hi = m.y;
                         L.species = int(m.z & 3u); L.k = int(m.z >> 2);
-                        L.trem = double(__uint_as_float(m.w));
+                        L.th = __uint_as_float(m.w); L.tlo = 0.0f;
                         L.ctr = 0u; L.slot = -1;
                         has = true;
                     } else {
@@ -906,7 +932,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
                         else { sp = 2; sl = v - nsp0 - nsp1; }
                         L.species = sp;
                         load_slot(L, A.xw[sp], A.ps[sp], A.meta[sp], sl);
-                        L.trem += dt;
+                        dd_add(L.th, L.tlo, dt_hi, dt_lo);
                         L.slot = int(sl);
                         L.k = 0;
                         has = (L.ctr != PCL_DEAD_CTR);
@@ -927,39 +953,45 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
             continue;
         }
 
-        // ---------------- one sub-step (or a step boundary) per busy lane
+        // ---------------- one sub-step per busy lane, and the step boundary in the
+        // same iteration when the sub-step used up the clock
         int fin = 0;  // 1: survives the launch, 2: removed
         if (has) {
             const SpeciesHdr& S = H->sp[L.species];
-            if (L.alive && L.trem > double(kEpsT) && L.nsub < kSubstepCap) {
+            bool boundary = true;
+            if (L.alive && dd_val(L.th, L.tlo) > kEpsT && L.nsub < kSubstepCap) {
                 float tnext = L.s / L.r;
-                bool coll = L.trem > double(tnext);
-                float h = coll ? tnext : float(L.trem);
+                // trem > tnext with the low word (th - tnext is exact near the decision)
+                bool coll = __fadd_rn(__fsub_rn(L.th, tnext), L.tlo) > 0.0f;
+                float h = coll ? tnext : dd_val(L.th, L.tlo);
                 if (!coll) L.s -= h * L.r;
                 push(L, S, K, h);
-                L.trem = coll ? (L.trem - double(tnext)) : 0.0;
+                if (coll) dd_add(L.th, L.tlo, -tnext, 0.0f);
+                else { L.th = 0.0f; L.tlo = 0.0f; }
                 L.nsub += 1;
                 if (coll) collide(L, K, S);
-                if (!L.alive) fin = 2;
-            } else {
-                if (L.nsub >= kSubstepCap) { err(K, PCL_E_SUBSTEP_CAP); L.trem = 0.0; }
-                if (!L.alive) {
+                // advance1!'s loop ends once the clock is spent (mixed_population.jl:66)
+                boundary = !(dd_val(L.th, L.tlo) > kEpsT);
+            } else if (L.nsub >= kSubstepCap) {
+                err(K, PCL_E_SUBSTEP_CAP);
+                L.th = 0.0f; L.tlo = 0.0f;
+            }
+            if (!L.alive) {
+                fin = 2;
+            } else if (boundary) {
+                float E = kin_energy(L.species, L.px, L.py, L.pz);
+                if (E < S.cut) {  // droplow! (population.jl:273-284)
                     fin = 2;
                 } else {
-                    float E = kin_energy(L.species, L.px, L.py, L.pz);
-                    if (E < S.cut) {  // droplow! (population.jl:273-284)
-                        fin = 2;
+                    atomicAdd(&tal[T_LEND + 3 * L.k + L.species], 1u);
+                    if (L.k + 1 >= nsteps) {
+                        fin = 1;
                     } else {
-                        atomicAdd(&tal[T_LEND + 3 * L.k + L.species], 1u);
-                        if (L.k + 1 >= nsteps) {
-                            fin = 1;
-                        } else {
-                            L.k += 1;
-                            L.nsub = 0;
-                            L.trem += dt;  // remainder below eps(Float64) carries over (mixed_population.jl:65)
-                            L.r = setr(S, K, E);  // advance_init! of the next step
-                            atomicAdd(&tal[T_LSTART + L.k], 1u);
-                        }
+                        L.k += 1;
+                        L.nsub = 0;
+                        dd_add(L.th, L.tlo, dt_hi, dt_lo);  // remainder below eps carries over (mixed_population.jl:65)
+                        L.r = setr(S, K, E);  // advance_init! of the next step
+                        atomicAdd(&tal[T_LSTART + L.k], 1u);
                     }
                 }
             }
@@ -979,7 +1011,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
                 if (slot < A.cap[lsp]) {
                     A.xw[lsp][slot] = make_float4(L.x, L.y, L.z, L.w);
                     A.ps[lsp][slot] = make_float4(L.px, L.py, L.pz, L.s);
-                    A.meta[lsp][slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-float(L.trem)));
+                    A.meta[lsp][slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-dd_val(L.th, L.tlo)));
                 } else {
                     err(K, PCL_E_CAPACITY);
                 }
@@ -990,7 +1022,7 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
             const int sp = L.species;
             A.xw[sp][L.slot] = make_float4(L.x, L.y, L.z, L.w);
             A.ps[sp][L.slot] = make_float4(L.px, L.py, L.pz, L.s);
-            A.meta[sp][L.slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-float(L.trem)));
+            A.meta[sp][L.slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-dd_val(L.th, L.tlo)));
         } else if (fin == 2 && L.slot >= 0) {
             A.meta[L.species][L.slot].z = PCL_DEAD_CTR;
             atomicAdd(&tal[T_DEAD + L.species], 1u);
@@ -1012,6 +1044,16 @@ __global__ void __launch_bounds__(256, 2) k_step(StepArgs A) {
         else if (i < T_LSTART) atomicAdd(&ctl->live_end[(i - T_LEND) / 3][(i - T_LEND) % 3], vv);
         else atomicAdd(&ctl->live_start[i - T_LSTART], vv);
     }
+}
+
+// The step kernel is instantiated for 2, 3 and 4 resident 256-thread blocks
+// per SM (register budgets 128, 85 and 64); the launch shape is a tunable.
+cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A) {
+    void (*kern)(StepArgs) = (minb == 2) ? k_step<2> : (minb == 3) ? k_step<3> : k_step<4>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    kern<<<grid, threads, smem, stream>>>(A);
+    return cudaGetLastError();
 }
 
 // Launch prologue: snapshot the work space and clear per-launch counters.
@@ -1188,7 +1230,7 @@ __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, cons
     K.H = H; K.blob = reinterpret_cast<const float*>(smem); K.stk = nullptr; K.top = nullptr; K.tal = tal;
     K.A = &A; K.cap = capbuf; K.ncap = &ncap;
     Lane L;
-    L.x = L.y = L.z = 0.0f; L.w = 1.0f; L.trem = 0.0; L.k = 0; L.s = 0.0f;
+    L.x = L.y = L.z = 0.0f; L.w = 1.0f; L.th = 0.0f; L.tlo = 0.0f; L.k = 0; L.s = 0.0f;
     L.px = p_in[3 * i]; L.py = p_in[3 * i + 1]; L.pz = p_in[3 * i + 2];
     L.sid_lo = sid[2 * i]; L.sid_hi = sid[2 * i + 1]; L.ctr = 0u; L.rvalid = false;
     L.species = species; L.alive = true; L.slot = -1; L.nsub = 0;

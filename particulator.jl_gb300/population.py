@@ -148,7 +148,8 @@ class MultiPopulation:
     keywords select the device, the Philox seed and the launch shape."""
 
     def __init__(self, *pairs, seed: int = 0, device: int = 0, steps_per_launch: int = 1,
-                 compaction_period: int = 1, block_size: int = 0, grid_blocks: int = 0, **named):
+                 compaction_period: int = 1, block_size: int = 0, grid_blocks: int = 0, blocks_per_sm: int = 0,
+                 **named):
         index = {}
         for name, pop in list(pairs) + list(named.items()):
             key = SPECIES_BY_NAME[name] if isinstance(name, str) else int(name)
@@ -161,6 +162,7 @@ class MultiPopulation:
         cfg.compaction_period = compaction_period
         cfg.block_size = block_size
         cfg.grid_blocks = grid_blocks
+        cfg.blocks_per_sm = blocks_per_sm
         self.config = cfg
         h = C.c_void_p()
         rc = _lib.lib().pcl_create(C.byref(cfg), C.byref(h))

@@ -66,7 +66,10 @@ def test_all_processes(pcl, oracle, air, ctx):
         pn = np.linalg.norm(p, axis=1)[clean]
         for q in range(3):
             live = ok[clean][:, q] >= 0
-            dp = np.linalg.norm(gp[clean][:, q] - op[clean][:, q], axis=1)[live] / pn[live]
+            # relative to the larger of the incoming and outgoing momentum (annihilation
+            # photons carry far more momentum than a slow positron)
+            scale = np.maximum(pn, np.linalg.norm(op[clean][:, q], axis=1))[live]
+            dp = np.linalg.norm(gp[clean][:, q] - op[clean][:, q], axis=1)[live] / scale
             if live.any():
                 if dp.max() > RTOL:
                     i = np.argmax(dp)
