@@ -285,6 +285,25 @@ int pcl_test_sampler(void* ctx, int species, int proc_index, int64_t n, const do
                      const uint64_t* sid, double* out_p, double* out_s, int32_t* out_kind,
                      uint32_t* out_ctr);
 
+/* ---- compaction without device allocation --------------------------------
+ * No counterpart in the reference: an extra entry point for callers that
+ * cannot call cudaMalloc (a host whose memory pool owns the device, code on a
+ * stream being captured, a latency-critical loop that must not allocate or
+ * synchronise).  Same result as pcl_compact for one species, on device
+ * buffers the caller owns: the n slots of xw/ps/meta (packed layout, dead
+ * slots included) are compacted in order into out_xw/out_ps/out_meta and the
+ * live count is written to the device int64 *n_out.  Scratch lives in a
+ * static device array of PCL_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library keeps until exit; n above PCL_NOALLOC_MAX_SLOTS returns
+ * PCL_ERR_CAPACITY.  All calls share that array, so calls that overlap on the
+ * GPU race.  The first call on each device looks up the array's address;
+ * make it before any stream capture.  `stream` is a cudaStream_t (NULL =
+ * default stream).  Context-free errors: pcl_last_error(NULL). */
+#define PCL_NOALLOC_MAX_SLOTS (1 << 25)
+#define PCL_NOALLOC_SCRATCH_BYTES 196864
+int pcl_compact_noalloc(int64_t n, const float* xw, const float* ps, const uint32_t* meta,
+                        float* out_xw, float* out_ps, uint32_t* out_meta, int64_t* n_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

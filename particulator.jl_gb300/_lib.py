@@ -20,6 +20,7 @@ PCL_ERR_UNSUPPORTED = -4
 PCL_ERR_STATE = -5
 PCL_ERR_TIMEOUT = -6
 PCL_ERR_NUMERIC = -7
+NOALLOC_MAX_SLOTS = 1 << 25
 
 ELECTRON, PHOTON, POSITRON = 0, 1, 2
 SPECIES_TRACKED, SPECIES_TALLY_ONLY = 0, 1
@@ -109,6 +110,8 @@ _SIGS = {
     "pcl_timer_start": (C.c_int, [C.c_void_p]),
     "pcl_timer_stop": (C.c_int, [C.c_void_p, _P(_d)]),
     "pcl_kernel_stats": (C.c_int, [C.c_void_p, _P(_d), _P(_i64), _P(_i64), _P(_d), C.c_int]),
+    "pcl_compact_noalloc": (C.c_int, [_i64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p]),
     "pcl_test_sampler": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _i64, _P(_d), _P(_u64), _P(_d), _P(_d),
                                    _P(_i32), _P(_u32)]),
 }

@@ -27,6 +27,7 @@ __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, cons
                                const uint32_t* sid, float* out_p, float* out_s, int* out_kind,
                                uint32_t* out_ctr);
 size_t step_smem_bytes(int blob_bytes, int threads);
+const char* noalloc_last_error();
 constexpr int kTile = 2048;
 
 // Host Philox4x32-10 (same function as the device one; used to draw initial s).
@@ -470,7 +471,7 @@ int pcl_device_count(void) {
 }
 
 const char* pcl_last_error(void* ctx) {
-    if (!ctx) return "null context";
+    if (!ctx) return noalloc_last_error();
     return static_cast<Ctx*>(ctx)->last_error.c_str();
 }
 
