@@ -59,6 +59,12 @@ extern "C" {
 #define PCL_PROC_BETHE_HEITLER   8  /* bethe_heitler.jl:1-193         */
 #define PCL_PROC_BHABHA          9  /* bhaba.jl:4-91                  */
 #define PCL_PROC_ANNIHILATION   10  /* anihilation.jl:1-67            */
+/* Low-energy swarm processes (slow-electron.jl:70-139), applied to the
+ * relativistic electron state with a linear-grid table (the reference's
+ * SlowElectronState path is not wired into advance!): */
+#define PCL_PROC_ELASTIC        11  /* Elastic(mass_ratio): isotropic in the centre of mass (slow-electron.jl:133-139) */
+#define PCL_PROC_EXCITATION     12  /* Excitation(threshold): loses the threshold, isotropic (slow-electron.jl:108-114) */
+#define PCL_PROC_NULL_COLLISION 13  /* NullCollision as an explicit table entry (collisions.jl:3,58; lxcat.jl:115-119) */
 
 #define PCL_MAX_PROC      16   /* processes per species table              */
 #define PCL_MAX_ORDER      4   /* Chebyshev terms per interval             */
@@ -92,6 +98,9 @@ extern "C" {
  *                    log(k/T) [naux2 = ncum][naux] column-major (pcum fastest),
  *                    exactly the fields of SeltzerBerger (seltzer.jl:9-21)
  *   COMPTON, KN_COMPTON, BETHE_HEITLER : Z only
+ *   ELASTIC        : param[0] = electron / target mass ratio
+ *   EXCITATION     : param[0] = threshold (J)
+ *   NULL_COLLISION : none
  */
 typedef struct pcl_process {
     int32_t kind;
@@ -114,7 +123,7 @@ typedef struct pcl_config {
     int32_t  block_size;       /* threads per block of the step kernel (0 = 256)      */
     int32_t  grid_blocks;      /* persistent grid size (0 = 2 x SM count)             */
     int32_t  steps_per_launch; /* time steps fused into one launch (0/1 = one)        */
-    int32_t  compaction_period;/* compact dead slots every this many steps (0 = 1)    */
+    int32_t  compaction_period;/* compact dead slots every this many steps (0 = 8)    */
     int32_t  use_graph;        /* capture the step sequence of pcl_run in a CUDA graph */
     int32_t  blocks_per_sm;    /* resident step-kernel blocks per SM: 2, 3 or 4 (0 = 4) */
     int32_t  reserved[3];
@@ -182,6 +191,13 @@ int pcl_build_collision_table(int species, int nproc, const pcl_process* procs, 
                               double safety, int nintervals, int order, double max_energy,
                               double* rate, double* ratebound, int32_t* perm);
 
+/* compratebound (collision_table.jl:152-167) is linear in Fdt, so the rate bound
+ * of a table for any field is A + Fdt * B: A = the summed process fits,
+ * B = the fit of gamma^3 v |d(sum nu)/dE| safety.  Inputs as written by
+ * pcl_build_collision_table; A and B are [order][nintervals+1] column-major. */
+int pcl_ratebound_split(int species, int order, int nproc, int nintervals, double xmax, const double* rate,
+                        double safety, double* A, double* B);
+
 /* ChebContinuumLoss(ContinuumLoss(nel, I, Tcut), Tmax, n) (continuum.jl:36-43,
  * 63-139).  Writes k (number of binary intervals), xmax = 2^k Tcut, and the
  * electron / positron coefficient matrices ec, pc [n][k+1] column-major
@@ -209,11 +225,35 @@ int pcl_set_collision_table(void* ctx, int species, int order, int nproc, int ni
                             double xmax, const double* rate, const double* ratebound,
                             const pcl_process* procs);
 
+/* The linear-grid CollisionTable (collision_table.jl:15-57): rates on the
+ * energy grid LinRange(e0, e1, n) (J), rate[j + nproc*k] = rate of table
+ * process j at grid point k (the reference's rate[j, k], column-major), and a
+ * rate bound that is either one number (nrb = 1: ratebound(x::Number), line 232)
+ * or one value per grid point (nrb = n, interpolated, lines 234-242).
+ * Energies are located with indweight(LinRange) (util.jl:23-32). */
+int pcl_set_linear_table(void* ctx, int species, int nproc, int n, double e0, double e1, const double* rate,
+                         const double* ratebound, int nrb, const pcl_process* procs);
+
 /* RK2Pusher(CombinedForcing(ElectromagneticField(HomogeneousField(E), HomogeneousField(B)),
  *           ChebContinuumLoss(...)))  (pusher.jl:37-63, field.jl:4-8,54-70, continuum.jl:25-57).
  * cl_order = 0 disables continuum losses. */
 int pcl_set_forcing(void* ctx, const double E[3], const double B[3], int cl_order, int cl_k,
                     double cl_xmax, const double* cl_ec, const double* cl_pc);
+
+/* Batched form: nswarm (1..256) independent swarms share one context and every
+ * launch; particle i belongs to swarm (sid >> 56) and its secondaries inherit
+ * that (their other 56 stream-id bits are drawn as usual).  Swarm s feels the
+ * homogeneous field E[3s..3s+2] (V/m; B stays global) and its lepton rate bound
+ * is A + Fdt[s] B (pcl_ratebound_split with the safety factor given), the
+ * table compratebound builds for that field.  A swarm run alone (nswarm = 1)
+ * and the same swarm inside a batch execute the same arithmetic.  nswarm = 0
+ * returns to the classic single population.  No reference counterpart: the
+ * reference runs one MultiPopulation per swarm. */
+int pcl_set_swarms(void* ctx, int nswarm, const double* E, const double* Fdt, double safety);
+
+/* Per-swarm FP64 moments of one species: out[6*s + q] = {live, sum w,
+ * sum w E (J), sum w z, sum w z^2, sum w (x^2 + y^2)} (m). */
+int pcl_swarm_moments(void* ctx, int species, int nswarm, double* out);
 
 /* Replace the species' population with n particles (SI, FP64): x[3n], p[3n]
  * (interleaved xyz), w[n], t[n] (absolute, s).  s[n] = normalised time to the

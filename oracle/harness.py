@@ -34,6 +34,9 @@ def lib():
         L.orc_set_table.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _d, _P(_d), _P(_d),
                                     _P(C.c_int32), _P(C.c_int32), _P(_d), _P(C.c_int32)]
         L.orc_set_sb.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _P(_d), _P(_d)]
+        L.orc_set_swarms.argtypes = [C.c_void_p, C.c_int, _P(_d), _P(_d), _P(_d)]
+        L.orc_set_linear_table.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _d, _d, _P(_d), _P(_d),
+                                           _P(C.c_int32), _P(_d)]
         L.orc_set_forcing.argtypes = [C.c_void_p, _P(_d), _P(_d), C.c_int, C.c_int, _d, _P(_d), _P(_d)]
         L.orc_upload.argtypes = [C.c_void_p, C.c_int, C.c_int64, _P(_d), _P(_d), _P(_d), _P(_d), _P(_d),
                                  _P(C.c_uint64), _P(C.c_uint32)]
@@ -84,6 +87,20 @@ class OracleWorld:
         for sp, tab in tabs.items():
             if tab is None:
                 continue
+            if hasattr(tab, "energy"):  # linear-grid CollisionTable
+                n = tab.nproc
+                kinds = np.array([p.kind for p in tab.proc], np.int32)
+                params = np.zeros((max(1, n), 8))
+                for j, proc in enumerate(tab.proc):
+                    params[j] = list(proc.to_c(1.0).param)
+                e0, e1, ng = tab.energy
+                rate = np.ascontiguousarray(tab.rate.T)
+                rb = np.ascontiguousarray(np.broadcast_to(tab.ratebound, (ng,)) if len(tab.ratebound) == 1
+                                          else tab.ratebound, dtype=float)
+                self._keep += [kinds, params, rate, rb]
+                L.orc_set_linear_table(self.h, int(sp), n, ng, e0, e1, _p(rate), _p(rb), _p(kinds, C.c_int32),
+                                       _p(params))
+                continue
             n = tab.nproc
             kinds = np.array([p.kind for p in tab.proc] or [0], np.int32)
             Z = np.zeros(max(1, n), np.int32)
@@ -111,6 +128,23 @@ class OracleWorld:
         else:
             self._keep += [cl.ec, cl.pc]
             L.orc_set_forcing(self.h, _p(E), _p(B), cl.n, cl.bints.k, cl.bints.xmax, _p(cl.ec), _p(cl.pc))
+
+    def set_swarms(self, tabs, E, Fdt, safety=1.15):
+        """Swarm mode: per-swarm field E [n,3] (V/m) and the rate bound of the
+        lepton tables for each swarm's Fdt, A + Fdt B from ratebound_split."""
+        import particulator_gb300 as pcl
+        E = np.ascontiguousarray(np.asarray(E, dtype=float).reshape(-1, 3))
+        Fdt = np.asarray(Fdt, dtype=float)
+        rbs = {}
+        for sp in (0, 2):
+            tab = tabs.get(sp)
+            if tab is None or not hasattr(tab, "b") or tab.nproc == 0:
+                rbs[sp] = None
+                continue
+            A, B = pcl.ratebound_split(tab, safety)
+            rbs[sp] = np.ascontiguousarray(np.concatenate([A + f * B for f in Fdt]))
+        self._keep += [E, rbs[0], rbs[2]]
+        lib().orc_set_swarms(self.h, len(Fdt), _p(E), _p(rbs[0]), _p(rbs[2]))
 
     def upload(self, sp, a):
         n = len(a.w)

@@ -73,7 +73,8 @@ constexpr double EPS_T = 2.220446049250313e-16;  // eps(Float64) (mixed_populati
 
 enum { ELECTRON = 0, PHOTON = 1, POSITRON = 2 };
 enum {
-    P_MOLLER = 1, P_RBEB, P_SB, P_COULOMB, P_COMPTON, P_KN, P_PE, P_BH, P_BHABHA, P_ANN
+    P_MOLLER = 1, P_RBEB, P_SB, P_COULOMB, P_COMPTON, P_KN, P_PE, P_BH, P_BHABHA, P_ANN, P_ELASTIC, P_EXCITATION,
+    P_NULL
 };
 enum { E_RATEBOUND = 0, E_TABLE_RANGE, E_REJECT_CAP, E_SUBSTEP_CAP, E_SPILL, E_CAPACITY, E_KINEMATICS, E_NEG_RATE };
 constexpr int REJECT_CAP = 10000;
@@ -105,9 +106,30 @@ struct Proc {
 struct Table {
     int order = 1, nproc = 0, k = 1;
     double xmax = 1.0;
-    std::vector<double> rate, rb;  // a[k,j,i] column-major, rb[k,i]
+    std::vector<double> rate, rb;  // a[k,j,i] column-major, rb[k,i]; linear: rate[j,k], rb[k]
     std::vector<Proc> procs;
+    // CollisionTable on LinRange(e0, e1, n) (collision_table.jl:15-57)
+    bool linear = false;
+    double e0 = 0, e1 = 0;
+    int n = 0;
 };
+
+// LinRange(a, b, len)[i] for 0-based i (Julia's lerp form)
+static inline double linrange(double a, double b, int len, int i) {
+    double d = double(len - 1);
+    return (a * (d - i) + b * i) / d;
+}
+
+// indweight(::LinRange, x) (util.jl:23-32): 0-based left index and weight;
+// outside the grid the end interval is extrapolated (counted).
+static inline int indweight(const Table& T, double x, double& w, bool& oor) {
+    double step = (T.e1 - T.e0) / (T.n - 1);
+    int i = int(std::floor((x - T.e0) / step));
+    if (i < 0) { i = 0; oor = true; }
+    if (i > T.n - 2) { i = T.n - 2; oor = true; }
+    w = (linrange(T.e0, T.e1, T.n, i + 1) - x) / step;
+    return i;
+}
 
 struct Part {
     double x[3], p[3], w, t, s, r;
@@ -150,6 +172,10 @@ struct World {
     double tie_tol = 2e-5;
     Species sp[3];
     double E[3] = {0, 0, 0}, B[3] = {0, 0, 0};
+    // swarm mode: swarm = top 8 bits of the stream id; per-swarm field and rate bound
+    int nswarm = 0;
+    std::vector<double> swarm_E;          // [nswarm][3]
+    std::vector<double> swarm_rb[3];      // [nswarm][order*(k+1)] per species (empty: table's own)
     int cl_order = 0, cl_k = 0;
     double cl_xmax = 0;
     std::vector<double> ec, pc;
@@ -240,6 +266,18 @@ static double setr(Walker& Wk, int species) {
     Wk.near(eng, S.cut, S.cut);
     if (eng < S.cut) return 0.0;
     const Table& T = S.tab;
+    if (T.linear) {
+        double w;
+        bool oor = false;
+        int i = indweight(T, eng, w, oor);
+        if (oor) Wk.err(E_TABLE_RANGE);
+        double r = w * T.rb[i] + (1 - w) * T.rb[i + 1];
+        if (!(r > 0)) {
+            if (T.nproc > 0) Wk.err(E_NEG_RATE);
+            return 0.0;
+        }
+        return r;
+    }
     double t[4];
     bool oor = false;
     double edge = 1.0;
@@ -247,7 +285,13 @@ static double setr(Walker& Wk, int species) {
     if (oor) Wk.err(E_TABLE_RANGE);
     if (T.nproc > 0) Wk.near(edge, 0.0, 1.0);
     double r = 0.0;
-    for (int q = 0; q < T.order; ++q) r += T.rb[q + T.order * i] * t[q];
+    const double* rb = T.rb.data();
+    const World& Wd = *Wk.W;
+    if (Wd.nswarm > 0 && !Wd.swarm_rb[species].empty()) {
+        int sw = std::min(int(Wk.P->sid >> 56), Wd.nswarm - 1);
+        rb = Wd.swarm_rb[species].data() + size_t(sw) * T.order * (T.k + 1);
+    }
+    for (int q = 0; q < T.order; ++q) r += rb[q + T.order * i] * t[q];
     if (!(r > 0)) {
         if (T.nproc > 0) Wk.err(E_NEG_RATE);
         return 0.0;
@@ -277,9 +321,11 @@ static void force(Walker& Wk, int species, const double* p, double* f) {
     double v[3];
     velocity(species, p, v);
     double q = (species == ELECTRON ? -1.0 : 1.0) * e;
-    f[0] = q * (W.E[0] + (v[1] * W.B[2] - v[2] * W.B[1]));
-    f[1] = q * (W.E[1] + (v[2] * W.B[0] - v[0] * W.B[2]));
-    f[2] = q * (W.E[2] + (v[0] * W.B[1] - v[1] * W.B[0]));
+    const double* Ef = W.E;
+    if (W.nswarm > 0) Ef = W.swarm_E.data() + 3 * size_t(std::min(int(Wk.P->sid >> 56), W.nswarm - 1));
+    f[0] = q * (Ef[0] + (v[1] * W.B[2] - v[2] * W.B[1]));
+    f[1] = q * (Ef[1] + (v[2] * W.B[0] - v[0] * W.B[2]));
+    f[2] = q * (Ef[2] + (v[0] * W.B[1] - v[1] * W.B[0]));
     if (W.cl_order > 0) {
         double x = kinenergy(species, p);
         const std::vector<double>& a = (species == ELECTRON) ? W.ec : W.pc;
@@ -689,6 +735,39 @@ static void s_ann(Walker& Wk, double eng) {
     child(Wk, PHOTON, pb, sb, 1);
 }
 
+// randsphere() (util.jl:4-12)
+static void randsphere(Walker& Wk, double* d) {
+    double phi = 2 * pi * Wk.rand();
+    double sp = std::sin(phi), cp = std::cos(phi);
+    double u = 2 * Wk.rand() - 1;
+    double v = std::sqrt(1 - u * u);
+    d[0] = v * cp; d[1] = v * sp; d[2] = u;
+}
+
+// collide(::Elastic, ...) (slow-electron.jl:133-139) on the momentum
+static void s_elastic(Walker& Wk, const Proc& P) {
+    Part& L = *Wk.P;
+    double mr = P.p[0];
+    double cm[3], d[3];
+    for (int a = 0; a < 3; ++a) cm[a] = (mr / (1 + mr)) * L.p[a];
+    double dv[3] = {L.p[0] - cm[0], L.p[1] - cm[1], L.p[2] - cm[2]};
+    double dn = std::sqrt(dot3(dv, dv));
+    randsphere(Wk, d);
+    for (int a = 0; a < 3; ++a) L.p[a] = d[a] * dn + cm[a];
+    L.s = Wk.nextcoll();
+}
+
+// collide(::Excitation, ...) (slow-electron.jl:108-114)
+static void s_excitation(Walker& Wk, const Proc& P, double eng) {
+    Part& L = *Wk.P;
+    double E1 = std::max(0.0, eng - P.p[0]);
+    double pn = momentum_norm_from_kin(E1);
+    double d[3];
+    randsphere(Wk, d);
+    for (int a = 0; a < 3; ++a) L.p[a] = d[a] * pn;
+    L.s = Wk.nextcoll();
+}
+
 static void sample(Walker& Wk, const Proc& P, int species, double eng) {
     switch (P.kind) {
         case P_COULOMB: s_coulomb(Wk, P, species); break;
@@ -701,6 +780,9 @@ static void sample(Walker& Wk, const Proc& P, int species, double eng) {
         case P_BH: s_bh(Wk, P, eng); break;
         case P_BHABHA: s_bhabha(Wk, P, eng); break;
         case P_ANN: s_ann(Wk, eng); break;
+        case P_ELASTIC: s_elastic(Wk, P); break;
+        case P_EXCITATION: s_excitation(Wk, P, eng); break;
+        case P_NULL: Wk.P->s = Wk.nextcoll(); break;  // NullOutcome (collisions.jl:83-88)
         default: Wk.err(E_KINEMATICS); break;
     }
 }
@@ -735,6 +817,7 @@ static void flush_kids(Walker& Wk, uint32_t ctr0, SpawnBuf& out) {
         n.s = k.s;
         n.active = true;
         n.sid = k.idx ? (uint64_t(c2) | (uint64_t(d) << 32)) : (uint64_t(a) | (uint64_t(b) << 32));
+        if (W.nswarm > 0) n.sid = (n.sid & 0x00FFFFFFFFFFFFFFull) | (Wk.P->sid & 0xFF00000000000000ull);
         n.ctr = 0;
         n.tie = Wk.P->tie;
         Walker Wc{&n, Wk.W, Wk.C};
@@ -754,21 +837,35 @@ static void do_one_collision(Walker& Wk, int species, SpawnBuf& out) {
     Wk.near(eng, S.cut, S.cut);
     if (!(eng >= S.cut)) return;
     const Table& T = S.tab;
-    double t[4];
-    bool oor = false;
-    double edge = 1.0;
-    int i = precheb(eng, T.k, T.xmax, T.order, t, oor, &edge);
-    if (oor) Wk.err(E_TABLE_RANGE);
-    Wk.near(edge, 0.0, 1.0);
     uint32_t ctr0 = L.ctr;
-    double xi = Wk.rand() * L.r;
     int j = 0;
-    for (; j < T.nproc; ++j) {
-        double nu = 0;
-        for (int q = 0; q < T.order; ++q) nu += T.rate[q + T.order * (j + T.nproc * i)] * t[q];
-        Wk.near(nu, xi, L.r);
-        if (nu > xi) break;
-        xi -= nu;
+    if (T.linear) {  // rate(::CollisionTable, j, pre) (collision_table.jl:249-256)
+        double w;
+        bool oor = false;
+        int i = indweight(T, eng, w, oor);
+        if (oor) Wk.err(E_TABLE_RANGE);
+        double xi = Wk.rand() * L.r;
+        for (; j < T.nproc; ++j) {
+            double nu = w * T.rate[j + size_t(T.nproc) * i] + (1 - w) * T.rate[j + size_t(T.nproc) * (i + 1)];
+            Wk.near(nu, xi, L.r);
+            if (nu > xi) break;
+            xi -= nu;
+        }
+    } else {
+        double t[4];
+        bool oor = false;
+        double edge = 1.0;
+        int i = precheb(eng, T.k, T.xmax, T.order, t, oor, &edge);
+        if (oor) Wk.err(E_TABLE_RANGE);
+        Wk.near(edge, 0.0, 1.0);
+        double xi = Wk.rand() * L.r;
+        for (; j < T.nproc; ++j) {
+            double nu = 0;
+            for (int q = 0; q < T.order; ++q) nu += T.rate[q + T.order * (j + T.nproc * i)] * t[q];
+            Wk.near(nu, xi, L.r);
+            if (nu > xi) break;
+            xi -= nu;
+        }
     }
     if (j == T.nproc) {  // NullOutcome: setr!, s = nextcoll() (collisions.jl:83-88)
         Wk.C->nulls[species] += 1;
@@ -913,6 +1010,41 @@ int orc_set_table(void* w, int species, int order, int nproc, int nint, double x
         T.procs[j].Z = Z[j];
         T.procs[j].np = nparam[j];
         for (int q = 0; q < 8; ++q) T.procs[j].p[q] = params[8 * j + q];
+    }
+    return 0;
+}
+
+int orc_set_linear_table(void* w, int species, int nproc, int n, double e0, double e1, const double* rate,
+                         const double* rb, const int32_t* kinds, const double* params) {
+    World* W = static_cast<World*>(w);
+    if (species < 0 || species > 2 || nproc < 0 || nproc > 16 || n < 2) return -1;
+    Table& T = W->sp[species].tab;
+    T = Table();
+    T.linear = true;
+    T.nproc = nproc; T.n = n; T.e0 = e0; T.e1 = e1;
+    T.rate.assign(rate, rate + size_t(nproc) * n);
+    T.rb.assign(rb, rb + n);
+    T.procs.assign(nproc, Proc());
+    for (int j = 0; j < nproc; ++j) {
+        T.procs[j].kind = kinds[j];
+        for (int q = 0; q < 8; ++q) T.procs[j].p[q] = params[8 * j + q];
+    }
+    return 0;
+}
+
+// swarm mode: E[nswarm][3] (V/m); rb_e / rb_p = per-swarm rate-bound tables of
+// the electron / positron Chebyshev tables (NULL: keep the table's own)
+int orc_set_swarms(void* w, int nswarm, const double* E, const double* rb_e, const double* rb_p) {
+    World* W = static_cast<World*>(w);
+    W->nswarm = nswarm;
+    W->swarm_E.assign(E, E + 3 * size_t(nswarm));
+    const double* src[3] = {rb_e, nullptr, rb_p};
+    for (int s = 0; s < 3; ++s) {
+        W->swarm_rb[s].clear();
+        if (!src[s]) continue;
+        const Table& T = W->sp[s].tab;
+        size_t len = size_t(T.order) * (T.k + 1) * nswarm;
+        W->swarm_rb[s].assign(src[s], src[s] + len);
     }
     return 0;
 }

@@ -9,10 +9,10 @@ from . import _lib, constants, data
 from ._lib import (ELECTRON, PHOTON, POSITRON, PCLError, lib, LIB_PATH)
 from .processes import (Moller, RBEB, SeltzerBerger, RelativisticCoulomb, Compton, KleinNishinaCompton,
                         PhotoElectric, BetheHeitler, Bhaba, Bhabha, PositronAnihilation, PositronAnnihilation,
-                        N2_ORBITALS, O2_ORBITALS, ORBITALS, totalcs)
+                        N2_ORBITALS, O2_ORBITALS, ORBITALS, totalcs, Elastic, Excitation, NullCollision)
 from .tables import (Electron, Photon, Positron, BinaryIntervals, ChebyshevCollisionTable,
                      collision_table_from_processes, ContinuumLoss, ChebContinuumLoss, speed,
-                     momentum_norm_from_kin, precheb)
+                     momentum_norm_from_kin, precheb, CollisionTable, lxcat_table, ratebound_split)
 from .forcing import (HomogeneousField, ElectromagneticField, NullForcing, CombinedForcing, RK2Pusher)
 from .population import (ElectronState, PhotonState, PositronState, ParticleArrays, Population, MultiPopulation,
                          init, advance, run, nparticles, nactives, weight, meanenergy, maxenergy, spread, posvar,

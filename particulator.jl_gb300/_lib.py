@@ -10,7 +10,9 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libparticulator_gb300.so")
+# PCL_LIB_PATH selects another build of the same library (e.g. a variant built
+# with different compile-time options); the default is the in-tree build.
+LIB_PATH = os.environ.get("PCL_LIB_PATH") or os.path.join(HERE, "_build", "libparticulator_gb300.so")
 
 PCL_OK = 0
 PCL_ERR_INVALID = -1
@@ -35,6 +37,9 @@ PROC_PHOTOELECTRIC = 7
 PROC_BETHE_HEITLER = 8
 PROC_BHABHA = 9
 PROC_ANNIHILATION = 10
+PROC_ELASTIC = 11
+PROC_EXCITATION = 12
+PROC_NULL_COLLISION = 13
 
 MAX_PROC = 16
 NERR = 8
@@ -81,6 +86,7 @@ _SIGS = {
     "pcl_totalcs": (C.c_int, [_P(Process), _i64, _P(_d), _P(_d)]),
     "pcl_build_collision_table": (C.c_int, [C.c_int, C.c_int, _P(Process), _d, _d, C.c_int, C.c_int, _d,
                                             _P(_d), _P(_d), _P(_i32)]),
+    "pcl_ratebound_split": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_int, _d, _P(_d), _d, _P(_d), _P(_d)]),
     "pcl_build_continuum_loss": (C.c_int, [_d, _d, _d, _d, C.c_int, _P(C.c_int), _P(_d), _P(_d), _P(_d),
                                            C.c_int]),
     "pcl_create": (C.c_int, [_P(Config), _P(C.c_void_p)]),
@@ -91,7 +97,11 @@ _SIGS = {
     "pcl_set_species": (C.c_int, [C.c_void_p, C.c_int, _d, _i64, C.c_int]),
     "pcl_set_collision_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _d, _P(_d), _P(_d),
                                           _P(Process)]),
+    "pcl_set_linear_table": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _d, _d, _P(_d), _P(_d), C.c_int,
+                                       _P(Process)]),
     "pcl_set_forcing": (C.c_int, [C.c_void_p, _P(_d), _P(_d), C.c_int, C.c_int, _d, _P(_d), _P(_d)]),
+    "pcl_set_swarms": (C.c_int, [C.c_void_p, C.c_int, _P(_d), _P(_d), _d]),
+    "pcl_swarm_moments": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_d)]),
     "pcl_upload": (C.c_int, [C.c_void_p, C.c_int, _i64, _P(_d), _P(_d), _P(_d), _P(_d), _P(_d), _P(_u64),
                              _u64]),
     "pcl_download": (C.c_int, [C.c_void_p, C.c_int, _P(_i64), _P(_d), _P(_d), _P(_d), _P(_d), _P(_d),

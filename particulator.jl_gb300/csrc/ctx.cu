@@ -13,6 +13,8 @@
 #include "physconst.h"
 #include "../../include/particulator_gb300.h"
 
+extern "C" int pcl_ratebound_split(int, int, int, int, double, const double*, double, double*, double*);
+
 namespace pcl {
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A);
 __global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long cap2);
@@ -23,6 +25,8 @@ __global__ void k_compact_scan(CompactArgs C);
 __global__ void k_compact_scatter(CompactArgs C);
 __global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta, long long n, int species,
                           double* out);
+__global__ void k_swarm_moments(const float4* xw, const float4* ps, const uint4* meta, long long n, int species,
+                                int nswarm, double* out);
 __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, const float* p_in,
                                const uint32_t* sid, float* out_p, float* out_s, int* out_kind,
                                uint32_t* out_ctr);
@@ -58,6 +62,10 @@ struct SpeciesState {
     std::vector<double> rate, rb;
     std::vector<pcl_process> procs;
     std::vector<int> sb_index;
+    // linear-grid table (table_kind 1)
+    int table_kind = 0;
+    int lin_n = 0;
+    double lin_e0 = 0, lin_e1 = 0;
     // tally-only histogram
     int hist_bins = 0;
     double hist_emin = 0, hist_emax = 0;
@@ -85,6 +93,10 @@ struct Ctx {
     int cl_order = 0, cl_k = 0;
     double cl_xmax = 0;
     std::vector<double> cl_ec, cl_pc;
+    // batched swarms
+    int nswarm = 0;
+    double swarm_safety = 1.1;
+    std::vector<double> swarm_E, swarm_Fdt;   // [nswarm][3] V/m, [nswarm] N s
     // blob
     bool blob_dirty = true;
     std::vector<unsigned char> blob;
@@ -223,6 +235,12 @@ static void pack_proc(const pcl_process& P, int sbi, DevProc& D) {
             D.p[5] = float(50e6 * eV / mc2);
             break;
         }
+        case PCL_PROC_ELASTIC:
+            D.p[0] = float(P.param[0]);
+            break;
+        case PCL_PROC_EXCITATION:
+            D.p[0] = float(P.param[0] / mc2);
+            break;
         default:
             break;
     }
@@ -248,16 +266,27 @@ static int build_blob(Ctx* c) {
         h.xscale = float(1.0 / (S.xmax / mc2));
         h.cut = S.set ? float(S.cut / mc2) : INFINITY;
         h.charge = charge[s];
-        const int nI = S.nint + 1;
-        h.rate_off = off();
-        for (int i = 0; i < nI; ++i)
-            for (int j = 0; j < S.nproc; ++j)
+        h.table_kind = S.table_kind;
+        if (S.table_kind == 1) {
+            h.lin_n = S.lin_n;
+            h.lin_e0 = float(S.lin_e0 / mc2);
+            h.lin_inv_step = float(1.0 / ((S.lin_e1 - S.lin_e0) / (S.lin_n - 1) / mc2));
+            h.rate_off = off();
+            for (size_t q = 0; q < S.rate.size(); ++q) data.push_back(float(rate_to_dev(S.rate[q])));
+            h.rb_off = off();
+            for (int i = 0; i < S.lin_n; ++i) data.push_back(float(rate_to_dev(S.rb[i])));
+        } else {
+            const int nI = S.nint + 1;
+            h.rate_off = off();
+            for (int i = 0; i < nI; ++i)
+                for (int j = 0; j < S.nproc; ++j)
+                    for (int k = 0; k < S.order; ++k)
+                        data.push_back(float(rate_to_dev(S.rate[k + S.order * (j + S.nproc * i)])));
+            h.rb_off = off();
+            for (int i = 0; i < nI; ++i)
                 for (int k = 0; k < S.order; ++k)
-                    data.push_back(float(rate_to_dev(S.rate[k + S.order * (j + S.nproc * i)])));
-        h.rb_off = off();
-        for (int i = 0; i < nI; ++i)
-            for (int k = 0; k < S.order; ++k)
-                data.push_back(S.rb.empty() ? 0.0f : float(rate_to_dev(S.rb[k + S.order * i])));
+                    data.push_back(S.rb.empty() ? 0.0f : float(rate_to_dev(S.rb[k + S.order * i])));
+        }
         h.cl_off = -1;
         if (c->cl_order > 0 && s != PCL_PHOTON) {
             const std::vector<double>& cf = (s == PCL_ELECTRON) ? c->cl_ec : c->cl_pc;
@@ -267,6 +296,20 @@ static int build_blob(Ctx* c) {
             h.cl_xscale = float(1.0 / (c->cl_xmax / mc2));
             for (int i = 0; i <= c->cl_k; ++i)
                 for (int k = 0; k < c->cl_order; ++k) data.push_back(float(force_to_dev(cf[k + c->cl_order * i])));
+        }
+        h.rbB_off = -1;
+        if (c->nswarm > 0 && S.table_kind == 0 && S.nproc > 0 && s != PCL_PHOTON) {
+            // swarm mode: the rate bound of swarm k is A + Fdt_k B (compratebound is linear in Fdt)
+            const int nI = S.nint + 1;
+            std::vector<double> A(size_t(S.order) * nI), Bt(size_t(S.order) * nI);
+            pcl_ratebound_split(s, S.order, S.nproc, S.nint, S.xmax, S.rate.data(), c->swarm_safety, A.data(),
+                                Bt.data());
+            h.rb_off = off();
+            for (int i = 0; i < nI; ++i)
+                for (int k = 0; k < S.order; ++k) data.push_back(float(rate_to_dev(A[k + S.order * i])));
+            h.rbB_off = off();
+            for (int i = 0; i < nI; ++i)
+                for (int k = 0; k < S.order; ++k) data.push_back(float(rate_to_dev(Bt[k + S.order * i])));
         }
         for (int j = 0; j < S.nproc; ++j) pack_proc(S.procs[j], S.sb_index[j], h.proc[j]);
         if (S.hist_bins > 0) {
@@ -288,6 +331,17 @@ static int build_blob(Ctx* c) {
     for (int a = 0; a < 3; ++a) {
         H.E[a] = float(force_to_dev(e * c->E[a]));            // per unit charge
         H.B[a] = float(e * c->B[a] / m_e * NS);
+    }
+    H.nswarm = c->nswarm;
+    H.swarm_off = off();
+    if (c->nswarm > 0) {
+        for (int k = 0; k < c->nswarm; ++k) {
+            for (int a = 0; a < 3; ++a) data.push_back(float(force_to_dev(e * c->swarm_E[3 * k + a])));
+            data.push_back(float(c->swarm_Fdt[k]));
+        }
+    } else {
+        for (int a = 0; a < 3; ++a) data.push_back(H.E[a]);
+        data.push_back(0.0f);
     }
     while (data.size() % 4) data.push_back(0.0f);
     size_t bytes = sizeof(BlobHdr) + data.size() * 4;
@@ -442,7 +496,7 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
     for (int k = 0; k < nsteps; ++k) c->particle_steps += (long long)c->h_ctl->live_start[k];
     for (int s = 0; s < 3; ++s) c->live[s] = (long long)c->h_ctl->live_end[nsteps - 1][s];
     c->steps_since_compact += nsteps;
-    int period = c->cfg.compaction_period > 0 ? c->cfg.compaction_period : 1;
+    int period = c->cfg.compaction_period > 0 ? c->cfg.compaction_period : 8;
     if (c->steps_since_compact >= period) {
         if ((rc = compact_all(c))) return rc;
     }
@@ -564,6 +618,7 @@ int pcl_set_collision_table(void* ctx, int species, int order, int nproc, int ni
         return fail(c, PCL_ERR_INVALID, "bad collision table");
     SpeciesState& S = c->sp[species];
     const int nI = nintervals + 1;
+    S.table_kind = 0;
     S.order = order; S.nproc = nproc; S.nint = nintervals; S.xmax = xmax;
     S.rate.assign(rate, rate + size_t(order) * nproc * nI);
     if (nproc == 0) S.rate.clear();
@@ -573,7 +628,7 @@ int pcl_set_collision_table(void* ctx, int species, int order, int nproc, int ni
     CK(cudaSetDevice(c->device));
     for (int j = 0; j < nproc; ++j) {
         const pcl_process& P = procs[j];
-        if (P.kind < PCL_PROC_MOLLER || P.kind > PCL_PROC_ANNIHILATION)
+        if (P.kind < PCL_PROC_MOLLER || P.kind > PCL_PROC_NULL_COLLISION)
             return fail(c, PCL_ERR_UNSUPPORTED, "unsupported process kind");
         if (P.kind == PCL_PROC_SELTZER_BERGER) {
             if (!P.aux0 || !P.aux2 || P.naux < 2 || P.naux2 < 2)
@@ -608,6 +663,32 @@ int pcl_set_collision_table(void* ctx, int species, int order, int nproc, int ni
     return PCL_OK;
 }
 
+int pcl_set_linear_table(void* ctx, int species, int nproc, int n, double e0, double e1, const double* rate,
+                         const double* ratebound, int nrb, const pcl_process* procs) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (nproc < 0 || nproc > PCL_MAX_PROC || n < 2 || !(e1 > e0) || !ratebound || (nrb != 1 && nrb != n) ||
+        (nproc > 0 && (!rate || !procs)))
+        return fail(c, PCL_ERR_INVALID, "bad linear collision table");
+    for (int j = 0; j < nproc; ++j)
+        if (procs[j].kind != PCL_PROC_ELASTIC && procs[j].kind != PCL_PROC_EXCITATION &&
+            procs[j].kind != PCL_PROC_NULL_COLLISION && procs[j].kind != PCL_PROC_REL_COULOMB)
+            return fail(c, PCL_ERR_UNSUPPORTED, "process kind not supported on a linear-grid table");
+    SpeciesState& S = c->sp[species];
+    S.table_kind = 1;
+    S.nproc = nproc; S.order = 1; S.nint = 1; S.xmax = e1;
+    S.lin_n = n; S.lin_e0 = e0; S.lin_e1 = e1;
+    S.rate.assign(rate, rate + size_t(nproc) * n);
+    S.rb.resize(n);
+    for (int i = 0; i < n; ++i) S.rb[i] = ratebound[nrb == 1 ? 0 : i];
+    S.procs.assign(procs, procs + nproc);
+    S.sb_index.assign(nproc, -1);
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
 int pcl_set_forcing(void* ctx, const double E[3], const double B[3], int cl_order, int cl_k, double cl_xmax,
                     const double* cl_ec, const double* cl_pc) {
     Ctx* c = static_cast<Ctx*>(ctx);
@@ -624,6 +705,57 @@ int pcl_set_forcing(void* ctx, const double E[3], const double B[3], int cl_orde
         c->cl_pc.assign(cl_pc, cl_pc + size_t(cl_order) * (cl_k + 1));
     }
     c->blob_dirty = true;
+    return PCL_OK;
+}
+
+static int get_n(Ctx* c, int species, long long& n) {
+    unsigned long long nn = 0;
+    CK(d2h(c, &nn, &c->d_ctl->n[species], sizeof(nn)));
+    n = std::min<long long>((long long)nn, c->sp[species].cap);
+    return PCL_OK;
+}
+
+int pcl_set_swarms(void* ctx, int nswarm, const double* E, const double* Fdt, double safety) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    if (nswarm < 0 || nswarm > 256 || (nswarm > 0 && (!E || !Fdt)) || !(safety >= 0))
+        return fail(c, PCL_ERR_INVALID, "bad swarm description");
+    c->nswarm = nswarm;
+    c->swarm_safety = safety;
+    if (nswarm > 0) {
+        c->swarm_E.assign(E, E + 3 * size_t(nswarm));
+        c->swarm_Fdt.assign(Fdt, Fdt + nswarm);
+    } else {
+        c->swarm_E.clear();
+        c->swarm_Fdt.clear();
+    }
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
+int pcl_swarm_moments(void* ctx, int species, int nswarm, double* out) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !out) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (nswarm < 1 || nswarm > 256) return fail(c, PCL_ERR_INVALID, "nswarm out of range");
+    SpeciesState& S = c->sp[species];
+    CK(cudaSetDevice(c->device));
+    long long slots = 0;
+    if (S.cap > 0 && (rc = get_n(c, species, slots))) return rc;
+    double* d = nullptr;
+    CK(cudaMallocAsync(&d, sizeof(double) * 6 * nswarm, c->stream));
+    CK(cudaMemsetAsync(d, 0, sizeof(double) * 6 * nswarm, c->stream));
+    if (slots > 0) {
+        int blocks = int(std::min<long long>(4 * c->sm_count, (slots + 255) / 256));
+        k_swarm_moments<<<blocks, 256, 0, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], slots, species,
+                                                         nswarm, d);
+        CK(cudaGetLastError());
+    }
+    CK(cudaMemcpyAsync(out, d, sizeof(double) * 6 * nswarm, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaFreeAsync(d, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < nswarm; ++k) out[6 * k + 2] = e_to_si(out[6 * k + 2]);
     return PCL_OK;
 }
 
@@ -674,12 +806,6 @@ int pcl_upload(void* ctx, int species, int64_t n, const double* x, const double*
     return PCL_OK;
 }
 
-static int get_n(Ctx* c, int species, long long& n) {
-    unsigned long long nn = 0;
-    CK(d2h(c, &nn, &c->d_ctl->n[species], sizeof(nn)));
-    n = std::min<long long>((long long)nn, c->sp[species].cap);
-    return PCL_OK;
-}
 
 int pcl_download(void* ctx, int species, int64_t* n, double* x, double* p, double* w, double* t, double* s,
                  uint64_t* sid, uint32_t* ctr) {

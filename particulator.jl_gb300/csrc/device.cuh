@@ -48,6 +48,11 @@ struct SpeciesHdr {
     int32_t hist_bins;    // tally-only: histogram bins (0 = none)
     float   hist_lmin;    // log(Emin) (device energy units)
     float   hist_linv;    // bins / (log Emax - log Emin)
+    int32_t rbB_off;      // swarm mode: float offset of B in ratebound = A + Fdt B (device rate per N s), -1 = none
+    int32_t table_kind;   // 0: Chebyshev on binary intervals, 1: linear energy grid
+    int32_t lin_n;        // linear grid: points
+    float   lin_e0;       // linear grid: first energy (m_e c^2)
+    float   lin_inv_step; // linear grid: 1 / step
     DevProc proc[16];
 };
 
@@ -65,7 +70,8 @@ struct BlobHdr {
     float B[3];        // e B / m_e per ns       (times beta x B)
     int32_t nsb;
     int32_t bytes;     // total blob size (multiple of 16)
-    int32_t pad[2];
+    int32_t nswarm;    // swarm mode: swarms batched in this context (0: classic single population)
+    int32_t swarm_off; // float offset of [nswarm][4] = {E field (device units), Fdt (N s)}
 };
 
 // Device-side counters of one context (global memory, zeroed per launch

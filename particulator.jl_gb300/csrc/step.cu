@@ -27,6 +27,15 @@
 #include "device.cuh"
 #include "../../include/particulator_gb300.h"
 
+// Samplers of rare events (photon, positron, bremsstrahlung, swarm) are inlined
+// (measured faster than out-of-line calls, whose ABI spills in the 64-register
+// build); PCL_OUTLINE_RARE keeps them out of line instead.
+#ifdef PCL_OUTLINE_RARE
+#define PCL_RARE __noinline__
+#else
+#define PCL_RARE __forceinline__
+#endif
+
 namespace pcl {
 
 constexpr int   kWarpStack   = 32;          // child-stack entries per warp
@@ -70,6 +79,7 @@ struct Lane {
     uint32_t c0, c1, c2, c3;   // Philox words not yet consumed (front = c0)
     int slot;                  // input slot, or -1 for a secondary (appended on finish)
     int species;
+    int sw;                    // swarm of a batched context (top 8 bits of the stream id)
     int k;                     // time step within this launch
     int nsub;
     bool alive, rvalid;
@@ -150,6 +160,14 @@ __device__ __forceinline__ float kin_energy(int species, float px, float py, flo
     return __fdividef(p2 * ig, 1.0f + ig);
 }
 
+// The same with IEEE square root and division: used once per collision for the
+// energy handed to setr! and the samplers, where FP32 rounding feeds decisions.
+__device__ __forceinline__ float kin_energy_exact(int species, float px, float py, float pz) {
+    float p2 = px * px + py * py + pz * pz;
+    if (species == PCL_PHOTON) return sqrtf(p2);
+    return p2 / (sqrtf(1.0f + p2) + 1.0f);
+}
+
 // precheb (cheby.jl:127-143).  Energies beyond the table (x >= xmax, where the
 // reference indexes past its array) extrapolate the last interval.
 __device__ __forceinline__ int precheb(float x, int k, float xscale, float t[4], bool& oor) {
@@ -193,13 +211,37 @@ __device__ __forceinline__ float cheb_dot(const float* a, const float t[4], int 
 }
 
 // setr! (collisions.jl:63-74): r = ratebound(E) above the cut, else 0.
-__device__ __forceinline__ float setr(const SpeciesHdr& S, const KCtx& K, float E) {
+// indweight(LinRange, x) (util.jl:23-32): left grid point i and weight w of
+// point i (1 - w of point i + 1).  Outside the grid the end interval is
+// extrapolated (the reference asserts 0 <= w <= 1 there).
+__device__ __forceinline__ int lin_index(const SpeciesHdr& S, const KCtx& K, float E, float& w) {
+    float u = (E - S.lin_e0) * S.lin_inv_step;
+    int i = int(floorf(u));
+    if (i < 0) { i = 0; err(K, PCL_E_TABLE_RANGE); }
+    else if (i > S.lin_n - 2) { i = S.lin_n - 2; err(K, PCL_E_TABLE_RANGE); }
+    w = float(i + 1) - u;
+    return i;
+}
+
+__device__ __forceinline__ float setr(const SpeciesHdr& S, const KCtx& K, float E, int sw) {
     if (E < S.cut) return 0.0f;
-    float t[4];
-    bool oor = false;
-    int i = precheb(E, S.k, S.xscale, t, oor);
-    if (oor) err(K, PCL_E_TABLE_RANGE);
-    float rb = cheb_dot(K.blob + S.rb_off + i * S.order, t, S.order);
+    float rb;
+    if (S.table_kind == 1) {  // ratebound(::CollisionTable) (collision_table.jl:231-242)
+        float w;
+        int i = lin_index(S, K, E, w);
+        const float* b = K.blob + S.rb_off + i;
+        rb = w * b[0] + (1.0f - w) * b[1];
+    } else {
+        float t[4];
+        bool oor = false;
+        int i = precheb(E, S.k, S.xscale, t, oor);
+        if (oor) err(K, PCL_E_TABLE_RANGE);
+        rb = cheb_dot(K.blob + S.rb_off + i * S.order, t, S.order);
+        if (S.rbB_off >= 0) {  // batched swarms: compratebound is linear in Fdt
+            const float fdt = K.blob[K.H->swarm_off + 4 * sw + 3];   // Fdt (N s)
+            rb += fdt * cheb_dot(K.blob + S.rbB_off + i * S.order, t, S.order);
+        }
+    }
     if (!(rb > 0.0f)) {
         if (S.nproc > 0) err(K, PCL_E_NEG_RATE);
         return 0.0f;
@@ -219,14 +261,14 @@ __device__ __forceinline__ float cl_mag(const SpeciesHdr& S, const KCtx& K, floa
 
 // force(CombinedForcing(ElectromagneticField, ChebContinuumLoss), lepton)
 // (pusher.jl:14-23, field.jl:54-70, continuum.jl:45-57).  Returns beta too.
-__device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K, float px, float py,
+__device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K, int sw, float px, float py,
                                              float pz, float& bx, float& by, float& bz, float& fx,
                                              float& fy, float& fz) {
     float p2 = px * px + py * py + pz * pz;
     float ig = rsqrtf(1.0f + p2);   // 1 / gamma
     bx = px * ig; by = py * ig; bz = pz * ig;
     const float q = S.charge;
-    const float* E = K.H->E;
+    const float* E = (K.H->nswarm > 0) ? K.blob + K.H->swarm_off + 4 * sw : K.H->E;
     const float* B = K.H->B;
     fx = q * (E[0] + (by * B[2] - bz * B[1]));
     fy = q * (E[1] + (bz * B[0] - bx * B[2]));
@@ -247,11 +289,11 @@ __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K
         return;
     }
     float b1x, b1y, b1z, f1x, f1y, f1z;
-    lepton_force(S, K, L.px, L.py, L.pz, b1x, b1y, b1z, f1x, f1y, f1z);
+    lepton_force(S, K, L.sw, L.px, L.py, L.pz, b1x, b1y, b1z, f1x, f1y, f1z);
     const float h23 = h * (2.0f / 3.0f);
     float qx = L.px + h23 * f1x, qy = L.py + h23 * f1y, qz = L.pz + h23 * f1z;
     float b2x, b2y, b2z, f2x, f2y, f2z;
-    lepton_force(S, K, qx, qy, qz, b2x, b2y, b2z, f2x, f2y, f2z);
+    lepton_force(S, K, L.sw, qx, qy, qz, b2x, b2y, b2z, f2x, f2y, f2z);
     const float hc = h * kCns;
     L.x += hc * (0.25f * b1x + 0.75f * b2x);
     L.y += hc * (0.25f * b1y + 0.75f * b2y);
@@ -339,6 +381,7 @@ __device__ void emit(Lane& L, const KCtx& K, int sp, float cpx, float cpy, float
     uint32_t a = ctr0, b = L.sid_lo, c = L.sid_hi, d = 1u;
     philox4x32_10(a, b, c, d, K.A->key0, K.A->key1);
     uint32_t slo = cidx ? c : a, shi = cidx ? d : b;
+    if (K.H->nswarm > 0) shi = (shi & 0x00FFFFFFu) | (L.sid_hi & 0xFF000000u);  // inherit the swarm
     atomicAdd(&K.tal[T_SPAWN + sp], 1u);
     float4 e0 = make_float4(L.x, L.y, L.z, L.w);
     float4 e1 = make_float4(cpx, cpy, cpz, cs);
@@ -419,7 +462,7 @@ __device__ void s_moller(Lane& L, const KCtx& K, const DevProc& P, float E, uint
 }
 
 // rbeb.jl:54-80, 156-196
-__device__ void s_rbeb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+__device__ PCL_RARE void s_rbeb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
     const float B = P.p[0];
     if (!(E > B)) {  // below threshold: the reference asserts; count it and treat as null
         err(K, PCL_E_KINEMATICS);
@@ -466,7 +509,7 @@ __device__ void s_rbeb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32
 // seltzer.jl:67-122 with the photon angle of util.jl:143-159.  The inverse-CDF
 // lookup reproduces the reference's interpolation weights as written
 // (seltzer.jl:278-284, off-diagonal corners included).
-__device__ void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+__device__ PCL_RARE void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
     const SBHdr& T = K.H->sb[P.sb];
     const float* data = K.A->sb_data[P.sb];
     uint32_t bits = next_bits(L, K.A->key0, K.A->key1);
@@ -511,7 +554,7 @@ __device__ void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t
 // 1 - eps is carried explicitly (-expm1 in the first branch,
 // (1 - e0^2)(1 - U)/(1 + eps) in the second): eps -> 1 for low-energy photons
 // and the direct difference would lose most of its FP32 bits.
-__device__ void s_compton(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
+__device__ PCL_RARE void s_compton(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
     const float e0 = 1.0f / (1.0f + 2.0f * E);
     const float a1 = log1pf(2.0f * E);
     const float ome0sq = (2.0f * E * e0) * (1.0f + e0);   // 1 - e0^2
@@ -548,7 +591,7 @@ __device__ void s_compton(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
 }
 
 // photo_electric.jl:38-52, 60-99
-__device__ void s_photoelectric(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+__device__ PCL_RARE void s_photoelectric(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
     float b = P.p[0];
     for (int m = 0; m < P.nbind; ++m) { b = P.p[m]; if (E > b) break; }
     if (!(E > b)) err(K, PCL_E_KINEMATICS);
@@ -587,7 +630,7 @@ __device__ __forceinline__ float screen2(float d) {
 }
 
 // bethe_heitler.jl:5-25, 85-146
-__device__ void s_bethe_heitler(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+__device__ PCL_RARE void s_bethe_heitler(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
     const float e0 = 1.0f / E;
     if (!(e0 < 0.5f)) err(K, PCL_E_KINEMATICS);
     float eps;
@@ -644,7 +687,7 @@ __device__ void s_bethe_heitler(Lane& L, const KCtx& K, const DevProc& P, float 
 }
 
 // bhaba.jl:9-33, 55-91
-__device__ void s_bhabha(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+__device__ PCL_RARE void s_bhabha(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
     const float e0 = P.p[0] / E;
     const float g = 1.0f + E;
     const float y = 1.0f / (g + 1.0f);
@@ -679,26 +722,32 @@ __device__ void s_bhabha(Lane& L, const KCtx& K, const DevProc& P, float E, uint
 }
 
 // anihilation.jl:6-23, 39-67
-__device__ void s_annihilation(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
+__device__ PCL_RARE void s_annihilation(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
+    // Exact rewrites for FP32: eps_min = (1 - q)/2 = 1/((E + 2)(1 + q)) (1 - q
+    // cancels at high E), eps = eps_min exp(U ln(eps_max/eps_min)) with
+    // eps - eps_min = eps_min expm1(U L) and eps_max - eps = -eps_max expm1((U - 1) L),
+    // so sin^2 = 2 (E + 2)(eps_max - eps)(eps - eps_min) / (eps^2 P^2) has no cancellation.
     const float g = 1.0f + E;
-    const float q = sqrtf(E / (E + 2.0f));
-    const float emax = 0.5f * (1.0f + q), emin = 0.5f * (1.0f - q);
-    const float ratio = emax / emin;
-    float eps = 0.5f;
+    const float Ep2 = E + 2.0f;
+    const float q = sqrtf(E / Ep2);
+    const float emin = 1.0f / (Ep2 * (1.0f + q));
+    const float emax = 0.5f * (1.0f + q);
+    const float Lr = logf(emax / emin);
+    float eps = 0.5f, u = 0.5f, ex = 0.0f;
     int it = 0;
     for (;;) {
-        eps = emin * powf(ratio, U(L, K));
+        u = U(L, K);
+        ex = expm1f(u * Lr);
+        eps = emin + emin * ex;                       // eps_min (eps_max/eps_min)^U
         float gg = 1.0f - eps + (2.0f * g * eps - 1.0f) / (eps * (g + 1.0f) * (g + 1.0f));
         if (U(L, K) < gg) break;
         if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
     }
-    // with d = eps - 1/2 (exact): eps (gamma + 1) - 1 = E/2 + d (E + 2) and
-    // 1 - cos^2 = (E + 2)(q - 2d)(q + 2d) / (2 eps^2 P^2), P^2 = E (E + 2)
-    const float d = eps - 0.5f;
-    const float P2 = E * (E + 2.0f);
-    const float iP = rsqrtf(P2);
-    float cth = (0.5f * E + d * (E + 2.0f)) * iP / eps;
-    float sth = sqrtf(fmaxf(0.0f, (E + 2.0f) * (q - 2.0f * d) * (q + 2.0f * d) * 0.5f)) * iP / eps;
+    const float lo = emin * ex;                       // eps - eps_min
+    const float hi = -emax * expm1f((u - 1.0f) * Lr); // eps_max - eps
+    const float iP = rsqrtf(E * Ep2);                 // 1 / sqrt(gamma^2 - 1)
+    float cth = (eps * Ep2 - 1.0f) * iP / eps;
+    float sth = sqrtf(fmaxf(0.0f, 2.0f * Ep2 * lo * hi)) * iP / eps;
     float sph, cph;
     sincos_2pi(U(L, K), sph, cph);
     float ax, ay, az;
@@ -709,6 +758,40 @@ __device__ void s_annihilation(Lane& L, const KCtx& K, float E, uint32_t ctr0) {
     L.alive = false;
     emit(L, K, PCL_PHOTON, ax, ay, az, sa, 0, ctr0);
     emit(L, K, PCL_PHOTON, bx, by, bz, sb, 1, ctr0);
+}
+
+
+// randsphere() (util.jl:4-12): phi = 2 pi rand(), u = 2 rand() - 1
+__device__ __forceinline__ void randsphere(Lane& L, const KCtx& K, float& x, float& y, float& z) {
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float u = 2.0f * U(L, K) - 1.0f;
+    float v = sqrtf(fmaxf(0.0f, (1.0f - u) * (1.0f + u)));
+    x = v * cph; y = v * sph; z = u;
+}
+
+// collide(::Elastic, ...) (slow-electron.jl:133-139) on the momentum:
+// p_cm = m/(1+m) p, p' = randsphere() |p - p_cm| + p_cm
+__device__ PCL_RARE void s_elastic(Lane& L, const KCtx& K, const DevProc& P) {
+    const float f = P.p[0] / (1.0f + P.p[0]);
+    float cx = f * L.px, cy = f * L.py, cz = f * L.pz;
+    float dx = L.px - cx, dy = L.py - cy, dz = L.pz - cz;
+    float dn = sqrtf(dx * dx + dy * dy + dz * dz);
+    float ux, uy, uz;
+    randsphere(L, K, ux, uy, uz);
+    L.px = ux * dn + cx; L.py = uy * dn + cy; L.pz = uz * dn + cz;
+    L.s = nextcoll(L, K);
+}
+
+// collide(::Excitation, ...) (slow-electron.jl:108-114): E1 = max(0, E - threshold),
+// isotropic direction
+__device__ PCL_RARE void s_excitation(Lane& L, const KCtx& K, const DevProc& P, float E) {
+    float E1 = fmaxf(0.0f, E - P.p[0]);
+    float pn = sqrtf(E1 * (E1 + 2.0f));
+    float ux, uy, uz;
+    randsphere(L, K, ux, uy, uz);
+    L.px = ux * pn; L.py = uy * pn; L.pz = uz * pn;
+    L.s = nextcoll(L, K);
 }
 
 // Dispatch one real collision with table position j; updates the primary
@@ -727,32 +810,47 @@ __device__ void sample_process(Lane& L, const KCtx& K, const SpeciesHdr& S, cons
         case PCL_PROC_BETHE_HEITLER: s_bethe_heitler(L, K, P, E, ctr0); break;
         case PCL_PROC_BHABHA: s_bhabha(L, K, P, E, ctr0); break;
         case PCL_PROC_ANNIHILATION: s_annihilation(L, K, E, ctr0); break;
+        case PCL_PROC_ELASTIC: s_elastic(L, K, P); break;
+        case PCL_PROC_EXCITATION: s_excitation(L, K, P, E); break;
+        case PCL_PROC_NULL_COLLISION: L.s = nextcoll(L, K); break;  // NullOutcome (collisions.jl:83-88)
         default: err(K, PCL_E_KINEMATICS); break;
     }
-    if (L.alive) L.r = setr(S, K, kin_energy(L.species, L.px, L.py, L.pz));
+    if (L.alive) L.r = setr(S, K, kin_energy_exact(L.species, L.px, L.py, L.pz), L.sw);
 }
 
 // do_one_collision! (collisions.jl:142-199)
 __device__ void collide(Lane& L, const KCtx& K, const SpeciesHdr& S) {
     if (L.r == 0.0f) return;
-    float E = kin_energy(L.species, L.px, L.py, L.pz);
+    float E = kin_energy_exact(L.species, L.px, L.py, L.pz);
     if (!(E >= S.cut)) return;
-    float t[4];
-    bool oor = false;
-    int i = precheb(E, S.k, S.xscale, t, oor);
-    if (oor) err(K, PCL_E_TABLE_RANGE);
     const uint32_t ctr0 = L.ctr;
-    float xi = U(L, K) * L.r;
-    const float* a = K.blob + S.rate_off + i * S.nproc * S.order;
     int j = 0;
-    for (; j < S.nproc; ++j) {
-        float nu = cheb_dot(a + j * S.order, t, S.order);
-        if (nu > xi) break;
-        xi -= nu;
+    if (S.table_kind == 1) {  // rate(::CollisionTable, j, pre) (collision_table.jl:249-256)
+        float w;
+        int i = lin_index(S, K, E, w);
+        float xi = U(L, K) * L.r;
+        const float* a = K.blob + S.rate_off + i * S.nproc;
+        for (; j < S.nproc; ++j) {
+            float nu = w * a[j] + (1.0f - w) * a[j + S.nproc];
+            if (nu > xi) break;
+            xi -= nu;
+        }
+    } else {
+        float t[4];
+        bool oor = false;
+        int i = precheb(E, S.k, S.xscale, t, oor);
+        if (oor) err(K, PCL_E_TABLE_RANGE);
+        float xi = U(L, K) * L.r;
+        const float* a = K.blob + S.rate_off + i * S.nproc * S.order;
+        for (; j < S.nproc; ++j) {
+            float nu = cheb_dot(a + j * S.order, t, S.order);
+            if (nu > xi) break;
+            xi -= nu;
+        }
     }
     if (j == S.nproc) {  // NullOutcome (collisions.jl:83-88)
         atomicAdd(&K.tal[T_NULL + L.species], 1u);
-        L.r = setr(S, K, E);
+        L.r = setr(S, K, E, L.sw);
         L.s = nextcoll(L, K);
         return;
     }
@@ -886,7 +984,8 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 L.species = int(sk & 3u); L.k = int(sk >> 2);
                 L.th = c.w; L.tlo = 0.0f;
                 L.ctr = 0u; L.rvalid = false; L.slot = -1; L.alive = true; L.nsub = 0;
-                L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz));
+                L.sw = (H->nswarm > 0) ? min(int(L.sid_hi >> 24), H->nswarm - 1) : 0;
+                L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz), L.sw);
                 has = true;
             }
             __syncwarp();
@@ -940,7 +1039,8 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                     }
                     if (has) {
                         L.rvalid = false; L.alive = true; L.nsub = 0;
-                        L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz));
+                        L.sw = (H->nswarm > 0) ? min(int(L.sid_hi >> 24), H->nswarm - 1) : 0;
+                        L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz), L.sw);
                     }
                 }
                 cur += tk;
@@ -990,7 +1090,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         L.k += 1;
                         L.nsub = 0;
                         dd_add(L.th, L.tlo, dt_hi, dt_lo);  // remainder below eps carries over (mixed_population.jl:65)
-                        L.r = setr(S, K, E);  // advance_init! of the next step
+                        L.r = setr(S, K, E, L.sw);  // advance_init! of the next step
                         atomicAdd(&tal[T_LSTART + L.k], 1u);
                     }
                 }
@@ -1210,6 +1310,43 @@ __global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta,
     }
 }
 
+// FP64 moments per swarm of a batched context: out[sw][6] = {live, sum w,
+// sum w E, sum w z, sum w z^2, sum w x^2 + y^2}; lanes of one warp are grouped
+// by swarm before the atomics.
+__global__ void k_swarm_moments(const float4* xw, const float4* ps, const uint4* meta, long long n, int species,
+                                int nswarm, double* out) {
+    for (long long i0 = (long long)blockIdx.x * blockDim.x; i0 < n; i0 += (long long)gridDim.x * blockDim.x) {
+        long long i = i0 + threadIdx.x;
+        bool live = false;
+        int sw = 0;
+        double v[6] = {0, 0, 0, 0, 0, 0};
+        if (i < n) {
+            uint4 m = meta[i];
+            if (m.z != PCL_DEAD_CTR) {
+                live = true;
+                sw = min(int(m.y >> 24), nswarm - 1);
+                float4 a = xw[i], b = ps[i];
+                double p2 = double(b.x) * b.x + double(b.y) * b.y + double(b.z) * b.z;
+                double E = (species == PCL_PHOTON) ? sqrt(p2) : p2 / (sqrt(1.0 + p2) + 1.0);
+                double w = a.w;
+                v[0] = 1.0; v[1] = w; v[2] = w * E; v[3] = w * a.z; v[4] = w * double(a.z) * a.z;
+                v[5] = w * (double(a.x) * a.x + double(a.y) * a.y);
+            }
+        }
+        unsigned act = __ballot_sync(0xffffffffu, live);
+        if (live) {
+            unsigned grp = __match_any_sync(act, sw);
+            int leader = __ffs(grp) - 1;
+            // every lane of the group sums the group's values; the leader commits
+            for (int q = 0; q < 6; ++q) {
+                double tot = 0.0;
+                for (unsigned g = grp; g; g &= g - 1) tot += __shfl_sync(grp, v[q], __ffs(g) - 1);
+                if ((threadIdx.x & 31) == leader) atomicAdd(&out[6 * sw + q], tot);
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------- sampler test ----
 // Test hook behind pcl_test_sampler: force table position j for n primaries.
 __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, const float* p_in,
@@ -1233,10 +1370,10 @@ __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, cons
     L.x = L.y = L.z = 0.0f; L.w = 1.0f; L.th = 0.0f; L.tlo = 0.0f; L.k = 0; L.s = 0.0f;
     L.px = p_in[3 * i]; L.py = p_in[3 * i + 1]; L.pz = p_in[3 * i + 2];
     L.sid_lo = sid[2 * i]; L.sid_hi = sid[2 * i + 1]; L.ctr = 0u; L.rvalid = false;
-    L.species = species; L.alive = true; L.slot = -1; L.nsub = 0;
+    L.species = species; L.alive = true; L.slot = -1; L.nsub = 0; L.sw = 0;
     const SpeciesHdr& S = H->sp[species];
     float E = kin_energy(species, L.px, L.py, L.pz);
-    L.r = setr(S, K, E);
+    L.r = setr(S, K, E, 0);
     const DevProc& P = S.proc[j];
     sample_process(L, K, S, P, E, 0u);
     for (int q = 0; q < 3; ++q) out_kind[3 * i + q] = -1;

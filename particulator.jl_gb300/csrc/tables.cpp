@@ -576,6 +576,33 @@ extern "C" int pcl_build_collision_table(int species, int nproc, const pcl_proce
     return PCL_OK;
 }
 
+extern "C" int pcl_ratebound_split(int species, int order, int nproc, int nintervals, double xmax,
+                                   const double* rate, double safety, double* A, double* B) {
+    if (species < 0 || species >= PCL_NSPECIES || order < 1 || order > PCL_MAX_ORDER || nproc < 0 ||
+        nproc > PCL_MAX_PROC || nintervals < 1 || nintervals > PCL_MAX_INTERVALS || !(xmax > 0) || !A || !B ||
+        (nproc > 0 && !rate))
+        return PCL_ERR_INVALID;
+    BinaryIntervals b{nintervals, xmax};
+    const int nI = nintervals + 1;
+    for (int i = 0; i < nI; ++i)
+        for (int k = 0; k < order; ++k) {
+            double s = 0.0;
+            for (int j = 0; j < nproc; ++j) s += rate[k + order * (j + nproc * i)];
+            A[k + order * i] = s;
+        }
+    const int st = 1, ld = order * nproc;
+    chebfit(
+        [&](double eng) {
+            if (nproc == 0 || species == PCL_PHOTON) return 0.0;
+            double df = 0.0;
+            for (int j = 0; j < nproc; ++j) df += chebdiff(eng, b, rate + order * j, order, st, ld);
+            double g = 1 + eng / (si::m_e * si::c * si::c);
+            return g * g * g * speed(species, eng) * std::fabs(df) * safety;
+        },
+        b, order, B);
+    return PCL_OK;
+}
+
 // ---- continuum losses (continuum.jl:63-139) ----
 namespace pcl {
 static void x0x1(double C, double& x0, double& x1) {

@@ -15,7 +15,7 @@ import numpy as np
 from . import _lib
 from . import constants as co
 from .forcing import RK2Pusher
-from .tables import Electron, Photon, Positron, PARTICLE_NAMES, ChebyshevCollisionTable
+from .tables import Electron, Photon, Positron, PARTICLE_NAMES, ChebyshevCollisionTable, CollisionTable
 
 SPECIES_BY_NAME = {"electron": Electron, "photon": Photon, "positron": Positron}
 
@@ -148,7 +148,7 @@ class MultiPopulation:
     keywords select the device, the Philox seed and the launch shape."""
 
     def __init__(self, *pairs, seed: int = 0, device: int = 0, steps_per_launch: int = 1,
-                 compaction_period: int = 1, block_size: int = 0, grid_blocks: int = 0, blocks_per_sm: int = 0,
+                 compaction_period: int = 0, block_size: int = 0, grid_blocks: int = 0, blocks_per_sm: int = 0,
                  **named):
         index = {}
         for name, pop in list(pairs) + list(named.items()):
@@ -185,7 +185,15 @@ class MultiPopulation:
         _lib.check(L.pcl_set_species(self.ctx, key, pop.energy_cut, pop.max_particles, flags), self.ctx,
                    "pcl_set_species")
         tab = pop.collisions
-        if tab is not None:
+        if isinstance(tab, CollisionTable):
+            procs = tab.c_procs()
+            self._keep.append((procs, tab))
+            rate = np.ascontiguousarray(tab.rate.T)   # rate[j + nproc * k]
+            rb = np.ascontiguousarray(tab.ratebound, dtype=float)
+            e0, e1, n = tab.energy
+            _lib.check(L.pcl_set_linear_table(self.ctx, key, tab.nproc, n, e0, e1, _lib.dptr(rate), _lib.dptr(rb),
+                                              len(rb), procs), self.ctx, "pcl_set_linear_table")
+        elif tab is not None:
             procs = tab.c_procs()
             self._keep.append((procs, tab))
             rate = np.ascontiguousarray(tab.rate) if tab.nproc else np.zeros(1)
@@ -230,6 +238,25 @@ class MultiPopulation:
                                    _lib.dptr(cl.ec), _lib.dptr(cl.pc))
         _lib.check(rc, self.ctx, "pcl_set_forcing")
         self._pusher_key = key
+
+    def set_swarms(self, E, Fdt, safety: float = 1.15):
+        """Swarm mode (pcl_set_swarms): swarm s (top 8 bits of a particle's
+        stream id) feels field E[s] (V/m) and uses the rate bound for Fdt[s]."""
+        E = np.ascontiguousarray(np.asarray(E, dtype=float).reshape(-1, 3))
+        Fdt = np.ascontiguousarray(np.asarray(Fdt, dtype=float).reshape(-1))
+        self._keep.append((E, Fdt))
+        _lib.check(_lib.lib().pcl_set_swarms(self.ctx, len(Fdt), _lib.dptr(E), _lib.dptr(Fdt), float(safety)),
+                   self.ctx, "pcl_set_swarms")
+        self.nswarm = len(Fdt)
+
+    def swarm_moments(self, particle, nswarm: int | None = None) -> np.ndarray:
+        """Per-swarm FP64 moments [nswarm, 6]: live, sum w, sum w E (J), sum w z,
+        sum w z^2, sum w (x^2 + y^2)."""
+        key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        ns = nswarm or getattr(self, "nswarm", 1)
+        out = np.zeros(6 * ns)
+        _lib.check(_lib.lib().pcl_swarm_moments(self.ctx, key, ns, _lib.dptr(out)), self.ctx, "pcl_swarm_moments")
+        return out.reshape(ns, 6)
 
     def tallies(self) -> _lib.Tallies:
         t = _lib.Tallies()

@@ -191,6 +191,37 @@ class SeltzerBerger(_Proc):
         p.naux2 = self.ncum
 
 
+class Elastic(_Proc):
+    """Elastic(mass_ratio) (slow-electron.jl:82-84, 133-139): isotropic scattering
+    in the centre of mass frame of an electron and a target of mass m / mass_ratio."""
+    kind = _lib.PROC_ELASTIC
+
+    def __init__(self, mass_ratio: float):
+        self.mass_ratio = float(mass_ratio)
+
+    def _fill(self, p):
+        p.param[0] = self.mass_ratio
+        p.nparam = 1
+
+
+class Excitation(_Proc):
+    """Excitation(threshold) (slow-electron.jl:70-72, 108-114): the electron loses
+    `threshold` and leaves isotropically."""
+    kind = _lib.PROC_EXCITATION
+
+    def __init__(self, threshold: float):
+        self.threshold = float(threshold)
+
+    def _fill(self, p):
+        p.param[0] = self.threshold
+        p.nparam = 1
+
+
+class NullCollision(_Proc):
+    """NullCollision (collisions.jl:3, 58) as an explicit table entry."""
+    kind = _lib.PROC_NULL_COLLISION
+
+
 def totalcs(proc: _Proc, energy) -> np.ndarray:
     """Total cross section per target (m^2) at kinetic energies (J)."""
     E = np.ascontiguousarray(np.atleast_1d(np.asarray(energy, dtype=np.float64)))

@@ -4,6 +4,7 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass, field
+from typing import Callable, Sequence
 
 import numpy as np
 
@@ -159,3 +160,70 @@ class ChebContinuumLoss:
         a = (self.ec if particle == Electron else self.pc).reshape(self.bints.k + 1, self.n)
         i, t = precheb(eng, self.bints, self.n)
         return float(sum(a[i, q] * t[q] for q in range(self.n)))
+
+
+@dataclass
+class CollisionTable:
+    """CollisionTable (collision_table.jl:15-57): rates of processes j on the linear
+    energy grid LinRange(e0, e1, n), rate[j, k] (1/s), and a rate bound that is one
+    number or one value per grid point."""
+    proc: tuple
+    energy: tuple            # (e0, e1, n) in J
+    rate: np.ndarray         # (nproc, n)
+    ratebound: np.ndarray    # (1,) or (n,)
+    particle: int = Electron
+
+    def __len__(self):
+        return len(self.proc)
+
+    @property
+    def nproc(self):
+        return len(self.proc)
+
+    def grid(self) -> np.ndarray:
+        e0, e1, n = self.energy
+        i = np.arange(n)
+        return (e0 * (n - 1 - i) + e1 * i) / (n - 1)
+
+    def c_procs(self):
+        arr = (_lib.Process * max(1, self.nproc))()
+        for j, p in enumerate(self.proc):
+            arr[j] = p.to_c(1.0)
+        return arr
+
+
+def lxcat_table(entries: Sequence, energy: tuple, null: bool = True, particle: int = Electron) -> CollisionTable:
+    """A linear-grid table built the way load_lxcat builds one (lxcat.jl:17-134):
+    nu_j = density_j * v * sigma_j(E) with v = sqrt(2 E / m) on the grid, a
+    NullCollision filling up to the maximum total rate, which is the constant
+    rate bound, and the processes ordered by their rate summed over the grid
+    (descending).  ``entries`` are ``(process, density, sigma)`` with
+    ``sigma(E)`` in m^2 for energies in J."""
+    e0, e1, n = energy
+    i = np.arange(n)
+    E = (e0 * (n - 1 - i) + e1 * i) / (n - 1)
+    v = np.sqrt(2 * E / co.electron_mass)
+    procs = [p for p, _, _ in entries]
+    rate = np.array([dens * v * np.asarray(sig(E), dtype=float) for _, dens, sig in entries])
+    total = rate.sum(axis=0)
+    maxrate = float(total.max())
+    if null:
+        from .processes import NullCollision
+        procs.append(NullCollision())
+        rate = np.vstack([rate, maxrate - total])
+    perm = sorted(range(len(procs)), key=lambda j: -float(rate[j].sum()))
+    return CollisionTable(tuple(procs[j] for j in perm), (float(e0), float(e1), int(n)),
+                          np.ascontiguousarray(rate[perm]), np.array([maxrate]), particle)
+
+
+def ratebound_split(tab: ChebyshevCollisionTable, safety: float = 1.1):
+    """(A, B) with compratebound(Fdt) = A + Fdt B (collision_table.jl:152-167),
+    each [order][k+1] flat like ``tab.ratebound``."""
+    nI = tab.b.k + 1
+    A = np.zeros(tab.order * nI)
+    B = np.zeros(tab.order * nI)
+    rate = np.ascontiguousarray(tab.rate) if tab.nproc else np.zeros(1)
+    rc = _lib.lib().pcl_ratebound_split(int(tab.particle), tab.order, tab.nproc, tab.b.k, tab.b.xmax,
+                                        _lib.dptr(rate), float(safety), _lib.dptr(A), _lib.dptr(B))
+    _lib.check(rc, None, "pcl_ratebound_split")
+    return A, B

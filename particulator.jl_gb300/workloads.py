@@ -13,10 +13,10 @@ import numpy as np
 from . import constants as co
 from .forcing import CombinedForcing, ElectromagneticField, HomogeneousField, RK2Pusher
 from .population import MultiPopulation, ParticleArrays, Population
-from .processes import (BetheHeitler, Bhaba, Compton, Moller, ORBITALS, PhotoElectric, PositronAnihilation,
-                        RelativisticCoulomb, SeltzerBerger)
+from .processes import (BetheHeitler, Bhaba, Compton, Elastic, Excitation, Moller, ORBITALS, PhotoElectric,
+                        PositronAnihilation, RelativisticCoulomb, SeltzerBerger)
 from .tables import (ChebContinuumLoss, ContinuumLoss, Electron, Photon, Positron,
-                     collision_table_from_processes, momentum_norm_from_kin)
+                     collision_table_from_processes, lxcat_table, momentum_norm_from_kin)
 
 KEV = 1e3 * co.eV
 MEV = 1e6 * co.eV
@@ -140,3 +140,84 @@ def avalanche(n: int = 10000, kin: float = 1 * MEV, efield: float = 5e5, dt: flo
     mp = MultiPopulation(("electron", electrons), ("photon", photons), ("positron", positrons), seed=seed, **cfg)
     cl = air_continuum_loss(comp, Tcut=cut_e)
     return Workload(mp, pusher((0.0, 0.0, -efield), cl=cl), dt, 1.0, "rrea-air-0.5MVm")
+
+
+def reid_table(density: float, emax: float = 8.0 * co.eV, n: int = 4001, mass_ratio: float = 4e-3):
+    """Reid's ramp model gas: elastic sigma = 6e-20 m^2 (constant), inelastic
+    sigma = 10e-20 (eps - 0.2 eV)/eV m^2 above a 0.2 eV threshold, on a linear
+    grid [0, emax] with the constant majorant of load_lxcat."""
+    thr = 0.2 * co.eV
+    el = (Elastic(mass_ratio), density, lambda E: np.full_like(E, 6e-20))
+    ex = (Excitation(thr), density, lambda E: np.where(E > thr, 10e-20 * (E - thr) / co.eV, 0.0))
+    return lxcat_table([el, ex], (0.0, emax, n))
+
+
+def reid_ramp(n: int = 1 << 20, EN_Td: float = 12.0, density: float = 2.504e25, dt: float = 1e-12, seed: int = 2,
+              mean_energy: float = 1.0 * co.eV, emax: float = 8.0 * co.eV, **cfg) -> Workload:
+    """Low-energy swarm in Reid's ramp model gas: n electrons with a Maxwellian of
+    the given mean energy, field E = (E/N) N along -z, no energy cut."""
+    tab = reid_table(density, emax)
+    rng = np.random.Generator(np.random.Philox(seed))
+    kT = 2.0 / 3.0 * mean_energy
+    p = rng.normal(scale=np.sqrt(co.electron_mass * kT), size=(n, 3))
+    arr = ParticleArrays(np.zeros((n, 3)), p, np.ones(n), np.zeros(n))
+    electrons = Population(n + n // 8, arr, tab, 0.0, particle=Electron)
+    mp = MultiPopulation(("electron", electrons), seed=seed, **cfg)
+    E = EN_Td * co.Td * density
+    return Workload(mp, pusher((0.0, 0.0, -E)), dt, 1.0, f"reid-ramp-{EN_Td:g}Td")
+
+
+@dataclass
+class SwarmBatch:
+    mpopl: MultiPopulation
+    pusher: RK2Pusher
+    dt: float
+    E: np.ndarray          # [nswarm] field magnitudes (V/m, along -z)
+    n0: np.ndarray         # [nswarm] initial electrons
+    tables: tuple          # (electron, photon, positron) tables of the batch
+    arrays: list           # per-swarm initial ParticleArrays (electrons)
+
+
+def swarm_initial(nswarm: int = 256, e_range=(3e5, 3e6), n_range=(1e2, 1e5), seed: int = 3, kin: float = 1 * MEV):
+    """Fields log-spaced over e_range, initial sizes log-uniform over n_range
+    (Philox seed), electrons at `kin` with isotropic directions at the origin;
+    stream ids carry the swarm in their top 8 bits."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    E = np.geomspace(e_range[0], e_range[1], nswarm)
+    n0 = np.exp(rng.uniform(np.log(n_range[0]), np.log(n_range[1]), nswarm)).astype(int)
+    arrays = []
+    for s in range(nswarm):
+        p = isotropic(int(n0[s]), kin, rng)
+        sid = (np.uint64(s) << np.uint64(56)) | np.arange(n0[s], dtype=np.uint64)
+        arrays.append(ParticleArrays(np.zeros((n0[s], 3)), p, np.ones(n0[s]), np.zeros(n0[s]), sid=sid))
+    return E, n0, arrays
+
+
+def swarm_batch(nswarm: int = 256, e_range=(3e5, 3e6), n_range=(1e2, 1e5), seed: int = 3, dt: float = 1e-12,
+                swarms=None, growth: float = 1.5, **cfg) -> SwarmBatch:
+    """`nswarm` independent avalanche swarms in one context (swarm mode): each
+    has its own field and rate bound; photons and positrons are tracked as in
+    the mixed avalanche.  ``swarms`` restricts the batch to a subset (e.g. one
+    swarm run alone)."""
+    comp = air_composition()
+    E, n0, arrays = swarm_initial(nswarm, e_range, n_range, seed)
+    sel = list(range(nswarm)) if swarms is None else list(swarms)
+    Fdt = co.elementary_charge * E * dt
+    et, gt, pt = beam_tables(comp, float(E[sel[0]]), dt)
+    x = np.concatenate([arrays[s].x for s in sel]); p = np.concatenate([arrays[s].p for s in sel])
+    sid = np.concatenate([arrays[s].sid for s in sel])
+    n = len(sid)
+    arr = ParticleArrays(x, p, np.ones(n), np.zeros(n), sid=sid)
+    cap = int(growth * n) + (1 << 14)
+    mp = MultiPopulation(("electron", Population(cap, arr, et, 10 * KEV, particle=Electron)),
+                         ("photon", Population(max(cap // 2, 1 << 14), ParticleArrays.empty(), gt, 5 * KEV,
+                                               particle=Photon)),
+                         ("positron", Population(max(cap // 16, 1 << 12), ParticleArrays.empty(), pt, 10 * KEV,
+                                                 particle=Positron)),
+                         seed=seed, **cfg)
+    Evec = np.zeros((nswarm, 3))
+    Evec[:, 2] = -E
+    # a subset keeps its swarm ids: all swarms are described, the subset populated
+    mp.set_swarms(Evec, Fdt, safety=1.15)
+    cl = air_continuum_loss(comp)
+    return SwarmBatch(mp, pusher((0.0, 0.0, -float(E[sel[0]])), cl=cl), dt, E, n0, (et, gt, pt), arrays)

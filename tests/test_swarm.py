@@ -1,0 +1,213 @@
+"""Low-energy swarm (Reid's ramp model gas) on the linear-grid table:
+sampler invariants in the oracle (CPU), device parity against the oracle, and
+the FP32-device versus Float64-oracle comparison of swarm observables."""
+import numpy as np
+import pytest
+
+EV = 1.6021766208e-19
+
+
+@pytest.fixture(scope="module")
+def reid(pcl):
+    N = 2.504e25
+    tab = pcl.workloads.reid_table(N)
+    return N, tab
+
+
+def _pusher(pcl, N, EN):
+    return pcl.workloads.pusher((0.0, 0.0, -EN * pcl.co.Td * N))
+
+
+def _maxwell(pcl, n, mean_ev, seed):
+    rng = np.random.default_rng(seed)
+    kT = 2.0 / 3.0 * mean_ev * EV
+    p = rng.normal(scale=np.sqrt(pcl.co.electron_mass * kT), size=(n, 3))
+    return p
+
+
+def test_lxcat_table_layout(pcl, reid):
+    N, tab = reid
+    names = [type(p).__name__ for p in tab.proc]
+    assert names == ["NullCollision", "Excitation", "Elastic"]
+    E = tab.grid()
+    tot = tab.rate.sum(axis=0)
+    np.testing.assert_allclose(tot, tab.ratebound[0], rtol=1e-12)  # null fills up to the majorant
+    v = np.sqrt(2 * E / pcl.co.electron_mass)
+    el = tab.rate[names.index("Elastic")]
+    np.testing.assert_allclose(el, N * v * 6e-20, rtol=1e-12)
+
+
+def test_swarm_samplers_oracle(pcl, oracle, reid):
+    N, tab = reid
+    W = oracle.OracleWorld(3, {pcl.Electron: tab}, {pcl.Electron: 0.0}, _pusher(pcl, N, 12.0))
+    p = _maxwell(pcl, 2000, 2.0, 1)
+    sid = np.arange(2000, dtype=np.uint64)
+    E = pcl.kinenergy(pcl.Electron, p)
+    names = [type(q).__name__ for q in tab.proc]
+    # Elastic: |p - p_cm| is kept, p_cm = m/(1+m) p
+    j = names.index("Elastic")
+    op, os_, ok, oc, ot = W.sample(pcl.Electron, j, p, sid)
+    mr = tab.proc[j].mass_ratio
+    cm = mr / (1 + mr) * p
+    np.testing.assert_allclose(np.linalg.norm(op[:, 0] - cm, axis=1), np.linalg.norm(p - cm, axis=1), rtol=1e-12)
+    assert np.all(oc == 3)  # randsphere (2) + s
+    # Excitation: loses the threshold (or stops)
+    j = names.index("Excitation")
+    op, os_, ok, oc, ot = W.sample(pcl.Electron, j, p, sid)
+    E1 = pcl.kinenergy(pcl.Electron, op[:, 0])
+    # momentum_norm_from_kin cancels near E1 = 0 (electron.jl:51): 1e-7 relative there
+    np.testing.assert_allclose(E1, np.maximum(0, E - 0.2 * EV), rtol=1e-7, atol=1e-30)
+
+
+def _swarm(pcl, reid, n, EN, seed, **cfg):
+    N, tab = reid
+    p = _maxwell(pcl, n, 1.0, seed)
+    arr = pcl.ParticleArrays(np.zeros((n, 3)), p, np.ones(n), np.zeros(n))
+    mp = pcl.MultiPopulation(("electron", pcl.Population(n + 64, arr, tab, 0.0, particle=pcl.Electron)),
+                             seed=seed, **cfg)
+    return mp
+
+
+@pytest.mark.gpu
+def test_swarm_parity(pcl, oracle, gpu, reid):
+    """A few steps of 1 ps (~35 sub-steps each, mostly null collisions): draws
+    bit-exact and momenta within 1e-5 against the oracle."""
+    N, tab = reid
+    pusher = _pusher(pcl, N, 24.0)
+    mp = _swarm(pcl, reid, 4096, 24.0, 7)
+    W = oracle.OracleWorld(7, {pcl.Electron: tab}, {pcl.Electron: 0.0}, pusher)
+    W.upload(pcl.Electron, mp.get(pcl.Electron).particles())
+    for k in range(3):
+        pcl.advance(mp, pusher, (k + 1) * 1e-12)
+        W.advance((k + 1) * 1e-12, 4)
+    rep = oracle.compare_populations(mp.get(pcl.Electron).particles(), W.download(pcl.Electron), pcl.Electron,
+                                     rtol=1e-5, stol=2e-4)
+    assert rep["ok"], str(rep)
+    t = mp.tallies()
+    c = W.counters()
+    assert abs(int(np.sum(t.collisions[0])) - int(c["coll"][0].sum())) <= 4 * (c["ties"] + 1)
+    mp.close()
+
+
+@pytest.mark.gpu
+def test_swarm_observables_fp32_vs_fp64(pcl, oracle, gpu, reid):
+    """Drift velocity, mean energy and longitudinal diffusion of the FP32 device
+    against the Float64 oracle from the same initial swarm and streams, after
+    the swarm relaxes: within the combined statistical error (4 sigma)."""
+    N, tab = reid
+    EN = 12.0
+    pusher = _pusher(pcl, N, EN)
+    n, steps, dt = 8192, 120, 2e-12
+    mp = _swarm(pcl, reid, n, EN, 11)
+    W = oracle.OracleWorld(11, {pcl.Electron: tab}, {pcl.Electron: 0.0}, pusher)
+    W.upload(pcl.Electron, mp.get(pcl.Electron).particles())
+    zg, zo, tt = [], [], []
+    for k in range(steps):
+        t = (k + 1) * dt
+        pcl.advance(mp, pusher, t)
+        W.advance(t, 8)
+        if k >= steps // 2:
+            m = mp.get(pcl.Electron).moments()
+            zg.append(m[4] / m[0])
+            zo.append(np.mean(W.download(pcl.Electron).x[:, 2]))
+            tt.append(t)
+    g = mp.get(pcl.Electron).particles()
+    o = W.download(pcl.Electron)
+    Eg, Eo = pcl.kinenergy(0, g.p), pcl.kinenergy(0, o.p)
+    se = np.hypot(Eg.std() / np.sqrt(len(Eg)), Eo.std() / np.sqrt(len(Eo)))
+    assert abs(Eg.mean() - Eo.mean()) < 4 * se + 1e-3 * Eo.mean(), (Eg.mean() / EV, Eo.mean() / EV)
+    Wg = np.polyfit(tt, zg, 1)[0]
+    Wo = np.polyfit(tt, zo, 1)[0]
+    assert Wg > 0 and Wo > 0
+    vz_sd = np.hypot(np.std(g.p[:, 2]), np.std(o.p[:, 2])) / pcl.co.electron_mass / np.sqrt(n)
+    assert abs(Wg - Wo) < 4 * vz_sd + 0.02 * Wo, (Wg, Wo)
+    Dg, Do = np.var(g.x[:, 2]), np.var(o.x[:, 2])
+    assert abs(Dg - Do) < 0.1 * Do, (Dg, Do)
+    mp.close()
+
+
+# ------------------------------------------------- batched swarms (swarm mode) --
+def test_ratebound_split_is_linear_in_fdt(pcl, air):
+    """A + Fdt B reproduces compratebound (collision_table.jl:152-167) for any Fdt."""
+    comp = pcl.workloads.air_composition()
+    for particle, procs in ((pcl.Electron, pcl.workloads.electron_processes(comp)),
+                            (pcl.Positron, pcl.workloads.positron_processes(comp))):
+        base = pcl.collision_table_from_processes(procs, particle, 0.0, safety=1.15)
+        A, B = pcl.ratebound_split(base, 1.15)
+        for Fdt in (0.0, 1e-25, 3e-24):
+            tab = pcl.collision_table_from_processes(procs, particle, Fdt, safety=1.15)
+            np.testing.assert_allclose(A + Fdt * B, tab.ratebound, rtol=1e-9,
+                                       atol=1e-12 * np.abs(tab.ratebound).max())
+
+
+def _batch(pcl, swarms=None, **cfg):
+    return pcl.workloads.swarm_batch(8, e_range=(4e5, 3e6), n_range=(40, 400), seed=5, swarms=swarms, **cfg)
+
+
+def _by_sid(a):
+    o = np.argsort(a.sid)
+    return a.sid[o], a.p[o], a.x[o], a.s[o], a.ctr[o]
+
+
+@pytest.mark.gpu
+def test_batched_equals_alone(pcl, gpu):
+    """Swarm mode processes each swarm independently: a swarm run inside the
+    batch and run alone give bit-identical particles (matched by stream id)."""
+    b = _batch(pcl)
+    for k in range(6):
+        pcl.advance(b.mpopl, b.pusher, (k + 1) * b.dt)
+    for s in (1, 6):
+        a = _batch(pcl, swarms=[s])
+        for k in range(6):
+            pcl.advance(a.mpopl, a.pusher, (k + 1) * a.dt)
+        for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
+            g = b.mpopl.get(sp).particles()
+            m = (g.sid >> np.uint64(56)) == s
+            ga = a.mpopl.get(sp).particles()
+            assert np.all((ga.sid >> np.uint64(56)) == s)
+            x, y = _by_sid(type(g)(**{f: getattr(g, f)[m] for f in ("x", "p", "w", "t", "s", "sid", "ctr")})), \
+                _by_sid(ga)
+            for u, v in zip(x, y):
+                np.testing.assert_array_equal(u, v)
+        a.mpopl.close()
+    b.mpopl.close()
+
+
+@pytest.mark.gpu
+def test_batched_oracle_parity(pcl, oracle, gpu):
+    """The batch against the oracle in swarm mode: per-swarm field and rate
+    bound, children inheriting the swarm bits."""
+    b = _batch(pcl)
+    et, gt, pt = b.tables
+    tabs = {pcl.Electron: et, pcl.Photon: gt, pcl.Positron: pt}
+    W = oracle.OracleWorld(5, tabs, {pcl.Electron: 10e3 * EV, pcl.Photon: 5e3 * EV, pcl.Positron: 10e3 * EV},
+                           b.pusher)
+    Evec = np.zeros((len(b.E), 3))
+    Evec[:, 2] = -b.E
+    W.set_swarms(tabs, Evec, pcl.co.elementary_charge * b.E * b.dt, safety=1.15)
+    W.upload(pcl.Electron, b.mpopl.get(pcl.Electron).particles())
+    for k in range(4):
+        pcl.advance(b.mpopl, b.pusher, (k + 1) * b.dt)
+        W.advance((k + 1) * b.dt, 4)
+    for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
+        rep = oracle.compare_populations(b.mpopl.get(sp).particles(), W.download(sp), sp, rtol=3e-5, stol=1e-4)
+        assert rep["ok"], (sp, str(rep))
+    b.mpopl.close()
+
+
+@pytest.mark.gpu
+def test_swarm_moments(pcl, gpu):
+    """Per-swarm moments on the device against the downloaded particles."""
+    b = _batch(pcl)
+    for k in range(3):
+        pcl.advance(b.mpopl, b.pusher, (k + 1) * b.dt)
+    m = b.mpopl.swarm_moments(pcl.Electron, len(b.E))
+    g = b.mpopl.get(pcl.Electron).particles()
+    sw = (g.sid >> np.uint64(56)).astype(int)
+    E = pcl.kinenergy(pcl.Electron, g.p)
+    for s in range(len(b.E)):
+        q = sw == s
+        ref = [q.sum(), g.w[q].sum(), (g.w * E)[q].sum(), (g.w * g.x[:, 2])[q].sum(),
+               (g.w * g.x[:, 2] ** 2)[q].sum(), (g.w * (g.x[:, 0] ** 2 + g.x[:, 1] ** 2))[q].sum()]
+        np.testing.assert_allclose(m[s], ref, rtol=1e-5, atol=1e-30)
+    b.mpopl.close()
