@@ -208,6 +208,84 @@ def run_reference(args):
     return 0
 
 
+def run_swarms(args, pcl):
+    """Batched swarms: `nswarm` avalanche swarms (fields log-spaced over
+    0.3-3 MV/m, initial sizes log-uniform over 1e2-1e5, Philox seed 3) in one
+    context, advanced by graph-replayed multi-step launches, against the same
+    swarms run one after another, each in its own context with one plain launch
+    per swarm per step.  Both timed on the wall clock of the device stream(s)."""
+    L = pcl.lib()
+    dt = 1e-12
+    nsw = args.nswarm
+    init = pcl.workloads.swarm_initial(nsw)
+    comp = pcl.workloads.air_composition()
+    tables = pcl.workloads.beam_tables(comp, float(init[0][0]), dt)
+    K = args.steps_per_launch if args.steps_per_launch > 1 else 8
+    steps = max(K, (args.steps + K - 1) // K * K)
+    # ---- batched: one context, swarm mode, CUDA-graph launch groups of K steps
+    b = pcl.workloads.swarm_batch(nsw, tables=tables, initial=init, use_graph=True, steps_per_launch=K)
+    mp = b.mpopl
+    t = args.warmup * dt
+    pcl.run(mp, b.pusher, t, dt)
+    L.pcl_sync(mp.ctx)
+    tal0 = mp.tallies()
+    L.pcl_kernel_stats(mp.ctx, None, None, None, None, 1)
+    with Clocks(0) as clk:
+        L.pcl_timer_start(mp.ctx)
+        t += steps * dt
+        pcl.run(mp, b.pusher, t, dt)
+        ms = C.c_double()
+        L.pcl_timer_stop(mp.ctx, C.byref(ms))
+    tal1 = mp.tallies()
+    kms = C.c_double(); kl = C.c_int64(); nl = C.c_int64(); kb = C.c_double()
+    L.pcl_kernel_stats(mp.ctx, C.byref(kms), C.byref(kl), C.byref(nl), C.byref(kb), 1)
+    ps_b = tal1.particle_steps - tal0.particle_steps
+    v_b = ps_b / (ms.value / 1e3)
+    mom = mp.swarm_moments(pcl.Electron, nsw)
+    peak, peak_kind = _peaks()
+    achieved = (kb.value / max(kl.value, 1)) / (kms.value / max(kl.value, 1) / 1e3) / 1e9
+    # ---- sequential: one context per swarm, one plain launch per swarm per step
+    seq = []
+    for sw in range(nsw):
+        seq.append(pcl.workloads.swarm_batch(nsw, swarms=[sw], tables=tables, initial=init, use_graph=False,
+                                             steps_per_launch=1))
+    ts = 0.0
+    for k in range(args.warmup):
+        ts += dt
+        for q in seq:
+            pcl.advance(q.mpopl, q.pusher, ts)
+    s0 = sum(q.mpopl.tallies().particle_steps for q in seq)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        ts += dt
+        for q in seq:
+            pcl.advance(q.mpopl, q.pusher, ts)
+    for q in seq:
+        L.pcl_sync(q.mpopl.ctx)
+    el_s = time.perf_counter() - t0
+    ps_s = sum(q.mpopl.tallies().particle_steps for q in seq) - s0
+    live_seq = np.array([q.mpopl.tallies().live[0] for q in seq])
+    for q in seq:
+        q.mpopl.close()
+    line = {"metric": f"particle-steps/s on 1 GB300 (batched: {nsw} avalanche swarms in one context)",
+            "value": v_b, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+            "ms_per_step": ms.value / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"swarms{nsw}-air-0.3-3MVm", "nswarm": nsw, "seed_electrons": int(init[1].sum()),
+                       "dt_s": dt, "steps_per_launch": K, "use_graph": True,
+                       "live_at_end": list(tal1.live), "max_swarm_live": int(mom[:, 0].max())},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None, "kernel": "k_step"},
+            "sequential_plain": {"value": ps_s / el_s, "unit": UNIT, "ms_per_step": 1e3 * el_s / steps,
+                                 "launch_groups_per_step": nsw,
+                                 "live_electrons_match": bool(np.array_equal(live_seq, mom[:, 0].astype(int)))},
+            "batched_over_sequential": v_b / (ps_s / el_s),
+            "cpu_baseline": None, "gpu_launches": int(nl.value), "clocks": clk.summary()}
+    print(json.dumps(line))
+    mp.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -222,9 +300,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--steps-per-launch", type=int, default=1)
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
+    ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms"])
+    ap.add_argument("--nswarm", type=int, default=256)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "swarms":
+        if args.warmup < 3:
+            args.warmup = 3
+        import __graft_entry__ as graft
+        graft.build()
+        return run_swarms(args, graft.load_package())
     if args.warmup < 3:
         args.warmup = 3
     ws, rank = _dist()

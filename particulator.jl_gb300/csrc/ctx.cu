@@ -17,6 +17,7 @@ extern "C" int pcl_ratebound_split(int, int, int, int, double, const double*, do
 
 namespace pcl {
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A);
+cudaError_t prepare_step(int minb, size_t smem);
 __global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long cap2);
 __global__ void k_begin_spill(Control* ctl, unsigned long long* in_n, unsigned long long* out_n);
 
@@ -122,6 +123,11 @@ struct Ctx {
     long long live[3] = {0, 0, 0};
     long long steps_since_compact = 0;
     int sticky = PCL_OK;
+    // CUDA graphs of launch groups (use_graph), keyed by every launch parameter
+    struct GraphEntry { std::vector<unsigned char> key; cudaGraphExec_t exec; };
+    std::vector<GraphEntry> graphs;
+    unsigned long long* h_spn = nullptr;  // pinned mirror of d_spn
+    long long graph_launches = 0;
     // instrumentation
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
     double k_ms = 0.0, k_bytes = 0.0;
@@ -412,9 +418,7 @@ static int readback(Ctx* c) {
     return PCL_OK;
 }
 
-static int compact_all(Ctx* c) {
-    int rc = ensure_tiles(c);
-    if (rc) return rc;
+static CompactArgs make_compact_args(Ctx* c) {
     CompactArgs C;
     std::memset(&C, 0, sizeof(C));
     long long capmax = 0;
@@ -429,19 +433,95 @@ static int compact_all(Ctx* c) {
     }
     C.n = c->d_ctl->n;
     C.n_out = c->d_nnew;
-    int nt = int(std::max<long long>(1, (capmax + kTile - 1) / kTile));
-    C.ntiles_max = nt;
-    dim3 g(nt, 3);
+    C.ntiles_max = int(std::max<long long>(1, (capmax + kTile - 1) / kTile));
+    return C;
+}
+
+// Enqueue the compaction (no host state change: the caller flips buffers).
+static cudaError_t enqueue_compact(Ctx* c, const CompactArgs& C) {
+    dim3 g(C.ntiles_max, 3);
     k_compact_count<<<g, 256, 0, c->stream>>>(C);
     k_compact_scan<<<3, 1024, 0, c->stream>>>(C);
     k_compact_scatter<<<g, 256, 0, c->stream>>>(C);
-    CK(cudaGetLastError());
-    c->launches += 3;
-    CK(cudaMemcpyAsync(c->d_ctl->n, c->d_nnew, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToDevice,
-                       c->stream));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return cudaMemcpyAsync(c->d_ctl->n, c->d_nnew, sizeof(unsigned long long) * 3, cudaMemcpyDeviceToDevice,
+                           c->stream);
+}
+
+static void flip_buffers(Ctx* c) {
     for (int s = 0; s < 3; ++s)
         if (c->sp[s].cap > 0) c->sp[s].cur = 1 - c->sp[s].cur;
     c->steps_since_compact = 0;
+}
+
+static int compact_all(Ctx* c) {
+    int rc = ensure_tiles(c);
+    if (rc) return rc;
+    CK(enqueue_compact(c, make_compact_args(c)));
+    c->launches += 3;
+    flip_buffers(c);
+    return PCL_OK;
+}
+
+// One launch group as a CUDA graph: prologue, step kernel, two spill passes
+// (each a no-op when its queue is empty), the compaction when due, and the
+// read-back of the control block and spill counts.  Graphs are cached by the
+// bytes of every launch parameter, so a replay is identical to a fresh capture.
+static int run_group_graph(Ctx* c, const StepArgs& A, const StepArgs& P0, const StepArgs& P1,
+                           const CompactArgs* C, int minb, int grid, int threads, size_t smem) {
+    std::vector<unsigned char> key;
+    auto put = [&key](const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        key.insert(key.end(), b, b + n);
+    };
+    put(&A, sizeof(A)); put(&P0, sizeof(P0)); put(&P1, sizeof(P1));
+    int hdr[4] = {minb, grid, threads, C ? 1 : 0};
+    put(hdr, sizeof(hdr)); put(&smem, sizeof(smem));
+    if (C) put(C, sizeof(*C));
+    long long caps[3] = {c->sp[0].cap, c->sp[1].cap, c->sp[2].cap};
+    put(caps, sizeof(caps));
+    cudaGraphExec_t exec = nullptr;
+    for (auto& g : c->graphs)
+        if (g.key == key) { exec = g.exec; break; }
+    if (!exec) {
+        CK(prepare_step(minb, smem));
+        CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = cudaSuccess;
+        auto q = [&e](cudaError_t r) { if (e == cudaSuccess) e = r; };
+        k_begin<<<1, 64, 0, c->stream>>>(c->d_ctl, caps[0], caps[1], caps[2]);
+        q(cudaGetLastError());
+        q(cudaMemsetAsync(c->d_spn, 0, 2 * sizeof(unsigned long long), c->stream));
+        // external records: event-record nodes that fire on every replay, so
+        // the step kernel stays timed by events on its own stream
+        q(cudaEventRecordWithFlags(c->ev_k0, c->stream, cudaEventRecordExternal));
+        q(launch_step(minb, grid, threads, smem, c->stream, A));
+        q(cudaEventRecordWithFlags(c->ev_k1, c->stream, cudaEventRecordExternal));
+        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 1, c->d_spn + 0);
+        q(cudaGetLastError());
+        q(launch_step(minb, grid, threads, smem, c->stream, P0));
+        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 0, c->d_spn + 1);
+        q(cudaGetLastError());
+        q(launch_step(minb, grid, threads, smem, c->stream, P1));
+        if (C) q(enqueue_compact(c, *C));
+        q(cudaMemcpyAsync(c->h_ctl, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
+        q(cudaMemcpyAsync(c->h_spn, c->d_spn, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+        if (e == cudaSuccess) e = e2;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, g, 0);
+        if (g) cudaGraphDestroy(g);
+        CK(e);
+        if (c->graphs.size() >= 8) {
+            cudaGraphExecDestroy(c->graphs.front().exec);
+            c->graphs.erase(c->graphs.begin());
+        }
+        c->graphs.push_back({std::move(key), exec});
+    }
+    CK(cudaGraphLaunch(exec, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->graph_launches += 1;
+    c->launches += C ? 11 : 8;
     return PCL_OK;
 }
 
@@ -453,14 +533,31 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
     const double dt = t_to_dev(dt_si);
     const int threads = block_threads(c);
     const size_t smem = step_smem_bytes(int(c->blob.size()), threads);
-    k_begin<<<1, 64, 0, c->stream>>>(c->d_ctl, c->sp[0].cap, c->sp[1].cap, c->sp[2].cap);
-    CK(cudaMemsetAsync(c->d_spn, 0, 2 * sizeof(unsigned long long), c->stream));
+    const int period = c->cfg.compaction_period > 0 ? c->cfg.compaction_period : 8;
+    const bool graph = c->cfg.use_graph != 0;
+    bool compacted = false, host_passes = false;
+    int in = 1;  // the main pass writes spill queue 1 (sp_out = 1 - sp_in(0))
     StepArgs A = make_args(c, dt, nsteps, 0, 0);
-    CK(cudaEventRecord(c->ev_k0, c->stream));
-    CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, A));
-    CK(cudaEventRecord(c->ev_k1, c->stream));
-    c->launches += 2;
-    if ((rc = readback(c))) return rc;
+    if (graph) {
+        const bool due = c->steps_since_compact + nsteps >= period;
+        if (due && (rc = ensure_tiles(c))) return rc;
+        CompactArgs C;
+        if (due) C = make_compact_args(c);
+        StepArgs P0 = make_args(c, dt, nsteps, 1, 1), P1 = make_args(c, dt, nsteps, 1, 0);
+        if ((rc = run_group_graph(c, A, P0, P1, due ? &C : nullptr, blocks_per_sm(c), grid_blocks(c), threads,
+                                  smem)))
+            return rc;
+        if (due) { flip_buffers(c); compacted = true; }
+        // after the two in-graph passes the last queue written is 1 again
+    } else {
+        k_begin<<<1, 64, 0, c->stream>>>(c->d_ctl, c->sp[0].cap, c->sp[1].cap, c->sp[2].cap);
+        CK(cudaMemsetAsync(c->d_spn, 0, 2 * sizeof(unsigned long long), c->stream));
+        CK(cudaEventRecord(c->ev_k0, c->stream));
+        CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, A));
+        CK(cudaEventRecord(c->ev_k1, c->stream));
+        c->launches += 2;
+        if ((rc = readback(c))) return rc;
+    }
     {
         float ms = 0.0f;
         CK(cudaEventElapsedTime(&ms, c->ev_k0, c->ev_k1));
@@ -475,11 +572,12 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
         c->k_bytes += 48.0 * nstart + 48.0 * nout + 4.0 * ndead;
     }
     // spill passes: queue written by the previous pass is the next pass's input
-    int in = 1;  // main pass wrote spill queue index 1 (sp_out = 1 - sp_in(0))
     for (int pass = 0; pass < 64; ++pass) {
         unsigned long long pending = 0;
-        CK(d2h(c, &pending, c->d_spn + in, sizeof(pending)));
+        if (graph && pass == 0) pending = c->h_spn[in];
+        else CK(d2h(c, &pending, c->d_spn + in, sizeof(pending)));
         if (pending == 0) break;
+        host_passes = true;
         if ((long long)pending > c->sp_cap) pending = (unsigned long long)c->sp_cap;
         CK(h2d(c, c->d_spn + in, &pending, sizeof(pending)));
         k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + in, c->d_spn + (1 - in));
@@ -489,16 +587,18 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
         in = 1 - in;
         if (pass == 63) return fail(c, PCL_ERR_TIMEOUT, "spill passes did not drain");
     }
-    if ((rc = readback(c))) return rc;
+    // the last read-back holds the final counters unless host passes ran after it
+    if (host_passes && (rc = readback(c))) return rc;
     if (c->h_ctl->timeout) return fail(c, PCL_ERR_TIMEOUT, "table staging wait timed out");
     c->t += dt_si * nsteps;
     c->steps += nsteps;
     for (int k = 0; k < nsteps; ++k) c->particle_steps += (long long)c->h_ctl->live_start[k];
     for (int s = 0; s < 3; ++s) c->live[s] = (long long)c->h_ctl->live_end[nsteps - 1][s];
-    c->steps_since_compact += nsteps;
-    int period = c->cfg.compaction_period > 0 ? c->cfg.compaction_period : 8;
-    if (c->steps_since_compact >= period) {
-        if ((rc = compact_all(c))) return rc;
+    if (!compacted) {
+        c->steps_since_compact += nsteps;
+        if (c->steps_since_compact >= period) {
+            if ((rc = compact_all(c))) return rc;
+        }
     }
     if (c->h_ctl->err[PCL_E_CAPACITY] > 0) return fail(c, PCL_ERR_CAPACITY, "population capacity exceeded");
     return PCL_OK;
@@ -544,6 +644,7 @@ int pcl_create(const pcl_config* cfg, void** out) {
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaMalloc(&c->d_ctl, sizeof(Control)) != cudaSuccess ||
         cudaMallocHost(&c->h_ctl, sizeof(Control)) != cudaSuccess ||
+        cudaMallocHost(&c->h_spn, 2 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&c->d_spn, 2 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&c->d_nnew, 3 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&c->d_mom, 16 * sizeof(double)) != cudaSuccess ||
@@ -571,6 +672,8 @@ void pcl_destroy(void* ctx) {
     cudaFree(c->d_spn); cudaFree(c->d_blob); cudaFree(c->d_ctl); cudaFree(c->d_tile_cnt);
     cudaFree(c->d_tile_off); cudaFree(c->d_nnew); cudaFree(c->d_mom);
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
+    if (c->h_spn) cudaFreeHost(c->h_spn);
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
     for (cudaEvent_t ev : {c->ev_k0, c->ev_k1, c->ev_t0, c->ev_t1})
         if (ev) cudaEventDestroy(ev);
     if (c->stream) cudaStreamDestroy(c->stream);

@@ -951,7 +951,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     long long nsp0, nsp1, total;
     if (A.spill_mode) {
         nsp0 = 0; nsp1 = 0;
-        total = (long long)(*A.sp_in_n);
+        total = min((long long)(*A.sp_in_n), A.sp_cap);
     } else {
         nsp0 = (long long)ctl->n_start[0];
         nsp1 = (long long)ctl->n_start[1];
@@ -1150,10 +1150,22 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 // per SM (register budgets 128, 85 and 64); the launch shape is a tunable.
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A) {
     void (*kern)(StepArgs) = (minb == 2) ? k_step<2> : (minb == 3) ? k_step<3> : k_step<4>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    // the shared-memory attribute is set outside stream capture (prepare_step
+    // runs first); during capture the launch is only recorded
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(stream, &cs);
     if (e != cudaSuccess) return e;
+    if (cs == cudaStreamCaptureStatusNone) {
+        e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+    }
     kern<<<grid, threads, smem, stream>>>(A);
     return cudaGetLastError();
+}
+
+cudaError_t prepare_step(int minb, size_t smem) {
+    void (*kern)(StepArgs) = (minb == 2) ? k_step<2> : (minb == 3) ? k_step<3> : k_step<4>;
+    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
 }
 
 // Launch prologue: snapshot the work space and clear per-launch counters.

@@ -149,7 +149,7 @@ class MultiPopulation:
 
     def __init__(self, *pairs, seed: int = 0, device: int = 0, steps_per_launch: int = 1,
                  compaction_period: int = 0, block_size: int = 0, grid_blocks: int = 0, blocks_per_sm: int = 0,
-                 **named):
+                 use_graph: bool = False, **named):
         index = {}
         for name, pop in list(pairs) + list(named.items()):
             key = SPECIES_BY_NAME[name] if isinstance(name, str) else int(name)
@@ -163,6 +163,7 @@ class MultiPopulation:
         cfg.block_size = block_size
         cfg.grid_blocks = grid_blocks
         cfg.blocks_per_sm = blocks_per_sm
+        cfg.use_graph = 1 if use_graph else 0
         self.config = cfg
         h = C.c_void_p()
         rc = _lib.lib().pcl_create(C.byref(cfg), C.byref(h))

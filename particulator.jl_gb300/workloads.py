@@ -194,16 +194,18 @@ def swarm_initial(nswarm: int = 256, e_range=(3e5, 3e6), n_range=(1e2, 1e5), see
 
 
 def swarm_batch(nswarm: int = 256, e_range=(3e5, 3e6), n_range=(1e2, 1e5), seed: int = 3, dt: float = 1e-12,
-                swarms=None, growth: float = 1.5, **cfg) -> SwarmBatch:
+                swarms=None, growth: float = 1.5, tables=None, initial=None, **cfg) -> SwarmBatch:
     """`nswarm` independent avalanche swarms in one context (swarm mode): each
     has its own field and rate bound; photons and positrons are tracked as in
     the mixed avalanche.  ``swarms`` restricts the batch to a subset (e.g. one
-    swarm run alone)."""
+    swarm run alone); ``tables`` and ``initial`` reuse what an earlier call
+    built (the rates do not depend on the field, only the rate bound does, and
+    swarm mode replaces that per swarm)."""
     comp = air_composition()
-    E, n0, arrays = swarm_initial(nswarm, e_range, n_range, seed)
+    E, n0, arrays = initial if initial is not None else swarm_initial(nswarm, e_range, n_range, seed)
     sel = list(range(nswarm)) if swarms is None else list(swarms)
     Fdt = co.elementary_charge * E * dt
-    et, gt, pt = beam_tables(comp, float(E[sel[0]]), dt)
+    et, gt, pt = tables if tables is not None else beam_tables(comp, float(E[sel[0]]), dt)
     x = np.concatenate([arrays[s].x for s in sel]); p = np.concatenate([arrays[s].p for s in sel])
     sid = np.concatenate([arrays[s].sid for s in sel])
     n = len(sid)
