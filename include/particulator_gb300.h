@@ -344,6 +344,31 @@ int pcl_test_sampler(void* ctx, int species, int proc_index, int64_t n, const do
 int pcl_compact_noalloc(int64_t n, const float* xw, const float* ps, const uint32_t* meta,
                         float* out_xw, float* out_ps, uint32_t* out_meta, int64_t* n_out, void* stream);
 
+/* ---- learned inverse-CDF sampler network ---------------------------------
+ * No single counterpart in the reference: a learned replacement for the
+ * secondary-energy samplers of SeltzerBerger.collide (seltzer.jl:97-122) and
+ * Moller.collide (moller.jl:64-87).  One network maps (a, b) to one output,
+ * a = (log10(T / eV) - 6) / 2 over T in [1e4, 1e8] eV, b = 2u - 1 with u the
+ * sampler's uniform; layers 2 -> 128 -> 128 -> 128 -> 1 with GELU, the two
+ * 128 x 128 layers in BF16 on the tensor cores with FP32 accumulation.
+ * Parameters are PCL_MLP_NPARAM floats: W1[128][2], b1[128], W2[128][128],
+ * b2[128], W3[128][128], b3[128], w4[128], b4. */
+#define PCL_MLP_NPARAM 33537
+int pcl_mlp_create(int device, uint64_t seed, void** out);
+void pcl_mlp_destroy(void* mlp);
+const char* pcl_mlp_last_error(void* mlp);
+int pcl_mlp_set_params(void* mlp, const float* params, int64_t n);
+int pcl_mlp_get_params(void* mlp, float* params, int64_t n);
+/* y[i] = net(x[2i], x[2i+1]) for host arrays */
+int pcl_mlp_forward(void* mlp, int64_t n, const float* x, float* y);
+/* gradient of mean((net(x) - t)^2) over the n rows, and the loss */
+int pcl_mlp_gradient(void* mlp, int64_t n, const float* x, const float* t, float* grad, double* loss);
+/* Adam (beta 0.9 / 0.999, cosine decay to 5 % of lr) over `steps` minibatches
+ * of `batch` rows (a multiple of 128) drawn from the n-row dataset; *loss =
+ * mean loss of the last 100 steps */
+int pcl_mlp_train(void* mlp, int64_t n, const float* x, const float* t, int64_t steps, int32_t batch, double lr,
+                  uint64_t seed, double* loss);
+
 #ifdef __cplusplus
 }
 #endif

@@ -18,7 +18,8 @@ from .population import (ElectronState, PhotonState, PositronState, ParticleArra
                          init, advance, run, nparticles, nactives, weight, meanenergy, maxenergy, spread, posvar,
                          repack, droplow, kinenergy, AbstractCallback, VoidCallback, CombinedCallback,
                          CollisionCounter, PopulationTargetCallback, ParticleCountCallback)
-from . import workloads
+from . import workloads, learned
+from .learned import SamplerNet
 
 co = constants
 __version__ = "0.1.0"

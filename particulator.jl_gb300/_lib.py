@@ -124,7 +124,17 @@ _SIGS = {
                                       C.c_void_p, C.c_void_p, C.c_void_p]),
     "pcl_test_sampler": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _i64, _P(_d), _P(_u64), _P(_d), _P(_d),
                                    _P(_i32), _P(_u32)]),
+    "pcl_mlp_create": (C.c_int, [C.c_int, _u64, _P(C.c_void_p)]),
+    "pcl_mlp_destroy": (None, [C.c_void_p]),
+    "pcl_mlp_last_error": (C.c_char_p, [C.c_void_p]),
+    "pcl_mlp_set_params": (C.c_int, [C.c_void_p, _P(C.c_float), _i64]),
+    "pcl_mlp_get_params": (C.c_int, [C.c_void_p, _P(C.c_float), _i64]),
+    "pcl_mlp_forward": (C.c_int, [C.c_void_p, _i64, _P(C.c_float), _P(C.c_float)]),
+    "pcl_mlp_gradient": (C.c_int, [C.c_void_p, _i64, _P(C.c_float), _P(C.c_float), _P(C.c_float), _P(_d)]),
+    "pcl_mlp_train": (C.c_int, [C.c_void_p, _i64, _P(C.c_float), _P(C.c_float), _i64, _i32, _d, _u64, _P(_d)]),
 }
+
+MLP_NPARAM = 33537
 
 _lib = None
 
@@ -181,6 +191,11 @@ def u32ptr(a):
 
 def i32ptr(a):
     return None if a is None else a.ctypes.data_as(_P(_i32))
+
+
+def fptr(a):
+    """Pointer to a contiguous float32 numpy array (or None)."""
+    return None if a is None else a.ctypes.data_as(_P(C.c_float))
 
 
 def i64ptr(a):
