@@ -369,6 +369,30 @@ int pcl_mlp_gradient(void* mlp, int64_t n, const float* x, const float* t, float
 int pcl_mlp_train(void* mlp, int64_t n, const float* x, const float* t, int64_t steps, int32_t batch, double lr,
                   uint64_t seed, double* loss);
 
+/* ---- learned sampler in the step ------------------------------------------
+ * A context can hand the secondary-energy draw of a Seltzer-Berger or Moller
+ * process to a network: the collision is suspended, the network evaluates all
+ * suspended collisions of the launch in one batch on the tensor cores, and a
+ * resume pass finishes them (angles, secondary, rest of the step).  The table
+ * sampler is kept outside the trained range T in [1e4, 1e8] eV and where the
+ * network is not monotone in u (checked on a grid when it is attached).
+ * Outputs, both in [0, 1] and increasing in u: PCL_LEARN_SB h with
+ * ln(k / T) = (1 - h) ln(kmin / T), kmin / T the table's pcum = 0 value at T;
+ * PCL_LEARN_MOLLER v with eps = e0 / (1 - v (1 - 2 e0)), e0 = tcut / T. */
+#define PCL_LEARN_SB     1
+#define PCL_LEARN_MOLLER 2
+/* Attach (mlp != NULL) or detach the network of table position proc_index. */
+int pcl_set_learned(void* ctx, int species, int proc_index, int kind, void* mlp);
+/* Training set from the table sampler of proc_index: per_T samples at each of
+ * nT energies a_g = -1 + 2 g / (nT - 1), histogrammed on the device and turned
+ * into Q quantile targets per energy: x_out[2 (g Q + i) + {0,1}] = (a_g,
+ * 2 u_i - 1), u_i = (i + 1/2) / Q, t_out[g Q + i] = the output variable.
+ * Energies outside the kind's domain give no rows; *nrows = rows written. */
+int pcl_learn_data(void* ctx, int species, int proc_index, int kind, int nT, int64_t per_T, int Q, uint64_t seed,
+                   float* x_out, float* t_out, int64_t* nrows);
+/* Collisions answered by a network and rounds run since the context was made. */
+int pcl_learn_stats(void* ctx, int64_t* suspended, int64_t* rounds);
+
 #ifdef __cplusplus
 }
 #endif

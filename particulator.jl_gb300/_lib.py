@@ -132,6 +132,10 @@ _SIGS = {
     "pcl_mlp_forward": (C.c_int, [C.c_void_p, _i64, _P(C.c_float), _P(C.c_float)]),
     "pcl_mlp_gradient": (C.c_int, [C.c_void_p, _i64, _P(C.c_float), _P(C.c_float), _P(C.c_float), _P(_d)]),
     "pcl_mlp_train": (C.c_int, [C.c_void_p, _i64, _P(C.c_float), _P(C.c_float), _i64, _i32, _d, _u64, _P(_d)]),
+    "pcl_set_learned": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    "pcl_learn_stats": (C.c_int, [C.c_void_p, _P(_i64), _P(_i64)]),
+    "pcl_learn_data": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, _u64,
+                                 _P(C.c_float), _P(C.c_float), _P(_i64)]),
 }
 
 MLP_NPARAM = 33537

@@ -18,6 +18,14 @@ extern "C" int pcl_ratebound_split(int, int, int, int, double, const double*, do
 namespace pcl {
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A);
 cudaError_t prepare_step(int minb, size_t smem);
+__global__ void k_learn_hist(StepArgs A, int species, int j, int kind, int nT, long long per_T, int nbins,
+                             float hmin, float hmax, unsigned long long sid_base, unsigned int* hist);
+__global__ void k_learn_x(const float4* ps, const float4* m2, long long n, float* X);
+__global__ void k_learn_pick(const float4* m2, long long n, const float* Yk, long long stride, LearnPick which,
+                             float* Y);
+namespace mlp {
+cudaError_t infer(void* handle, const float* X, long long n, float* Y, cudaStream_t stream);
+}
 __global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long cap2);
 __global__ void k_begin_spill(Control* ctl, unsigned long long* in_n, unsigned long long* out_n);
 
@@ -123,6 +131,23 @@ struct Ctx {
     long long live[3] = {0, 0, 0};
     long long steps_since_compact = 0;
     int sticky = PCL_OK;
+    // learned sampler: network per (species, table position), suspended-collision queues
+    void* learn_net[3][16] = {};
+    int learn_kind[3][16] = {};
+    uint32_t learn_ok[3][16][2] = {};
+    std::vector<void*> nets;       // distinct attached networks
+    LearnPick pick{};
+    bool learn_on = false;
+    float4* lq_xw[2] = {nullptr, nullptr};
+    float4* lq_ps[2] = {nullptr, nullptr};
+    uint4* lq_m1[2] = {nullptr, nullptr};
+    float4* lq_m2[2] = {nullptr, nullptr};
+    float* lq_x = nullptr;         // [cap][2] network inputs
+    float* lq_yk = nullptr;        // [nets][cap] outputs per network
+    float* lq_y = nullptr;         // [cap] output of each collision's network
+    unsigned long long* d_lqn = nullptr;  // [2]
+    long long lq_cap = 0, lq_nets_cap = 0;
+    long long learn_rounds = 0, learn_suspended = 0;
     // CUDA graphs of launch groups (use_graph), keyed by every launch parameter
     struct GraphEntry { std::vector<unsigned char> key; cudaGraphExec_t exec; };
     std::vector<GraphEntry> graphs;
@@ -317,7 +342,12 @@ static int build_blob(Ctx* c) {
             for (int i = 0; i < nI; ++i)
                 for (int k = 0; k < S.order; ++k) data.push_back(float(rate_to_dev(Bt[k + S.order * i])));
         }
-        for (int j = 0; j < S.nproc; ++j) pack_proc(S.procs[j], S.sb_index[j], h.proc[j]);
+        for (int j = 0; j < S.nproc; ++j) {
+            pack_proc(S.procs[j], S.sb_index[j], h.proc[j]);
+            h.proc[j].learn = c->learn_net[s][j] ? c->learn_kind[s][j] : 0;
+            h.proc[j].learn_ok[0] = c->learn_ok[s][j][0];
+            h.proc[j].learn_ok[1] = c->learn_ok[s][j][1];
+        }
         if (S.hist_bins > 0) {
             h.hist_bins = S.hist_bins;
             double lmin = std::log(S.hist_emin / mc2), lmax = std::log(S.hist_emax / mc2);
@@ -331,6 +361,10 @@ static int build_blob(Ctx* c) {
         h.ne = c->sb[b].ne;
         h.ncum = c->sb[b].ncum;
         h.inv_dp = float(c->sb[b].ncum - 1);
+        double ym = 0.0;
+        for (int j = 0; j + 1 < h.ne; ++j)
+            ym = std::max(ym, std::fabs(c->sb[b].data[size_t(j + 1) * h.ncum] - c->sb[b].data[size_t(j) * h.ncum]));
+        h.ymargin = float(ym);
         h.le_off = off();
         for (int j = 0; j < h.ne; ++j) data.push_back(float(c->sb[b].log_energy[j] - std::log(mc2)));
     }
@@ -394,7 +428,62 @@ static StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, int sp_
     A.nsteps = nsteps;
     A.spill_mode = spill_mode;
     A.blob_bytes = int(c->blob.size());
+    if (c->learn_on) {  // suspended collisions go to queue 0 unless set_lq says otherwise
+        A.lq_out_xw = c->lq_xw[0]; A.lq_out_ps = c->lq_ps[0]; A.lq_out_m1 = c->lq_m1[0]; A.lq_out_m2 = c->lq_m2[0];
+        A.lq_out_n = c->d_lqn;
+        A.lq_cap = c->lq_cap;
+    }
     return A;
+}
+
+// Suspended-collision queues of a pass: output queue `out`, input queue `in` (-1: none).
+static void set_lq(StepArgs& A, Ctx* c, int out, int in) {
+    if (!c->learn_on) return;
+    A.lq_out_xw = c->lq_xw[out]; A.lq_out_ps = c->lq_ps[out]; A.lq_out_m1 = c->lq_m1[out];
+    A.lq_out_m2 = c->lq_m2[out]; A.lq_out_n = c->d_lqn + out;
+    if (in >= 0) {
+        A.lq_in_xw = c->lq_xw[in]; A.lq_in_ps = c->lq_ps[in]; A.lq_in_m1 = c->lq_m1[in]; A.lq_in_m2 = c->lq_m2[in];
+        A.lq_in_n = c->d_lqn + in;
+        A.lq_in_y = c->lq_y;
+    }
+    A.lq_cap = c->lq_cap;
+}
+
+static void free_lq(Ctx* c) {
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(c->lq_xw[b]); cudaFree(c->lq_ps[b]); cudaFree(c->lq_m1[b]); cudaFree(c->lq_m2[b]);
+        c->lq_xw[b] = c->lq_ps[b] = nullptr; c->lq_m1[b] = nullptr; c->lq_m2[b] = nullptr;
+    }
+    cudaFree(c->lq_x); cudaFree(c->lq_yk); cudaFree(c->lq_y); cudaFree(c->d_lqn);
+    c->lq_x = c->lq_yk = c->lq_y = nullptr; c->d_lqn = nullptr;
+    c->lq_cap = 0; c->lq_nets_cap = 0;
+}
+
+// Queues sized for 1/64 of the largest population (at least 64 Ki collisions);
+// a full queue makes the step use the table sampler for the excess.
+static int ensure_lq(Ctx* c) {
+    if (!c->learn_on) return PCL_OK;
+    long long capmax = 0;
+    for (auto& s : c->sp) capmax = std::max(capmax, s.cap);
+    long long want = std::max<long long>(1 << 16, capmax / 64);
+    long long nn = std::max<long long>(1, (long long)c->nets.size());
+    if (want <= c->lq_cap && nn <= c->lq_nets_cap) return PCL_OK;
+    CK(cudaStreamSynchronize(c->stream));
+    free_lq(c);
+    for (int b = 0; b < 2; ++b) {
+        CK(cudaMalloc(&c->lq_xw[b], sizeof(float4) * want));
+        CK(cudaMalloc(&c->lq_ps[b], sizeof(float4) * want));
+        CK(cudaMalloc(&c->lq_m1[b], sizeof(uint4) * want));
+        CK(cudaMalloc(&c->lq_m2[b], sizeof(float4) * want));
+    }
+    CK(cudaMalloc(&c->lq_x, sizeof(float) * 2 * want));
+    CK(cudaMalloc(&c->lq_yk, sizeof(float) * nn * want));
+    CK(cudaMalloc(&c->lq_y, sizeof(float) * want));
+    CK(cudaMalloc(&c->d_lqn, 2 * sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(c->d_lqn, 0, 2 * sizeof(unsigned long long), c->stream));
+    c->lq_cap = want;
+    c->lq_nets_cap = nn;
+    return PCL_OK;
 }
 
 static int blocks_per_sm(Ctx* c) {
@@ -492,6 +581,7 @@ static int run_group_graph(Ctx* c, const StepArgs& A, const StepArgs& P0, const 
         k_begin<<<1, 64, 0, c->stream>>>(c->d_ctl, caps[0], caps[1], caps[2]);
         q(cudaGetLastError());
         q(cudaMemsetAsync(c->d_spn, 0, 2 * sizeof(unsigned long long), c->stream));
+        if (c->learn_on) q(cudaMemsetAsync(c->d_lqn, 0, 2 * sizeof(unsigned long long), c->stream));
         // external records: event-record nodes that fire on every replay, so
         // the step kernel stays timed by events on its own stream
         q(cudaEventRecordWithFlags(c->ev_k0, c->stream, cudaEventRecordExternal));
@@ -525,19 +615,78 @@ static int run_group_graph(Ctx* c, const StepArgs& A, const StepArgs& P0, const 
     return PCL_OK;
 }
 
-// One launch of `nsteps` steps of length dt (seconds), plus spill passes.
+// Spill passes: the queue written by the previous pass is the next pass's
+// input, starting from spill queue `in`; suspended collisions of these passes
+// go to learned queue `lq_out`.  *ran = whether any pass ran.
+static int drain_spills(Ctx* c, double dt, int nsteps, int threads, size_t smem, int in, int lq_out, bool* ran,
+                        const unsigned long long* known_pending) {
+    for (int pass = 0; pass < 64; ++pass) {
+        unsigned long long pending = 0;
+        if (pass == 0 && known_pending) pending = *known_pending;
+        else CK(d2h(c, &pending, c->d_spn + in, sizeof(pending)));
+        if (pending == 0) return PCL_OK;
+        *ran = true;
+        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + in, c->d_spn + (1 - in));
+        StepArgs S = make_args(c, dt, nsteps, 1, in);
+        set_lq(S, c, lq_out, -1);
+        CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, S));
+        c->launches += 2;
+        in = 1 - in;
+    }
+    return fail(c, PCL_ERR_TIMEOUT, "spill passes did not drain");
+}
+
+// Learned-sampler rounds: the networks answer every collision suspended so
+// far (one batched tensor-core forward pass per attached network), a resume
+// pass finishes them and carries the particles to the end of the launch
+// (suspending again into the other queue where they collide again), then the
+// spill passes drain.  Bounded number of rounds.
+static int learned_rounds(Ctx* c, double dt, int nsteps, int threads, size_t smem, bool* ran) {
+    int lin = 0;
+    for (int round = 0; round < 64; ++round) {
+        unsigned long long n = 0;
+        CK(d2h(c, &n, c->d_lqn + lin, sizeof(n)));
+        if (n == 0) return PCL_OK;
+        *ran = true;
+        const long long m = std::min<long long>((long long)n, c->lq_cap);
+        const int grid = int(std::max<long long>(1, std::min<long long>((m + 255) / 256, 4ll * c->sm_count)));
+        k_learn_x<<<grid, 256, 0, c->stream>>>(c->lq_ps[lin], c->lq_m2[lin], m, c->lq_x);
+        CK(cudaGetLastError());
+        for (size_t k = 0; k < c->nets.size(); ++k)
+            CK(mlp::infer(c->nets[k], c->lq_x, m, c->lq_yk + k * c->lq_cap, c->stream));
+        k_learn_pick<<<grid, 256, 0, c->stream>>>(c->lq_m2[lin], m, c->lq_yk, c->lq_cap, c->pick, c->lq_y);
+        CK(cudaGetLastError());
+        CK(cudaMemsetAsync(c->d_lqn + (1 - lin), 0, sizeof(unsigned long long), c->stream));
+        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 0, c->d_spn + 1);  // head 0, spill queue 1 empty
+        StepArgs R = make_args(c, dt, nsteps, 2, 0);
+        set_lq(R, c, 1 - lin, lin);
+        CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, R));
+        c->launches += 4 + (long long)c->nets.size();
+        c->learn_rounds += 1;
+        c->learn_suspended += m;
+        bool dummy = false;
+        int rc = drain_spills(c, dt, nsteps, threads, smem, 1, 1 - lin, &dummy, nullptr);
+        if (rc) return rc;
+        lin = 1 - lin;
+    }
+    return fail(c, PCL_ERR_TIMEOUT, "learned-sampler rounds did not drain");
+}
+
+// One launch of `nsteps` steps of length dt (seconds), plus spill passes and,
+// with a learned sampler attached, the learned rounds.
 static int launch_steps(Ctx* c, double dt_si, int nsteps) {
     int rc = build_blob(c);
     if (rc) return rc;
     if ((rc = ensure_spill(c))) return rc;
+    if ((rc = ensure_lq(c))) return rc;
     const double dt = t_to_dev(dt_si);
     const int threads = block_threads(c);
     const size_t smem = step_smem_bytes(int(c->blob.size()), threads);
     const int period = c->cfg.compaction_period > 0 ? c->cfg.compaction_period : 8;
     const bool graph = c->cfg.use_graph != 0;
     bool compacted = false, host_passes = false;
-    int in = 1;  // the main pass writes spill queue 1 (sp_out = 1 - sp_in(0))
     StepArgs A = make_args(c, dt, nsteps, 0, 0);
+    unsigned long long pending0 = 0;
     if (graph) {
         const bool due = c->steps_since_compact + nsteps >= period;
         if (due && (rc = ensure_tiles(c))) return rc;
@@ -548,15 +697,17 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
                                   smem)))
             return rc;
         if (due) { flip_buffers(c); compacted = true; }
-        // after the two in-graph passes the last queue written is 1 again
+        pending0 = c->h_spn[1];  // the two in-graph passes leave the last queue written in 1
     } else {
         k_begin<<<1, 64, 0, c->stream>>>(c->d_ctl, c->sp[0].cap, c->sp[1].cap, c->sp[2].cap);
         CK(cudaMemsetAsync(c->d_spn, 0, 2 * sizeof(unsigned long long), c->stream));
+        if (c->learn_on) CK(cudaMemsetAsync(c->d_lqn, 0, 2 * sizeof(unsigned long long), c->stream));
         CK(cudaEventRecord(c->ev_k0, c->stream));
         CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, A));
         CK(cudaEventRecord(c->ev_k1, c->stream));
         c->launches += 2;
         if ((rc = readback(c))) return rc;
+        CK(d2h(c, &pending0, c->d_spn + 1, sizeof(pending0)));
     }
     {
         float ms = 0.0f;
@@ -571,22 +722,8 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
         }
         c->k_bytes += 48.0 * nstart + 48.0 * nout + 4.0 * ndead;
     }
-    // spill passes: queue written by the previous pass is the next pass's input
-    for (int pass = 0; pass < 64; ++pass) {
-        unsigned long long pending = 0;
-        if (graph && pass == 0) pending = c->h_spn[in];
-        else CK(d2h(c, &pending, c->d_spn + in, sizeof(pending)));
-        if (pending == 0) break;
-        host_passes = true;
-        if ((long long)pending > c->sp_cap) pending = (unsigned long long)c->sp_cap;
-        CK(h2d(c, c->d_spn + in, &pending, sizeof(pending)));
-        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + in, c->d_spn + (1 - in));
-        StepArgs S = make_args(c, dt, nsteps, 1, in);
-        CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, S));
-        c->launches += 2;
-        in = 1 - in;
-        if (pass == 63) return fail(c, PCL_ERR_TIMEOUT, "spill passes did not drain");
-    }
+    if ((rc = drain_spills(c, dt, nsteps, threads, smem, 1, 0, &host_passes, &pending0))) return rc;
+    if (c->learn_on && (rc = learned_rounds(c, dt, nsteps, threads, smem, &host_passes))) return rc;
     // the last read-back holds the final counters unless host passes ran after it
     if (host_passes && (rc = readback(c))) return rc;
     if (c->h_ctl->timeout) return fail(c, PCL_ERR_TIMEOUT, "table staging wait timed out");
@@ -673,6 +810,7 @@ void pcl_destroy(void* ctx) {
     cudaFree(c->d_tile_off); cudaFree(c->d_nnew); cudaFree(c->d_mom);
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
     if (c->h_spn) cudaFreeHost(c->h_spn);
+    free_lq(c);
     for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
     for (cudaEvent_t ev : {c->ev_k0, c->ev_k1, c->ev_t0, c->ev_t1})
         if (ev) cudaEventDestroy(ev);
@@ -1189,6 +1327,143 @@ int pcl_kernel_stats(void* ctx, double* step_kernel_ms, int64_t* step_launches, 
     if (launches) *launches = c->launches;
     if (step_bytes) *step_bytes = c->k_bytes;
     if (reset) { c->k_ms = 0; c->k_launches = 0; c->launches = 0; c->k_bytes = 0; }
+    return PCL_OK;
+}
+
+static int learn_kind_ok(const pcl_process& P, int kind) {
+    return (kind == PCL_LEARN_SB && P.kind == PCL_PROC_SELTZER_BERGER) ||
+           (kind == PCL_LEARN_MOLLER && P.kind == PCL_PROC_MOLLER);
+}
+
+int pcl_set_learned(void* ctx, int species, int proc_index, int kind, void* mlp) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    if (proc_index < 0 || proc_index >= S.nproc || proc_index >= 16) return fail(c, PCL_ERR_INVALID, "process index");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    if (!mlp) {
+        c->learn_net[species][proc_index] = nullptr;
+        c->learn_kind[species][proc_index] = 0;
+        c->learn_ok[species][proc_index][0] = c->learn_ok[species][proc_index][1] = 0u;
+    } else {
+        if (!learn_kind_ok(S.procs[proc_index], kind))
+            return fail(c, PCL_ERR_UNSUPPORTED, "learned sampler kind does not match the process");
+        // where the network is monotone in u: 64 bins of a, 4 energies each, 257 values of u
+        const int nb = 64, ne = 4, nu = 257;
+        std::vector<float> x(2 * nb * ne * nu), y(nb * ne * nu);
+        for (int b = 0; b < nb; ++b)
+            for (int e = 0; e < ne; ++e)
+                for (int i = 0; i < nu; ++i) {
+                    size_t r = (size_t(b) * ne + e) * nu + i;
+                    x[2 * r] = -1.0f + (float(b) + (float(e) + 0.5f) / ne) * (2.0f / nb);
+                    x[2 * r + 1] = 2.0f * (float(i) + 0.5f) / nu - 1.0f;
+                }
+        rc = pcl_mlp_forward(mlp, int64_t(y.size()), x.data(), y.data());
+        if (rc) return fail(c, rc, std::string("network evaluation: ") + pcl_mlp_last_error(mlp));
+        uint32_t ok[2] = {0u, 0u};
+        for (int b = 0; b < nb; ++b) {
+            bool mono = true;
+            for (int e = 0; e < ne && mono; ++e)
+                for (int i = 1; i < nu && mono; ++i) {
+                    size_t r = (size_t(b) * ne + e) * nu + i;
+                    if (!(y[r] >= y[r - 1]) || !std::isfinite(y[r])) mono = false;
+                }
+            if (mono) ok[b >> 5] |= 1u << (b & 31);
+        }
+        c->learn_net[species][proc_index] = mlp;
+        c->learn_kind[species][proc_index] = kind;
+        c->learn_ok[species][proc_index][0] = ok[0];
+        c->learn_ok[species][proc_index][1] = ok[1];
+    }
+    // distinct networks and the pick table
+    c->nets.clear();
+    for (int k = 0; k < 48; ++k) c->pick.net[k] = -1;
+    for (int sp = 0; sp < 3; ++sp)
+        for (int j = 0; j < 16; ++j) {
+            void* n = c->learn_net[sp][j];
+            if (!n) continue;
+            int idx = -1;
+            for (size_t q = 0; q < c->nets.size(); ++q)
+                if (c->nets[q] == n) idx = int(q);
+            if (idx < 0) { idx = int(c->nets.size()); c->nets.push_back(n); }
+            c->pick.net[sp * 16 + j] = int8_t(idx);
+        }
+    c->learn_on = !c->nets.empty();
+    c->blob_dirty = true;
+    return ensure_lq(c);
+}
+
+int pcl_learn_data(void* ctx, int species, int proc_index, int kind, int nT, int64_t per_T, int Q, uint64_t seed,
+                   float* x_out, float* t_out, int64_t* nrows) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    if (proc_index < 0 || proc_index >= S.nproc) return fail(c, PCL_ERR_INVALID, "process index");
+    if (nT < 2 || nT > 65536 || per_T < 1 || Q < 2 || !x_out || !t_out || !nrows)
+        return fail(c, PCL_ERR_INVALID, "learn_data sizes");
+    const pcl_process& P = S.procs[proc_index];
+    if (!learn_kind_ok(P, kind)) return fail(c, PCL_ERR_UNSUPPORTED, "learned sampler kind does not match the process");
+    CK(cudaSetDevice(c->device));
+    if ((rc = build_blob(c))) return rc;
+    const int nbins = 4096;
+    const float hmin = 0.0f, hmax = 1.0f;   // both output variables lie in [0, 1]
+    unsigned int* hist = nullptr;
+    const size_t hn = size_t(nT) * nbins;
+    CK(cudaMallocAsync(&hist, sizeof(unsigned int) * hn, c->stream));
+    CK(cudaMemsetAsync(hist, 0, sizeof(unsigned int) * hn, c->stream));
+    StepArgs A = make_args(c, 0.0, 1, 0, 0);
+    const size_t smem = c->blob.size() + 16;
+    CK(cudaFuncSetAttribute(k_learn_hist, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const long long total = (long long)nT * per_T;
+    const int grid = int(std::max<long long>(1, std::min<long long>((total + 255) / 256, 8ll * c->sm_count)));
+    const unsigned long long sid_base = (0xA5ull << 56) | ((seed & 0xFFFFull) << 40);
+    k_learn_hist<<<grid, 256, smem, c->stream>>>(A, species, proc_index, kind, nT, (long long)per_T, nbins, hmin, hmax,
+                                                  sid_base, hist);
+    CK(cudaGetLastError());
+    std::vector<unsigned int> h(hn);
+    CK(cudaMemcpyAsync(h.data(), hist, sizeof(unsigned int) * hn, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaFreeAsync(hist, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    const double dh = double(hmax - hmin) / nbins;
+    int64_t r = 0;
+    std::vector<double> cum(nbins + 1);
+    for (int g = 0; g < nT; ++g) {
+        const double a = -1.0 + 2.0 * g / double(nT - 1);
+        if (kind == PCL_LEARN_MOLLER) {
+            const double T = std::pow(10.0, 6.0 + 2.0 * a) * si::e;
+            if (!(P.param[0] < 0.45 * T)) continue;   // degenerate kinematic range: no rows
+        }
+        const unsigned int* hg = h.data() + size_t(g) * nbins;
+        cum[0] = 0.0;
+        for (int b = 0; b < nbins; ++b) cum[b + 1] = cum[b] + hg[b];
+        const double N = cum[nbins];
+        if (N <= 0) continue;
+        int b = 0;
+        for (int i = 0; i < Q; ++i) {
+            const double u = (i + 0.5) / Q;
+            const double target = u * N;
+            while (b < nbins - 1 && cum[b + 1] < target) ++b;
+            const double f = hg[b] ? (target - cum[b]) / hg[b] : 0.5;
+            x_out[2 * r] = float(a);
+            x_out[2 * r + 1] = float(2.0 * u - 1.0);
+            t_out[r] = float(hmin + (b + std::min(1.0, std::max(0.0, f))) * dh);
+            ++r;
+        }
+    }
+    *nrows = r;
+    return PCL_OK;
+}
+
+int pcl_learn_stats(void* ctx, int64_t* suspended, int64_t* rounds) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    if (suspended) *suspended = c->learn_suspended;
+    if (rounds) *rounds = c->learn_rounds;
     return PCL_OK;
 }
 

@@ -27,8 +27,10 @@ struct DevProc {
     int32_t kind;
     int32_t sb;       // Seltzer-Berger table index, -1 otherwise
     int32_t nbind;    // photoelectric: number of binding energies
-    int32_t pad;
+    int32_t learn;    // learned sampler: 0 none, PCL_LEARN_SB, PCL_LEARN_MOLLER
     float   p[8];     // kind-specific, see ctx.cu:pack_proc
+    uint32_t learn_ok[2];  // 64 bins of a = (log10(T/eV) - 6) / 2 over [-1, 1): network used where set
+    uint32_t pad[2];
 };
 
 struct SpeciesHdr {
@@ -61,6 +63,7 @@ struct SBHdr {
     int32_t ncum;      // cumulative-probability points (pcum = LinRange(0, 1, ncum))
     int32_t le_off;    // float offset of log(T / m_e c^2) [ne] in the blob
     float   inv_dp;    // ncum - 1
+    float   ymargin;   // largest step of the pcum = 0 column between grid energies
 };
 
 struct BlobHdr {
@@ -115,8 +118,23 @@ struct StepArgs {
     uint32_t key0, key1;                 // Philox key
     double dt;                           // step length (ns)
     int nsteps;                          // steps in this launch
-    int spill_mode;                      // 0: populations, 1: spill queue
+    int spill_mode;                      // 0: populations, 1: spill queue, 2: suspended collisions (resume)
     int blob_bytes;
+    // learned sampler: collisions handed to the network are suspended into
+    // lq_out (xw, ps, m1 = {sid_lo, sid_hi, ctr, ctr0}, m2 = {th, tlo, u,
+    // species | k << 2 | j << 8 | nsub << 16}); a resume pass reads lq_in and
+    // the network outputs lq_in_y.  lq_out_n == nullptr: no learned mode.
+    float4* lq_out_xw; float4* lq_out_ps; uint4* lq_out_m1; float4* lq_out_m2;
+    unsigned long long* lq_out_n;
+    const float4* lq_in_xw; const float4* lq_in_ps; const uint4* lq_in_m1; const float4* lq_in_m2;
+    const float* lq_in_y;
+    const unsigned long long* lq_in_n;
+    long long lq_cap;
+};
+
+// Network index of each (species, table position) with a learned sampler (-1: none).
+struct LearnPick {
+    int8_t net[48];
 };
 
 // Arguments of the compaction kernels (repack!, population.jl:229-259).

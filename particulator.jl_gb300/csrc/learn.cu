@@ -127,6 +127,18 @@ static uint64_t splitmix(uint64_t& s) {
     return z ^ (z >> 31);
 }
 
+// Batched inference on device arrays, on the caller's stream (the step's
+// learned rounds).  The handle's kernels attributes are set at creation.
+cudaError_t infer(void* handle, const float* X, long long n, float* Y, cudaStream_t stream) {
+    Handle* h = static_cast<Handle*>(handle);
+    if (n <= 0) return cudaSuccess;
+    long long ntiles = (n + kH - 1) / kH;
+    int grid = int(std::min<long long>(ntiles, 2ll * h->sm_count));
+    k_mlp_forward<<<grid, 128, kFwdSmem, stream>>>(net_of(h), X, n, Y, TrainBuf{}, nullptr, nullptr, nullptr,
+                                                     h->d_err);
+    return cudaGetLastError();
+}
+
 }  // namespace mlp
 }  // namespace pcl
 

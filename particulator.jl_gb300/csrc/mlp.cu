@@ -229,7 +229,7 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward(Net net, const float* X,
     float* r_w4 = s.red;          // [128] dL/dw4
     float* r_b3 = s.red + kH;     // [128] dL/db3
     float* r_b4 = s.red + 2 * kH; // [1] dL/db4, [2] loss
-    for (int i = t; i < 2 * kH + 2; i += blockDim.x) s.red[i] = 0.0f;
+    for (int i = t; i < 2 * kH + 3; i += blockDim.x) s.red[i] = 0.0f;
     load_tile(sW2, net.W2, false);
     load_tile(sW3, net.W3, false);
     uint32_t tbase = setup(s);

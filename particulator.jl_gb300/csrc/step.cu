@@ -428,6 +428,24 @@ __device__ void s_coulomb(Lane& L, const KCtx& K, const DevProc& P) {
     L.s = nextcoll(L, K);
 }
 
+// moller.jl:19-37: energies, Lehtinen angles, shared azimuth, secondary
+__device__ __forceinline__ void moller_tail(Lane& L, const KCtx& K, float E, float eps, uint32_t ctr0) {
+    float E2 = eps * E, E1 = E - E2;
+    float p1 = sqrtf(E1 * (E1 + 2.0f)), p2 = sqrtf(E2 * (E2 + 2.0f));
+    float c1, s1, cc2, s2;
+    lehtinen(E, E1, E2, c1, s1);
+    lehtinen(E, E2, E1, cc2, s2);
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float ax, ay, az, bx, by, bz;
+    turn(L.px, L.py, L.pz, c1, s1, cph, sph, p1, ax, ay, az);
+    turn(L.px, L.py, L.pz, cc2, s2, cph, -sph, p2, bx, by, bz);
+    L.px = ax; L.py = ay; L.pz = az;
+    L.s = nextcoll(L, K);
+    float cs = nextcoll(L, K);
+    emit(L, K, PCL_ELECTRON, bx, by, bz, cs, 0, ctr0);
+}
+
 // moller.jl:13-37, 64-87
 __device__ void s_moller(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
     const float e0 = P.p[0] / E;
@@ -445,20 +463,7 @@ __device__ void s_moller(Lane& L, const KCtx& K, const DevProc& P, float E, uint
         if (U(L, K) < gg) break;
         if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
     }
-    float E2 = eps * E, E1 = E - E2;
-    float p1 = sqrtf(E1 * (E1 + 2.0f)), p2 = sqrtf(E2 * (E2 + 2.0f));
-    float c1, s1, cc2, s2;
-    lehtinen(E, E1, E2, c1, s1);
-    lehtinen(E, E2, E1, cc2, s2);
-    float sph, cph;
-    sincos_2pi(U(L, K), sph, cph);
-    float ax, ay, az, bx, by, bz;
-    turn(L.px, L.py, L.pz, c1, s1, cph, sph, p1, ax, ay, az);
-    turn(L.px, L.py, L.pz, cc2, s2, cph, -sph, p2, bx, by, bz);
-    L.px = ax; L.py = ay; L.pz = az;
-    L.s = nextcoll(L, K);
-    float cs = nextcoll(L, K);
-    emit(L, K, PCL_ELECTRON, bx, by, bz, cs, 0, ctr0);
+    moller_tail(L, K, E, eps, ctr0);
 }
 
 // rbeb.jl:54-80, 156-196
@@ -506,6 +511,21 @@ __device__ PCL_RARE void s_rbeb(Lane& L, const KCtx& K, const DevProc& P, float 
     emit(L, K, PCL_ELECTRON, bx, by, bz, cs, 0, ctr0);
 }
 
+// seltzer.jl:74-90: photon direction (modified Tsai, util.jl:143-159), recoil, photon
+__device__ __forceinline__ void sb_tail(Lane& L, const KCtx& K, float E, float k, uint32_t ctr0) {
+    if (!(k < E)) err(K, PCL_E_KINEMATICS);
+    float xt = tsai_x(L, K, E);
+    float cth = 1.0f - 2.0f * xt, sth = 2.0f * sqrtf(xt * (1.0f - xt));
+    float sph, cph;
+    sincos_2pi(U(L, K), sph, cph);
+    float gx, gy, gz;
+    turn(L.px, L.py, L.pz, cth, sth, cph, sph, k, gx, gy, gz);
+    L.px -= gx; L.py -= gy; L.pz -= gz;
+    L.s = nextcoll(L, K);
+    float cs = nextcoll(L, K);
+    emit(L, K, PCL_PHOTON, gx, gy, gz, cs, 0, ctr0);
+}
+
 // seltzer.jl:67-122 with the photon angle of util.jl:143-159.  The inverse-CDF
 // lookup reproduces the reference's interpolation weights as written
 // (seltzer.jl:278-284, off-diagonal corners included).
@@ -537,17 +557,7 @@ __device__ PCL_RARE void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E,
     float S = u11 * (xb - x) * (y2 - y) + u12 * (x - xa) * (y2 - y) + u21 * (xb - x) * (y - y1) +
               u22 * (x - xa) * (y - y1);
     float k = E * expf(S / A);
-    if (!(k < E)) err(K, PCL_E_KINEMATICS);
-    float xt = tsai_x(L, K, E);
-    float cth = 1.0f - 2.0f * xt, sth = 2.0f * sqrtf(xt * (1.0f - xt));
-    float sph, cph;
-    sincos_2pi(U(L, K), sph, cph);
-    float gx, gy, gz;
-    turn(L.px, L.py, L.pz, cth, sth, cph, sph, k, gx, gy, gz);
-    L.px -= gx; L.py -= gy; L.pz -= gz;
-    L.s = nextcoll(L, K);
-    float cs = nextcoll(L, K);
-    emit(L, K, PCL_PHOTON, gx, gy, gz, cs, 0, ctr0);
+    sb_tail(L, K, E, k, ctr0);
 }
 
 // compton.jl:9-28, 119-144 (Compton and KleinNishinaCompton share the sampler)
@@ -818,6 +828,75 @@ __device__ void sample_process(Lane& L, const KCtx& K, const SpeciesHdr& S, cons
     if (L.alive) L.r = setr(S, K, kin_energy_exact(L.species, L.px, L.py, L.pz), L.sw);
 }
 
+// ------------------------------------------------------- learned sampler -
+// Network input a = (log10(T / eV) - 6) / 2; the network is used where its
+// 64-bin map over a in [-1, 1) is set (trained range, monotone in u) and, for
+// Moller, where the kinematic range is not degenerate (e0 = tcut / T < 0.45).
+__device__ __forceinline__ float learn_a(float E) {
+    return (log10f(E * 510998.95f) - 6.0f) * 0.5f;
+}
+
+__device__ __forceinline__ bool learned_here(const DevProc& P, float E) {
+    float a = learn_a(E);
+    if (!(a >= -1.0f && a < 1.0f)) return false;
+    int bin = min(int((a + 1.0f) * 32.0f), 63);
+    if (!((P.learn_ok[bin >> 5] >> (bin & 31)) & 1u)) return false;
+    if (P.learn == PCL_LEARN_MOLLER && !(P.p[0] < 0.45f * E)) return false;
+    return true;
+}
+
+// Suspend the collision: one uniform is drawn for the network, the particle
+// goes to the suspended-collision queue and leaves this pass (its input slot,
+// if any, is marked dead; the resume pass appends it).  False when the queue is
+// full (the table sampler then runs instead).
+__device__ bool suspend(Lane& L, const KCtx& K, int j, uint32_t ctr0) {
+    const float u = U(L, K);
+    const StepArgs& A = *K.A;
+    unsigned long long q = atomicAdd(A.lq_out_n, 1ull);
+    if ((long long)q >= A.lq_cap) return false;
+    A.lq_out_xw[q] = make_float4(L.x, L.y, L.z, L.w);
+    A.lq_out_ps[q] = make_float4(L.px, L.py, L.pz, L.s);
+    A.lq_out_m1[q] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, ctr0);
+    uint32_t pk = uint32_t(L.species) | (uint32_t(L.k) << 2) | (uint32_t(j) << 8) |
+                  (uint32_t(min(L.nsub, 0xFFFF)) << 16);
+    A.lq_out_m2[q] = make_float4(L.th, L.tlo, u, __uint_as_float(pk));
+    L.alive = false;
+    return true;
+}
+
+// Lower bound of ln(k / T) of a Seltzer-Berger table at energy E: its
+// pcum = 0 column, linear in ln T between grid energies, lowered by the
+// column's largest step between grid energies (the table sampler's bilinear
+// weights can reach the lower corner of either bracketing energy).  The
+// bremsstrahlung network's output h = 1 - ln(k / T) / ymin lies in [0, 1].
+__device__ __forceinline__ float sb_ymin(const KCtx& K, const DevProc& P, float E) {
+    const SBHdr& T = K.H->sb[P.sb];
+    const float* data = K.A->sb_data[P.sb];
+    const float* le = K.blob + T.le_off;
+    const float y = logf(E);
+    int lo = 0, hi = T.ne;
+    while (lo < hi) { int mid = (lo + hi) >> 1; if (le[mid] < y) lo = mid + 1; else hi = mid; }
+    const int j1 = min(max(lo - 1, 0), T.ne - 2), j2 = j1 + 1;
+    const float w = fminf(fmaxf((y - le[j1]) / (le[j2] - le[j1]), 0.0f), 1.0f);
+    return (1.0f - w) * __ldg(data + (size_t)j1 * T.ncum) + w * __ldg(data + (size_t)j2 * T.ncum) - T.ymargin;
+}
+
+// Finish a suspended collision with the network output y (the part of the
+// sampler after its energy draw), then setr! as after every collision.
+__device__ void learned_outcome(Lane& L, const KCtx& K, const SpeciesHdr& S, const DevProc& P, float E, float y,
+                                uint32_t ctr0) {
+    if (P.learn == PCL_LEARN_SB) {
+        const float h = fminf(fmaxf(y, 0.0f), 1.0f);
+        // k < T strictly (seltzer.jl:73)
+        sb_tail(L, K, E, E * expf(fminf((1.0f - h) * sb_ymin(K, P, E), -1e-6f)), ctr0);
+    } else {
+        const float e0 = P.p[0] / E;
+        const float v = fminf(fmaxf(y, 0.0f), 1.0f);
+        moller_tail(L, K, E, e0 / (1.0f - v * (1.0f - 2.0f * e0)), ctr0);
+    }
+    if (L.alive) L.r = setr(S, K, kin_energy_exact(L.species, L.px, L.py, L.pz), L.sw);
+}
+
 // do_one_collision! (collisions.jl:142-199)
 __device__ void collide(Lane& L, const KCtx& K, const SpeciesHdr& S) {
     if (L.r == 0.0f) return;
@@ -855,7 +934,9 @@ __device__ void collide(Lane& L, const KCtx& K, const SpeciesHdr& S) {
         return;
     }
     atomicAdd(&K.tal[T_COLL + 16 * L.species + j], 1u);
-    sample_process(L, K, S, S.proc[j], E, ctr0);
+    const DevProc& P = S.proc[j];
+    if (P.learn && K.A->lq_out_n && learned_here(P, E) && suspend(L, K, j, ctr0)) return;
+    sample_process(L, K, S, P, E, ctr0);
 }
 
 // ---------------------------------------------------------- TMA staging --
@@ -949,7 +1030,10 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 
     // work space: concatenated species ranges, or the spill queue
     long long nsp0, nsp1, total;
-    if (A.spill_mode) {
+    if (A.spill_mode == 2) {
+        nsp0 = 0; nsp1 = 0;
+        total = min((long long)(*A.lq_in_n), A.lq_cap);
+    } else if (A.spill_mode) {
         nsp0 = 0; nsp1 = 0;
         total = min((long long)(*A.sp_in_n), A.sp_cap);
     } else {
@@ -1014,7 +1098,23 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 int rk = __popc(need & lt);
                 if (!has && rk < tk) {
                     long long v = cur + rk;
-                    if (A.spill_mode) {
+                    if (A.spill_mode == 2) {
+                        float4 a = A.lq_in_xw[v], b = A.lq_in_ps[v];
+                        uint4 m1 = A.lq_in_m1[v];
+                        float4 m2 = A.lq_in_m2[v];
+                        const uint32_t pk = __float_as_uint(m2.w);
+                        L.x = a.x; L.y = a.y; L.z = a.z; L.w = a.w;
+                        L.px = b.x; L.py = b.y; L.pz = b.z; L.s = b.w;
+                        L.sid_lo = m1.x; L.sid_hi = m1.y; L.ctr = m1.z;
+                        L.species = int(pk & 3u); L.k = int((pk >> 2) & 63u); L.nsub = int(pk >> 16);
+                        L.th = m2.x; L.tlo = m2.y;
+                        L.slot = -1; L.alive = true; L.rvalid = false;
+                        L.sw = (H->nswarm > 0) ? min(int(L.sid_hi >> 24), H->nswarm - 1) : 0;
+                        const SpeciesHdr& S = H->sp[L.species];
+                        const float E = kin_energy_exact(L.species, L.px, L.py, L.pz);
+                        learned_outcome(L, K, S, S.proc[(pk >> 8) & 15u], E, A.lq_in_y[v], m1.w);
+                        has = true;
+                    } else if (A.spill_mode) {
                         float4 a = A.sp_in_xw[v], b = A.sp_in_ps[v];
                         uint4 m = A.sp_in_meta[v];
                         L.x = a.x; L.y = a.y; L.z = a.z; L.w = a.w;
@@ -1037,7 +1137,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         has = (L.ctr != PCL_DEAD_CTR);
                         if (has) atomicAdd(&tal[T_LSTART + 0], 1u);
                     }
-                    if (has) {
+                    if (has && A.spill_mode != 2) {
                         L.rvalid = false; L.alive = true; L.nsub = 0;
                         L.sw = (H->nswarm > 0) ? min(int(L.sid_hi >> 24), H->nswarm - 1) : 0;
                         L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz), L.sw);
@@ -1411,6 +1511,84 @@ __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, cons
         out_kind[3 * i + c + 1] = ks[c];
     }
     out_ctr[i] = L.ctr;
+}
+
+// ------------------------------------------------ learned-sampler data --
+// Training data: samples of the table sampler of process j at nT energies
+// a_g = -1 + 2 g / (nT - 1), T = 10^(6 + 2 a_g) eV, primary along z, each
+// sample histogrammed (nbins over [hmin, hmax)) in the network's output
+// variable: ln(k / T) of the photon (bremsstrahlung) or v = (1 - e0 / eps) /
+// (1 - 2 e0) of the secondary (Moller).
+__global__ void k_learn_hist(StepArgs A, int species, int j, int kind, int nT, long long per_T, int nbins,
+                             float hmin, float hmax, unsigned long long sid_base, unsigned int* hist) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(smem + A.blob_bytes);
+    __shared__ uint32_t tal[T_WORDS];
+    for (int i = threadIdx.x; i < T_WORDS; i += blockDim.x) tal[i] = 0u;
+    bool ok = stage_blob(smem, A.blob, A.blob_bytes, mbar);
+    if (__syncthreads_or(!ok)) return;
+    const BlobHdr* H = reinterpret_cast<const BlobHdr*>(smem);
+    float capbuf[8];
+    int ncap = 0;
+    KCtx K;
+    K.H = H; K.blob = reinterpret_cast<const float*>(smem); K.stk = nullptr; K.top = nullptr; K.tal = tal;
+    K.A = &A; K.cap = capbuf; K.ncap = &ncap;
+    const SpeciesHdr& S = H->sp[species];
+    const DevProc& P = S.proc[j];
+    const long long total = (long long)nT * per_T;
+    const float scale = float(nbins) / (hmax - hmin);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int g = int(i / per_T);
+        const float a = (nT > 1) ? -1.0f + 2.0f * float(g) / float(nT - 1) : 0.0f;
+        const float E0 = exp10f(6.0f + 2.0f * a) / 510998.95f;
+        Lane L;
+        L.x = L.y = L.z = 0.0f; L.w = 1.0f; L.th = 0.0f; L.tlo = 0.0f; L.k = 0; L.s = 0.0f;
+        L.px = 0.0f; L.py = 0.0f; L.pz = sqrtf(E0 * (E0 + 2.0f));
+        const unsigned long long sid = sid_base + (unsigned long long)i;
+        L.sid_lo = uint32_t(sid); L.sid_hi = uint32_t(sid >> 32); L.ctr = 0u; L.rvalid = false;
+        L.species = species; L.alive = true; L.slot = -1; L.nsub = 0; L.sw = 0; L.r = 0.0f;
+        const float E = kin_energy_exact(species, 0.0f, 0.0f, L.pz);
+        ncap = 0;
+        sample_process(L, K, S, P, E, 0u);
+        if (ncap < 1) continue;
+        const float cx = capbuf[0], cy = capbuf[1], cz = capbuf[2];
+        float h;
+        if (kind == PCL_LEARN_SB) {
+            h = 1.0f - logf(sqrtf(cx * cx + cy * cy + cz * cz) / E) / sb_ymin(K, P, E);
+        } else {
+            const float p2 = cx * cx + cy * cy + cz * cz;
+            const float eps = p2 / (sqrtf(1.0f + p2) + 1.0f) / E;
+            const float e0 = P.p[0] / E;
+            h = (1.0f - e0 / eps) / (1.0f - 2.0f * e0);
+        }
+        int b = int(floorf((h - hmin) * scale));
+        b = min(max(b, 0), nbins - 1);
+        atomicAdd(&hist[(size_t)g * nbins + b], 1u);
+    }
+}
+
+// Network inputs of the suspended collisions: (a, 2u - 1).
+__global__ void k_learn_x(const float4* ps, const float4* m2, long long n, float* X) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float4 b = ps[i];
+        float4 q = m2[i];
+        int sp = int(__float_as_uint(q.w) & 3u);
+        X[2 * i] = learn_a(kin_energy_exact(sp, b.x, b.y, b.z));
+        X[2 * i + 1] = 2.0f * q.z - 1.0f;
+    }
+}
+
+// Output of the network attached to each suspended collision's process:
+// Y[i] = Yk[which[species][j] * stride + i].
+__global__ void k_learn_pick(const float4* m2, long long n, const float* Yk, long long stride, LearnPick which,
+                             float* Y) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        uint32_t pk = __float_as_uint(m2[i].w);
+        int sp = int(pk & 3u), j = int((pk >> 8) & 15u);
+        int w = which.net[sp * 16 + j];
+        Y[i] = Yk[(long long)max(w, 0) * stride + i];
+    }
 }
 
 // Shared-memory bytes of k_step for a block of `threads`.

@@ -3,9 +3,11 @@ table samplers (Seltzer-Berger photon energy, Moller secondary energy) and used
 by the step in place of them inside its trained range.
 
 Inputs a = (log10(T / eV) - 6) / 2 for T in [1e4, 1e8] eV, b = 2u - 1.
-Outputs: bremsstrahlung y = ln(k / T); Moller v with
-eps = e0 / (1 - v (1 - 2 e0)), e0 = tcut / T (v is the proposal's uniform of
-moller.jl:70, so v ~ u where the rejection accepts everything).
+Outputs, both in [0, 1] and increasing in u: bremsstrahlung h with
+ln(k / T) = (1 - h) ln(kmin / T), kmin / T the Seltzer-Berger table's pcum = 0
+value at T; Moller v with eps = e0 / (1 - v (1 - 2 e0)), e0 = tcut / T (v is
+the proposal's uniform of moller.jl:70, so v ~ u where the rejection accepts
+everything).
 """
 from __future__ import annotations
 
@@ -83,3 +85,46 @@ class SamplerNet:
             self.close()
         except Exception:
             pass
+
+
+def learn_data(mpopl, species: int, proc_index: int, kind: int, *, samples: float = 1e8, nT: int = 1024,
+               Q: int = 1024, seed: int = 0):
+    """Training set of the network for table position `proc_index` of
+    `species` in `mpopl` (pcl_learn_data): `samples` draws of the table sampler
+    spread over nT energies, turned into Q quantile targets per energy.
+    Returns (x (rows, 2) float32, t (rows,) float32)."""
+    per_T = max(1, int(samples // nT))
+    x = np.zeros((nT * Q, 2), np.float32)
+    t = np.zeros(nT * Q, np.float32)
+    rows = C.c_int64()
+    _lib.check(_lib.lib().pcl_learn_data(mpopl.ctx, int(species), int(proc_index), int(kind), int(nT), per_T, int(Q),
+                                         int(seed), _lib.fptr(x), _lib.fptr(t), C.byref(rows)),
+               mpopl.ctx, "pcl_learn_data")
+    return x[:rows.value], t[:rows.value]
+
+
+def train_sampler(mpopl, species: int, proc_index: int, kind: int, *, samples: float = 1e8, nT: int = 1024,
+                  Q: int = 1024, steps: int = 8000, batch: int = 8192, lr: float = 2e-3, seed: int = 0,
+                  device: int = 0):
+    """Generate the training set on the device from the table sampler and
+    train a network on it with the tensor-core kernels.  Returns (net, loss)."""
+    x, t = learn_data(mpopl, species, proc_index, kind, samples=samples, nT=nT, Q=Q, seed=seed)
+    net = SamplerNet(device=device, seed=seed)
+    loss = net.train(x, t, steps=steps, batch=batch, lr=lr, seed=seed)
+    return net, loss
+
+
+def table_positions(tab, kind: int):
+    """Table positions of a collision table whose process the kind replaces."""
+    from .processes import Moller, SeltzerBerger
+    cls = SeltzerBerger if kind == LEARN_SB else Moller
+    return [j for j, p in enumerate(tab.proc) if isinstance(p, cls)]
+
+
+def sb_ymin(sb, T):
+    """Lower bound of ln(k / T) of a SeltzerBerger table at kinetic energies
+    T (J), as the device computes it: the pcum = 0 column, linear in ln T
+    between grid energies, lowered by the column's largest step."""
+    le = np.asarray(sb.log_energy)
+    col = np.asarray(sb.data).reshape(len(le), -1)[:, 0]
+    return np.interp(np.log(np.asarray(T, dtype=float)), le, col) - np.max(np.abs(np.diff(col)))

@@ -259,6 +259,22 @@ class MultiPopulation:
         _lib.check(_lib.lib().pcl_swarm_moments(self.ctx, key, ns, _lib.dptr(out)), self.ctx, "pcl_swarm_moments")
         return out.reshape(ns, 6)
 
+    def set_learned(self, particle, proc_index: int, kind: int, net=None):
+        """Attach (net) or detach (None) a learned sampler for one table
+        position (pcl_set_learned)."""
+        key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        h = net.h if net is not None else None
+        if net is not None:
+            self._keep.append(net)
+        _lib.check(_lib.lib().pcl_set_learned(self.ctx, key, int(proc_index), int(kind), h), self.ctx,
+                   "pcl_set_learned")
+
+    def learn_stats(self):
+        """(collisions answered by a network, learned rounds) so far."""
+        a, b = C.c_int64(), C.c_int64()
+        _lib.check(_lib.lib().pcl_learn_stats(self.ctx, C.byref(a), C.byref(b)), self.ctx, "pcl_learn_stats")
+        return a.value, b.value
+
     def tallies(self) -> _lib.Tallies:
         t = _lib.Tallies()
         _lib.check(_lib.lib().pcl_get_tallies(self.ctx, C.byref(t)), self.ctx, "pcl_get_tallies")
