@@ -286,6 +286,84 @@ def run_swarms(args, pcl):
     return 0
 
 
+def run_learned(args, pcl):
+    """Learned form of the 16M avalanche: the Seltzer-Berger and Moller
+    secondary-energy draws go to networks trained here on 1e8 table-sampler
+    samples each (tensor-core training kernels), the rest of the step as in
+    the plain form.  Both forms run from the same initial state; the line
+    reports the learned value with the plain value, spawn counts and the
+    networks' training cost beside it."""
+    L = pcl.lib()
+    co = pcl.co
+    t_train0 = time.perf_counter()
+    mp, pusher, dt, extra = build_workload(pcl, args.n, seed=0, device=0, blocks_per_sm=args.bps)
+    et = extra["tables"][0]
+    nets = []
+    attach = []
+    for kind in (pcl.learned.LEARN_SB, pcl.learned.LEARN_MOLLER):
+        pos = pcl.learned.table_positions(et, kind)
+        targets = pos if kind == pcl.learned.LEARN_SB else pos[:1]   # Moller: one network for both Z
+        for j in targets:
+            net, loss = pcl.learned.train_sampler(mp, pcl.Electron, j, kind, samples=1e8, nT=1024, Q=1024,
+                                                  steps=8000, batch=8192, lr=2e-3, seed=j)
+            nets.append((j, kind, loss))
+            for q in (pos if kind == pcl.learned.LEARN_MOLLER else [j]):
+                attach.append((q, kind, net))
+    t_train = time.perf_counter() - t_train0
+    results = {}
+    for form in ("plain", "learned"):
+        if form == "learned":
+            for q, kind, net in attach:
+                mp.set_learned(pcl.Electron, q, kind, net)
+        t = 0.0
+        for _ in range(args.warmup):
+            t += dt
+            pcl.advance(mp, pusher, t)
+        L.pcl_sync(mp.ctx)
+        tal0 = mp.tallies()
+        s0 = mp.learn_stats()
+        L.pcl_kernel_stats(mp.ctx, None, None, None, None, 1)
+        with Clocks(0) as clk:
+            L.pcl_timer_start(mp.ctx)
+            for _ in range(args.steps):
+                t += dt
+                pcl.advance(mp, pusher, t)
+            ms = C.c_double()
+            L.pcl_timer_stop(mp.ctx, C.byref(ms))
+        tal1 = mp.tallies()
+        s1 = mp.learn_stats()
+        kms = C.c_double(); kl = C.c_int64(); nl = C.c_int64(); kb = C.c_double()
+        L.pcl_kernel_stats(mp.ctx, C.byref(kms), C.byref(kl), C.byref(nl), C.byref(kb), 1)
+        ps = tal1.particle_steps - tal0.particle_steps
+        results[form] = dict(value=ps / (ms.value / 1e3), ms=ms.value, clocks=clk.summary(), launches=int(nl.value),
+                             spawned=[int(tal1.spawned[q] - tal0.spawned[q]) for q in range(3)],
+                             live=list(tal1.live), learned_collisions=int(s1[0] - s0[0]),
+                             rounds=int(s1[1] - s0[1]), kbytes=kb.value, kms=kms.value, kl=kl.value)
+        mp.close()
+        if form == "plain":
+            mp, pusher, dt, extra = build_workload(pcl, args.n, seed=0, device=0, blocks_per_sm=args.bps)
+    r, p0 = results["learned"], results["plain"]
+    peak, peak_kind = _peaks()
+    achieved = (r["kbytes"] / max(r["kl"], 1)) / (r["kms"] / max(r["kl"], 1) / 1e3) / 1e9
+    line = {"metric": "particle-steps/s on 1 GB300 (learned form: network samplers, mixed avalanche at 2^24)",
+            "value": r["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+bf16", "data": "synthetic",
+            "config": {"workload": "rrea-air-0.5MVm-16M-learned", "seed_electrons": args.n, "dt_s": 1e-12,
+                       "networks": [{"table_position": j, "kind": k, "train_loss": l} for j, k, l in nets],
+                       "training_s": t_train, "training_samples_per_network": 1e8},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "peak_kind": peak_kind, "traffic": None, "kernel": "k_step"},
+            "learned": {"collisions_per_step": r["learned_collisions"] / args.steps,
+                        "rounds_per_step": r["rounds"] / args.steps, "spawned": r["spawned"], "live": r["live"]},
+            "plain": {"value": p0["value"], "ms_per_step": p0["ms"] / args.steps, "spawned": p0["spawned"],
+                      "live": p0["live"]},
+            "learned_over_plain": r["value"] / p0["value"],
+            "cpu_baseline": None, "gpu_launches": r["launches"], "clocks": r["clocks"]}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -300,17 +378,18 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--steps-per-launch", type=int, default=1)
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
-    ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms"])
+    ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned"])
     ap.add_argument("--nswarm", type=int, default=256)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload == "swarms":
+    if args.workload in ("swarms", "learned"):
         if args.warmup < 3:
             args.warmup = 3
         import __graft_entry__ as graft
         graft.build()
-        return run_swarms(args, graft.load_package())
+        fn = run_swarms if args.workload == "swarms" else run_learned
+        return fn(args, graft.load_package())
     if args.warmup < 3:
         args.warmup = 3
     ws, rank = _dist()

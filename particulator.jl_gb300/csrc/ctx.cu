@@ -617,7 +617,7 @@ static int run_group_graph(Ctx* c, const StepArgs& A, const StepArgs& P0, const 
 
 // Spill passes: the queue written by the previous pass is the next pass's
 // input, starting from spill queue `in`; suspended collisions of these passes
-// go to learned queue `lq_out`.  *ran = whether any pass ran.
+// go to learned queue `lq_out` (-1: none suspended).  *ran = whether any pass ran.
 static int drain_spills(Ctx* c, double dt, int nsteps, int threads, size_t smem, int in, int lq_out, bool* ran,
                         const unsigned long long* known_pending) {
     for (int pass = 0; pass < 64; ++pass) {
@@ -628,7 +628,8 @@ static int drain_spills(Ctx* c, double dt, int nsteps, int threads, size_t smem,
         *ran = true;
         k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + in, c->d_spn + (1 - in));
         StepArgs S = make_args(c, dt, nsteps, 1, in);
-        set_lq(S, c, lq_out, -1);
+        if (lq_out >= 0) set_lq(S, c, lq_out, -1);
+        else S.lq_out_n = nullptr;   // no suspension in these passes
         CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, S));
         c->launches += 2;
         in = 1 - in;
@@ -636,14 +637,17 @@ static int drain_spills(Ctx* c, double dt, int nsteps, int threads, size_t smem,
     return fail(c, PCL_ERR_TIMEOUT, "spill passes did not drain");
 }
 
-// Learned-sampler rounds: the networks answer every collision suspended so
-// far (one batched tensor-core forward pass per attached network), a resume
-// pass finishes them and carries the particles to the end of the launch
-// (suspending again into the other queue where they collide again), then the
-// spill passes drain.  Bounded number of rounds.
+// Learned-sampler round: the networks answer every collision suspended by
+// the launch (one batched tensor-core forward pass per attached network), a
+// resume pass finishes them and carries the particles to the end of the
+// launch, then the spill passes drain.  The resume pass and its spill passes
+// use the table sampler for any further collision of those particles in the
+// same launch (kLearnRounds = 1: one host round trip per launch).
+constexpr int kLearnRounds = 1;
+
 static int learned_rounds(Ctx* c, double dt, int nsteps, int threads, size_t smem, bool* ran) {
     int lin = 0;
-    for (int round = 0; round < 64; ++round) {
+    for (int round = 0; round < kLearnRounds; ++round) {
         unsigned long long n = 0;
         CK(d2h(c, &n, c->d_lqn + lin, sizeof(n)));
         if (n == 0) return PCL_OK;
@@ -660,16 +664,20 @@ static int learned_rounds(Ctx* c, double dt, int nsteps, int threads, size_t sme
         k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 0, c->d_spn + 1);  // head 0, spill queue 1 empty
         StepArgs R = make_args(c, dt, nsteps, 2, 0);
         set_lq(R, c, 1 - lin, lin);
-        CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, R));
+        const bool last = round + 1 == kLearnRounds;
+        if (last) R.lq_out_n = nullptr;   // no further suspension
+        // a grid sized to the suspended collisions (8 warps of 32 per CTA)
+        const int rgrid = int(std::min<long long>(grid_blocks(c), std::max<long long>(1, (m + 255) / 256)));
+        CK(launch_step(blocks_per_sm(c), rgrid, threads, smem, c->stream, R));
         c->launches += 4 + (long long)c->nets.size();
         c->learn_rounds += 1;
         c->learn_suspended += m;
         bool dummy = false;
-        int rc = drain_spills(c, dt, nsteps, threads, smem, 1, 1 - lin, &dummy, nullptr);
+        int rc = drain_spills(c, dt, nsteps, threads, smem, 1, last ? -1 : 1 - lin, &dummy, nullptr);
         if (rc) return rc;
         lin = 1 - lin;
     }
-    return fail(c, PCL_ERR_TIMEOUT, "learned-sampler rounds did not drain");
+    return PCL_OK;
 }
 
 // One launch of `nsteps` steps of length dt (seconds), plus spill passes and,
