@@ -364,6 +364,175 @@ def run_learned(args, pcl):
     return 0
 
 
+def _oracle_world(pcl, seed, tabs, cuts, pusher, tally_only=()):
+    from oracle.harness import OracleWorld
+    return OracleWorld(seed, tabs, cuts, pusher, tally_only=tally_only)
+
+
+def run_plain(args, pcl):
+    """Electrons only in air at 1 MV/m: 1000 e- at 1 MeV along +z, 50 ns in
+    steps of 1 ps (5e4 steps, 64 per launch), Moller / Seltzer-Berger /
+    Coulomb, continuum loss below 10 keV, bremsstrahlung photons tallied.  The
+    whole run is timed on the GPU; the oracle (C++ Float64, all host threads)
+    runs the first 2000 steps of the same particles and streams, both for the
+    CPU baseline and for a paired comparison with a GPU run of those steps."""
+    from oracle.harness import compare_populations
+    L = pcl.lib()
+    threads = os.cpu_count() or 1
+    wl = pcl.workloads.plain_electrons(n=1000, tfinal=50e-9, seed=1, steps_per_launch=64)
+    mp, pusher, dt = wl.mpopl, wl.pusher, wl.dt
+    nsteps = int(round(wl.tfinal / dt))
+    mp.set_pusher(pusher)
+    pcl.run(mp, pusher, 64 * dt, dt)   # warm-up launch (64 steps)
+    tal0 = mp.tallies()
+    with Clocks(0) as clk:
+        L.pcl_timer_start(mp.ctx)
+        pcl.run(mp, pusher, wl.tfinal, dt)
+        ms = C.c_double()
+        L.pcl_timer_stop(mp.ctx, C.byref(ms))
+    tal1 = mp.tallies()
+    ps = tal1.particle_steps - tal0.particle_steps
+    e = mp.get(pcl.Electron).particles()
+    obs = {"electrons": int(tal1.live[0]), "mean_energy_eV": float(np.mean(pcl.kinenergy(0, e.p)) / pcl.co.eV),
+           "mean_z_m": float(np.mean(e.x[:, 2])), "photons_tallied": int(tal1.tally_count[1]),
+           "photon_energy_J": float(tal1.tally_wE[1])}
+    nl = C.c_int64()
+    L.pcl_kernel_stats(mp.ctx, None, None, C.byref(nl), None, 1)
+    mp.close()
+    # paired GPU vs oracle over the first 2000 steps (same particles, seed, streams)
+    k = 2000
+    wb = pcl.workloads.plain_electrons(n=1000, tfinal=k * dt, seed=1)
+    eb = wb.mpopl.get(pcl.Electron)
+    W = _oracle_world(pcl, 1, {pcl.Electron: eb.collisions}, {pcl.Electron: eb.energy_cut, pcl.Photon: 0.0},
+                      wb.pusher, tally_only=(pcl.Photon,))
+    W.upload(pcl.Electron, eb.particles())
+    t0 = time.perf_counter()
+    pst = 0
+    for i in range(k):
+        pst += len(W.download(pcl.Electron).w) if i % 100 == 0 else 0
+        W.advance((i + 1) * dt, threads)
+    cpu_s = time.perf_counter() - t0
+    c = W.counters()
+    pcl.run(wb.mpopl, wb.pusher, k * dt, dt)
+    rep = compare_populations(eb.particles(), W.download(pcl.Electron), pcl.Electron, rtol=1e-3, stol=1e-2)
+    tb = wb.mpopl.tallies()
+    wb.mpopl.close()
+    n_orc = rep["n_orc"]
+    cpu_value = (n_orc + 1000) / 2 * k / cpu_s
+    line = {"metric": "particle-steps/s on 1 GB300 (electrons only, air, 1 MV/m, 1000 e- for 50 ns)",
+            "value": ps / (ms.value / 1e3), "unit": UNIT, "n_gpus": 1, "steps": nsteps - 64, "warmup": 64,
+            "ms_per_step": ms.value / (nsteps - 64), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "electrons-air-1MVm-1000", "dt_s": dt, "steps_per_launch": 64},
+            "observables": obs,
+            "paired_2000_steps": {"gpu_electrons": int(tb.live[0]), "oracle_electrons": int(n_orc),
+                                  "gpu_photons": int(tb.tally_count[1]), "oracle_photons": int(c["tally_count"][1]),
+                                  "ties": rep["ties"], "max_dp_rel": rep["max_dp_rel"], "ok": rep["ok"]},
+            "cpu_baseline": {"value": cpu_value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"the first {k} steps of the same 1000 electrons ({cpu_s:.1f} s), C++ Float64 oracle"},
+            "gpu_launches": int(nl.value), "clocks": clk.summary()}
+    print(json.dumps(line))
+    return 0
+
+
+def _swarm_obs(t, z, zz, E):
+    """drift velocity (fit of <z>), longitudinal diffusion (fit of var z / 2),
+    mean energy (mean over the window)."""
+    t = np.asarray(t); z = np.asarray(z); var = np.asarray(zz) - z ** 2
+    W = np.polyfit(t, z, 1)[0]
+    D = np.polyfit(t, var, 1)[0] / 2
+    return float(W), float(D), float(np.mean(E))
+
+
+def run_reid(args, pcl):
+    """Reid's ramp model gas at E/N = 1, 3, 12, 24, 48 Td: 2^20 electrons
+    (Maxwellian, 1 eV mean, Philox seed 2), dt = 1 ps, 1000 relaxation steps
+    and 2000 measured steps (16 per launch).  FP32 device against the Float64
+    oracle: the oracle follows the first 4096 electrons with the same streams
+    (paired: the difference is the device's rounding error) and its own
+    statistics give the FP64 reference of each observable."""
+    L = pcl.lib()
+    threads = os.cpu_count() or 1
+    dt = 1e-12
+    relax, meas, every = 1000, 2000, 100
+    n, nsub = 1 << 20, 4096
+    rows = []
+    total_ps = 0.0
+    total_ms = 0.0
+    cpu_ps = 0.0
+    cpu_s = 0.0
+    clk_all = None
+    for EN in (1.0, 3.0, 12.0, 24.0, 48.0):
+        wl = pcl.workloads.reid_ramp(n=n, EN_Td=EN, dt=dt, steps_per_launch=16)
+        mp, pusher = wl.mpopl, wl.pusher
+        e = mp.get(pcl.Electron)
+        init = e.particles()
+        sub = pcl.ParticleArrays(init.x[:nsub], init.p[:nsub], init.w[:nsub], init.t[:nsub], init.s[:nsub],
+                                 init.sid[:nsub], init.ctr[:nsub])
+        W = _oracle_world(pcl, 2, {pcl.Electron: e.collisions}, {pcl.Electron: 0.0}, pusher)
+        W.upload(pcl.Electron, sub)
+        mp.set_pusher(pusher)
+        t = 0.0
+        gt, gz, gzz, gE = [], [], [], []
+        ot, oz, ozz, oE = [], [], [], []
+        pz_g, pz_o, pE_g, pE_o = [], [], [], []
+        tal0 = mp.tallies()
+        with Clocks(0) as clk:
+            L.pcl_timer_start(mp.ctx)
+            for blk in range((relax + meas) // every):
+                t1 = (blk + 1) * every * dt
+                pcl.run(mp, pusher, t1, dt)
+                if (blk + 1) * every > relax:
+                    m = e.moments()
+                    gt.append(t1); gz.append(m[4] / m[0]); gzz.append(m[7] / m[0]); gE.append(m[1] / m[0])
+            ms = C.c_double()
+            L.pcl_timer_stop(mp.ctx, C.byref(ms))
+        clk_all = clk.summary()
+        tal1 = mp.tallies()
+        total_ps += tal1.particle_steps - tal0.particle_steps
+        total_ms += ms.value
+        # oracle: the first nsub electrons, same streams
+        c0 = time.perf_counter()
+        for blk in range((relax + meas) // every):
+            for i in range(every):
+                W.advance((blk * every + i + 1) * dt, threads)
+            if (blk + 1) * every > relax:
+                o = W.download(pcl.Electron)
+                Eo = pcl.kinenergy(0, o.p)
+                ot.append((blk + 1) * every * dt); oz.append(np.mean(o.x[:, 2])); ozz.append(np.mean(o.x[:, 2] ** 2))
+                oE.append(np.mean(Eo))
+        el = time.perf_counter() - c0
+        cpu_s += el
+        cpu_ps += nsub * (relax + meas)
+        g = e.particles()
+        o = W.download(pcl.Electron)
+        sel = g.sid < nsub
+        og = np.argsort(g.sid[sel]); oo = np.argsort(o.sid)
+        dE = (np.mean(pcl.kinenergy(0, g.p[sel][og])) - np.mean(pcl.kinenergy(0, o.p[oo]))) / np.mean(
+            pcl.kinenergy(0, o.p[oo]))
+        dz = (np.mean(g.x[sel][og][:, 2]) - np.mean(o.x[oo][:, 2])) / max(abs(np.mean(o.x[oo][:, 2])), 1e-30)
+        Wg, Dg, Eg = _swarm_obs(gt, gz, gzz, gE)
+        Wo, Do, Eo_ = _swarm_obs(ot, oz, ozz, oE)
+        rows.append({"EN_Td": EN, "gpu": {"W_m_s": Wg, "DL_m2_s": Dg, "mean_energy_eV": Eg / pcl.co.eV},
+                     "oracle_fp64_4096": {"W_m_s": Wo, "DL_m2_s": Do, "mean_energy_eV": Eo_ / pcl.co.eV},
+                     "paired_rel_diff": {"mean_energy": float(dE), "mean_z": float(dz)},
+                     "oracle_ties": int(W.counters()["ties"])})
+        mp.close()
+    line = {"metric": "particle-steps/s on 1 GB300 (Reid ramp swarm, 2^20 e-, 5 E/N values)",
+            "value": total_ps / (total_ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": relax + meas, "warmup": 0,
+            "ms_per_step": total_ms / (5 * (relax + meas)), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "reid-ramp-2^20", "dt_s": dt, "steps_per_launch": 16, "relax_steps": relax,
+                       "measured_steps": meas},
+            "observables": rows,
+            "cpu_baseline": {"value": cpu_ps / cpu_s, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"the first {nsub} electrons of each E/N, all {relax + meas} steps "
+                                       f"({cpu_s:.1f} s), C++ Float64 oracle"},
+            "clocks": clk_all}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -378,17 +547,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--steps-per-launch", type=int, default=1)
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
-    ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned"])
+    ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned", "plain", "reid"])
     ap.add_argument("--nswarm", type=int, default=256)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload in ("swarms", "learned"):
+    if args.workload != "rrea16M":
         if args.warmup < 3:
             args.warmup = 3
         import __graft_entry__ as graft
         graft.build()
-        fn = run_swarms if args.workload == "swarms" else run_learned
+        fn = {"swarms": run_swarms, "learned": run_learned, "plain": run_plain, "reid": run_reid}[args.workload]
         return fn(args, graft.load_package())
     if args.warmup < 3:
         args.warmup = 3
