@@ -344,6 +344,28 @@ int pcl_test_sampler(void* ctx, int species, int proc_index, int64_t n, const do
 int pcl_compact_noalloc(int64_t n, const float* xw, const float* ps, const uint32_t* meta,
                         float* out_xw, float* out_ps, uint32_t* out_meta, int64_t* n_out, void* stream);
 
+/* ---- launch autotuner -------------------------------------------------------
+ * No counterpart in the reference (its loop has no launch shape).  Advances
+ * the simulation by up to steps_budget real steps of dt (the physics does not
+ * depend on the launch parameters) while a coordinate search times candidate
+ * launch shapes with CUDA events: blocks per SM {2, 3, 4}, steps per launch
+ * {1, 2, 4, 8, 16}, compaction period {2, 4, 8, 16, 32}, graph replay {0, 1},
+ * in that order, each trial a whole number of launches and compactions.  The
+ * context keeps the fastest shape (particle-steps per second). */
+typedef struct pcl_tune_result {
+    int32_t blocks_per_sm, steps_per_launch, compaction_period, use_graph;
+    double  rate;              /* particle-steps per second of the kept shape */
+    int32_t trials;
+    int32_t steps;             /* steps advanced by the search */
+    int32_t reserved[2];
+} pcl_tune_result;
+int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* out);
+/* Set the launch shape directly (e.g. one tuned on another context of the
+ * same workload): blocks per SM (2-4), steps per launch (1-64), compaction
+ * period (>= 1), graph replay (0/1). */
+int pcl_set_launch(void* ctx, int32_t blocks_per_sm, int32_t steps_per_launch, int32_t compaction_period,
+                   int32_t use_graph);
+
 /* ---- learned inverse-CDF sampler network ---------------------------------
  * No single counterpart in the reference: a learned replacement for the
  * secondary-energy samplers of SeltzerBerger.collide (seltzer.jl:97-122) and

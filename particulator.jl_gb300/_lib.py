@@ -76,6 +76,11 @@ class RunOpts(C.Structure):
     _fields_ = [("target_species", _i32), ("target_ismax", _i32), ("target_n", _i64), ("max_steps", _i64)]
 
 
+class TuneResult(C.Structure):
+    _fields_ = [("blocks_per_sm", _i32), ("steps_per_launch", _i32), ("compaction_period", _i32),
+                ("use_graph", _i32), ("rate", _d), ("trials", _i32), ("steps", _i32), ("reserved", _i32 * 2)]
+
+
 class Packed(C.Structure):
     _fields_ = [("xw", _P(C.c_float)), ("ps", _P(C.c_float)), ("meta", _P(_u32))]
 
@@ -133,6 +138,8 @@ _SIGS = {
     "pcl_mlp_gradient": (C.c_int, [C.c_void_p, _i64, _P(C.c_float), _P(C.c_float), _P(C.c_float), _P(_d)]),
     "pcl_mlp_train": (C.c_int, [C.c_void_p, _i64, _P(C.c_float), _P(C.c_float), _i64, _i32, _d, _u64, _P(_d)]),
     "pcl_set_learned": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    "pcl_autotune": (C.c_int, [C.c_void_p, _d, _i32, _P(TuneResult)]),
+    "pcl_set_launch": (C.c_int, [C.c_void_p, _i32, _i32, _i32, _i32]),
     "pcl_learn_stats": (C.c_int, [C.c_void_p, _P(_i64), _P(_i64)]),
     "pcl_learn_data": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, _u64,
                                  _P(C.c_float), _P(C.c_float), _P(_i64)]),

@@ -1152,16 +1152,19 @@ int pcl_run(void* ctx, double tfinal, double dt, const pcl_run_opts* opts, pcl_t
     if (!(dt > 0)) return fail(c, PCL_ERR_INVALID, "dt must be > 0");
     CK(cudaSetDevice(c->device));
     const int K = std::max(1, c->cfg.steps_per_launch);
+    // run.jl:6-27 steps while t < tfinal; the step count is fixed once, with a
+    // tolerance, so that accumulated rounding of the clock never adds a step
+    const long long total = (long long)std::ceil((tfinal - c->t) / dt - 1e-6);
     long long done = 0;
-    while (c->t < tfinal) {
-        // run.jl:6-27: advance!, droplow!, onstep (population target)
-        long long left = (long long)std::ceil((tfinal - c->t) / dt - 1e-9);
-        int ns = int(std::min<long long>(K, std::max<long long>(1, left)));
+    while (done < total) {
+        // advance!, droplow!, onstep (population target)
+        int ns = int(std::min<long long>(K, total - done));
         if (opts && opts->max_steps > 0) ns = int(std::min<long long>(ns, opts->max_steps - done));
         if (ns <= 0) break;
         int rc = launch_steps(c, dt, ns);
         if (rc) return rc;
         done += ns;
+        if (done == total && std::fabs(c->t - tfinal) < 1e-6 * dt) c->t = tfinal;
         if (opts && opts->target_species >= 0 && opts->target_species < 3) {
             long long live = c->live[opts->target_species];
             bool cont = opts->target_ismax ? (live < opts->target_n) : (live > opts->target_n);
@@ -1464,6 +1467,86 @@ int pcl_learn_data(void* ctx, int species, int proc_index, int kind, int nT, int
         }
     }
     *nrows = r;
+    return PCL_OK;
+}
+
+int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* out) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !(dt > 0) || steps_budget < 16) return PCL_ERR_INVALID;
+    bool any = false;
+    for (auto& sp : c->sp) any = any || sp.set;
+    if (!any) return fail(c, PCL_ERR_STATE, "no species set");
+    CK(cudaSetDevice(c->device));
+    const int bps_c[] = {2, 3, 4}, k_c[] = {1, 2, 4, 8, 16}, per_c[] = {2, 4, 8, 16, 32}, g_c[] = {0, 1};
+    const int ntrials = 3 + 5 + 5 + 2;
+    // steps per trial: a multiple of the largest steps-per-launch and period tried
+    int len = std::max(32, (steps_budget / ntrials) / 32 * 32);
+    pcl_config best = c->cfg;
+    best.blocks_per_sm = blocks_per_sm(c);
+    if (best.steps_per_launch < 1) best.steps_per_launch = 1;
+    if (best.compaction_period < 1) best.compaction_period = 8;
+    double best_rate = -1.0;
+    int trials = 0, done = 0;
+    auto trial = [&](const pcl_config& cfg, double& rate) -> int {
+        c->cfg = cfg;
+        int rc = compact_all(c);   // every trial starts from a compacted population
+        if (rc) return rc;
+        const long long ps0 = c->particle_steps;
+        CK(cudaEventRecord(c->ev_t0, c->stream));
+        int left = len;
+        while (left > 0) {
+            int ns = std::min(left, std::max(1, cfg.steps_per_launch));
+            if ((rc = launch_steps(c, dt, ns))) return rc;
+            left -= ns;
+        }
+        CK(cudaEventRecord(c->ev_t1, c->stream));
+        CK(cudaEventSynchronize(c->ev_t1));
+        float ms = 0.0f;
+        CK(cudaEventElapsedTime(&ms, c->ev_t0, c->ev_t1));
+        rate = double(c->particle_steps - ps0) / (double(ms) * 1e-3);
+        done += len;
+        ++trials;
+        return PCL_OK;
+    };
+    auto consider = [&](pcl_config cfg) -> int {
+        if (done + len > steps_budget) return PCL_OK;
+        double r = 0.0;
+        int rc = trial(cfg, r);
+        if (rc) return rc;
+        if (r > best_rate) { best_rate = r; best = cfg; }
+        return PCL_OK;
+    };
+    int rc = PCL_OK;
+    for (int v : bps_c) { pcl_config q = best; q.blocks_per_sm = v; if ((rc = consider(q))) return rc; }
+    const pcl_config after_bps = best;
+    for (int v : k_c) { pcl_config q = after_bps; q.steps_per_launch = v; if ((rc = consider(q))) return rc; }
+    const pcl_config after_k = best;
+    for (int v : per_c) { pcl_config q = after_k; q.compaction_period = v; if ((rc = consider(q))) return rc; }
+    const pcl_config after_p = best;
+    for (int v : g_c) { pcl_config q = after_p; q.use_graph = v; if ((rc = consider(q))) return rc; }
+    c->cfg = best;
+    if (out) {
+        std::memset(out, 0, sizeof(*out));
+        out->blocks_per_sm = best.blocks_per_sm;
+        out->steps_per_launch = best.steps_per_launch;
+        out->compaction_period = best.compaction_period;
+        out->use_graph = best.use_graph;
+        out->rate = best_rate;
+        out->trials = trials;
+        out->steps = done;
+    }
+    return PCL_OK;
+}
+
+int pcl_set_launch(void* ctx, int32_t bps, int32_t spl, int32_t period, int32_t use_graph) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || bps < 2 || bps > 4 || spl < 1 || spl > PCL_MAX_STEPS_PER_LAUNCH || period < 1 ||
+        (use_graph != 0 && use_graph != 1))
+        return PCL_ERR_INVALID;
+    c->cfg.blocks_per_sm = bps;
+    c->cfg.steps_per_launch = spl;
+    c->cfg.compaction_period = period;
+    c->cfg.use_graph = use_graph;
     return PCL_OK;
 }
 

@@ -269,6 +269,31 @@ class MultiPopulation:
         _lib.check(_lib.lib().pcl_set_learned(self.ctx, key, int(proc_index), int(kind), h), self.ctx,
                    "pcl_set_learned")
 
+    def autotune(self, pusher: RK2Pusher, dt: float, steps: int = 480) -> dict:
+        """Choose the launch shape (blocks per SM, steps per launch, compaction
+        period, graph replay) by timing real steps of dt (pcl_autotune); the
+        population advances by the steps the search uses."""
+        self.set_pusher(pusher)
+        r = _lib.TuneResult()
+        _lib.check(_lib.lib().pcl_autotune(self.ctx, float(dt), int(steps), C.byref(r)), self.ctx, "pcl_autotune")
+        t = _lib.Tallies()
+        _lib.check(_lib.lib().pcl_get_tallies(self.ctx, C.byref(t)), self.ctx, "pcl_get_tallies")
+        self.t = t.t
+        for f in ("blocks_per_sm", "steps_per_launch", "compaction_period", "use_graph"):
+            setattr(self.config, f, getattr(r, f))
+        return {"blocks_per_sm": r.blocks_per_sm, "steps_per_launch": r.steps_per_launch,
+                "compaction_period": r.compaction_period, "use_graph": r.use_graph, "rate": r.rate,
+                "trials": r.trials, "steps": r.steps}
+
+    def set_launch(self, blocks_per_sm: int, steps_per_launch: int, compaction_period: int, use_graph: bool):
+        """Set the launch shape (pcl_set_launch)."""
+        _lib.check(_lib.lib().pcl_set_launch(self.ctx, int(blocks_per_sm), int(steps_per_launch),
+                                             int(compaction_period), 1 if use_graph else 0), self.ctx, "pcl_set_launch")
+        self.config.blocks_per_sm = blocks_per_sm
+        self.config.steps_per_launch = steps_per_launch
+        self.config.compaction_period = compaction_period
+        self.config.use_graph = 1 if use_graph else 0
+
     def learn_stats(self):
         """(collisions answered by a network, learned rounds) so far."""
         a, b = C.c_int64(), C.c_int64()

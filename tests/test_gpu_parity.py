@@ -119,6 +119,34 @@ def test_graph_matches_plain(pcl, gpu, air):
     a.close(); b.close()
 
 
+def test_autotune_keeps_physics(pcl, gpu, air):
+    """The autotuner advances real steps and keeps a valid launch shape; the
+    population it leaves equals a plain run of the same number of steps
+    (launch shapes do not change the physics; a multi-step launch keeps the
+    sub-eps remainder of a step as a double-float where separate launches
+    round it to FP32, so a rare particle may differ in its last bits)."""
+    pusher = _pusher(pcl, air, E=2e6)
+    a = _mixed(pcl, air, n=(2048, 1024, 512), seed=21)
+    r = a.autotune(pusher, 1e-12, steps=480)
+    assert r["blocks_per_sm"] in (2, 3, 4) and r["steps_per_launch"] in (1, 2, 4, 8, 16)
+    assert r["compaction_period"] in (2, 4, 8, 16, 32) and r["use_graph"] in (0, 1)
+    assert r["trials"] == 15 and r["steps"] == 480 and r["rate"] > 0
+    ta = a.tallies()
+    assert ta.steps == 480
+    b = _mixed(pcl, air, n=(2048, 1024, 512), seed=21)
+    pcl.run(b, pusher, 480e-12, 1e-12)
+    tb = b.tallies()
+    for s in range(3):
+        assert abs(ta.live[s] - tb.live[s]) <= 2 + ta.live[s] // 1000
+    for k in a.index:
+        pa, pb = a.get(k).particles(), b.get(k).particles()
+        common, ia, ib = np.intersect1d(pa.sid, pb.sid, return_indices=True)
+        assert len(common) >= 0.999 * max(len(pa.sid), len(pb.sid)) - 2
+        dp = np.linalg.norm(pa.p[ia] - pb.p[ib], axis=1) / np.maximum(np.linalg.norm(pb.p[ib], axis=1), 1e-300)
+        assert np.mean(dp > 1e-5) <= 1e-3, np.sort(dp)[-5:]
+    a.close(); b.close()
+
+
 def test_electrons_tally_photons(pcl, oracle, gpu):
     """Electrons-only workload with bremsstrahlung photons tallied."""
     wl = pcl.workloads.plain_electrons(n=1000, tfinal=20e-12, seed=1)
