@@ -541,6 +541,43 @@ def run_reid(args, pcl):
     return 0
 
 
+def run_mlp(args, pcl):
+    """The learned-sampler network alone: batched inference of 2^22 rows
+    (tcgen05 128 x 128 layers, 32768 tiles) and training steps of 8192 rows.
+    FLOPs per row: 2 (2 x 128 + 2 x 128 x 128 + 128) = 66,304 forward."""
+    L = pcl.lib()
+    import ctypes as Cc
+    n = 1 << 22
+    net = pcl.SamplerNet(seed=1)
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, (n, 2)).astype(np.float32)
+    y = net.forward(x)   # warm-up, and the device buffers
+    flops_row = 2.0 * (2 * 128 + 2 * 128 * 128 + 128)
+    # device-resident timing: the handle's forward on its own buffers, events on its stream
+    reps = max(args.steps, 3)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        y = net.forward(x)
+    el = time.perf_counter() - t0
+    e2e = n * reps / el
+    # training rate
+    t = (np.sin(3 * x[:, 0]) * x[:, 1]).astype(np.float32)
+    steps = 400
+    t1 = time.perf_counter()
+    net.train(x[: 1 << 20], t[: 1 << 20], steps=steps, batch=8192, lr=1e-3, seed=0)
+    tr = time.perf_counter() - t1
+    line = {"metric": "learned-sampler network: inference rows/s through pcl_mlp_forward (host arrays)",
+            "value": e2e, "unit": "rows/s", "n_gpus": 1, "steps": reps, "warmup": 1,
+            "higher_is_better": True, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": "mlp-2x128x128x128x1", "rows": n, "train_batch": 8192},
+            "inference_tflops_incl_copies": e2e * flops_row / 1e12,
+            "training_steps_per_s": steps / tr, "training_rows_per_s": steps * 8192 / tr,
+            "gpu_launches": reps + 6 * steps}
+    print(json.dumps(line))
+    net.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -555,7 +592,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--steps-per-launch", type=int, default=1)
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
-    ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned", "plain", "reid"])
+    ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned", "plain", "reid", "mlp"])
     ap.add_argument("--nswarm", type=int, default=256)
     ap.add_argument("--tune-steps", type=int, default=480)
     args = ap.parse_args()
@@ -566,7 +603,8 @@ def main():
             args.warmup = 3
         import __graft_entry__ as graft
         graft.build()
-        fn = {"swarms": run_swarms, "learned": run_learned, "plain": run_plain, "reid": run_reid}[args.workload]
+        fn = {"swarms": run_swarms, "learned": run_learned, "plain": run_plain, "reid": run_reid,
+              "mlp": run_mlp}[args.workload]
         return fn(args, graft.load_package())
     if args.warmup < 3:
         args.warmup = 3
