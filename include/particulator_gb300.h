@@ -239,6 +239,31 @@ int pcl_set_linear_table(void* ctx, int species, int nproc, int n, double e0, do
  * cl_order = 0 disables continuum losses. */
 int pcl_set_forcing(void* ctx, const double E[3], const double B[3], int cl_order, int cl_k,
                     double cl_xmax, const double* cl_ec, const double* cl_pc);
+/* Position-dependent electric field replacing the homogeneous E of
+ * pcl_set_forcing (field.jl:10-52), SI: kind 0 homogeneous (no params),
+ * 1 DoubleLayerField {z1, z2, vx, vy, vz}, 2 StepField {z, v1x, v1y, v1z, v2x,
+ * v2y, v2z}, 3 ConfinedDoubleLayerField {sx, sy, sz, ez0}.  Evaluated at each
+ * RK2 stage's position (pusher.jl:41-63).  Batched swarms keep their own
+ * homogeneous fields. */
+int pcl_set_field(void* ctx, int kind, const double* params, int nparams);
+/* WallCallback{P}(coord, v, drop) (callback.jl:146-184): while advancing,
+ * a particle of `species` crossing the plane x[coord] = v (coord 0-2; -1
+ * removes the wall) in the +axis direction is recorded as lincomb(new, old, w)
+ * of its sub-step (electron.jl:127-132), which draws s like any state
+ * constructor, and is dropped if drop != 0.  Records go to a device buffer of
+ * `capacity`; pcl_get_wall copies them out (SI: x, p, w, t) and clears it
+ * (species == NULL: *n = pending records). */
+/* roulette! (population.jl:291-311): keep each live particle of `species`
+ * with probability pkeep (one draw from its stream), dividing its weight by
+ * pkeep, else remove it.  split! (population.jl:318-335): divide each live
+ * particle's weight by 1 + p and add Poisson(p) copies (one draw; copies get
+ * stream ids derived from the parent's).  As RouletteCallback / SplitCallback
+ * (callback.jl:210-247) do, follow with pcl_compact. */
+int pcl_roulette(void* ctx, int species, double pkeep);
+int pcl_split(void* ctx, int species, double p);
+int pcl_set_wall(void* ctx, int species, int coord, double v, int drop, int64_t capacity);
+int pcl_get_wall(void* ctx, int64_t* n, int32_t* species, uint64_t* sid, double* x, double* p, double* w,
+                 double* t);
 
 /* Batched form: nswarm (1..256) independent swarms share one context and every
  * launch; particle i belongs to swarm (sid >> 56) and its secondaries inherit

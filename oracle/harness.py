@@ -35,6 +35,12 @@ def lib():
                                     _P(C.c_int32), _P(C.c_int32), _P(_d), _P(C.c_int32)]
         L.orc_set_sb.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _P(_d), _P(_d)]
         L.orc_set_swarms.argtypes = [C.c_void_p, C.c_int, _P(_d), _P(_d), _P(_d)]
+        L.orc_set_field.argtypes = [C.c_void_p, C.c_int, _P(_d), C.c_int]
+        L.orc_set_wall.argtypes = [C.c_void_p, C.c_int, C.c_int, _d, C.c_int]
+        L.orc_roulette.argtypes = [C.c_void_p, C.c_int, _d]
+        L.orc_split.argtypes = [C.c_void_p, C.c_int, _d]
+        L.orc_get_wall.argtypes = [C.c_void_p, _P(C.c_int32), _P(C.c_uint64), _P(_d), _P(_d), _P(_d), _P(_d)]
+        L.orc_get_wall.restype = C.c_int64
         L.orc_set_linear_table.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _d, _d, _P(_d), _P(_d),
                                            _P(C.c_int32), _P(_d)]
         L.orc_set_forcing.argtypes = [C.c_void_p, _P(_d), _P(_d), C.c_int, C.c_int, _d, _P(_d), _P(_d)]
@@ -128,6 +134,10 @@ class OracleWorld:
         else:
             self._keep += [cl.ec, cl.pc]
             L.orc_set_forcing(self.h, _p(E), _p(B), cl.n, cl.bints.k, cl.bints.xmax, _p(cl.ec), _p(cl.pc))
+        kind, fparams = pusher.device_efield()
+        fp = np.ascontiguousarray(np.asarray(fparams, dtype=float)) if fparams else np.zeros(1)
+        self._keep.append(fp)
+        L.orc_set_field(self.h, int(kind), _p(fp), len(fparams))
 
     def set_swarms(self, tabs, E, Fdt, safety=1.15):
         """Swarm mode: per-swarm field E [n,3] (V/m) and the rate bound of the
@@ -145,6 +155,25 @@ class OracleWorld:
             rbs[sp] = np.ascontiguousarray(np.concatenate([A + f * B for f in Fdt]))
         self._keep += [E, rbs[0], rbs[2]]
         lib().orc_set_swarms(self.h, len(Fdt), _p(E), _p(rbs[0]), _p(rbs[2]))
+
+    def roulette(self, sp, pkeep):
+        lib().orc_roulette(self.h, int(sp), float(pkeep))
+
+    def split(self, sp, p):
+        lib().orc_split(self.h, int(sp), float(p))
+
+    def set_wall(self, sp, coord0, v, drop=True):
+        lib().orc_set_wall(self.h, int(sp), int(coord0), float(v), 1 if drop else 0)
+
+    def get_wall(self):
+        """(species, sid, x, p, w, t) of every crossing recorded so far."""
+        L = lib()
+        n = L.orc_get_wall(self.h, None, None, None, None, None, None)
+        sp = np.zeros(n, np.int32); sid = np.zeros(n, np.uint64)
+        x = np.zeros((n, 3)); p = np.zeros((n, 3)); w = np.zeros(n); t = np.zeros(n)
+        if n:
+            L.orc_get_wall(self.h, _p(sp, C.c_int32), _p(sid, C.c_uint64), _p(x), _p(p), _p(w), _p(t))
+        return sp, sid, x, p, w, t
 
     def upload(self, sp, a):
         n = len(a.w)
@@ -208,10 +237,11 @@ def philox(ctr, key):
     return list(o)
 
 
-def compare_populations(gpu, orc, species, rtol=1e-5, xtol=None, max_unmatched_frac=0.01, stol=None):
+def compare_populations(gpu, orc, species, rtol=1e-5, xtol=None, max_unmatched_frac=0.01, stol=None, max_bad=0):
     """Match GPU and oracle particles by stream id.  Oracle particles not in a
-    tie lineage must exist on the GPU with the same draw counter, and
-    momenta / s / positions within tolerance.  Returns a report dict."""
+    tie lineage must exist on the GPU with the same draw counter (up to
+    `max_bad` exceptions), and momenta / s / positions within tolerance.
+    Returns a report dict."""
     rep = {"species": int(species), "n_gpu": len(gpu.w), "n_orc": len(orc.w), "ties": int(orc.tie.sum())}
     og = {int(s): i for i, s in enumerate(np.asarray(gpu.sid, dtype=np.uint64))}
     clean = np.nonzero(orc.tie == 0)[0]
@@ -243,13 +273,15 @@ def compare_populations(gpu, orc, species, rtol=1e-5, xtol=None, max_unmatched_f
         dx = np.linalg.norm(gpu.x[ig] - orc.x[io], axis=1)
         scale = xtol if xtol is not None else max(1e-6, float(np.linalg.norm(orc.x[io], axis=1).max()))
         rep["max_dx_rel"] = float(dx.max() / scale)
-        rep["w_equal"] = bool(np.array_equal(gpu.w[ig], orc.w[io]))
+        # weights are 1 unless roulette / split rescaled them (FP32 on the device)
+        rep["w_equal"] = bool(np.allclose(gpu.w[ig], orc.w[io], rtol=1e-6, atol=0.0))
     else:
         rep.update(max_dp_rel=0.0, max_ds=0.0, max_dx_rel=0.0, w_equal=True)
     extra = len(gpu.w) - len(ig)
     rep["gpu_unmatched"] = int(extra)
     tie_budget = int(orc.tie.sum()) + max(2, int(max_unmatched_frac * max(1, len(orc.w))))
     stol = 2 * rtol if stol is None else stol
-    rep["ok"] = (missing == 0 and bad_ctr == 0 and rep["max_dp_rel"] <= rtol and rep["max_ds"] <= stol
+    rep["ok"] = (missing <= max_bad and bad_ctr + missing <= max_bad and rep["max_dp_rel"] <= rtol
+                 and rep["max_ds"] <= stol
                  and rep["max_dx_rel"] <= 10 * rtol and rep["w_equal"] and extra <= tie_budget)
     return rep

@@ -50,6 +50,7 @@
 #include <cstdint>
 #include <cstring>
 #include <vector>
+#include <mutex>
 #include <thread>
 #include <algorithm>
 #include <limits>
@@ -143,6 +144,9 @@ struct Species {
     bool set = false;
     double cut = std::numeric_limits<double>::infinity();
     bool tally_only = false;
+    int wall_coord = -1;        // WallCallback (callback.jl:146-184): axis, position, drop
+    double wall_v = 0.0;
+    bool wall_drop = true;
     Table tab;
     std::vector<Part> parts;
 };
@@ -172,6 +176,14 @@ struct World {
     double tie_tol = 2e-5;
     Species sp[3];
     double E[3] = {0, 0, 0}, B[3] = {0, 0, 0};
+    // position-dependent E (field.jl:10-52): 0 homogeneous, 1 double layer
+    // {z1, z2, v[3]}, 2 step {z, v1[3], v2[3]}, 3 confined double layer {sx, sy, sz, ez0}
+    int field_kind = 0;
+    double fp[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // wall crossings: {species, sid, x[3], p[3], w, t}
+    struct WallRec { int species; uint64_t sid; double x[3], p[3], w, t; };
+    mutable std::vector<WallRec> wall;   // appended by walkers (which see a const World)
+    mutable std::mutex wall_mu;
     // swarm mode: swarm = top 8 bits of the stream id; per-swarm field and rate bound
     int nswarm = 0;
     std::vector<double> swarm_E;          // [nswarm][3]
@@ -314,14 +326,49 @@ static inline void velocity(int species, const double* p, double* v) {
 
 // force(CombinedForcing(ElectromagneticField, ChebContinuumLoss), s)
 // (pusher.jl:14-23, field.jl:54-70, continuum.jl:45-57)
-static void force(Walker& Wk, int species, const double* p, double* f) {
+// E at position r (field.jl:4-52).  The double-layer and step fields jump at
+// their planes: a stage position within the tie tolerance of one is a tie.
+static void efield(Walker& Wk, const World& W, const double* r, double* Eo) {
+    const double* fp = W.fp;
+    switch (W.field_kind) {
+        case 1: {  // DoubleLayerField: v between z1 and z2, else 0
+            const double sc = std::max(std::fabs(fp[1] - fp[0]), 1e-9);
+            Wk.near(r[2], fp[0], sc);
+            Wk.near(r[2], fp[1], sc);
+            bool in = fp[0] < r[2] && r[2] < fp[1];
+            for (int a = 0; a < 3; ++a) Eo[a] = in ? fp[2 + a] : 0.0;
+            break;
+        }
+        case 2: {  // StepField: v1 below z, v2 above
+            Wk.near(r[2], fp[0], std::max(std::fabs(fp[0]), 1e-3));
+            bool below = r[2] < fp[0];
+            for (int a = 0; a < 3; ++a) Eo[a] = below ? fp[1 + a] : fp[4 + a];
+            break;
+        }
+        case 3: {  // ConfinedDoubleLayerField
+            double sx = fp[0], sy = fp[1], sz = fp[2], ez0 = fp[3];
+            double g = ez0 * std::exp(-(r[0] * r[0] / (2 * sx * sx) + r[1] * r[1] / (2 * sy * sy) +
+                                        r[2] * r[2] / (2 * sz * sz)));
+            Eo[0] = -(g * r[0] * r[2]) / (sx * sx);
+            Eo[1] = -(g * r[1] * r[2]) / (sy * sy);
+            Eo[2] = g - (g * r[2] * r[2]) / (sz * sz);
+            break;
+        }
+        default:
+            for (int a = 0; a < 3; ++a) Eo[a] = W.E[a];
+    }
+}
+
+static void force(Walker& Wk, int species, const double* p, double* f, const double* r) {
     f[0] = f[1] = f[2] = 0.0;
     if (species == PHOTON) return;
     const World& W = *Wk.W;
     double v[3];
     velocity(species, p, v);
     double q = (species == ELECTRON ? -1.0 : 1.0) * e;
-    const double* Ef = W.E;
+    double Eloc[3];
+    efield(Wk, W, r, Eloc);
+    const double* Ef = Eloc;
     if (W.nswarm > 0) Ef = W.swarm_E.data() + 3 * size_t(std::min(int(Wk.P->sid >> 56), W.nswarm - 1));
     f[0] = q * (Ef[0] + (v[1] * W.B[2] - v[2] * W.B[1]));
     f[1] = q * (Ef[1] + (v[2] * W.B[0] - v[0] * W.B[2]));
@@ -347,11 +394,15 @@ static void force(Walker& Wk, int species, const double* p, double* f) {
 static void advance_particle(Walker& Wk, int species, double dt) {
     Part& y = *Wk.P;
     double v1[3], f1[3], v2[3], f2[3], p2[3];
+    double x2[3];
     velocity(species, y.p, v1);
-    force(Wk, species, y.p, f1);
-    for (int a = 0; a < 3; ++a) p2[a] = y.p[a] + 2 * dt * f1[a] / 3;
+    force(Wk, species, y.p, f1, y.x);
+    for (int a = 0; a < 3; ++a) {
+        p2[a] = y.p[a] + 2 * dt * f1[a] / 3;
+        x2[a] = y.x[a] + 2 * dt * v1[a] / 3;
+    }
     velocity(species, p2, v2);
-    force(Wk, species, p2, f2);
+    force(Wk, species, p2, f2, x2);
     for (int a = 0; a < 3; ++a) {
         y.x[a] = y.x[a] + dt * (v1[a] / 4 + 3 * v2[a] / 4);
         y.p[a] = y.p[a] + dt * (f1[a] / 4 + 3 * f2[a] / 4);
@@ -895,7 +946,37 @@ static void advance_one(Walker& Wk, int species, double tfinal, SpawnBuf& out) {
         if (std::isfinite(tnext)) Wk.near(trem, tnext, std::max(trem, tnext));
         if (trem > tnext) { dt = tnext; collides = true; }
         else { dt = trem; collides = false; L.s -= dt * L.r; }
+        const Species& Sp = Wk.W->sp[species];
+        double xo[3], po[3], to = L.t;
+        if (Sp.wall_coord >= 0) { std::memcpy(xo, L.x, sizeof(xo)); std::memcpy(po, L.p, sizeof(po)); }
         advance_particle(Wk, species, dt);
+        if (Sp.wall_coord >= 0) {
+            // onadvance(WallCallback) (callback.jl:167-184): a crossing in the +axis
+            // direction records lincomb(new, old, w) (electron.jl:127-132; its
+            // constructor draws s) and drops the particle if asked to
+            const int q = Sp.wall_coord;
+            const double v = Sp.wall_v;
+            Wk.near(L.x[q], v, std::fabs(L.x[q] - xo[q]) + std::fabs(v));
+            Wk.near(xo[q], v, std::fabs(L.x[q] - xo[q]) + std::fabs(v));
+            if (xo[q] < v && v < L.x[q]) {
+                const double w = (v - xo[q]) / (L.x[q] - xo[q]);
+                World::WallRec r;
+                r.species = species;
+                r.sid = L.sid;
+                for (int a = 0; a < 3; ++a) {
+                    r.x[a] = L.x[a] * w + xo[a] * (1 - w);
+                    r.p[a] = L.p[a] * w + po[a] * (1 - w);
+                }
+                r.w = L.w;
+                r.t = L.t * w + to * (1 - w);
+                (void)Wk.rand();
+                {
+                    std::lock_guard<std::mutex> g(Wk.W->wall_mu);
+                    Wk.W->wall.push_back(r);
+                }
+                if (Sp.wall_drop) L.active = false;
+            }
+        }
         if (collides && L.active) do_one_collision(Wk, species, out);
         trem -= dt;
     }
@@ -1056,6 +1137,90 @@ int orc_set_sb(void* w, int species, int j, int ne, int ncum, const double* log_
     T.procs[j].le.assign(log_energy, log_energy + ne);
     T.procs[j].data.assign(data, data + size_t(ne) * ncum);
     T.procs[j].ncum = ncum;
+    return 0;
+}
+
+// roulette! / split! (population.jl:291-335) on the particles of a species,
+// draws as the device takes them: one from the particle's stream each; split
+// copies take stream ids from Philox block (ctr, sid, 2 + j/2) of the parent.
+static uint32_t stream_word(const World& W, uint32_t ctr, uint64_t sid) {
+    uint32_t a = ctr >> 2, b = uint32_t(sid), c2 = uint32_t(sid >> 32), d = 0;
+    philox(a, b, c2, d, W.k0, W.k1);
+    const uint32_t q[4] = {a, b, c2, d};
+    return q[ctr & 3u];
+}
+
+int orc_roulette(void* w, int species, double pkeep) {
+    World* W = static_cast<World*>(w);
+    for (Part& P : W->sp[species].parts) {
+        if (!P.active) continue;
+        const uint32_t v = stream_word(*W, P.ctr, P.sid);
+        const double u = double(((v >> 9) << 1) | 1u) * 5.9604644775390625e-8;
+        P.ctr += 1;
+        if (u < pkeep) P.w /= pkeep;
+        else P.active = false;
+    }
+    auto& v = W->sp[species].parts;
+    v.erase(std::remove_if(v.begin(), v.end(), [](const Part& q) { return !q.active; }), v.end());
+    return 0;
+}
+
+int orc_split(void* w, int species, double p) {
+    World* W = static_cast<World*>(w);
+    auto& v = W->sp[species].parts;
+    const size_t n0 = v.size();
+    const float pf = float(p);
+    for (size_t i = 0; i < n0; ++i) {
+        if (!v[i].active) continue;
+        v[i].w /= (1.0 + p);
+        const uint32_t word = stream_word(*W, v[i].ctr, v[i].sid);
+        const uint32_t ctr0 = v[i].ctr;
+        v[i].ctr += 1;
+        const float u = float(double(((word >> 9) << 1) | 1u) * 5.9604644775390625e-8);
+        // Poisson(p) by inversion, in FP32 as the device does it
+        int k = 0;
+        float P = std::exp(-pf), F = P;
+        while (u > F && k < 1024) { ++k; P *= pf / float(k); F += P; }
+        for (int j = 0; j < k; ++j) {
+            uint32_t a = ctr0, b = uint32_t(v[i].sid), c2 = uint32_t(v[i].sid >> 32), d = 2u + uint32_t(j >> 1);
+            philox(a, b, c2, d, W->k0, W->k1);
+            Part q = v[i];
+            q.sid = (j & 1) ? (uint64_t(c2) | (uint64_t(d) << 32)) : (uint64_t(a) | (uint64_t(b) << 32));
+            q.ctr = 0;
+            v.push_back(q);
+        }
+    }
+    return 0;
+}
+
+int orc_set_wall(void* w, int species, int coord, double v, int drop) {
+    World* W = static_cast<World*>(w);
+    W->sp[species].wall_coord = coord;
+    W->sp[species].wall_v = v;
+    W->sp[species].wall_drop = drop != 0;
+    return 0;
+}
+
+// wall records so far: species, sid, x[3n], p[3n], w, t; returns the count
+// (arrays may be NULL to query it)
+int64_t orc_get_wall(void* w, int32_t* species, uint64_t* sid, double* x, double* p, double* wt, double* t) {
+    World* W = static_cast<World*>(w);
+    const size_t n = W->wall.size();
+    if (species) {
+        for (size_t i = 0; i < n; ++i) {
+            const World::WallRec& r = W->wall[i];
+            species[i] = r.species; sid[i] = r.sid; wt[i] = r.w; t[i] = r.t;
+            for (int a = 0; a < 3; ++a) { x[3 * i + a] = r.x[a]; p[3 * i + a] = r.p[a]; }
+        }
+    }
+    return int64_t(n);
+}
+
+// position-dependent E (SI): kind 1 {z1, z2, vx, vy, vz}, 2 {z, v1[3], v2[3]}, 3 {sx, sy, sz, ez0}
+int orc_set_field(void* w, int kind, const double* params, int n) {
+    World* W = static_cast<World*>(w);
+    W->field_kind = kind;
+    for (int i = 0; i < 8; ++i) W->fp[i] = (i < n) ? params[i] : 0.0;
     return 0;
 }
 

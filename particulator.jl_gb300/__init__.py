@@ -13,11 +13,13 @@ from .processes import (Moller, RBEB, SeltzerBerger, RelativisticCoulomb, Compto
 from .tables import (Electron, Photon, Positron, BinaryIntervals, ChebyshevCollisionTable,
                      collision_table_from_processes, ContinuumLoss, ChebContinuumLoss, speed,
                      momentum_norm_from_kin, precheb, CollisionTable, lxcat_table, ratebound_split)
-from .forcing import (HomogeneousField, ElectromagneticField, NullForcing, CombinedForcing, RK2Pusher)
+from .forcing import (HomogeneousField, DoubleLayerField, StepField, ConfinedDoubleLayerField, ElectromagneticField,
+                      NullForcing, CombinedForcing, RK2Pusher)
 from .population import (ElectronState, PhotonState, PositronState, ParticleArrays, Population, MultiPopulation,
                          init, advance, run, nparticles, nactives, weight, meanenergy, maxenergy, spread, posvar,
                          repack, droplow, kinenergy, AbstractCallback, VoidCallback, CombinedCallback,
-                         CollisionCounter, PopulationTargetCallback, ParticleCountCallback)
+                         CollisionCounter, PopulationTargetCallback, ParticleCountCallback, WallCallback,
+                         RouletteCallback, SplitCallback)
 from . import workloads, learned
 from .learned import SamplerNet
 

@@ -21,6 +21,10 @@ cudaError_t prepare_step(int minb, size_t smem);
 __global__ void k_learn_hist(StepArgs A, int species, int j, int kind, int nT, long long per_T, int nbins,
                              float hmin, float hmax, unsigned long long sid_base, unsigned int* hist);
 __global__ void k_learn_x(const float4* ps, const float4* m2, long long n, float* X);
+__global__ void k_roulette(float4* xw, uint4* meta, long long n, float pkeep, uint32_t k0, uint32_t k1,
+                           unsigned long long* dead);
+__global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, uint32_t k0,
+                        uint32_t k1, unsigned long long* nslots, unsigned long long* lost);
 __global__ void k_learn_pick(const float4* m2, long long n, const float* Yk, long long stride, LearnPick which,
                              float* Y);
 namespace mlp {
@@ -69,6 +73,9 @@ struct SpeciesState {
     int order = 1, nproc = 0, nint = 1;
     double xmax = 1.0;
     std::vector<double> rate, rb;
+    int wall_coord = -1;
+    double wall_v = 0.0;
+    int wall_drop = 1;
     std::vector<pcl_process> procs;
     std::vector<int> sb_index;
     // linear-grid table (table_kind 1)
@@ -99,6 +106,8 @@ struct Ctx {
     std::vector<SBTable> sb;
     // forcing
     double E[3] = {0, 0, 0}, B[3] = {0, 0, 0};
+    int field_kind = 0;
+    double field_p[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // SI
     int cl_order = 0, cl_k = 0;
     double cl_xmax = 0;
     std::vector<double> cl_ec, cl_pc;
@@ -148,6 +157,11 @@ struct Ctx {
     unsigned long long* d_lqn = nullptr;  // [2]
     long long lq_cap = 0, lq_nets_cap = 0;
     long long learn_rounds = 0, learn_suspended = 0;
+    // WallCallback records (device) and the context time at each launch start
+    float4* d_wall_xw = nullptr; float4* d_wall_pt = nullptr; uint4* d_wall_meta = nullptr;
+    unsigned long long* d_wall_n = nullptr;
+    long long wall_cap = 0;
+    std::vector<double> launch_t0 = std::vector<double>(1, 0.0);   // index = device launch_seq
     // CUDA graphs of launch groups (use_graph), keyed by every launch parameter
     struct GraphEntry { std::vector<unsigned char> key; cudaGraphExec_t exec; };
     std::vector<GraphEntry> graphs;
@@ -298,6 +312,9 @@ static int build_blob(Ctx* c) {
         h.cut = S.set ? float(S.cut / mc2) : INFINITY;
         h.charge = charge[s];
         h.table_kind = S.table_kind;
+        h.wall_coord = (S.wall_coord >= 0 && c->wall_cap > 0) ? S.wall_coord : -1;
+        h.wall_v = float(S.wall_v);
+        h.wall_drop = S.wall_drop;
         if (S.table_kind == 1) {
             h.lin_n = S.lin_n;
             h.lin_e0 = float(S.lin_e0 / mc2);
@@ -372,6 +389,23 @@ static int build_blob(Ctx* c) {
         H.E[a] = float(force_to_dev(e * c->E[a]));            // per unit charge
         H.B[a] = float(e * c->B[a] / m_e * NS);
     }
+    H.field_kind = c->field_kind;
+    {
+        const double* q = c->field_p;
+        auto fe = [&](double v) { return float(force_to_dev(e * v)); };
+        switch (c->field_kind) {
+            case 1: H.fp[0] = float(q[0]); H.fp[1] = float(q[1]);
+                    for (int a = 0; a < 3; ++a) H.fp[2 + a] = fe(q[2 + a]);
+                    break;
+            case 2: H.fp[0] = float(q[0]);
+                    for (int a = 0; a < 6; ++a) H.fp[1 + a] = fe(q[1 + a]);
+                    break;
+            case 3: for (int a = 0; a < 3; ++a) H.fp[a] = float(q[a]);
+                    H.fp[3] = fe(q[3]);
+                    break;
+            default: break;
+        }
+    }
     H.nswarm = c->nswarm;
     H.swarm_off = off();
     if (c->nswarm > 0) {
@@ -428,6 +462,8 @@ static StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, int sp_
     A.nsteps = nsteps;
     A.spill_mode = spill_mode;
     A.blob_bytes = int(c->blob.size());
+    A.wall_xw = c->d_wall_xw; A.wall_pt = c->d_wall_pt; A.wall_meta = c->d_wall_meta;
+    A.wall_n = c->d_wall_n; A.wall_cap = c->wall_cap;
     if (c->learn_on) {  // suspended collisions go to queue 0 unless set_lq says otherwise
         A.lq_out_xw = c->lq_xw[0]; A.lq_out_ps = c->lq_ps[0]; A.lq_out_m1 = c->lq_m1[0]; A.lq_out_m2 = c->lq_m2[0];
         A.lq_out_n = c->d_lqn;
@@ -694,6 +730,7 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
     const bool graph = c->cfg.use_graph != 0;
     bool compacted = false, host_passes = false;
     StepArgs A = make_args(c, dt, nsteps, 0, 0);
+    c->launch_t0.push_back(c->t);   // k_begin advances the device launch counter to match
     unsigned long long pending0 = 0;
     if (graph) {
         const bool due = c->steps_since_compact + nsteps >= period;
@@ -819,6 +856,7 @@ void pcl_destroy(void* ctx) {
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
     if (c->h_spn) cudaFreeHost(c->h_spn);
     free_lq(c);
+    cudaFree(c->d_wall_xw); cudaFree(c->d_wall_pt); cudaFree(c->d_wall_meta); cudaFree(c->d_wall_n);
     for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
     for (cudaEvent_t ev : {c->ev_k0, c->ev_k1, c->ev_t0, c->ev_t1})
         if (ev) cudaEventDestroy(ev);
@@ -955,6 +993,136 @@ int pcl_set_forcing(void* ctx, const double E[3], const double B[3], int cl_orde
     }
     c->blob_dirty = true;
     return PCL_OK;
+}
+
+int pcl_set_field(void* ctx, int kind, const double* params, int nparams) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    static const int need[4] = {0, 5, 7, 4};
+    if (kind < 0 || kind > 3 || nparams < need[kind] || (need[kind] > 0 && !params))
+        return fail(c, PCL_ERR_INVALID, "field kind or parameters");
+    if (kind == 3 && !(params[0] > 0 && params[1] > 0 && params[2] > 0))
+        return fail(c, PCL_ERR_INVALID, "confined double layer widths must be > 0");
+    c->field_kind = kind;
+    for (int i = 0; i < 8; ++i) c->field_p[i] = (i < need[kind]) ? params[i] : 0.0;
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
+static int get_n(Ctx* c, int species, long long& n);
+
+int pcl_roulette(void* ctx, int species, double pkeep) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (!(pkeep > 0.0 && pkeep <= 1.0)) return fail(c, PCL_ERR_INVALID, "keep probability must be in (0, 1]");
+    CK(cudaSetDevice(c->device));
+    SpeciesState& S = c->sp[species];
+    long long n = 0;
+    if (S.cap <= 0 || (rc = get_n(c, species, n)) || n == 0) return rc;
+    unsigned long long* killed = nullptr;
+    CK(cudaMallocAsync(&killed, sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(killed, 0, sizeof(unsigned long long), c->stream));
+    const int grid = int(std::min<long long>((n + 255) / 256, 8ll * c->sm_count));
+    k_roulette<<<grid, 256, 0, c->stream>>>(S.xw[S.cur], S.meta[S.cur], n, float(pkeep), uint32_t(c->cfg.seed),
+                                            uint32_t(c->cfg.seed >> 32), killed);
+    CK(cudaGetLastError());
+    unsigned long long hk = 0;
+    CK(cudaMemcpyAsync(&hk, killed, sizeof(hk), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaFreeAsync(killed, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->live[species] = std::max<long long>(0, c->live[species] - (long long)hk);
+    return PCL_OK;
+}
+
+int pcl_split(void* ctx, int species, double p) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (!(p >= 0.0 && p <= 64.0)) return fail(c, PCL_ERR_INVALID, "mean number of copies must be in [0, 64]");
+    CK(cudaSetDevice(c->device));
+    SpeciesState& S = c->sp[species];
+    long long n = 0;
+    if (S.cap <= 0 || (rc = get_n(c, species, n)) || n == 0) return rc;
+    unsigned long long* lost = nullptr;
+    CK(cudaMallocAsync(&lost, sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(lost, 0, sizeof(unsigned long long), c->stream));
+    const int grid = int(std::min<long long>((n + 255) / 256, 8ll * c->sm_count));
+    k_split<<<grid, 256, 0, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], n, S.cap, float(p),
+                                         uint32_t(c->cfg.seed), uint32_t(c->cfg.seed >> 32), &c->d_ctl->n[species],
+                                         lost);
+    CK(cudaGetLastError());
+    unsigned long long hl = 0;
+    CK(cudaMemcpyAsync(&hl, lost, sizeof(hl), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaFreeAsync(lost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    long long nn = 0;
+    if ((rc = get_n(c, species, nn))) return rc;
+    c->live[species] += nn - n;
+    if (hl) return fail(c, PCL_ERR_CAPACITY, "split copies beyond the population capacity were lost");
+    return PCL_OK;
+}
+
+int pcl_set_wall(void* ctx, int species, int coord, double v, int drop, int64_t capacity) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (coord < -1 || coord > 2 || capacity < 0 || capacity > (1ll << 30))
+        return fail(c, PCL_ERR_INVALID, "wall axis or capacity");
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    SpeciesState& S = c->sp[species];
+    S.wall_coord = coord;
+    S.wall_v = v;
+    S.wall_drop = drop ? 1 : 0;
+    if (coord >= 0 && capacity > c->wall_cap) {
+        cudaFree(c->d_wall_xw); cudaFree(c->d_wall_pt); cudaFree(c->d_wall_meta); cudaFree(c->d_wall_n);
+        c->d_wall_xw = c->d_wall_pt = nullptr; c->d_wall_meta = nullptr; c->d_wall_n = nullptr; c->wall_cap = 0;
+        CK(cudaMalloc(&c->d_wall_xw, sizeof(float4) * capacity));
+        CK(cudaMalloc(&c->d_wall_pt, sizeof(float4) * capacity));
+        CK(cudaMalloc(&c->d_wall_meta, sizeof(uint4) * capacity));
+        CK(cudaMalloc(&c->d_wall_n, sizeof(unsigned long long)));
+        CK(cudaMemset(c->d_wall_n, 0, sizeof(unsigned long long)));
+        c->wall_cap = capacity;
+    }
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
+int pcl_get_wall(void* ctx, int64_t* n, int32_t* species, uint64_t* sid, double* x, double* p, double* w, double* t) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !n) return PCL_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    if (!c->d_wall_n) { *n = 0; return PCL_OK; }
+    unsigned long long cnt = 0;
+    CK(d2h(c, &cnt, c->d_wall_n, sizeof(cnt)));
+    const long long m = std::min<long long>((long long)cnt, c->wall_cap);
+    if (!species) { *n = m; return PCL_OK; }   // query
+    if (*n < m) { *n = m; return fail(c, PCL_ERR_INVALID, "output arrays too short for the wall records"); }
+    std::vector<float4> xw(m), pt(m);
+    std::vector<uint4> meta(m);
+    if (m > 0) {
+        CK(d2h(c, xw.data(), c->d_wall_xw, sizeof(float4) * m));
+        CK(d2h(c, pt.data(), c->d_wall_pt, sizeof(float4) * m));
+        CK(d2h(c, meta.data(), c->d_wall_meta, sizeof(uint4) * m));
+    }
+    for (long long i = 0; i < m; ++i) {
+        species[i] = int32_t(meta[i].z);
+        sid[i] = uint64_t(meta[i].x) | (uint64_t(meta[i].y) << 32);
+        x[3 * i] = xw[i].x; x[3 * i + 1] = xw[i].y; x[3 * i + 2] = xw[i].z;
+        w[i] = xw[i].w;
+        p[3 * i] = p_to_si(pt[i].x); p[3 * i + 1] = p_to_si(pt[i].y); p[3 * i + 2] = p_to_si(pt[i].z);
+        const size_t li = std::min<size_t>(meta[i].w, c->launch_t0.size() - 1);
+        t[i] = c->launch_t0[li] + double(pt[i].w) * NS;
+    }
+    *n = m;
+    const unsigned long long zero = 0;
+    CK(h2d(c, c->d_wall_n, &zero, sizeof(zero)));
+    return (long long)cnt > c->wall_cap ? fail(c, PCL_ERR_CAPACITY, "wall records beyond capacity were lost")
+                                         : PCL_OK;
 }
 
 static int get_n(Ctx* c, int species, long long& n) {

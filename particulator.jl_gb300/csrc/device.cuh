@@ -55,6 +55,10 @@ struct SpeciesHdr {
     int32_t lin_n;        // linear grid: points
     float   lin_e0;       // linear grid: first energy (m_e c^2)
     float   lin_inv_step; // linear grid: 1 / step
+    int32_t wall_coord;   // WallCallback (callback.jl:146-184): axis 0-2, -1 = none
+    float   wall_v;       // wall position (m)
+    int32_t wall_drop;    // drop the particle once recorded
+    int32_t pad_w;
     DevProc proc[16];
 };
 
@@ -75,6 +79,12 @@ struct BlobHdr {
     int32_t bytes;     // total blob size (multiple of 16)
     int32_t nswarm;    // swarm mode: swarms batched in this context (0: classic single population)
     int32_t swarm_off; // float offset of [nswarm][4] = {E field (device units), Fdt (N s)}
+    // position-dependent E (field.jl:10-52), lengths in m, fields in the units of E:
+    // 0 homogeneous (E), 1 double layer {z1, z2, v[3]}, 2 step {z, v1[3], v2[3]},
+    // 3 confined double layer {sx, sy, sz, ez0}
+    int32_t field_kind;
+    int32_t pad_f;
+    float   fp[8];
 };
 
 // Device-side counters of one context (global memory, zeroed per launch
@@ -95,7 +105,7 @@ struct Control {
     unsigned long long live_start[PCL_MAX_STEPS_PER_LAUNCH];   // particle-steps of step k
     unsigned long long dead[3];       // slots marked dead by this launch
     int                timeout;
-    int                pad;
+    unsigned int       launch_seq;    // launch groups so far (k_begin), tags wall records
 };
 
 // Arguments of the step kernel (passed by value).
@@ -130,6 +140,11 @@ struct StepArgs {
     const float* lq_in_y;
     const unsigned long long* lq_in_n;
     long long lq_cap;
+    // wall crossings: {x, y, z, w}, {px, py, pz, t (ns since the launch start)},
+    // {sid_lo, sid_hi, species, launch index}
+    float4* wall_xw; float4* wall_pt; uint4* wall_meta;
+    unsigned long long* wall_n;
+    long long wall_cap;
 };
 
 // Network index of each (species, table position) with a learned sampler (-1: none).

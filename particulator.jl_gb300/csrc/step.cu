@@ -259,20 +259,57 @@ __device__ __forceinline__ float cl_mag(const SpeciesHdr& S, const KCtx& K, floa
     return cheb_dot(K.blob + S.cl_off + i * S.cl_order, t, S.cl_order);
 }
 
+// E at position (x, y, z) (field.jl:4-52); a batched swarm's own field wins.
+__device__ __forceinline__ void efield(const KCtx& K, int sw, float x, float y, float z, float& ex, float& ey,
+                                       float& ez) {
+    const BlobHdr* H = K.H;
+    if (H->nswarm > 0) {
+        const float* E = K.blob + H->swarm_off + 4 * sw;
+        ex = E[0]; ey = E[1]; ez = E[2];
+        return;
+    }
+    const float* f = H->fp;
+    switch (H->field_kind) {
+        case 1: {  // DoubleLayerField
+            const bool in = f[0] < z && z < f[1];
+            ex = in ? f[2] : 0.0f; ey = in ? f[3] : 0.0f; ez = in ? f[4] : 0.0f;
+            break;
+        }
+        case 2: {  // StepField
+            const bool below = z < f[0];
+            ex = below ? f[1] : f[4]; ey = below ? f[2] : f[5]; ez = below ? f[3] : f[6];
+            break;
+        }
+        case 3: {  // ConfinedDoubleLayerField
+            const float sx = f[0], sy = f[1], sz = f[2];
+            const float g = f[3] * expf(-(x * x / (2.0f * sx * sx) + y * y / (2.0f * sy * sy) +
+                                          z * z / (2.0f * sz * sz)));
+            ex = -(g * x * z) / (sx * sx);
+            ey = -(g * y * z) / (sy * sy);
+            ez = g - (g * z * z) / (sz * sz);
+            break;
+        }
+        default:
+            ex = H->E[0]; ey = H->E[1]; ez = H->E[2];
+    }
+}
+
 // force(CombinedForcing(ElectromagneticField, ChebContinuumLoss), lepton)
-// (pusher.jl:14-23, field.jl:54-70, continuum.jl:45-57).  Returns beta too.
-__device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K, int sw, float px, float py,
-                                             float pz, float& bx, float& by, float& bz, float& fx,
-                                             float& fy, float& fz) {
+// (pusher.jl:14-23, field.jl:54-70, continuum.jl:45-57) at position (x, y, z).
+// Returns beta too.
+__device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K, int sw, float x, float y, float z,
+                                             float px, float py, float pz, float& bx, float& by, float& bz,
+                                             float& fx, float& fy, float& fz) {
     float p2 = px * px + py * py + pz * pz;
     float ig = rsqrtf(1.0f + p2);   // 1 / gamma
     bx = px * ig; by = py * ig; bz = pz * ig;
     const float q = S.charge;
-    const float* E = (K.H->nswarm > 0) ? K.blob + K.H->swarm_off + 4 * sw : K.H->E;
+    float ex, ey, ez;
+    efield(K, sw, x, y, z, ex, ey, ez);
     const float* B = K.H->B;
-    fx = q * (E[0] + (by * B[2] - bz * B[1]));
-    fy = q * (E[1] + (bz * B[0] - bx * B[2]));
-    fz = q * (E[2] + (bx * B[1] - by * B[0]));
+    fx = q * (ex + (by * B[2] - bz * B[1]));
+    fy = q * (ey + (bz * B[0] - bx * B[2]));
+    fz = q * (ez + (bx * B[1] - by * B[0]));
     float f = cl_mag(S, K, __fdividef(p2 * ig, 1.0f + ig));
     if (f != 0.0f && p2 > 0.0f) {
         float c = f * rsqrtf(p2);
@@ -289,11 +326,14 @@ __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K
         return;
     }
     float b1x, b1y, b1z, f1x, f1y, f1z;
-    lepton_force(S, K, L.sw, L.px, L.py, L.pz, b1x, b1y, b1z, f1x, f1y, f1z);
+    lepton_force(S, K, L.sw, L.x, L.y, L.z, L.px, L.py, L.pz, b1x, b1y, b1z, f1x, f1y, f1z);
     const float h23 = h * (2.0f / 3.0f);
     float qx = L.px + h23 * f1x, qy = L.py + h23 * f1y, qz = L.pz + h23 * f1z;
+    // second stage at x + 2 dt v1 / 3 (only a position-dependent field reads it)
+    const float c23 = (K.H->field_kind != 0) ? h23 * kCns : 0.0f;
     float b2x, b2y, b2z, f2x, f2y, f2z;
-    lepton_force(S, K, L.sw, qx, qy, qz, b2x, b2y, b2z, f2x, f2y, f2z);
+    lepton_force(S, K, L.sw, L.x + c23 * b1x, L.y + c23 * b1y, L.z + c23 * b1z, qx, qy, qz, b2x, b2y, b2z, f2x,
+                 f2y, f2z);
     const float hc = h * kCns;
     L.x += hc * (0.25f * b1x + 0.75f * b2x);
     L.y += hc * (0.25f * b1y + 0.75f * b2y);
@@ -301,6 +341,32 @@ __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K
     L.px += h * (0.25f * f1x + 0.75f * f2x);
     L.py += h * (0.25f * f1y + 0.75f * f2y);
     L.pz += h * (0.25f * f1z + 0.75f * f2z);
+}
+
+// push with the WallCallback's onadvance (callback.jl:167-184): a crossing of
+// the wall in the +axis direction records lincomb(new, old, w) (electron.jl:
+// 127-132), whose constructor draws s (one draw), and drops the particle if
+// the wall is set to.  t_in: sub-step start in ns since the launch start.
+__device__ __forceinline__ void push_wall(Lane& L, const SpeciesHdr& S, const KCtx& K, float h, float t_in) {
+    const float ox = L.x, oy = L.y, oz = L.z, opx = L.px, opy = L.py, opz = L.pz;
+    push(L, S, K, h);
+    const int q = S.wall_coord;
+    const float o = (q == 0) ? ox : (q == 1 ? oy : oz);
+    const float n = (q == 0) ? L.x : (q == 1 ? L.y : L.z);
+    const float v = S.wall_v;
+    if (!(o < v && v < n)) return;
+    const float w = (v - o) / (n - o), u = 1.0f - w;
+    const StepArgs& A = *K.A;
+    const unsigned long long r = atomicAdd(A.wall_n, 1ull);
+    if ((long long)r < A.wall_cap) {
+        A.wall_xw[r] = make_float4(L.x * w + ox * u, L.y * w + oy * u, L.z * w + oz * u, L.w);
+        A.wall_pt[r] = make_float4(L.px * w + opx * u, L.py * w + opy * u, L.pz * w + opz * u, t_in + w * h);
+        A.wall_meta[r] = make_uint4(L.sid_lo, L.sid_hi, uint32_t(L.species), A.ctl->launch_seq);
+    } else {
+        err(K, PCL_E_CAPACITY);
+    }
+    (void)U(L, K);
+    if (S.wall_drop) L.alive = false;
 }
 
 // turn(u, cos theta, phi, n) (util.jl:40-57).  s = hypot(mu_x, mu_y) replaces
@@ -1165,11 +1231,12 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 bool coll = __fadd_rn(__fsub_rn(L.th, tnext), L.tlo) > 0.0f;
                 float h = coll ? tnext : dd_val(L.th, L.tlo);
                 if (!coll) L.s -= h * L.r;
-                push(L, S, K, h);
+                if (S.wall_coord >= 0) push_wall(L, S, K, h, float(L.k + 1) * dt_hi - dd_val(L.th, L.tlo));
+                else push(L, S, K, h);
                 if (coll) dd_add(L.th, L.tlo, -tnext, 0.0f);
                 else { L.th = 0.0f; L.tlo = 0.0f; }
                 L.nsub += 1;
-                if (coll) collide(L, K, S);
+                if (coll && L.alive) collide(L, K, S);
                 // advance1!'s loop ends once the clock is spent (mixed_population.jl:66)
                 boundary = !(dd_val(L.th, L.tlo) > kEpsT);
             } else if (L.nsub >= kSubstepCap) {
@@ -1279,7 +1346,7 @@ __global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long 
         ctl->n_start[t] = n;
         ctl->dead[t] = 0;
     }
-    if (t == 0) { ctl->head = 0; ctl->spill_n = 0; ctl->timeout = 0; }
+    if (t == 0) { ctl->head = 0; ctl->spill_n = 0; ctl->timeout = 0; ctl->launch_seq += 1u; }
     for (int i = t; i < PCL_MAX_STEPS_PER_LAUNCH * 3; i += blockDim.x) ctl->live_end[i / 3][i % 3] = 0;
     for (int i = t; i < PCL_MAX_STEPS_PER_LAUNCH; i += blockDim.x) ctl->live_start[i] = 0;
 }
@@ -1511,6 +1578,73 @@ __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, cons
         out_kind[3 * i + c + 1] = ks[c];
     }
     out_ctr[i] = L.ctr;
+}
+
+// ------------------------------------------------- variance reduction ---
+// The particle's next stream word (the draw a Lane would take at counter ctr).
+__device__ __forceinline__ uint32_t stream_word(uint32_t ctr, uint32_t lo, uint32_t hi, uint32_t k0, uint32_t k1) {
+    uint32_t a = ctr >> 2, b = lo, c = hi, d = 0u;
+    philox4x32_10(a, b, c, d, k0, k1);
+    const uint32_t sh = ctr & 3u;
+    return sh == 0u ? a : (sh == 1u ? b : (sh == 2u ? c : d));
+}
+
+// roulette! (population.jl:291-311): keep a live particle with probability
+// pkeep (one draw from its stream) and divide its weight by pkeep, else
+// remove it.
+__global__ void k_roulette(float4* xw, uint4* meta, long long n, float pkeep, uint32_t k0, uint32_t k1,
+                           unsigned long long* dead) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        uint4 m = meta[i];
+        if (m.z == PCL_DEAD_CTR) continue;
+        const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
+        if (u < pkeep) {
+            xw[i].w = xw[i].w / pkeep;
+            meta[i].z = m.z + 1u;
+        } else {
+            meta[i].z = PCL_DEAD_CTR;
+            atomicAdd(dead, 1ull);
+        }
+    }
+}
+
+// split! (population.jl:318-335): divide a live particle's weight by 1 + p and
+// add Poisson(p) copies of it (number by inversion with one draw from its
+// stream; the reference draws it from Distributions.jl).  Copy j gets the
+// stream id of words (2(j%2), 2(j%2)+1) of Philox block (ctr, sid, 2 + j/2) of
+// its parent and a fresh counter; x, p, w, s and the step clock are copied.
+__global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, uint32_t k0,
+                        uint32_t k1, unsigned long long* nslots, unsigned long long* lost) {
+    const float e = expf(-p);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        uint4 m = meta[i];
+        if (m.z == PCL_DEAD_CTR) continue;
+        float4 a = xw[i];
+        a.w = a.w / (1.0f + p);
+        xw[i] = a;
+        const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
+        const uint32_t ctr0 = m.z;
+        meta[i].z = m.z + 1u;
+        int k = 0;
+        float P = e, F = e;
+        while (u > F && k < 1024) { ++k; P *= p / float(k); F += P; }
+        const float4 b = ps[i];
+        for (int j = 0; j < k; ++j) {
+            uint32_t c0 = ctr0, c1 = m.x, c2 = m.y, c3 = 2u + uint32_t(j >> 1);
+            philox4x32_10(c0, c1, c2, c3, k0, k1);
+            uint32_t lo = (j & 1) ? c2 : c0, hi = (j & 1) ? c3 : c1;
+            const unsigned long long q = atomicAdd(nslots, 1ull);
+            if ((long long)q < cap) {
+                xw[q] = a;
+                ps[q] = b;
+                meta[q] = make_uint4(lo, hi, 0u, m.w);
+            } else {
+                atomicAdd(lost, 1ull);
+            }
+        }
+    }
 }
 
 // ------------------------------------------------ learned-sampler data --

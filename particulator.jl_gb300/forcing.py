@@ -1,9 +1,10 @@
 """Fields, forcings and pushers (pusher.jl, field.jl, continuum.jl).
 
 The device integrates RK2Pusher(CombinedForcing(ElectromagneticField(E, B),
-ChebContinuumLoss)) with homogeneous E and B; these classes describe that
-pusher so that it can be handed to ``advance``/``run`` the way the reference
-takes its `pusher` argument.
+ChebContinuumLoss)) with a homogeneous B and an E that is homogeneous or one
+of the position-dependent fields of field.jl (double layer, step, confined
+double layer); these classes describe that pusher so that it can be handed to
+``advance``/``run`` the way the reference takes its `pusher` argument.
 """
 from __future__ import annotations
 
@@ -21,6 +22,40 @@ class HomogeneousField:
 
     def __post_init__(self):
         self.v = tuple(float(a) for a in self.v)
+
+
+@dataclass
+class DoubleLayerField:
+    """DoubleLayerField(z1, z2, v) (field.jl:10-16): v for z1 < z < z2, else 0."""
+    z1: float
+    z2: float
+    v: tuple
+
+    def device(self):
+        return 1, [float(self.z1), float(self.z2)] + [float(a) for a in self.v]
+
+
+@dataclass
+class StepField:
+    """StepField(z, v1, v2) (field.jl:19-27): v1 below z, v2 above."""
+    z: float
+    v1: tuple
+    v2: tuple
+
+    def device(self):
+        return 2, [float(self.z)] + [float(a) for a in self.v1] + [float(a) for a in self.v2]
+
+
+@dataclass
+class ConfinedDoubleLayerField:
+    """ConfinedDoubleLayerField(sx, sy, sz, ez0) (field.jl:30-52)."""
+    sx: float
+    sy: float
+    sz: float
+    ez0: float
+
+    def device(self):
+        return 3, [float(self.sx), float(self.sy), float(self.sz), float(self.ez0)]
 
 
 @dataclass
@@ -55,9 +90,12 @@ class RK2Pusher:
         cl = None
         for f in items:
             if isinstance(f, ElectromagneticField):
-                if not isinstance(f.e, HomogeneousField) or not isinstance(f.b, HomogeneousField):
-                    raise NotImplementedError("only homogeneous fields run on the device")
-                E += np.array(f.e.v)
+                if not isinstance(f.b, HomogeneousField):
+                    raise NotImplementedError("only a homogeneous B runs on the device")
+                if isinstance(f.e, HomogeneousField):
+                    E += np.array(f.e.v)
+                elif not hasattr(f.e, "device"):
+                    raise NotImplementedError(f"field {type(f.e).__name__} has no device implementation")
                 B += np.array(f.b.v)
             elif isinstance(f, ChebContinuumLoss):
                 if cl is not None:
@@ -68,3 +106,14 @@ class RK2Pusher:
             else:
                 raise NotImplementedError(f"forcing {type(f).__name__} has no device implementation")
         return E, B, cl
+
+    def device_efield(self):
+        """(kind, params) of the position-dependent E (pcl_set_field); kind 0
+        when E is homogeneous."""
+        items = self.forcing.tpl if isinstance(self.forcing, CombinedForcing) else (self.forcing,)
+        found = [f.e for f in items if isinstance(f, ElectromagneticField) and hasattr(f.e, "device")]
+        if not found:
+            return 0, []
+        if len(found) > 1 or np.any(self.device_forcing()[0] != 0):
+            raise NotImplementedError("one position-dependent E and no homogeneous E beside it")
+        return found[0].device()

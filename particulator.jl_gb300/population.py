@@ -226,7 +226,8 @@ class MultiPopulation:
 
     def set_pusher(self, pusher: RK2Pusher):
         E, B, cl = pusher.device_forcing()
-        key = (tuple(E), tuple(B), id(cl))
+        kind, fparams = pusher.device_efield()
+        key = (tuple(E), tuple(B), id(cl), kind, tuple(fparams))
         if key == self._pusher_key:
             return
         L = _lib.lib()
@@ -238,6 +239,8 @@ class MultiPopulation:
             rc = L.pcl_set_forcing(self.ctx, _lib.dptr(E), _lib.dptr(B), cl.n, cl.bints.k, cl.bints.xmax,
                                    _lib.dptr(cl.ec), _lib.dptr(cl.pc))
         _lib.check(rc, self.ctx, "pcl_set_forcing")
+        fp = np.ascontiguousarray(np.asarray(fparams, dtype=float)) if fparams else None
+        _lib.check(L.pcl_set_field(self.ctx, int(kind), _lib.dptr(fp), len(fparams)), self.ctx, "pcl_set_field")
         self._pusher_key = key
 
     def set_swarms(self, E, Fdt, safety: float = 1.15):
@@ -258,6 +261,16 @@ class MultiPopulation:
         out = np.zeros(6 * ns)
         _lib.check(_lib.lib().pcl_swarm_moments(self.ctx, key, ns, _lib.dptr(out)), self.ctx, "pcl_swarm_moments")
         return out.reshape(ns, 6)
+
+    def roulette(self, particle, pkeep: float):
+        """roulette!(pkeep, popl) (population.jl:291-311) on the device."""
+        key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        _lib.check(_lib.lib().pcl_roulette(self.ctx, key, float(pkeep)), self.ctx, "pcl_roulette")
+
+    def split(self, particle, p: float):
+        """split!(p, popl) (population.jl:318-335) on the device."""
+        key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        _lib.check(_lib.lib().pcl_split(self.ctx, key, float(p)), self.ctx, "pcl_split")
 
     def set_learned(self, particle, proc_index: int, kind: int, net=None):
         """Attach (net) or detach (None) a learned sampler for one table
@@ -379,6 +392,84 @@ class PopulationTargetCallback(AbstractCallback):
         return live < self.n if self.ismax else live > self.n
 
 
+class RouletteCallback(AbstractCallback):
+    """RouletteCallback(m) (callback.jl:210-227): after every step, each
+    population with more than m active particles gets roulette!(m / n), then
+    every population is repacked."""
+
+    def __init__(self, m: int):
+        self.m = int(m)
+
+    def onstep(self, mpopl, t):
+        for key, pop in mpopl.index.items():
+            if pop.tally_only or pop.max_particles == 0:
+                continue
+            n = nactives(pop)
+            if n > self.m:
+                mpopl.roulette(key, self.m / n)
+        _lib.check(_lib.lib().pcl_compact(mpopl.ctx), mpopl.ctx, "pcl_compact")
+        return True
+
+
+class SplitCallback(AbstractCallback):
+    """SplitCallback{S}(m, min_frac) (callback.jl:230-247): after every step,
+    if population S has fewer than m * min_frac active particles it gets
+    split!(m / n - 1), then is repacked."""
+
+    def __init__(self, particle, m: int, min_frac: float):
+        self.particle = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        self.m = int(m)
+        self.min_frac = float(min_frac)
+
+    def onstep(self, mpopl, t):
+        n = nactives(mpopl.get(self.particle))
+        if 0 < n < self.m * self.min_frac:
+            mpopl.split(self.particle, self.m / n - 1)
+        _lib.check(_lib.lib().pcl_compact(mpopl.ctx), mpopl.ctx, "pcl_compact")
+        return True
+
+
+class WallCallback(AbstractCallback):
+    """WallCallback{P}(coord, v, drop=true) (callback.jl:146-184): particles
+    of `particle` crossing the plane x[coord] = v (coord 1-3 as in Julia) in
+    the +axis direction are recorded, interpolated to the wall, and dropped if
+    `drop`.  Crossings are detected on the device during the step; `accum`
+    collects them (ParticleArrays with stream ids) after every device run."""
+
+    def __init__(self, particle, coord: int, v: float, drop: bool = True, capacity: int = 1 << 20):
+        self.particle = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        if coord not in (1, 2, 3):
+            raise ValueError("coord is 1, 2 or 3")
+        self.coord, self.v, self.drop, self.capacity = int(coord), float(v), bool(drop), int(capacity)
+        self.accum = []
+        self.t = []
+
+    def attach(self, mpopl):
+        _lib.check(_lib.lib().pcl_set_wall(mpopl.ctx, self.particle, self.coord - 1, self.v, 1 if self.drop else 0,
+                                           self.capacity), mpopl.ctx, "pcl_set_wall")
+
+    def collect(self, mpopl):
+        L = _lib.lib()
+        n = C.c_int64(0)
+        _lib.check(L.pcl_get_wall(mpopl.ctx, C.byref(n), None, None, None, None, None, None), mpopl.ctx,
+                   "pcl_get_wall")
+        m = n.value
+        if m == 0:
+            return
+        sp = np.zeros(m, np.int32); sid = np.zeros(m, np.uint64)
+        x = np.zeros((m, 3)); p = np.zeros((m, 3)); w = np.zeros(m); t = np.zeros(m)
+        _lib.check(L.pcl_get_wall(mpopl.ctx, C.byref(n), _lib.i32ptr(sp), _lib.u64ptr(sid), _lib.dptr(x),
+                                  _lib.dptr(p), _lib.dptr(w), _lib.dptr(t)), mpopl.ctx, "pcl_get_wall")
+        sel = sp == self.particle
+        self.accum.append(ParticleArrays(x[sel], p[sel], w[sel], t[sel], None, sid[sel]))
+
+    def states(self) -> ParticleArrays:
+        if not self.accum:
+            return ParticleArrays.empty()
+        return ParticleArrays(*[np.concatenate([getattr(a, f) for a in self.accum]) for f in ("x", "p", "w", "t")],
+                              None, np.concatenate([a.sid for a in self.accum]))
+
+
 class ParticleCountCallback(AbstractCallback):
     """ParticleCountCallback(particles) (callback.jl:190-204): total weight of
     each listed species at every output time."""
@@ -424,6 +515,9 @@ def run(mpopl: MultiPopulation, pusher: RK2Pusher, tfinal: float, dt: float, cal
             opts.target_species = c.particle
             opts.target_ismax = 1 if c.ismax else 0
             opts.target_n = c.n
+    walls = [c for c in cbs if isinstance(c, WallCallback)]
+    for w in walls:
+        w.attach(mpopl)
     t = mpopl.t
     nxt = t
     isave = 0
@@ -438,6 +532,8 @@ def run(mpopl: MultiPopulation, pusher: RK2Pusher, tfinal: float, dt: float, cal
                    "pcl_run")
         t = tallies.t
         mpopl.t = t
+        for w in walls:
+            w.collect(mpopl)
         cont = all(c.onstep(mpopl, t) for c in host_step) if host_step else True
         if opts.target_species >= 0:
             live = tallies.live[opts.target_species]

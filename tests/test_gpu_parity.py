@@ -35,10 +35,11 @@ def _oracle_from(oracle, pcl, mp, air, pusher, tally_only=()):
     return W
 
 
-def _check(pcl, oracle, mp, W, species=(0, 1, 2), rtol=RTOL, stol=None):
+def _check(pcl, oracle, mp, W, species=(0, 1, 2), rtol=RTOL, stol=None, max_bad=0):
     reports = []
     for k in species:
-        rep = oracle.compare_populations(mp.get(k).particles(), W.download(k), k, rtol=rtol, stol=stol)
+        rep = oracle.compare_populations(mp.get(k).particles(), W.download(k), k, rtol=rtol, stol=stol,
+                                         max_bad=max_bad)
         reports.append(rep)
         assert rep["ok"], str(rep)
     return reports
@@ -144,6 +145,121 @@ def test_autotune_keeps_physics(pcl, gpu, air):
         assert len(common) >= 0.999 * max(len(pa.sid), len(pb.sid)) - 2
         dp = np.linalg.norm(pa.p[ia] - pb.p[ib], axis=1) / np.maximum(np.linalg.norm(pb.p[ib], axis=1), 1e-300)
         assert np.mean(dp > 1e-5) <= 1e-3, np.sort(dp)[-5:]
+    a.close(); b.close()
+
+
+@pytest.mark.parametrize("kind", ["double_layer", "step", "confined"])
+def test_position_dependent_fields(pcl, oracle, gpu, air, kind):
+    """DoubleLayerField, StepField, ConfinedDoubleLayerField (field.jl:10-52),
+    evaluated at both RK2 stage positions, against the oracle."""
+    F = {"double_layer": pcl.DoubleLayerField(-0.004, 0.004, (0.0, 0.0, -1.5e6)),
+         "step": pcl.StepField(0.0, (0.0, 0.0, -1.5e6), (2e5, 0.0, 3e5)),
+         "confined": pcl.ConfinedDoubleLayerField(0.01, 0.008, 0.004, -1.5e6)}[kind]
+    pusher = pcl.RK2Pusher(pcl.CombinedForcing(pcl.ElectromagneticField(F, pcl.HomogeneousField((0.0, 0.0, 0.0))),
+                                               air["cl"]))
+    rng = np.random.default_rng(40)
+    pops = {pcl.Electron: random_population(pcl, pcl.Electron, 4096, 1e4, 3e7, rng, spread_x=0.004),
+            pcl.Positron: random_population(pcl, pcl.Positron, 1024, 1e4, 3e7, rng, spread_x=0.004)}
+    mp = pcl.MultiPopulation(*[(k, pcl.Population(1 << 15, pops[k], air["tabs"][k], air["cuts"][k], particle=k))
+                               for k in pops], (pcl.Photon, pcl.Population(1 << 15, [], air["tabs"][1],
+                                                                            air["cuts"][1], particle=pcl.Photon)),
+                             seed=40)
+    W = _oracle_from(oracle, pcl, mp, air, pusher)
+    for k in range(8):
+        pcl.advance(mp, pusher, (k + 1) * 5e-12)
+        W.advance((k + 1) * 5e-12, 4)
+    # 40 ps: s carries the FP32 rate-bound error once per collision (as the 25-ps
+    # test).  A field that jumps at a plane (double layer, step) can separate a
+    # trajectory whose earlier sub-step the tie tracking did not see as close
+    # (observed: 1 of ~4000 electrons in 8 steps): up to 2 draw-count mismatches
+    _check(pcl, oracle, mp, W, rtol=3 * RTOL, stol=4e-4, max_bad=0 if kind == "confined" else 2)
+    mp.close()
+
+
+@pytest.mark.parametrize("drop", [True, False])
+def test_wall_callback(pcl, oracle, gpu, air, drop):
+    """WallCallback (callback.jl:146-184): the same crossings as the oracle
+    (stream ids, interpolated positions on the wall, momenta, times), the
+    crossing's extra draw, and the dropped particles."""
+    pusher = _pusher(pcl, air, E=1e6)
+    rng = np.random.default_rng(50)
+    n = 4096
+    arr = random_population(pcl, pcl.Electron, n, 3e4, 3e7, rng, spread_x=0.002)
+    mp = pcl.MultiPopulation((pcl.Electron, pcl.Population(1 << 15, arr, air["tabs"][0], air["cuts"][0],
+                                                          particle=pcl.Electron)),
+                             (pcl.Photon, pcl.Population(1 << 15, [], air["tabs"][1], air["cuts"][1],
+                                                         particle=pcl.Photon)), seed=50)
+    wall = pcl.WallCallback(pcl.Electron, 3, 0.003, drop=drop)
+    W = _oracle_from(oracle, pcl, mp, {**air, "tabs": {0: air["tabs"][0], 1: air["tabs"][1]},
+                                       "cuts": {0: air["cuts"][0], 1: air["cuts"][1]}}, pusher)
+    W.set_wall(pcl.Electron, 2, 0.003, drop)
+    pcl.run(mp, pusher, 10 * 5e-12, 5e-12, wall)
+    for k in range(10):
+        W.advance((k + 1) * 5e-12, 4)
+    g = wall.states()
+    osp, osid, ox, op, ow, ot = W.get_wall()
+    assert len(g.w) > 100
+    og = dict(zip(g.sid.tolist(), range(len(g.w))))
+    ties = W.download(pcl.Electron).tie
+    matched = 0
+    for i in range(len(ow)):
+        j = og.get(int(osid[i]))
+        if j is None:
+            continue
+        matched += 1
+        assert abs(g.x[j, 2] - 0.003) < 1e-7
+        np.testing.assert_allclose(g.p[j], op[i], rtol=1e-4, atol=1e-4 * np.linalg.norm(op[i]))
+        assert abs(g.t[j] - ot[i]) < 1e-4 * 50e-12
+    assert matched >= 0.99 * len(ow) - 2 and abs(len(g.w) - len(ow)) <= max(2, 0.01 * len(ow)), \
+        (matched, len(g.w), len(ow))
+    rep = oracle.compare_populations(mp.get(0).particles(), W.download(pcl.Electron), pcl.Electron, rtol=3 * RTOL,
+                                     stol=2e-4)
+    assert rep["ok"], str(rep)
+    mp.close()
+
+
+def test_roulette_split_parity(pcl, oracle, gpu, air):
+    """roulette! and split! (population.jl:291-335) on the device against the
+    oracle: the same survivors and copies (stream ids), weights, and the same
+    evolution of the copies afterwards."""
+    mp = _mixed(pcl, air, n=(4096, 1024, 512), seed=60)
+    pusher = _pusher(pcl, air, E=1e6)
+    W = _oracle_from(oracle, pcl, mp, air, pusher)
+    pcl.advance(mp, pusher, 5e-12)
+    W.advance(5e-12, 4)
+    mp.roulette(pcl.Electron, 0.375)
+    W.roulette(pcl.Electron, 0.375)
+    pcl.repack(mp.get(pcl.Electron))
+    g, o = mp.get(0).particles(), W.download(0)
+    assert 0.3 * 4096 < len(g.w) < 0.45 * 4096
+    rep = oracle.compare_populations(g, o, pcl.Electron, rtol=3 * RTOL, max_unmatched_frac=0.002)
+    assert rep["ok"], str(rep)
+    mp.split(pcl.Positron, 0.75)
+    W.split(pcl.Positron, 0.75)
+    g, o = mp.get(2).particles(), W.download(2)
+    assert len(g.w) > 1.5 * 400
+    rep = oracle.compare_populations(g, o, pcl.Positron, rtol=3 * RTOL, max_unmatched_frac=0.002)
+    assert rep["ok"], str(rep)
+    for k in range(3):
+        pcl.advance(mp, pusher, (k + 2) * 5e-12)
+        W.advance((k + 2) * 5e-12, 4)
+    _check(pcl, oracle, mp, W, rtol=3 * RTOL, stol=2e-4)
+    mp.close()
+
+
+def test_roulette_callback_keeps_weight(pcl, gpu, air):
+    """RouletteCallback(m): populations stay near m while the total weight is
+    kept in expectation."""
+    pusher = _pusher(pcl, air, E=1e6)
+    a = _mixed(pcl, air, n=(8192, 2048, 512), seed=61)
+    b = _mixed(pcl, air, n=(8192, 2048, 512), seed=61)
+    pcl.run(a, pusher, 3e-12, 1e-12, pcl.RouletteCallback(2000))
+    pcl.run(b, pusher, 3e-12, 1e-12)
+    n = pcl.nactives(a.get(0))
+    wa, wb = pcl.weight(a.get(0)), pcl.weight(b.get(0))
+    # roulette at keep probability q adds variance n (1/q - 1) per application
+    sigma = np.sqrt(3 * 8192 * (8192 / 2000 - 1))
+    assert 1500 < n < 2600 and abs(wa - wb) < 6 * sigma, (n, wa, wb, sigma)
     a.close(); b.close()
 
 

@@ -112,3 +112,13 @@ def test_step_is_thread_count_independent(pcl, oracle, air):
         for a, b in zip(res[0], r):
             for u, v in zip(a, b):
                 assert np.array_equal(u, v)
+
+
+def test_field_shapes(pcl):
+    """The position-dependent fields' device parameters follow field.jl."""
+    assert pcl.DoubleLayerField(-1, 2, (0, 0, 5)).device() == (1, [-1.0, 2.0, 0.0, 0.0, 5.0])
+    assert pcl.StepField(0.5, (1, 2, 3), (4, 5, 6)).device() == (2, [0.5, 1.0, 2.0, 3.0, 4.0, 5.0, 6.0])
+    assert pcl.ConfinedDoubleLayerField(1, 2, 3, 4).device() == (3, [1.0, 2.0, 3.0, 4.0])
+    pusher = pcl.RK2Pusher(pcl.CombinedForcing(pcl.ElectromagneticField(pcl.StepField(0, (0, 0, 1), (0, 0, 2)),
+                                                                        pcl.HomogeneousField((0, 0, 0)))))
+    assert pusher.device_efield()[0] == 2 and np.all(pusher.device_forcing()[0] == 0)
