@@ -145,6 +145,7 @@ struct StepArgs {
     float4* wall_xw; float4* wall_pt; uint4* wall_meta;
     unsigned long long* wall_n;
     long long wall_cap;
+    int general;    // a position-dependent field or a wall is set: the general step kernel runs
 };
 
 // Network index of each (species, table position) with a learned sampler (-1: none).

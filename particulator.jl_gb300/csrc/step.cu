@@ -295,8 +295,10 @@ __device__ __forceinline__ void efield(const KCtx& K, int sw, float x, float y, 
 }
 
 // force(CombinedForcing(ElectromagneticField, ChebContinuumLoss), lepton)
-// (pusher.jl:14-23, field.jl:54-70, continuum.jl:45-57) at position (x, y, z).
+// (pusher.jl:14-23, field.jl:54-70, continuum.jl:45-57) at position (x, y, z);
+// GENERAL = false: homogeneous E (or the swarm's), position unused.
 // Returns beta too.
+template <bool GENERAL>
 __device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K, int sw, float x, float y, float z,
                                              float px, float py, float pz, float& bx, float& by, float& bz,
                                              float& fx, float& fy, float& fz) {
@@ -305,7 +307,12 @@ __device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K,
     bx = px * ig; by = py * ig; bz = pz * ig;
     const float q = S.charge;
     float ex, ey, ez;
-    efield(K, sw, x, y, z, ex, ey, ez);
+    if (GENERAL) {
+        efield(K, sw, x, y, z, ex, ey, ez);
+    } else {
+        const float* E = (K.H->nswarm > 0) ? K.blob + K.H->swarm_off + 4 * sw : K.H->E;
+        ex = E[0]; ey = E[1]; ez = E[2];
+    }
     const float* B = K.H->B;
     fx = q * (ex + (by * B[2] - bz * B[1]));
     fy = q * (ey + (bz * B[0] - bx * B[2]));
@@ -319,6 +326,7 @@ __device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K,
 
 // advance_particle(RK2Pusher, y, dt) (pusher.jl:41-63); photons move in a
 // straight line (photon.jl:46-52; both forcings vanish on photons).
+template <bool GENERAL>
 __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K, float h) {
     if (L.species == PCL_PHOTON) {
         float v = h * kCns * rsqrtf(L.px * L.px + L.py * L.py + L.pz * L.pz);
@@ -326,14 +334,14 @@ __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K
         return;
     }
     float b1x, b1y, b1z, f1x, f1y, f1z;
-    lepton_force(S, K, L.sw, L.x, L.y, L.z, L.px, L.py, L.pz, b1x, b1y, b1z, f1x, f1y, f1z);
+    lepton_force<GENERAL>(S, K, L.sw, L.x, L.y, L.z, L.px, L.py, L.pz, b1x, b1y, b1z, f1x, f1y, f1z);
     const float h23 = h * (2.0f / 3.0f);
     float qx = L.px + h23 * f1x, qy = L.py + h23 * f1y, qz = L.pz + h23 * f1z;
     // second stage at x + 2 dt v1 / 3 (only a position-dependent field reads it)
-    const float c23 = (K.H->field_kind != 0) ? h23 * kCns : 0.0f;
+    const float c23 = GENERAL ? h23 * kCns : 0.0f;
     float b2x, b2y, b2z, f2x, f2y, f2z;
-    lepton_force(S, K, L.sw, L.x + c23 * b1x, L.y + c23 * b1y, L.z + c23 * b1z, qx, qy, qz, b2x, b2y, b2z, f2x,
-                 f2y, f2z);
+    lepton_force<GENERAL>(S, K, L.sw, L.x + c23 * b1x, L.y + c23 * b1y, L.z + c23 * b1z, qx, qy, qz, b2x, b2y, b2z,
+                          f2x, f2y, f2z);
     const float hc = h * kCns;
     L.x += hc * (0.25f * b1x + 0.75f * b2x);
     L.y += hc * (0.25f * b1y + 0.75f * b2y);
@@ -349,7 +357,7 @@ __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K
 // the wall is set to.  t_in: sub-step start in ns since the launch start.
 __device__ __forceinline__ void push_wall(Lane& L, const SpeciesHdr& S, const KCtx& K, float h, float t_in) {
     const float ox = L.x, oy = L.y, oz = L.z, opx = L.px, opy = L.py, opz = L.pz;
-    push(L, S, K, h);
+    push<true>(L, S, K, h);
     const int q = S.wall_coord;
     const float o = (q == 0) ? ox : (q == 1 ? oy : oz);
     const float n = (q == 0) ? L.x : (q == 1 ? L.y : L.z);
@@ -1055,7 +1063,7 @@ __device__ __forceinline__ void load_slot(Lane& L, const float4* xw, const float
 }
 
 // ------------------------------------------------------------ the step ---
-template <int MINB>
+template <int MINB, bool GENERAL>
 __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwarps = blockDim.x >> 5;
@@ -1231,8 +1239,9 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 bool coll = __fadd_rn(__fsub_rn(L.th, tnext), L.tlo) > 0.0f;
                 float h = coll ? tnext : dd_val(L.th, L.tlo);
                 if (!coll) L.s -= h * L.r;
-                if (S.wall_coord >= 0) push_wall(L, S, K, h, float(L.k + 1) * dt_hi - dd_val(L.th, L.tlo));
-                else push(L, S, K, h);
+                if (!GENERAL) push<false>(L, S, K, h);
+                else if (S.wall_coord >= 0) push_wall(L, S, K, h, float(L.k + 1) * dt_hi - dd_val(L.th, L.tlo));
+                else push<true>(L, S, K, h);
                 if (coll) dd_add(L.th, L.tlo, -tnext, 0.0f);
                 else { L.th = 0.0f; L.tlo = 0.0f; }
                 L.nsub += 1;
@@ -1315,8 +1324,16 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 
 // The step kernel is instantiated for 2, 3 and 4 resident 256-thread blocks
 // per SM (register budgets 128, 85 and 64); the launch shape is a tunable.
+// The plain kernels (homogeneous field, no wall) come in 2, 3 and 4 blocks per
+// SM; the general one (position-dependent field or wall crossings) in 3, where it
+// needs no register spills.
+static void (*step_kernel(int minb, bool general))(StepArgs) {
+    if (general) return k_step<3, true>;
+    return (minb == 2) ? k_step<2, false> : (minb == 3) ? k_step<3, false> : k_step<4, false>;
+}
+
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A) {
-    void (*kern)(StepArgs) = (minb == 2) ? k_step<2> : (minb == 3) ? k_step<3> : k_step<4>;
+    void (*kern)(StepArgs) = step_kernel(minb, A.general != 0);
     // the shared-memory attribute is set outside stream capture (prepare_step
     // runs first); during capture the launch is only recorded
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1330,9 +1347,8 @@ cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream
     return cudaGetLastError();
 }
 
-cudaError_t prepare_step(int minb, size_t smem) {
-    void (*kern)(StepArgs) = (minb == 2) ? k_step<2> : (minb == 3) ? k_step<3> : k_step<4>;
-    return cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+cudaError_t prepare_step(int minb, size_t smem, bool general) {
+    return cudaFuncSetAttribute(step_kernel(minb, general), cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
 }
 
 // Launch prologue: snapshot the work space and clear per-launch counters.
