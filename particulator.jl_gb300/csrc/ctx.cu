@@ -464,7 +464,7 @@ static StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, int sp_
     A.blob_bytes = int(c->blob.size());
     A.wall_xw = c->d_wall_xw; A.wall_pt = c->d_wall_pt; A.wall_meta = c->d_wall_meta;
     A.wall_n = c->d_wall_n; A.wall_cap = c->wall_cap;
-    A.general = (c->field_kind != 0) ? 1 : 0;
+    A.general = (c->field_kind != 0 || c->learn_on) ? 1 : 0;
     for (int s = 0; s < 3; ++s)
         if (c->sp[s].wall_coord >= 0 && c->wall_cap > 0) A.general = 1;
     if (c->learn_on) {  // suspended collisions go to queue 0 unless set_lq says otherwise

@@ -971,7 +971,9 @@ __device__ void learned_outcome(Lane& L, const KCtx& K, const SpeciesHdr& S, con
     if (L.alive) L.r = setr(S, K, kin_energy_exact(L.species, L.px, L.py, L.pz), L.sw);
 }
 
-// do_one_collision! (collisions.jl:142-199)
+// do_one_collision! (collisions.jl:142-199).  LEARN: the learned samplers may
+// take the collision (general step kernel only).
+template <bool LEARN>
 __device__ void collide(Lane& L, const KCtx& K, const SpeciesHdr& S) {
     if (L.r == 0.0f) return;
     float E = kin_energy_exact(L.species, L.px, L.py, L.pz);
@@ -1009,7 +1011,7 @@ __device__ void collide(Lane& L, const KCtx& K, const SpeciesHdr& S) {
     }
     atomicAdd(&K.tal[T_COLL + 16 * L.species + j], 1u);
     const DevProc& P = S.proc[j];
-    if (P.learn && K.A->lq_out_n && learned_here(P, E) && suspend(L, K, j, ctr0)) return;
+    if (LEARN && P.learn && K.A->lq_out_n && learned_here(P, E) && suspend(L, K, j, ctr0)) return;
     sample_process(L, K, S, P, E, ctr0);
 }
 
@@ -1104,7 +1106,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 
     // work space: concatenated species ranges, or the spill queue
     long long nsp0, nsp1, total;
-    if (A.spill_mode == 2) {
+    if (GENERAL && A.spill_mode == 2) {
         nsp0 = 0; nsp1 = 0;
         total = min((long long)(*A.lq_in_n), A.lq_cap);
     } else if (A.spill_mode) {
@@ -1172,7 +1174,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 int rk = __popc(need & lt);
                 if (!has && rk < tk) {
                     long long v = cur + rk;
-                    if (A.spill_mode == 2) {
+                    if (GENERAL && A.spill_mode == 2) {
                         float4 a = A.lq_in_xw[v], b = A.lq_in_ps[v];
                         uint4 m1 = A.lq_in_m1[v];
                         float4 m2 = A.lq_in_m2[v];
@@ -1211,7 +1213,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         has = (L.ctr != PCL_DEAD_CTR);
                         if (has) atomicAdd(&tal[T_LSTART + 0], 1u);
                     }
-                    if (has && A.spill_mode != 2) {
+                    if (has && !(GENERAL && A.spill_mode == 2)) {
                         L.rvalid = false; L.alive = true; L.nsub = 0;
                         L.sw = (H->nswarm > 0) ? min(int(L.sid_hi >> 24), H->nswarm - 1) : 0;
                         L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz), L.sw);
@@ -1245,7 +1247,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 if (coll) dd_add(L.th, L.tlo, -tnext, 0.0f);
                 else { L.th = 0.0f; L.tlo = 0.0f; }
                 L.nsub += 1;
-                if (coll && L.alive) collide(L, K, S);
+                if (coll && L.alive) collide<GENERAL>(L, K, S);
                 // advance1!'s loop ends once the clock is spent (mixed_population.jl:66)
                 boundary = !(dd_val(L.th, L.tlo) > kEpsT);
             } else if (L.nsub >= kSubstepCap) {
@@ -1324,9 +1326,9 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 
 // The step kernel is instantiated for 2, 3 and 4 resident 256-thread blocks
 // per SM (register budgets 128, 85 and 64); the launch shape is a tunable.
-// The plain kernels (homogeneous field, no wall) come in 2, 3 and 4 blocks per
-// SM; the general one (position-dependent field or wall crossings) in 3, where it
-// needs no register spills.
+// The plain kernels (homogeneous field, no wall, no learned sampler) come in 2,
+// 3 and 4 blocks per SM; the general one (position-dependent field, wall
+// crossings, learned samplers) in 3, where it needs no register spills.
 static void (*step_kernel(int minb, bool general))(StepArgs) {
     if (general) return k_step<3, true>;
     return (minb == 2) ? k_step<2, false> : (minb == 3) ? k_step<3, false> : k_step<4, false>;
