@@ -129,7 +129,8 @@ def _profile_traffic():
     return None
 
 
-def build_workload(pcl, n_seed: int, seed: int, device: int, steps_per_launch: int = 1, blocks_per_sm: int = 0):
+def build_workload(pcl, n_seed: int, seed: int, device: int, steps_per_launch: int = 1, blocks_per_sm: int = 0,
+                   classic_step: bool = False):
     co = pcl.co
     comp = pcl.workloads.air_composition()
     dt = 1e-12
@@ -147,7 +148,8 @@ def build_workload(pcl, n_seed: int, seed: int, device: int, steps_per_launch: i
         ("electron", pcl.Population(cap_e, arr, et, 1e4 * co.eV, particle=pcl.Electron)),
         ("photon", pcl.Population(cap_g, [], gt, 5e3 * co.eV, particle=pcl.Photon)),
         ("positron", pcl.Population(cap_p, [], pt, 1e4 * co.eV, particle=pcl.Positron)),
-        seed=seed, device=device, steps_per_launch=steps_per_launch, blocks_per_sm=blocks_per_sm)
+        seed=seed, device=device, steps_per_launch=steps_per_launch, blocks_per_sm=blocks_per_sm,
+        classic_step=classic_step)
     mp.set_pusher(pusher)
     return mp, pusher, dt, dict(tables=(et, gt, pt), cl=cl, comp=comp)
 
@@ -592,9 +594,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--steps-per-launch", type=int, default=1)
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
+    ap.add_argument("--classic", type=int, default=0, help="1: classic step kernel (lanes collide in place)")
     ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned", "plain", "reid", "mlp"])
     ap.add_argument("--nswarm", type=int, default=256)
-    ap.add_argument("--tune-steps", type=int, default=480)
+    ap.add_argument("--tune-steps", type=int, default=512)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -615,7 +618,8 @@ def main():
     pcl = graft.load_package()
     L = pcl.lib()
     mp, pusher, dt, extra = build_workload(pcl, args.n, seed=rank, device=local,
-                                           steps_per_launch=args.steps_per_launch, blocks_per_sm=args.bps)
+                                           steps_per_launch=args.steps_per_launch, blocks_per_sm=args.bps,
+                                           classic_step=bool(args.classic))
     ctx = mp.ctx
     K = args.steps_per_launch
     # ---- warm-up
@@ -704,7 +708,8 @@ def main():
                 "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "rrea-air-0.5MVm-16M", "seed_electrons": args.n, "dt_s": dt,
-                           "steps_per_launch": K, "blocks_per_sm": args.bps or 4, "live_at_end": list(tal1.live),
+                           "steps_per_launch": K, "blocks_per_sm": (args.bps or 4) if args.classic else 3,
+                           "step_kernel": "classic" if args.classic else "event", "live_at_end": list(tal1.live),
                            "l2": "inputs larger than L2 (population > 800 MB)", "parallelism": f"replicas{ws}"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind,

@@ -121,12 +121,15 @@ typedef struct pcl_config {
     uint64_t seed;             /* Philox4x32-10 key for every particle stream        */
     int32_t  device;           /* CUDA device ordinal                                 */
     int32_t  block_size;       /* threads per block of the step kernel (0 = 256)      */
-    int32_t  grid_blocks;      /* persistent grid size (0 = 2 x SM count)             */
+    int32_t  grid_blocks;      /* persistent grid size (0 = blocks_per_sm x SM count) */
     int32_t  steps_per_launch; /* time steps fused into one launch (0/1 = one)        */
     int32_t  compaction_period;/* compact dead slots every this many steps (0 = 8)    */
     int32_t  use_graph;        /* capture the step sequence of pcl_run in a CUDA graph */
-    int32_t  blocks_per_sm;    /* resident step-kernel blocks per SM: 2, 3 or 4 (0 = 4) */
-    int32_t  reserved[3];
+    int32_t  blocks_per_sm;    /* classic kernel: resident blocks per SM, 2, 3 or 4 (0 = 4) */
+    int32_t  classic_step;     /* 0 (default): colliding particles are parked and collided in
+                                  full-warp batches (event kernel, 3 blocks per SM); 1: each
+                                  lane collides in place (blocks_per_sm applies)            */
+    int32_t  reserved[2];
 } pcl_config;
 
 /* ---- per-context tallies (FP64 / int64 on the device) -------------------- */
@@ -373,12 +376,13 @@ int pcl_compact_noalloc(int64_t n, const float* xw, const float* ps, const uint3
  * No counterpart in the reference (its loop has no launch shape).  Advances
  * the simulation by up to steps_budget real steps of dt (the physics does not
  * depend on the launch parameters) while a coordinate search times candidate
- * launch shapes with CUDA events: blocks per SM {2, 3, 4}, steps per launch
- * {1, 2, 4, 8, 16}, compaction period {2, 4, 8, 16, 32}, graph replay {0, 1},
- * in that order, each trial a whole number of launches and compactions.  The
- * context keeps the fastest shape (particle-steps per second). */
+ * launch shapes with CUDA events: step kernel {event, classic with 2, 3, 4
+ * blocks per SM}, steps per launch {1, 2, 4, 8, 16}, compaction period
+ * {2, 4, 8, 16, 32}, graph replay {0, 1}, in that order, each trial a whole
+ * number of launches and compactions.  The context keeps the fastest shape
+ * (particle-steps per second). */
 typedef struct pcl_tune_result {
-    int32_t blocks_per_sm, steps_per_launch, compaction_period, use_graph;
+    int32_t blocks_per_sm, steps_per_launch, compaction_period, use_graph;   /* blocks_per_sm 0: event kernel */
     double  rate;              /* particle-steps per second of the kept shape */
     int32_t trials;
     int32_t steps;             /* steps advanced by the search */
@@ -386,8 +390,9 @@ typedef struct pcl_tune_result {
 } pcl_tune_result;
 int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* out);
 /* Set the launch shape directly (e.g. one tuned on another context of the
- * same workload): blocks per SM (2-4), steps per launch (1-64), compaction
- * period (>= 1), graph replay (0/1). */
+ * same workload): blocks per SM (0: event kernel; 2-4: classic kernel with
+ * that many blocks per SM), steps per launch (1-64), compaction period
+ * (>= 1), graph replay (0/1). */
 int pcl_set_launch(void* ctx, int32_t blocks_per_sm, int32_t steps_per_launch, int32_t compaction_period,
                    int32_t use_graph);
 

@@ -17,7 +17,7 @@ extern "C" int pcl_ratebound_split(int, int, int, int, double, const double*, do
 
 namespace pcl {
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A);
-cudaError_t prepare_step(int minb, size_t smem, bool general);
+cudaError_t prepare_step(int minb, size_t smem, bool general, bool event);
 __global__ void k_learn_hist(StepArgs A, int species, int j, int kind, int nT, long long per_T, int nbins,
                              float hmin, float hmax, unsigned long long sid_base, unsigned int* hist);
 __global__ void k_learn_x(const float4* ps, const float4* m2, long long n, float* X);
@@ -43,7 +43,7 @@ __global__ void k_swarm_moments(const float4* xw, const float4* ps, const uint4*
 __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, const float* p_in,
                                const uint32_t* sid, float* out_p, float* out_s, int* out_kind,
                                uint32_t* out_ctr);
-size_t step_smem_bytes(int blob_bytes, int threads);
+size_t step_smem_bytes(int blob_bytes, int threads, bool event);
 const char* noalloc_last_error();
 constexpr int kTile = 2048;
 
@@ -467,6 +467,7 @@ static StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, int sp_
     A.general = (c->field_kind != 0 || c->learn_on) ? 1 : 0;
     for (int s = 0; s < 3; ++s)
         if (c->sp[s].wall_coord >= 0 && c->wall_cap > 0) A.general = 1;
+    A.event = (c->cfg.classic_step == 0) ? 1 : 0;
     if (c->learn_on) {  // suspended collisions go to queue 0 unless set_lq says otherwise
         A.lq_out_xw = c->lq_xw[0]; A.lq_out_ps = c->lq_ps[0]; A.lq_out_m1 = c->lq_m1[0]; A.lq_out_m2 = c->lq_m2[0];
         A.lq_out_n = c->d_lqn;
@@ -526,6 +527,7 @@ static int ensure_lq(Ctx* c) {
 }
 
 static int blocks_per_sm(Ctx* c) {
+    if (c->cfg.classic_step == 0) return 3;   // the event kernel's stash leaves room for 3 blocks per SM
     int b = c->cfg.blocks_per_sm;
     return (b >= 2 && b <= 4) ? b : 4;
 }
@@ -613,7 +615,7 @@ static int run_group_graph(Ctx* c, const StepArgs& A, const StepArgs& P0, const 
     for (auto& g : c->graphs)
         if (g.key == key) { exec = g.exec; break; }
     if (!exec) {
-        CK(prepare_step(minb, smem, A.general != 0));
+        CK(prepare_step(minb, smem, A.general != 0, A.event != 0));
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = cudaSuccess;
         auto q = [&e](cudaError_t r) { if (e == cudaSuccess) e = r; };
@@ -728,7 +730,7 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
     if ((rc = ensure_lq(c))) return rc;
     const double dt = t_to_dev(dt_si);
     const int threads = block_threads(c);
-    const size_t smem = step_smem_bytes(int(c->blob.size()), threads);
+    const size_t smem = step_smem_bytes(int(c->blob.size()), threads, c->cfg.classic_step == 0);
     const int period = c->cfg.compaction_period > 0 ? c->cfg.compaction_period : 8;
     const bool graph = c->cfg.use_graph != 0;
     bool compacted = false, host_passes = false;
@@ -1648,12 +1650,13 @@ int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* ou
     for (auto& sp : c->sp) any = any || sp.set;
     if (!any) return fail(c, PCL_ERR_STATE, "no species set");
     CK(cudaSetDevice(c->device));
-    const int bps_c[] = {2, 3, 4}, k_c[] = {1, 2, 4, 8, 16}, per_c[] = {2, 4, 8, 16, 32}, g_c[] = {0, 1};
-    const int ntrials = 3 + 5 + 5 + 2;
+    // step kernel: 0 = event, 2-4 = classic with that many blocks per SM
+    const int bps_c[] = {0, 2, 3, 4}, k_c[] = {1, 2, 4, 8, 16}, per_c[] = {2, 4, 8, 16, 32}, g_c[] = {0, 1};
+    const int ntrials = 4 + 5 + 5 + 2;
     // steps per trial: a multiple of the largest steps-per-launch and period tried
     int len = std::max(32, (steps_budget / ntrials) / 32 * 32);
     pcl_config best = c->cfg;
-    best.blocks_per_sm = blocks_per_sm(c);
+    best.blocks_per_sm = (c->cfg.classic_step == 0) ? 4 : blocks_per_sm(c);
     if (best.steps_per_launch < 1) best.steps_per_launch = 1;
     if (best.compaction_period < 1) best.compaction_period = 8;
     double best_rate = -1.0;
@@ -1688,7 +1691,12 @@ int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* ou
         return PCL_OK;
     };
     int rc = PCL_OK;
-    for (int v : bps_c) { pcl_config q = best; q.blocks_per_sm = v; if ((rc = consider(q))) return rc; }
+    for (int v : bps_c) {
+        pcl_config q = best;
+        q.classic_step = (v == 0) ? 0 : 1;
+        q.blocks_per_sm = (v == 0) ? 4 : v;
+        if ((rc = consider(q))) return rc;
+    }
     const pcl_config after_bps = best;
     for (int v : k_c) { pcl_config q = after_bps; q.steps_per_launch = v; if ((rc = consider(q))) return rc; }
     const pcl_config after_k = best;
@@ -1698,7 +1706,7 @@ int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* ou
     c->cfg = best;
     if (out) {
         std::memset(out, 0, sizeof(*out));
-        out->blocks_per_sm = best.blocks_per_sm;
+        out->blocks_per_sm = best.classic_step ? best.blocks_per_sm : 0;
         out->steps_per_launch = best.steps_per_launch;
         out->compaction_period = best.compaction_period;
         out->use_graph = best.use_graph;
@@ -1711,10 +1719,11 @@ int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* ou
 
 int pcl_set_launch(void* ctx, int32_t bps, int32_t spl, int32_t period, int32_t use_graph) {
     Ctx* c = static_cast<Ctx*>(ctx);
-    if (!c || bps < 2 || bps > 4 || spl < 1 || spl > PCL_MAX_STEPS_PER_LAUNCH || period < 1 ||
+    if (!c || !(bps == 0 || (bps >= 2 && bps <= 4)) || spl < 1 || spl > PCL_MAX_STEPS_PER_LAUNCH || period < 1 ||
         (use_graph != 0 && use_graph != 1))
         return PCL_ERR_INVALID;
-    c->cfg.blocks_per_sm = bps;
+    c->cfg.classic_step = (bps == 0) ? 0 : 1;
+    c->cfg.blocks_per_sm = (bps == 0) ? 4 : bps;
     c->cfg.steps_per_launch = spl;
     c->cfg.compaction_period = period;
     c->cfg.use_graph = use_graph;

@@ -146,6 +146,7 @@ struct StepArgs {
     unsigned long long* wall_n;
     long long wall_cap;
     int general;    // a position-dependent field or a wall is set: the general step kernel runs
+    int event;      // the event step kernel runs (parked collisions in full-warp batches)
 };
 
 // Network index of each (species, table position) with a learned sampler (-1: none).

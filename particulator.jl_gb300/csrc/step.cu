@@ -39,6 +39,7 @@
 namespace pcl {
 
 constexpr int   kWarpStack   = 32;          // child-stack entries per warp
+constexpr int   kCollStash   = 64;          // event kernel: parked collisions per warp
 constexpr int   kRejectCap   = 10000;       // rejection-loop iteration cap
 constexpr int   kSubstepCap  = 1 << 20;     // sub-steps per particle per step
 constexpr float kEpsT        = 2.220446049250313e-7f;  // eps(Float64) s in ns (mixed_population.jl:66)
@@ -971,6 +972,34 @@ __device__ void learned_outcome(Lane& L, const KCtx& K, const SpeciesHdr& S, con
     if (L.alive) L.r = setr(S, K, kin_energy_exact(L.species, L.px, L.py, L.pz), L.sw);
 }
 
+// Event kernel: a lane's whole state as 5 x 16 B (the collision stash).  The
+// Philox cache keeps at most three unconsumed words (c0..c2).
+__device__ __forceinline__ void park_lane(const Lane& L, float4* e) {
+    const uint32_t pk = uint32_t(L.species) | (uint32_t(L.k) << 2) | (uint32_t(L.sw) << 8) |
+                        (L.rvalid ? (1u << 16) : 0u);
+    e[0] = make_float4(L.x, L.y, L.z, L.w);
+    e[1] = make_float4(L.px, L.py, L.pz, L.s);
+    e[2] = make_float4(L.th, L.tlo, L.r, __uint_as_float(L.sid_lo));
+    e[3] = make_float4(__uint_as_float(L.sid_hi), __uint_as_float(L.ctr), __uint_as_float(L.c0),
+                       __uint_as_float(L.c1));
+    e[4] = make_float4(__uint_as_float(L.c2), __uint_as_float(pk), __int_as_float(L.slot), __int_as_float(L.nsub));
+}
+
+__device__ __forceinline__ void unpark_lane(Lane& L, const float4* e) {
+    const float4 a = e[0], b = e[1], c = e[2], d = e[3], f = e[4];
+    L.x = a.x; L.y = a.y; L.z = a.z; L.w = a.w;
+    L.px = b.x; L.py = b.y; L.pz = b.z; L.s = b.w;
+    L.th = c.x; L.tlo = c.y; L.r = c.z; L.sid_lo = __float_as_uint(c.w);
+    L.sid_hi = __float_as_uint(d.x); L.ctr = __float_as_uint(d.y); L.c0 = __float_as_uint(d.z);
+    L.c1 = __float_as_uint(d.w);
+    L.c2 = __float_as_uint(f.x);
+    const uint32_t pk = __float_as_uint(f.y);
+    L.species = int(pk & 3u); L.k = int((pk >> 2) & 63u); L.sw = int((pk >> 8) & 255u);
+    L.rvalid = ((pk >> 16) & 1u) != 0u;
+    L.slot = __float_as_int(f.z); L.nsub = __float_as_int(f.w);
+    L.alive = true;
+}
+
 // do_one_collision! (collisions.jl:142-199).  LEARN: the learned samplers may
 // take the collision (general step kernel only).
 template <bool LEARN>
@@ -1065,7 +1094,11 @@ __device__ __forceinline__ void load_slot(Lane& L, const float4* xw, const float
 }
 
 // ------------------------------------------------------------ the step ---
-template <int MINB, bool GENERAL>
+// EVENT: colliding particles are parked in a per-warp stash and collided in
+// batches that fill the warp's free lanes (see the loop), instead of each lane
+// colliding as soon as its push ends; each particle's sequence of operations
+// is unchanged.
+template <int MINB, bool GENERAL, bool EVENT>
 __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwarps = blockDim.x >> 5;
@@ -1080,9 +1113,15 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     uint32_t* tal = reinterpret_cast<uint32_t*>(tops + nwarps);
     unsigned long long* mbar =
         reinterpret_cast<unsigned long long*>(reinterpret_cast<uintptr_t>(tal + T_WORDS + 8) & ~uintptr_t(7));
+    // event kernel: collision stash after the mbarrier (16-B aligned), counters after it
+    float4* cs_all = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(mbar + 1) + 15) & ~uintptr_t(15));
+    int* cs_ns = reinterpret_cast<int*>(cs_all + size_t(nwarps) * kCollStash * 5);
+    float4* cs = cs_all + size_t(warp) * kCollStash * 5;
+    int* cs_n = cs_ns + warp;
 
     for (int i = threadIdx.x; i < T_WORDS; i += blockDim.x) tal[i] = 0u;
     if (lane == 0) tops[warp] = 0;
+    if (EVENT && lane == 0) *cs_n = 0;
     bool ok = stage_blob(smem, A.blob, A.blob_bytes, mbar);
     if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) atomicExch(&A.ctl->timeout, 1);
@@ -1126,6 +1165,27 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     bool has = false;
 
     for (;;) {
+        // ---------------- event kernel: collide parked particles in the free
+        // lanes once the stash can fill all of them (or nothing else is left)
+        if (EVENT) {
+            const unsigned empty = __ballot_sync(FULL, !has);
+            __syncwarp();
+            const int nstash = *cs_n;
+            const int ne = __popc(empty);
+            const bool drain = input_done && *K.top == 0;
+            if (ne > 0 && nstash > 0 && (nstash >= ne || drain)) {
+                const int take = min(ne, nstash);
+                const int rank = __popc(empty & lt);
+                if (!has && rank < take) {
+                    unpark_lane(L, cs + size_t(nstash - 1 - rank) * 5);
+                    has = true;
+                    collide<GENERAL>(L, K, H->sp[L.species]);
+                }
+                __syncwarp();
+                if (lane == 0) *cs_n = nstash - take;
+                __syncwarp();
+            }
+        }
         // ---------------- refill idle lanes: children first, then input
         unsigned need = __ballot_sync(FULL, !has);
         if (need) {
@@ -1225,13 +1285,14 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
         }
         if (__ballot_sync(FULL, has) == 0u) {
             // no work in this warp; the stack is empty because it is drained first
-            if (input_done) break;
+            if (input_done && (!EVENT || *cs_n == 0)) break;
             continue;
         }
 
         // ---------------- one sub-step per busy lane, and the step boundary in the
         // same iteration when the sub-step used up the clock
         int fin = 0;  // 1: survives the launch, 2: removed
+        bool park = false;
         if (has) {
             const SpeciesHdr& S = H->sp[L.species];
             bool boundary = true;
@@ -1247,14 +1308,17 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 if (coll) dd_add(L.th, L.tlo, -tnext, 0.0f);
                 else { L.th = 0.0f; L.tlo = 0.0f; }
                 L.nsub += 1;
-                if (coll && L.alive) collide<GENERAL>(L, K, S);
+                if (EVENT) park = coll && L.alive;
+                else if (coll && L.alive) collide<GENERAL>(L, K, S);
                 // advance1!'s loop ends once the clock is spent (mixed_population.jl:66)
-                boundary = !(dd_val(L.th, L.tlo) > kEpsT);
+                boundary = !park && !(dd_val(L.th, L.tlo) > kEpsT);
             } else if (L.nsub >= kSubstepCap) {
                 err(K, PCL_E_SUBSTEP_CAP);
                 L.th = 0.0f; L.tlo = 0.0f;
             }
-            if (!L.alive) {
+            if (park) {
+                // collided later, in a batch
+            } else if (!L.alive) {
                 fin = 2;
             } else if (boundary) {
                 float E = kin_energy(L.species, L.px, L.py, L.pz);
@@ -1272,6 +1336,30 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         atomicAdd(&tal[T_LSTART + L.k], 1u);
                     }
                 }
+            }
+        }
+
+        if (EVENT) {
+            // park the colliding particles; if the stash is full (possible with
+            // several steps per launch, where lanes keep particles across steps)
+            // the rest collide in place
+            const unsigned pm = __ballot_sync(FULL, park);
+            if (pm) {
+                __syncwarp();
+                const int base = *cs_n;
+                const int space = kCollStash - base;
+                const int rank = __popc(pm & lt);
+                if (park) {
+                    if (rank < space) {
+                        park_lane(L, cs + size_t(base + rank) * 5);
+                        has = false;
+                    } else {
+                        collide<GENERAL>(L, K, H->sp[L.species]);
+                    }
+                }
+                __syncwarp();
+                if (lane == 0) *cs_n = base + min(__popc(pm), space);
+                __syncwarp();
             }
         }
 
@@ -1329,13 +1417,14 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 // The plain kernels (homogeneous field, no wall, no learned sampler) come in 2,
 // 3 and 4 blocks per SM; the general one (position-dependent field, wall
 // crossings, learned samplers) in 3, where it needs no register spills.
-static void (*step_kernel(int minb, bool general))(StepArgs) {
-    if (general) return k_step<3, true>;
-    return (minb == 2) ? k_step<2, false> : (minb == 3) ? k_step<3, false> : k_step<4, false>;
+static void (*step_kernel(int minb, bool general, bool event))(StepArgs) {
+    if (general) return event ? k_step<3, true, true> : k_step<3, true, false>;
+    if (event) return k_step<3, false, true>;
+    return (minb == 2) ? k_step<2, false, false> : (minb == 3) ? k_step<3, false, false> : k_step<4, false, false>;
 }
 
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A) {
-    void (*kern)(StepArgs) = step_kernel(minb, A.general != 0);
+    void (*kern)(StepArgs) = step_kernel(minb, A.general != 0, A.event != 0);
     // the shared-memory attribute is set outside stream capture (prepare_step
     // runs first); during capture the launch is only recorded
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1349,8 +1438,9 @@ cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream
     return cudaGetLastError();
 }
 
-cudaError_t prepare_step(int minb, size_t smem, bool general) {
-    return cudaFuncSetAttribute(step_kernel(minb, general), cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+cudaError_t prepare_step(int minb, size_t smem, bool general, bool event) {
+    return cudaFuncSetAttribute(step_kernel(minb, general, event), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(smem));
 }
 
 // Launch prologue: snapshot the work space and clear per-launch counters.
@@ -1744,9 +1834,10 @@ __global__ void k_learn_pick(const float4* m2, long long n, const float* Yk, lon
 }
 
 // Shared-memory bytes of k_step for a block of `threads`.
-size_t step_smem_bytes(int blob_bytes, int threads) {
+size_t step_smem_bytes(int blob_bytes, int threads, bool event) {
     int nw = threads / 32;
     size_t b = size_t(blob_bytes) + size_t(nw) * kWarpStack * 3 * 16 + size_t(nw) * 4 + T_WORDS * 4 + 64;
+    if (event) b += 16 + size_t(nw) * kCollStash * 5 * 16 + size_t(nw) * 4;
     return (b + 15) & ~size_t(15);
 }
 

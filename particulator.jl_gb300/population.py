@@ -149,7 +149,7 @@ class MultiPopulation:
 
     def __init__(self, *pairs, seed: int = 0, device: int = 0, steps_per_launch: int = 1,
                  compaction_period: int = 0, block_size: int = 0, grid_blocks: int = 0, blocks_per_sm: int = 0,
-                 use_graph: bool = False, **named):
+                 use_graph: bool = False, classic_step: bool = False, **named):
         index = {}
         for name, pop in list(pairs) + list(named.items()):
             key = SPECIES_BY_NAME[name] if isinstance(name, str) else int(name)
@@ -164,6 +164,7 @@ class MultiPopulation:
         cfg.grid_blocks = grid_blocks
         cfg.blocks_per_sm = blocks_per_sm
         cfg.use_graph = 1 if use_graph else 0
+        cfg.classic_step = 1 if classic_step else 0
         self.config = cfg
         h = C.c_void_p()
         rc = _lib.lib().pcl_create(C.byref(cfg), C.byref(h))
@@ -294,15 +295,18 @@ class MultiPopulation:
         self.t = t.t
         for f in ("blocks_per_sm", "steps_per_launch", "compaction_period", "use_graph"):
             setattr(self.config, f, getattr(r, f))
+        self.config.classic_step = 0 if r.blocks_per_sm == 0 else 1
         return {"blocks_per_sm": r.blocks_per_sm, "steps_per_launch": r.steps_per_launch,
                 "compaction_period": r.compaction_period, "use_graph": r.use_graph, "rate": r.rate,
                 "trials": r.trials, "steps": r.steps}
 
     def set_launch(self, blocks_per_sm: int, steps_per_launch: int, compaction_period: int, use_graph: bool):
-        """Set the launch shape (pcl_set_launch)."""
+        """Set the launch shape (pcl_set_launch); blocks_per_sm 0 selects the
+        event step kernel, 2-4 the classic one."""
         _lib.check(_lib.lib().pcl_set_launch(self.ctx, int(blocks_per_sm), int(steps_per_launch),
                                              int(compaction_period), 1 if use_graph else 0), self.ctx, "pcl_set_launch")
         self.config.blocks_per_sm = blocks_per_sm
+        self.config.classic_step = 0 if blocks_per_sm == 0 else 1
         self.config.steps_per_launch = steps_per_launch
         self.config.compaction_period = compaction_period
         self.config.use_graph = 1 if use_graph else 0

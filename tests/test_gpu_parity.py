@@ -120,22 +120,66 @@ def test_graph_matches_plain(pcl, gpu, air):
     a.close(); b.close()
 
 
+@pytest.mark.parametrize("dt", [1e-12, 25e-12])
+def test_classic_kernel_vs_oracle(pcl, oracle, gpu, air, dt):
+    """The classic step kernel (each lane collides in place) against the
+    oracle; every other parity test runs the default event kernel."""
+    mp = _mixed(pcl, air, seed=3 if dt < 1e-11 else 4, classic_step=True)
+    pusher = _pusher(pcl, air)
+    W = _oracle_from(oracle, pcl, mp, air, pusher)
+    pcl.advance(mp, pusher, dt)
+    W.advance(dt, 4)
+    _check(pcl, oracle, mp, W, stol=2 * RTOL * max(1.0, dt / 1e-12 / 3))
+    t = mp.tallies()
+    c = W.counters()
+    diff = np.abs(np.array([list(t.collisions[s]) for s in range(3)]) - c["coll"]).sum()
+    assert diff <= 4 * (c["ties"] + 1), (diff, c["ties"])
+    mp.close()
+
+
+@pytest.mark.parametrize("spl", [1, 4])
+def test_event_kernel_matches_plain(pcl, gpu, air, spl):
+    """Event and plain step kernels over 12 steps of 25 ps: the same draw
+    counts for all but rounding-separated particles, momenta equal to FP32
+    rounding, collision counts equal to 1e-4."""
+    pusher = _pusher(pcl, air, E=2e6)
+    runs = []
+    for ev in (False, True):
+        mp = _mixed(pcl, air, n=(8192, 2048, 1024), seed=14, steps_per_launch=spl, classic_step=not ev)
+        pcl.run(mp, pusher, 12 * 25e-12, 25e-12)
+        runs.append(mp)
+    a, b = runs
+    ta, tb = a.tallies(), b.tallies()
+    ca = np.array([list(ta.collisions[s]) for s in range(3)]); cb = np.array([list(tb.collisions[s]) for s in range(3)])
+    assert np.abs(ca - cb).sum() <= 1e-4 * ca.sum() + 2
+    for k in a.index:
+        pa, pb = a.get(k).particles(), b.get(k).particles()
+        common, ia, ib = np.intersect1d(pa.sid, pb.sid, return_indices=True)
+        assert len(common) >= 0.995 * max(len(pa.sid), len(pb.sid))
+        same = pa.ctr[ia] == pb.ctr[ib]
+        assert same.mean() >= 0.995
+        dp = np.linalg.norm(pa.p[ia] - pb.p[ib], axis=1)[same] / np.linalg.norm(pb.p[ib], axis=1)[same]
+        assert np.quantile(dp, 0.99) < 1e-4, np.quantile(dp, [0.5, 0.99])
+    a.close(); b.close()
+
+
 def test_autotune_keeps_physics(pcl, gpu, air):
     """The autotuner advances real steps and keeps a valid launch shape; the
-    population it leaves equals a plain run of the same number of steps
-    (launch shapes do not change the physics; a multi-step launch keeps the
-    sub-eps remainder of a step as a double-float where separate launches
-    round it to FP32, so a rare particle may differ in its last bits)."""
+    population it leaves equals a plain run of the same number of steps up to
+    FP32 rounding (launch shapes do not change the physics, but the event and
+    classic kernels may round their inlined arithmetic differently, and a
+    multi-step launch keeps the sub-eps remainder of a step as a double-float
+    where separate launches round it to FP32)."""
     pusher = _pusher(pcl, air, E=2e6)
     a = _mixed(pcl, air, n=(2048, 1024, 512), seed=21)
-    r = a.autotune(pusher, 1e-12, steps=480)
-    assert r["blocks_per_sm"] in (2, 3, 4) and r["steps_per_launch"] in (1, 2, 4, 8, 16)
+    r = a.autotune(pusher, 1e-12, steps=512)
+    assert r["blocks_per_sm"] in (0, 2, 3, 4) and r["steps_per_launch"] in (1, 2, 4, 8, 16)
     assert r["compaction_period"] in (2, 4, 8, 16, 32) and r["use_graph"] in (0, 1)
-    assert r["trials"] == 15 and r["steps"] == 480 and r["rate"] > 0
+    assert r["trials"] == 16 and r["steps"] == 512 and r["rate"] > 0
     ta = a.tallies()
-    assert ta.steps == 480
+    assert ta.steps == 512
     b = _mixed(pcl, air, n=(2048, 1024, 512), seed=21)
-    pcl.run(b, pusher, 480e-12, 1e-12)
+    pcl.run(b, pusher, 512e-12, 1e-12)
     tb = b.tallies()
     for s in range(3):
         assert abs(ta.live[s] - tb.live[s]) <= 2 + ta.live[s] // 1000
@@ -144,7 +188,7 @@ def test_autotune_keeps_physics(pcl, gpu, air):
         common, ia, ib = np.intersect1d(pa.sid, pb.sid, return_indices=True)
         assert len(common) >= 0.999 * max(len(pa.sid), len(pb.sid)) - 2
         dp = np.linalg.norm(pa.p[ia] - pb.p[ib], axis=1) / np.maximum(np.linalg.norm(pb.p[ib], axis=1), 1e-300)
-        assert np.mean(dp > 1e-5) <= 1e-3, np.sort(dp)[-5:]
+        assert np.mean(dp > 1e-4) <= 2e-3, np.sort(dp)[-5:]
     a.close(); b.close()
 
 
