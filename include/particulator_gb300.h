@@ -65,6 +65,8 @@ extern "C" {
 #define PCL_PROC_ELASTIC        11  /* Elastic(mass_ratio): isotropic in the centre of mass (slow-electron.jl:133-139) */
 #define PCL_PROC_EXCITATION     12  /* Excitation(threshold): loses the threshold, isotropic (slow-electron.jl:108-114) */
 #define PCL_PROC_NULL_COLLISION 13  /* NullCollision as an explicit table entry (collisions.jl:3,58; lxcat.jl:115-119) */
+#define PCL_PROC_IONIZATION     14  /* Ionization(threshold): two electrons share E - threshold, isotropic (slow-electron.jl:117-127) */
+#define PCL_PROC_ATTACHMENT     15  /* Attachment(threshold): the electron is removed (slow-electron.jl:129-131) */
 
 #define PCL_MAX_PROC      16   /* processes per species table              */
 #define PCL_MAX_ORDER      4   /* Chebyshev terms per interval             */

@@ -75,7 +75,7 @@ constexpr double EPS_T = 2.220446049250313e-16;  // eps(Float64) (mixed_populati
 enum { ELECTRON = 0, PHOTON = 1, POSITRON = 2 };
 enum {
     P_MOLLER = 1, P_RBEB, P_SB, P_COULOMB, P_COMPTON, P_KN, P_PE, P_BH, P_BHABHA, P_ANN, P_ELASTIC, P_EXCITATION,
-    P_NULL
+    P_NULL, P_IONIZATION, P_ATTACHMENT
 };
 enum { E_RATEBOUND = 0, E_TABLE_RANGE, E_REJECT_CAP, E_SUBSTEP_CAP, E_SPILL, E_CAPACITY, E_KINEMATICS, E_NEG_RATE };
 constexpr int REJECT_CAP = 10000;
@@ -819,6 +819,21 @@ static void s_excitation(Walker& Wk, const Proc& P, double eng) {
     L.s = Wk.nextcoll();
 }
 
+// collide(::Ionization, ...) (slow-electron.jl:117-127)
+static void s_ionization(Walker& Wk, const Proc& P, double eng) {
+    Part& L = *Wk.P;
+    double E1 = 0.5 * std::max(0.0, eng - P.p[0]);
+    double pn = momentum_norm_from_kin(E1);
+    double u[3], v[3];
+    randsphere(Wk, u);
+    randsphere(Wk, v);
+    for (int a = 0; a < 3; ++a) L.p[a] = u[a] * pn;
+    L.s = Wk.nextcoll();
+    double cs = Wk.nextcoll();
+    double q[3] = {v[0] * pn, v[1] * pn, v[2] * pn};
+    child(Wk, ELECTRON, q, cs, 0);
+}
+
 static void sample(Walker& Wk, const Proc& P, int species, double eng) {
     switch (P.kind) {
         case P_COULOMB: s_coulomb(Wk, P, species); break;
@@ -833,6 +848,8 @@ static void sample(Walker& Wk, const Proc& P, int species, double eng) {
         case P_ANN: s_ann(Wk, eng); break;
         case P_ELASTIC: s_elastic(Wk, P); break;
         case P_EXCITATION: s_excitation(Wk, P, eng); break;
+        case P_IONIZATION: s_ionization(Wk, P, eng); break;
+        case P_ATTACHMENT: Wk.P->active = false; break;  // RemoveParticleOutcome
         case P_NULL: Wk.P->s = Wk.nextcoll(); break;  // NullOutcome (collisions.jl:83-88)
         default: Wk.err(E_KINEMATICS); break;
     }

@@ -9,10 +9,12 @@ from . import _lib, constants, data
 from ._lib import (ELECTRON, PHOTON, POSITRON, PCLError, lib, LIB_PATH)
 from .processes import (Moller, RBEB, SeltzerBerger, RelativisticCoulomb, Compton, KleinNishinaCompton,
                         PhotoElectric, BetheHeitler, Bhaba, Bhabha, PositronAnihilation, PositronAnnihilation,
-                        N2_ORBITALS, O2_ORBITALS, ORBITALS, totalcs, Elastic, Excitation, NullCollision)
+                        N2_ORBITALS, O2_ORBITALS, ORBITALS, totalcs, Elastic, Excitation, NullCollision, Ionization,
+                        Attachment)
 from .tables import (Electron, Photon, Positron, BinaryIntervals, ChebyshevCollisionTable,
                      collision_table_from_processes, ContinuumLoss, ChebContinuumLoss, speed,
-                     momentum_norm_from_kin, precheb, CollisionTable, lxcat_table, ratebound_split)
+                     momentum_norm_from_kin, precheb, CollisionTable, lxcat_table, ratebound_split, load_lxcat,
+                     lxcat_collision_table, LXCatSet)
 from .forcing import (HomogeneousField, DoubleLayerField, StepField, ConfinedDoubleLayerField, ElectromagneticField,
                       NullForcing, CombinedForcing, RK2Pusher)
 from .population import (ElectronState, PhotonState, PositronState, ParticleArrays, Population, MultiPopulation,

@@ -40,6 +40,8 @@ PROC_ANNIHILATION = 10
 PROC_ELASTIC = 11
 PROC_EXCITATION = 12
 PROC_NULL_COLLISION = 13
+PROC_IONIZATION = 14
+PROC_ATTACHMENT = 15
 
 MAX_PROC = 16
 NERR = 8

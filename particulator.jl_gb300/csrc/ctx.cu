@@ -284,6 +284,8 @@ static void pack_proc(const pcl_process& P, int sbi, DevProc& D) {
             D.p[0] = float(P.param[0]);
             break;
         case PCL_PROC_EXCITATION:
+        case PCL_PROC_IONIZATION:
+        case PCL_PROC_ATTACHMENT:
             D.p[0] = float(P.param[0] / mc2);
             break;
         default:
@@ -920,7 +922,7 @@ int pcl_set_collision_table(void* ctx, int species, int order, int nproc, int ni
     CK(cudaSetDevice(c->device));
     for (int j = 0; j < nproc; ++j) {
         const pcl_process& P = procs[j];
-        if (P.kind < PCL_PROC_MOLLER || P.kind > PCL_PROC_NULL_COLLISION)
+        if (P.kind < PCL_PROC_MOLLER || P.kind > PCL_PROC_ATTACHMENT)
             return fail(c, PCL_ERR_UNSUPPORTED, "unsupported process kind");
         if (P.kind == PCL_PROC_SELTZER_BERGER) {
             if (!P.aux0 || !P.aux2 || P.naux < 2 || P.naux2 < 2)
@@ -966,7 +968,8 @@ int pcl_set_linear_table(void* ctx, int species, int nproc, int n, double e0, do
         return fail(c, PCL_ERR_INVALID, "bad linear collision table");
     for (int j = 0; j < nproc; ++j)
         if (procs[j].kind != PCL_PROC_ELASTIC && procs[j].kind != PCL_PROC_EXCITATION &&
-            procs[j].kind != PCL_PROC_NULL_COLLISION && procs[j].kind != PCL_PROC_REL_COULOMB)
+            procs[j].kind != PCL_PROC_NULL_COLLISION && procs[j].kind != PCL_PROC_REL_COULOMB &&
+            procs[j].kind != PCL_PROC_IONIZATION && procs[j].kind != PCL_PROC_ATTACHMENT)
             return fail(c, PCL_ERR_UNSUPPORTED, "process kind not supported on a linear-grid table");
     SpeciesState& S = c->sp[species];
     S.table_kind = 1;

@@ -879,6 +879,21 @@ __device__ PCL_RARE void s_excitation(Lane& L, const KCtx& K, const DevProc& P, 
     L.s = nextcoll(L, K);
 }
 
+// collide(::Ionization, ...) (slow-electron.jl:117-127): the primary and a new
+// electron share E - threshold equally, each isotropic; draws: both
+// directions, then the primary's s (its state constructor) and the new one's.
+__device__ PCL_RARE void s_ionization(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+    const float E1 = 0.5f * fmaxf(0.0f, E - P.p[0]);
+    const float pn = sqrtf(E1 * (E1 + 2.0f));
+    float ux, uy, uz, vx, vy, vz;
+    randsphere(L, K, ux, uy, uz);
+    randsphere(L, K, vx, vy, vz);
+    L.px = ux * pn; L.py = uy * pn; L.pz = uz * pn;
+    L.s = nextcoll(L, K);
+    const float cs = nextcoll(L, K);
+    emit(L, K, PCL_ELECTRON, vx * pn, vy * pn, vz * pn, cs, 0, ctr0);
+}
+
 // Dispatch one real collision with table position j; updates the primary
 // (state change + setr!) or removes it, and emits secondaries (apply!,
 // collisions.jl:83-133).
@@ -897,6 +912,8 @@ __device__ void sample_process(Lane& L, const KCtx& K, const SpeciesHdr& S, cons
         case PCL_PROC_ANNIHILATION: s_annihilation(L, K, E, ctr0); break;
         case PCL_PROC_ELASTIC: s_elastic(L, K, P); break;
         case PCL_PROC_EXCITATION: s_excitation(L, K, P, E); break;
+        case PCL_PROC_IONIZATION: s_ionization(L, K, P, E, ctr0); break;
+        case PCL_PROC_ATTACHMENT: L.alive = false; break;   // RemoveParticleOutcome
         case PCL_PROC_NULL_COLLISION: L.s = nextcoll(L, K); break;  // NullOutcome (collisions.jl:83-88)
         default: err(K, PCL_E_KINEMATICS); break;
     }

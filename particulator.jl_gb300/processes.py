@@ -217,6 +217,32 @@ class Excitation(_Proc):
         p.nparam = 1
 
 
+class Ionization(_Proc):
+    """Ionization(threshold) (slow-electron.jl:74-76, 117-127): two electrons
+    share the energy above the threshold equally, both isotropic."""
+    kind = _lib.PROC_IONIZATION
+
+    def __init__(self, threshold: float):
+        self.threshold = float(threshold)
+
+    def _fill(self, p):
+        p.param[0] = self.threshold
+        p.nparam = 1
+
+
+class Attachment(_Proc):
+    """Attachment(threshold) (slow-electron.jl:78-80, 129-131): the electron is
+    removed."""
+    kind = _lib.PROC_ATTACHMENT
+
+    def __init__(self, threshold: float = 0.0):
+        self.threshold = float(threshold)
+
+    def _fill(self, p):
+        p.param[0] = self.threshold
+        p.nparam = 1
+
+
 class NullCollision(_Proc):
     """NullCollision (collisions.jl:3, 58) as an explicit table entry."""
     kind = _lib.PROC_NULL_COLLISION

@@ -227,3 +227,96 @@ def ratebound_split(tab: ChebyshevCollisionTable, safety: float = 1.1):
                                         _lib.dptr(rate), float(safety), _lib.dptr(A), _lib.dptr(B))
     _lib.check(rc, None, "pcl_ratebound_split")
     return A, B
+
+
+@dataclass
+class LXCatSet:
+    """What load_lxcat returns (lxcat.jl:17-134): processes and their rates
+    (nproc x len(energy), the null process included, sorted by the rate summed
+    over the grid, descending), the maximum total rate (the rate bound) and the
+    permutation back to the reading order."""
+    proc: tuple
+    rate: np.ndarray
+    maxrate: float
+    origperm: np.ndarray
+
+
+def load_lxcat(fnames, densities: dict, energy, photon_weight: float = 1.0,
+               photon_multiplier: float = 1.0) -> LXCatSet:
+    """load_lxcat(fnames, densities, energy; photon_weight, photon_multiplier)
+    (lxcat.jl:17-134).  Reads LXCat-style JSON files (a list of items with
+    target, kind, data [[E (eV), sigma (m^2)], ...], comment, and optional
+    rescale / weight_scale / threshold / mass_ratio), keeps the targets with a
+    density, interpolates each cross section linearly in energy (flat outside
+    its data) onto `energy` (J), scales by density and speed v = sqrt(2 E / m),
+    turns EFFECTIVE into ELASTIC by subtracting the target's excitation and
+    ionization rates (ensure_elastic, lxcat.jl:146-156) and adds the null
+    process up to the maximum total rate.  Targets are taken in reading order
+    (the reference iterates a Dict; the final order only depends on it for
+    equal summed rates).  PHOTOEMISSION items need the slow-electron photon
+    model, which has no device implementation, and are rejected."""
+    import json
+    from .processes import Elastic, Excitation, Ionization, Attachment, NullCollision
+    if isinstance(fnames, (str, bytes)):
+        fnames = [fnames]
+    db = []
+    for fn in fnames:
+        with open(fn) as f:
+            db.extend(json.load(f))
+    energy = np.asarray(energy, dtype=float)
+    v = np.sqrt(2 * energy / co.electron_mass)
+    targets: dict = {}
+    for item in db:
+        dens = float(densities.get(item["target"], 0.0))
+        if dens == 0.0:
+            continue
+        e0 = np.array([q[0] for q in item["data"]], dtype=float) * co.eV
+        cs0 = np.array([q[1] for q in item["data"]], dtype=float)
+        if "3-body" in item.get("comment", ""):
+            cs0 = cs0 * densities[item["target"]] / co.centi ** -3
+        if "rescale" in item:
+            cs0 = cs0 * item["rescale"]
+        if "weight_scale" in item:
+            cs0 = cs0 * item["weight_scale"]
+        if item["kind"] == "PHOTOEMISSION":
+            raise NotImplementedError("PHOTOEMISSION has no device implementation")
+        it = dict(item)
+        it["nu"] = dens * v * np.interp(energy, e0, cs0)
+        targets.setdefault(item["target"], []).append(it)
+    kinds = {"ATTACHMENT": lambda itm: Attachment(itm.get("threshold", 0.0) * co.eV),
+             "EXCITATION": lambda itm: Excitation(itm["threshold"] * co.eV),
+             "IONIZATION": lambda itm: Ionization(itm["threshold"] * co.eV),
+             "ELASTIC": lambda itm: Elastic(itm["mass_ratio"])}
+    procs, rows = [], []
+    for name, ps in targets.items():
+        for p in ps:  # ensure_elastic
+            if p["kind"] != "EFFECTIVE":
+                continue
+            for p2 in ps:
+                if p2 is not p and p2["kind"] in ("EXCITATION", "IONIZATION"):
+                    p["nu"] = p["nu"] - p2["nu"]
+            p["kind"] = "ELASTIC"
+        for p in ps:
+            procs.append(kinds[p["kind"]](p))
+            rows.append(p["nu"])
+    rate = np.array(rows) if rows else np.zeros((0, len(energy)))
+    total = rate.sum(axis=0)
+    maxrate = float(total.max()) if len(rows) else 0.0
+    procs.append(NullCollision())
+    rate = np.vstack([rate, maxrate - total])
+    inteng = rate.sum(axis=1)
+    perm = sorted(range(len(procs)), key=lambda j: -inteng[j])
+    origperm = np.argsort(perm)
+    return LXCatSet(tuple(procs[j] for j in perm), np.ascontiguousarray(rate[perm]), maxrate, origperm)
+
+
+def lxcat_collision_table(fnames, densities: dict, energy, particle: int = Electron, **kw) -> CollisionTable:
+    """CollisionTable on the linear grid `energy` (equally spaced, J) from
+    load_lxcat, with its maximum total rate as the constant rate bound."""
+    energy = np.asarray(energy, dtype=float)
+    n = len(energy)
+    step = (energy[-1] - energy[0]) / (n - 1)
+    if not np.allclose(np.diff(energy), step, rtol=1e-9, atol=0.0):
+        raise ValueError("the energy grid must be equally spaced")
+    r = load_lxcat(fnames, densities, energy, **kw)
+    return CollisionTable(r.proc, (float(energy[0]), float(energy[-1]), n), r.rate, np.array([r.maxrate]), particle)

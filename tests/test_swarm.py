@@ -211,3 +211,80 @@ def test_swarm_moments(pcl, gpu):
                (g.w * g.x[:, 2] ** 2)[q].sum(), (g.w * (g.x[:, 0] ** 2 + g.x[:, 1] ** 2))[q].sum()]
         np.testing.assert_allclose(m[s], ref, rtol=1e-5, atol=1e-30)
     b.mpopl.close()
+
+
+# ------------------------------------------------------------ LXCat loader --
+_LXCAT = [
+    {"target": "X", "kind": "EFFECTIVE", "mass_ratio": 2e-5, "comment": "made-up test set",
+     "data": [[0.0, 5e-20], [10.0, 8e-20], [100.0, 4e-20]]},
+    {"target": "X", "kind": "EXCITATION", "threshold": 5.0, "comment": "",
+     "data": [[5.0, 0.0], [20.0, 2e-20], [100.0, 1e-20]]},
+    {"target": "X", "kind": "IONIZATION", "threshold": 12.0, "comment": "",
+     "data": [[12.0, 0.0], [50.0, 3e-20], [100.0, 2e-20]]},
+    {"target": "X", "kind": "ATTACHMENT", "threshold": 0.0, "comment": "",
+     "data": [[0.0, 1e-22], [2.0, 5e-22], [100.0, 0.0]]},
+    {"target": "Y", "kind": "ELASTIC", "mass_ratio": 1e-5, "comment": "no density given: skipped",
+     "data": [[0.0, 1e-20], [100.0, 1e-20]]},
+]
+
+
+@pytest.fixture
+def lxcat_file(tmp_path):
+    import json
+    f = tmp_path / "set.json"
+    f.write_text(json.dumps(_LXCAT))
+    return str(f)
+
+
+def test_load_lxcat(pcl, lxcat_file):
+    """load_lxcat (lxcat.jl:17-156): densities, linear interpolation, the
+    EFFECTIVE -> ELASTIC correction, the null process and the ordering."""
+    N = 2e25
+    E = np.linspace(0.0, 100.0 * EV, 2001)
+    r = pcl.load_lxcat([lxcat_file], {"X": N}, E)
+    names = [type(p).__name__ for p in r.proc]
+    assert sorted(names) == ["Attachment", "Elastic", "Excitation", "Ionization", "NullCollision"]
+    inteng = r.rate.sum(axis=1)
+    assert np.all(np.diff(inteng) <= 0)
+    v = np.sqrt(2 * E / pcl.co.electron_mass)
+    sig = {k: np.interp(E / EV, [q[0] for q in it["data"]], [q[1] for q in it["data"]])
+           for k, it in zip(("eff", "exc", "ion", "att"), _LXCAT[:4])}
+    el = r.rate[names.index("Elastic")]
+    np.testing.assert_allclose(el, N * v * (sig["eff"] - sig["exc"] - sig["ion"]), rtol=1e-12, atol=1e-3)
+    np.testing.assert_allclose(r.rate[names.index("Ionization")], N * v * sig["ion"], rtol=1e-12)
+    tot = r.rate.sum(axis=0)
+    np.testing.assert_allclose(tot, r.maxrate, rtol=1e-12)
+    assert r.proc[names.index("Ionization")].threshold == pytest.approx(12 * EV)
+    # origperm maps the sorted order back to the reading order (EFFECTIVE first)
+    assert type(r.proc[r.origperm[0]]).__name__ == "Elastic"
+    tab = pcl.lxcat_collision_table([lxcat_file], {"X": N}, E)
+    assert tab.nproc == 5 and tab.energy[2] == 2001
+
+
+@pytest.mark.gpu
+def test_lxcat_swarm_parity(pcl, oracle, gpu, lxcat_file):
+    """A swarm on the loaded set at 300 Td (ionization and attachment both
+    active) against the oracle: secondaries from ionization, removals from
+    attachment, momenta within 1e-5."""
+    N = 2e25
+    E = np.linspace(0.0, 100.0 * EV, 2001)
+    tab = pcl.lxcat_collision_table([lxcat_file], {"X": N}, E)
+    pusher = pcl.workloads.pusher((0.0, 0.0, -300.0 * pcl.co.Td * N))
+    n = 4096
+    rng = np.random.default_rng(9)
+    p = _maxwell(pcl, n, 8.0, 9)
+    arr = pcl.ParticleArrays(np.zeros((n, 3)), p, np.ones(n), np.zeros(n))
+    mp = pcl.MultiPopulation(("electron", pcl.Population(8 * n, arr, tab, 0.0, particle=pcl.Electron)), seed=9)
+    W = oracle.OracleWorld(9, {pcl.Electron: tab}, {pcl.Electron: 0.0}, pusher)
+    W.upload(pcl.Electron, mp.get(pcl.Electron).particles())
+    for k in range(4):
+        pcl.advance(mp, pusher, (k + 1) * 1e-12)
+        W.advance((k + 1) * 1e-12, 4)
+    t = mp.tallies()
+    names = [type(q).__name__ for q in tab.proc]
+    assert t.collisions[0][names.index("Ionization")] > 100 and t.collisions[0][names.index("Attachment")] > 0
+    assert t.spawned[0] > 100
+    rep = oracle.compare_populations(mp.get(pcl.Electron).particles(), W.download(pcl.Electron), pcl.Electron,
+                                     rtol=1e-5, stol=2e-4)
+    assert rep["ok"], str(rep)
+    mp.close()
