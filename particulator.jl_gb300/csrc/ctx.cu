@@ -17,7 +17,7 @@ extern "C" int pcl_ratebound_split(int, int, int, int, double, const double*, do
 
 namespace pcl {
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A);
-cudaError_t prepare_step(int minb, size_t smem, bool general, bool event);
+cudaError_t prepare_step(int minb, size_t smem, bool general, bool event, bool learn);
 __global__ void k_learn_hist(StepArgs A, int species, int j, int kind, int nT, long long per_T, int nbins,
                              float hmin, float hmax, unsigned long long sid_base, unsigned int* hist);
 __global__ void k_learn_x(const float4* ps, const float4* m2, long long n, float* X);
@@ -466,7 +466,8 @@ static StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, int sp_
     A.blob_bytes = int(c->blob.size());
     A.wall_xw = c->d_wall_xw; A.wall_pt = c->d_wall_pt; A.wall_meta = c->d_wall_meta;
     A.wall_n = c->d_wall_n; A.wall_cap = c->wall_cap;
-    A.general = (c->field_kind != 0 || c->learn_on) ? 1 : 0;
+    A.general = (c->field_kind != 0) ? 1 : 0;
+    A.learn = c->learn_on ? 1 : 0;
     for (int s = 0; s < 3; ++s)
         if (c->sp[s].wall_coord >= 0 && c->wall_cap > 0) A.general = 1;
     A.event = (c->cfg.classic_step == 0) ? 1 : 0;
@@ -617,7 +618,7 @@ static int run_group_graph(Ctx* c, const StepArgs& A, const StepArgs& P0, const 
     for (auto& g : c->graphs)
         if (g.key == key) { exec = g.exec; break; }
     if (!exec) {
-        CK(prepare_step(minb, smem, A.general != 0, A.event != 0));
+        CK(prepare_step(minb, smem, A.general != 0, A.event != 0, A.learn != 0));
         CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         cudaError_t e = cudaSuccess;
         auto q = [&e](cudaError_t r) { if (e == cudaSuccess) e = r; };

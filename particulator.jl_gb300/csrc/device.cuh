@@ -147,6 +147,7 @@ struct StepArgs {
     long long wall_cap;
     int general;    // a position-dependent field or a wall is set: the general step kernel runs
     int event;      // the event step kernel runs (parked collisions in full-warp batches)
+    int learn;      // learned samplers attached: the kernel with suspend/resume runs
 };
 
 // Network index of each (species, table position) with a learned sampler (-1: none).

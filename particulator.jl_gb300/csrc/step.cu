@@ -1115,7 +1115,7 @@ __device__ __forceinline__ void load_slot(Lane& L, const float4* xw, const float
 // batches that fill the warp's free lanes (see the loop), instead of each lane
 // colliding as soon as its push ends; each particle's sequence of operations
 // is unchanged.
-template <int MINB, bool GENERAL, bool EVENT>
+template <int MINB, bool GENERAL, bool EVENT, bool LEARN>
 __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwarps = blockDim.x >> 5;
@@ -1162,7 +1162,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 
     // work space: concatenated species ranges, or the spill queue
     long long nsp0, nsp1, total;
-    if (GENERAL && A.spill_mode == 2) {
+    if (LEARN && A.spill_mode == 2) {
         nsp0 = 0; nsp1 = 0;
         total = min((long long)(*A.lq_in_n), A.lq_cap);
     } else if (A.spill_mode) {
@@ -1196,7 +1196,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 if (!has && rank < take) {
                     unpark_lane(L, cs + size_t(nstash - 1 - rank) * 5);
                     has = true;
-                    collide<GENERAL>(L, K, H->sp[L.species]);
+                    collide<LEARN>(L, K, H->sp[L.species]);
                 }
                 __syncwarp();
                 if (lane == 0) *cs_n = nstash - take;
@@ -1251,7 +1251,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 int rk = __popc(need & lt);
                 if (!has && rk < tk) {
                     long long v = cur + rk;
-                    if (GENERAL && A.spill_mode == 2) {
+                    if (LEARN && A.spill_mode == 2) {
                         float4 a = A.lq_in_xw[v], b = A.lq_in_ps[v];
                         uint4 m1 = A.lq_in_m1[v];
                         float4 m2 = A.lq_in_m2[v];
@@ -1290,7 +1290,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         has = (L.ctr != PCL_DEAD_CTR);
                         if (has) atomicAdd(&tal[T_LSTART + 0], 1u);
                     }
-                    if (has && !(GENERAL && A.spill_mode == 2)) {
+                    if (has && !(LEARN && A.spill_mode == 2)) {
                         L.rvalid = false; L.alive = true; L.nsub = 0;
                         L.sw = (H->nswarm > 0) ? min(int(L.sid_hi >> 24), H->nswarm - 1) : 0;
                         L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz), L.sw);
@@ -1326,7 +1326,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 else { L.th = 0.0f; L.tlo = 0.0f; }
                 L.nsub += 1;
                 if (EVENT) park = coll && L.alive;
-                else if (coll && L.alive) collide<GENERAL>(L, K, S);
+                else if (coll && L.alive) collide<LEARN>(L, K, S);
                 // advance1!'s loop ends once the clock is spent (mixed_population.jl:66)
                 boundary = !park && !(dd_val(L.th, L.tlo) > kEpsT);
             } else if (L.nsub >= kSubstepCap) {
@@ -1371,7 +1371,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         park_lane(L, cs + size_t(base + rank) * 5);
                         has = false;
                     } else {
-                        collide<GENERAL>(L, K, H->sp[L.species]);
+                        collide<LEARN>(L, K, H->sp[L.species]);
                     }
                 }
                 __syncwarp();
@@ -1431,17 +1431,22 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 
 // The step kernel is instantiated for 2, 3 and 4 resident 256-thread blocks
 // per SM (register budgets 128, 85 and 64); the launch shape is a tunable.
-// The plain kernels (homogeneous field, no wall, no learned sampler) come in 2,
-// 3 and 4 blocks per SM; the general one (position-dependent field, wall
-// crossings, learned samplers) in 3, where it needs no register spills.
-static void (*step_kernel(int minb, bool general, bool event))(StepArgs) {
-    if (general) return event ? k_step<3, true, true> : k_step<3, true, false>;
-    if (event) return k_step<3, false, true>;
-    return (minb == 2) ? k_step<2, false, false> : (minb == 3) ? k_step<3, false, false> : k_step<4, false, false>;
+// Instantiations: the classic kernels in 2, 3 and 4 blocks per SM, the event
+// kernel in 3 (its stash), each with or without the learned samplers'
+// suspend/resume (LEARN); the general kernel (position-dependent field, wall
+// crossings; learned samplers included) in 3, where it needs no register
+// spills.  Code a launch does not use stays out of its kernel.
+static void (*step_kernel(int minb, bool general, bool event, bool learn))(StepArgs) {
+    if (general) return event ? k_step<3, true, true, true> : k_step<3, true, false, true>;
+    if (learn) return event ? k_step<3, false, true, true> : k_step<3, true, false, true>;
+    if (event) return k_step<3, false, true, false>;
+    return (minb == 2)   ? k_step<2, false, false, false>
+           : (minb == 3) ? k_step<3, false, false, false>
+                         : k_step<4, false, false, false>;
 }
 
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A) {
-    void (*kern)(StepArgs) = step_kernel(minb, A.general != 0, A.event != 0);
+    void (*kern)(StepArgs) = step_kernel(minb, A.general != 0, A.event != 0, A.learn != 0);
     // the shared-memory attribute is set outside stream capture (prepare_step
     // runs first); during capture the launch is only recorded
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1455,8 +1460,8 @@ cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream
     return cudaGetLastError();
 }
 
-cudaError_t prepare_step(int minb, size_t smem, bool general, bool event) {
-    return cudaFuncSetAttribute(step_kernel(minb, general, event), cudaFuncAttributeMaxDynamicSharedMemorySize,
+cudaError_t prepare_step(int minb, size_t smem, bool general, bool event, bool learn) {
+    return cudaFuncSetAttribute(step_kernel(minb, general, event, learn), cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(smem));
 }
 
