@@ -234,6 +234,8 @@ def run_swarms(args, pcl):
     L.pcl_sync(mp.ctx)
     tal0 = mp.tallies()
     L.pcl_kernel_stats(mp.ctx, None, None, None, None, 1)
+    cap = 1 << 20   # each swarm held at 2^20 electrons (device roulette after every launch group)
+    mp.set_swarm_cap(cap, particles=(pcl.Electron,))
     with Clocks(0) as clk:
         L.pcl_timer_start(mp.ctx)
         t += steps * dt
@@ -281,7 +283,7 @@ def run_swarms(args, pcl):
             "ms_per_step": ms.value / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"swarms{nsw}-air-0.3-3MVm", "nswarm": nsw, "seed_electrons": int(init[1].sum()),
-                       "dt_s": dt, "autotuned": tune,
+                       "dt_s": dt, "autotuned": tune, "swarm_cap": 1 << 20,
                        "live_at_end": list(tal1.live), "max_swarm_live": int(mom[:, 0].max())},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None, "kernel": "k_step"},

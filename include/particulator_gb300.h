@@ -265,6 +265,10 @@ int pcl_set_field(void* ctx, int kind, const double* params, int nparams);
  * stream ids derived from the parent's).  As RouletteCallback / SplitCallback
  * (callback.jl:210-247) do, follow with pcl_compact. */
 int pcl_roulette(void* ctx, int species, double pkeep);
+/* Batched swarms: roulette! with keep probability pkeep[s] for swarm s (the
+ * top 8 bits of the stream id); pkeep >= 1 leaves a swarm untouched.  Used to
+ * hold each swarm at a population cap. */
+int pcl_roulette_swarms(void* ctx, int species, int nswarm, const double* pkeep);
 int pcl_split(void* ctx, int species, double p);
 int pcl_set_wall(void* ctx, int species, int coord, double v, int drop, int64_t capacity);
 int pcl_get_wall(void* ctx, int64_t* n, int32_t* species, uint64_t* sid, double* x, double* p, double* w,
@@ -284,6 +288,17 @@ int pcl_set_swarms(void* ctx, int nswarm, const double* E, const double* Fdt, do
 /* Per-swarm FP64 moments of one species: out[6*s + q] = {live, sum w,
  * sum w E (J), sum w z, sum w z^2, sum w (x^2 + y^2)} (m). */
 int pcl_swarm_moments(void* ctx, int species, int nswarm, double* out);
+/* Live particles of each swarm of one species (out[s], s < nswarm; with
+ * nswarm = 1 the whole population). */
+int pcl_swarm_counts(void* ctx, int species, int nswarm, int64_t* out);
+/* RouletteCallback(m) (callback.jl:210-227) on the device, per swarm: after
+ * every launch group of pcl_run, each swarm of `species` (the whole
+ * population when no swarms are set) with n > cap live particles gets
+ * roulette!(cap / n).  Counting and roulette run on the context stream with
+ * no host read-back; the removed particles are compacted with the next
+ * periodic compaction.  The reference checks after every step: with
+ * steps_per_launch = 1 so does this.  cap = 0 turns the cap off. */
+int pcl_set_swarm_cap(void* ctx, int species, int64_t cap);
 
 /* Replace the species' population with n particles (SI, FP64): x[3n], p[3n]
  * (interleaved xyz), w[n], t[n] (absolute, s).  s[n] = normalised time to the

@@ -110,10 +110,13 @@ _SIGS = {
     "pcl_set_field": (C.c_int, [C.c_void_p, C.c_int, _P(_d), C.c_int]),
     "pcl_roulette": (C.c_int, [C.c_void_p, C.c_int, _d]),
     "pcl_split": (C.c_int, [C.c_void_p, C.c_int, _d]),
+    "pcl_roulette_swarms": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_d)]),
     "pcl_set_wall": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _d, C.c_int, _i64]),
     "pcl_get_wall": (C.c_int, [C.c_void_p, _P(_i64), _P(_i32), _P(_u64), _P(_d), _P(_d), _P(_d), _P(_d)]),
     "pcl_set_swarms": (C.c_int, [C.c_void_p, C.c_int, _P(_d), _P(_d), _d]),
     "pcl_swarm_moments": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_d)]),
+    "pcl_swarm_counts": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_i64)]),
+    "pcl_set_swarm_cap": (C.c_int, [C.c_void_p, C.c_int, _i64]),
     "pcl_upload": (C.c_int, [C.c_void_p, C.c_int, _i64, _P(_d), _P(_d), _P(_d), _P(_d), _P(_d), _P(_u64),
                              _u64]),
     "pcl_download": (C.c_int, [C.c_void_p, C.c_int, _P(_i64), _P(_d), _P(_d), _P(_d), _P(_d), _P(_d),

@@ -25,6 +25,13 @@ __global__ void k_roulette(float4* xw, uint4* meta, long long n, float pkeep, ui
                            unsigned long long* dead);
 __global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, uint32_t k0,
                         uint32_t k1, unsigned long long* nslots, unsigned long long* lost);
+__global__ void k_roulette_swarms(float4* xw, uint4* meta, long long n, const float* pkeep, int nswarm, uint32_t k0,
+                                  uint32_t k1, unsigned long long* dead);
+__global__ void k_swarm_count(const uint4* meta, const unsigned long long* nslots, long long cap, int nswarm,
+                              unsigned int* counts);
+__global__ void k_roulette_cap(float4* xw, uint4* meta, const unsigned long long* nslots, long long slot_cap,
+                               const unsigned int* counts, int nswarm, unsigned long long cap, uint32_t k0,
+                               uint32_t k1);
 __global__ void k_learn_pick(const float4* m2, long long n, const float* Yk, long long stride, LearnPick which,
                              float* Y);
 namespace mlp {
@@ -39,7 +46,8 @@ __global__ void k_compact_scatter(CompactArgs C);
 __global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta, long long n, int species,
                           double* out);
 __global__ void k_swarm_moments(const float4* xw, const float4* ps, const uint4* meta, long long n, int species,
-                                int nswarm, double* out);
+                                int nswarm, double* partial);
+__global__ void k_swarm_reduce(const double* partial, int nblocks, int len, double* out);
 __global__ void k_test_sampler(StepArgs A, int species, int j, long long n, const float* p_in,
                                const uint32_t* sid, float* out_p, float* out_s, int* out_kind,
                                uint32_t* out_ctr);
@@ -133,6 +141,10 @@ struct Ctx {
     unsigned long long* d_nnew = nullptr;
     long long tiles_cap = 0;
     double* d_mom = nullptr;
+    void* d_scr = nullptr;                 // reusable scratch of the moment and roulette entry points
+    size_t scr_bytes = 0;
+    unsigned int* d_swcnt = nullptr;       // [3][256] live particles per swarm
+    long long swarm_cap[3] = {0, 0, 0};    // pcl_set_swarm_cap, 0 = off
     // accumulated host state
     double t = 0.0;
     long long steps = 0;
@@ -551,6 +563,42 @@ static int readback(Ctx* c) {
     return PCL_OK;
 }
 
+// Device scratch of at least `bytes`, kept across calls (grown by doubling).
+static int ensure_scratch(Ctx* c, size_t bytes) {
+    if (bytes <= c->scr_bytes) return PCL_OK;
+    const size_t nb = std::max(bytes, 2 * c->scr_bytes);
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaFree(c->d_scr));
+    c->d_scr = nullptr;
+    c->scr_bytes = 0;
+    CK(cudaMalloc(&c->d_scr, nb));
+    c->scr_bytes = nb;
+    return PCL_OK;
+}
+
+// The per-swarm population cap (pcl_set_swarm_cap) after a launch group:
+// count the live particles of each swarm, then roulette the swarms above the
+// cap, both on the context stream with the slot count read on the device.
+// Removed particles stay as dead slots until the next compaction.
+static int apply_swarm_caps(Ctx* c) {
+    for (int s = 0; s < 3; ++s) {
+        SpeciesState& S = c->sp[s];
+        if (c->swarm_cap[s] <= 0 || S.cap <= 0) continue;
+        const int ns = std::max(1, c->nswarm);
+        unsigned int* cnt = c->d_swcnt + 256 * s;
+        const int grid = int(std::min<long long>((S.cap + 255) / 256, 4ll * c->sm_count));
+        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned int) * ns, c->stream));
+        k_swarm_count<<<grid, 256, 0, c->stream>>>(S.meta[S.cur], &c->d_ctl->n[s], S.cap, ns, cnt);
+        CK(cudaGetLastError());
+        k_roulette_cap<<<grid, 256, 0, c->stream>>>(S.xw[S.cur], S.meta[S.cur], &c->d_ctl->n[s], S.cap, cnt, ns,
+                                                    (unsigned long long)c->swarm_cap[s], uint32_t(c->cfg.seed),
+                                                    uint32_t(c->cfg.seed >> 32));
+        CK(cudaGetLastError());
+        c->launches += 2;
+    }
+    return PCL_OK;
+}
+
 static CompactArgs make_compact_args(Ctx* c) {
     CompactArgs C;
     std::memset(&C, 0, sizeof(C));
@@ -838,6 +886,7 @@ int pcl_create(const pcl_config* cfg, void** out) {
         cudaMalloc(&c->d_spn, 2 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&c->d_nnew, 3 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&c->d_mom, 16 * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&c->d_swcnt, 3 * 256 * sizeof(unsigned int)) != cudaSuccess ||
         cudaEventCreate(&c->ev_k0) != cudaSuccess || cudaEventCreate(&c->ev_k1) != cudaSuccess ||
         cudaEventCreate(&c->ev_t0) != cudaSuccess || cudaEventCreate(&c->ev_t1) != cudaSuccess) {
         pcl_destroy(c);
@@ -860,7 +909,7 @@ void pcl_destroy(void* ctx) {
     for (auto& t : c->sb) cudaFree(t.d_data);
     for (int b = 0; b < 2; ++b) { cudaFree(c->sp_xw[b]); cudaFree(c->sp_ps[b]); cudaFree(c->sp_meta[b]); }
     cudaFree(c->d_spn); cudaFree(c->d_blob); cudaFree(c->d_ctl); cudaFree(c->d_tile_cnt);
-    cudaFree(c->d_tile_off); cudaFree(c->d_nnew); cudaFree(c->d_mom);
+    cudaFree(c->d_tile_off); cudaFree(c->d_nnew); cudaFree(c->d_mom); cudaFree(c->d_scr); cudaFree(c->d_swcnt);
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
     if (c->h_spn) cudaFreeHost(c->h_spn);
     free_lq(c);
@@ -1045,6 +1094,36 @@ int pcl_roulette(void* ctx, int species, double pkeep) {
     return PCL_OK;
 }
 
+int pcl_roulette_swarms(void* ctx, int species, int nswarm, const double* pkeep) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !pkeep || nswarm < 1 || nswarm > 256) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    std::vector<float> q(nswarm);
+    for (int i = 0; i < nswarm; ++i) {
+        if (!(pkeep[i] > 0.0)) return fail(c, PCL_ERR_INVALID, "keep probabilities must be > 0");
+        q[i] = float(std::min(1.0, pkeep[i]));
+    }
+    CK(cudaSetDevice(c->device));
+    SpeciesState& S = c->sp[species];
+    long long n = 0;
+    if (S.cap <= 0 || (rc = get_n(c, species, n)) || n == 0) return rc;
+    if ((rc = ensure_scratch(c, 256 + sizeof(float) * nswarm))) return rc;
+    unsigned long long* killed = static_cast<unsigned long long*>(c->d_scr);
+    float* dq = reinterpret_cast<float*>(static_cast<char*>(c->d_scr) + 256);
+    CK(cudaMemcpyAsync(dq, q.data(), sizeof(float) * nswarm, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemsetAsync(killed, 0, sizeof(unsigned long long), c->stream));
+    const int grid = int(std::min<long long>((n + 255) / 256, 8ll * c->sm_count));
+    k_roulette_swarms<<<grid, 256, 0, c->stream>>>(S.xw[S.cur], S.meta[S.cur], n, dq, nswarm,
+                                                   uint32_t(c->cfg.seed), uint32_t(c->cfg.seed >> 32), killed);
+    CK(cudaGetLastError());
+    unsigned long long hk = 0;
+    CK(cudaMemcpyAsync(&hk, killed, sizeof(hk), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->live[species] = std::max<long long>(0, c->live[species] - (long long)hk);
+    return PCL_OK;
+}
+
 int pcl_split(void* ctx, int species, double p) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c) return PCL_ERR_INVALID;
@@ -1169,19 +1248,55 @@ int pcl_swarm_moments(void* ctx, int species, int nswarm, double* out) {
     CK(cudaSetDevice(c->device));
     long long slots = 0;
     if (S.cap > 0 && (rc = get_n(c, species, slots))) return rc;
-    double* d = nullptr;
-    CK(cudaMallocAsync(&d, sizeof(double) * 6 * nswarm, c->stream));
-    CK(cudaMemsetAsync(d, 0, sizeof(double) * 6 * nswarm, c->stream));
+    const int len = 6 * nswarm;
+    const int blocks = int(std::max<long long>(1, std::min<long long>(2ll * c->sm_count, (slots + 255) / 256)));
+    if ((rc = ensure_scratch(c, sizeof(double) * len * (blocks + 1)))) return rc;
+    double* d = static_cast<double*>(c->d_scr);
+    double* part = d + len;
     if (slots > 0) {
-        int blocks = int(std::min<long long>(4 * c->sm_count, (slots + 255) / 256));
-        k_swarm_moments<<<blocks, 256, 0, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], slots, species,
-                                                         nswarm, d);
+        k_swarm_moments<<<blocks, 256, sizeof(double) * len, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur],
+                                                                          slots, species, nswarm, part);
         CK(cudaGetLastError());
+    } else {
+        CK(cudaMemsetAsync(part, 0, sizeof(double) * len * blocks, c->stream));
     }
-    CK(cudaMemcpyAsync(out, d, sizeof(double) * 6 * nswarm, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaFreeAsync(d, c->stream));
+    k_swarm_reduce<<<(len + 255) / 256, 256, 0, c->stream>>>(part, blocks, len, d);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(out, d, sizeof(double) * len, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     for (int k = 0; k < nswarm; ++k) out[6 * k + 2] = e_to_si(out[6 * k + 2]);
+    return PCL_OK;
+}
+
+int pcl_swarm_counts(void* ctx, int species, int nswarm, int64_t* out) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !out) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (nswarm < 1 || nswarm > 256) return fail(c, PCL_ERR_INVALID, "nswarm out of range");
+    SpeciesState& S = c->sp[species];
+    CK(cudaSetDevice(c->device));
+    std::vector<unsigned int> h(nswarm, 0u);
+    if (S.cap > 0) {
+        unsigned int* cnt = c->d_swcnt + 256 * species;
+        const int grid = int(std::min<long long>((S.cap + 255) / 256, 4ll * c->sm_count));
+        CK(cudaMemsetAsync(cnt, 0, sizeof(unsigned int) * nswarm, c->stream));
+        k_swarm_count<<<grid, 256, 0, c->stream>>>(S.meta[S.cur], &c->d_ctl->n[species], S.cap, nswarm, cnt);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(h.data(), cnt, sizeof(unsigned int) * nswarm, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    for (int k = 0; k < nswarm; ++k) out[k] = (int64_t)h[k];
+    return PCL_OK;
+}
+
+int pcl_set_swarm_cap(void* ctx, int species, int64_t cap) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (cap < 0 || cap > (int64_t)0xffffffffll) return fail(c, PCL_ERR_INVALID, "cap out of range");
+    c->swarm_cap[species] = (long long)cap;
     return PCL_OK;
 }
 
@@ -1339,7 +1454,7 @@ int pcl_run(void* ctx, double tfinal, double dt, const pcl_run_opts* opts, pcl_t
         if (opts && opts->max_steps > 0) ns = int(std::min<long long>(ns, opts->max_steps - done));
         if (ns <= 0) break;
         int rc = launch_steps(c, dt, ns);
-        if (rc) return rc;
+        if (rc || (rc = apply_swarm_caps(c))) return rc;
         done += ns;
         if (done == total && std::fabs(c->t - tfinal) < 1e-6 * dt) c->t = tfinal;
         if (opts && opts->target_species >= 0 && opts->target_species < 3) {

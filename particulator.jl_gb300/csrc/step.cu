@@ -1622,38 +1622,64 @@ __global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta,
 // FP64 moments per swarm of a batched context: out[sw][6] = {live, sum w,
 // sum w E, sum w z, sum w z^2, sum w x^2 + y^2}; lanes of one warp are grouped
 // by swarm before the atomics.
+// Per-swarm moments: live count, sum w, sum w E, sum w z, sum w z^2,
+// sum w (x^2 + y^2).  Per-particle values in FP32, sums in FP64: warp groups
+// of the same swarm combine by shuffles, each block accumulates in shared
+// memory and writes one partial row; k_swarm_reduce adds the rows.
 __global__ void k_swarm_moments(const float4* xw, const float4* ps, const uint4* meta, long long n, int species,
-                                int nswarm, double* out) {
+                                int nswarm, double* partial) {
+    extern __shared__ double acc[];
+    const int len = 6 * nswarm;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) acc[i] = 0.0;
+    __syncthreads();
     for (long long i0 = (long long)blockIdx.x * blockDim.x; i0 < n; i0 += (long long)gridDim.x * blockDim.x) {
         long long i = i0 + threadIdx.x;
         bool live = false;
         int sw = 0;
-        double v[6] = {0, 0, 0, 0, 0, 0};
+        float v[6] = {0, 0, 0, 0, 0, 0};
         if (i < n) {
             uint4 m = meta[i];
             if (m.z != PCL_DEAD_CTR) {
                 live = true;
                 sw = min(int(m.y >> 24), nswarm - 1);
                 float4 a = xw[i], b = ps[i];
-                double p2 = double(b.x) * b.x + double(b.y) * b.y + double(b.z) * b.z;
-                double E = (species == PCL_PHOTON) ? sqrt(p2) : p2 / (sqrt(1.0 + p2) + 1.0);
-                double w = a.w;
-                v[0] = 1.0; v[1] = w; v[2] = w * E; v[3] = w * a.z; v[4] = w * double(a.z) * a.z;
-                v[5] = w * (double(a.x) * a.x + double(a.y) * a.y);
+                const float E = kin_energy(species, b.x, b.y, b.z);
+                const float w = a.w;
+                v[0] = 1.0f; v[1] = w; v[2] = w * E; v[3] = w * a.z; v[4] = w * a.z * a.z;
+                v[5] = w * (a.x * a.x + a.y * a.y);
             }
         }
-        unsigned act = __ballot_sync(0xffffffffu, live);
-        if (live) {
+        const unsigned FULL = 0xffffffffu;
+        unsigned act = __ballot_sync(FULL, live);
+        if (!act) continue;
+        const int sw0 = __shfl_sync(FULL, sw, __ffs(act) - 1);
+        if (__all_sync(FULL, !live || sw == sw0)) {
+            // the usual case (swarms are contiguous): one butterfly sum per value
+            for (int q = 0; q < 6; ++q) {
+                float t = v[q];
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
+                if ((threadIdx.x & 31) == 0) atomicAdd(&acc[6 * sw0 + q], double(t));
+            }
+        } else if (live) {
             unsigned grp = __match_any_sync(act, sw);
             int leader = __ffs(grp) - 1;
-            // every lane of the group sums the group's values; the leader commits
             for (int q = 0; q < 6; ++q) {
                 double tot = 0.0;
-                for (unsigned g = grp; g; g &= g - 1) tot += __shfl_sync(grp, v[q], __ffs(g) - 1);
-                if ((threadIdx.x & 31) == leader) atomicAdd(&out[6 * sw + q], tot);
+                for (unsigned g = grp; g; g &= g - 1) tot += double(__shfl_sync(grp, v[q], __ffs(g) - 1));
+                if ((threadIdx.x & 31) == leader) atomicAdd(&acc[6 * sw + q], tot);
             }
         }
     }
+    __syncthreads();
+    for (int i = threadIdx.x; i < len; i += blockDim.x) partial[(size_t)blockIdx.x * len + i] = acc[i];
+}
+
+__global__ void k_swarm_reduce(const double* partial, int nblocks, int len, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= len) return;
+    double s = 0.0;
+    for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * len + i];
+    out[i] = s;
 }
 
 // ------------------------------------------------------- sampler test ----
@@ -1735,6 +1761,91 @@ __global__ void k_roulette(float4* xw, uint4* meta, long long n, float pkeep, ui
         } else {
             meta[i].z = PCL_DEAD_CTR;
             atomicAdd(dead, 1ull);
+        }
+    }
+}
+
+// roulette! with a keep probability per swarm (batched swarms: the swarm is
+// the top 8 bits of the stream id); pkeep >= 1 leaves a swarm untouched and
+// takes no draw.
+__global__ void k_roulette_swarms(float4* xw, uint4* meta, long long n, const float* pkeep, int nswarm, uint32_t k0,
+                                  uint32_t k1, unsigned long long* dead) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        uint4 m = meta[i];
+        if (m.z == PCL_DEAD_CTR) continue;
+        const float q = pkeep[min(int(m.y >> 24), nswarm - 1)];
+        if (!(q < 1.0f)) continue;
+        const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
+        if (u < q) {
+            xw[i].w = xw[i].w / q;
+            meta[i].z = m.z + 1u;
+        } else {
+            meta[i].z = PCL_DEAD_CTR;
+            atomicAdd(dead, 1ull);
+        }
+    }
+}
+
+// Live particles per swarm (the top 8 bits of the stream id; every particle
+// counts as swarm 0 when nswarm is 1), added into counts[0..nswarm), over the
+// min(*nslots, cap) slots of the species (read on the device, so that the
+// launch needs no host read-back).  A warp whose live particles share one
+// swarm adds them with one shared atomic.
+__global__ void k_swarm_count(const uint4* meta, const unsigned long long* nslots, long long cap, int nswarm,
+                              unsigned int* counts) {
+    __shared__ unsigned int h[256];
+    const long long n = min((long long)*nslots, cap);
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0u;
+    __syncthreads();
+    const unsigned FULL = 0xffffffffu;
+    const long long n32 = (n + 31) / 32 * 32;   // whole warps stay in the loop together
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n32;
+         i += (long long)gridDim.x * blockDim.x) {
+        int sw = -1;
+        if (i < n) {
+            const uint4 m = meta[i];
+            if (m.z != PCL_DEAD_CTR) sw = min(int(m.y >> 24), nswarm - 1);
+        }
+        const unsigned act = __ballot_sync(FULL, sw >= 0);
+        if (!act) continue;
+        const int sw0 = __shfl_sync(FULL, sw, __ffs(act) - 1);
+        if (__all_sync(FULL, sw < 0 || sw == sw0)) {
+            if ((threadIdx.x & 31) == 0) atomicAdd(&h[sw0], unsigned(__popc(act)));
+        } else {
+            const unsigned grp = __match_any_sync(FULL, sw);
+            if (sw >= 0 && (threadIdx.x & 31) == __ffs(grp) - 1) atomicAdd(&h[sw], unsigned(__popc(grp)));
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nswarm; i += blockDim.x)
+        if (h[i]) atomicAdd(&counts[i], h[i]);
+}
+
+// RouletteCallback (callback.jl:210-227) per swarm on the device: a swarm with
+// n > cap live particles gets roulette!(cap / n) (the keep probability rounded
+// to FP32 as in k_roulette_swarms), with n from k_swarm_count.  A block with
+// no swarm over the cap returns before it reads a particle.
+__global__ void k_roulette_cap(float4* xw, uint4* meta, const unsigned long long* nslots, long long slot_cap,
+                               const unsigned int* counts, int nswarm, unsigned long long cap, uint32_t k0,
+                               uint32_t k1) {
+    const long long n = min((long long)*nslots, slot_cap);
+    int over = 0;
+    for (int i = threadIdx.x; i < nswarm; i += blockDim.x) over |= (counts[i] > cap);
+    if (!__syncthreads_or(over)) return;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const uint4 m = meta[i];
+        if (m.z == PCL_DEAD_CTR) continue;
+        const unsigned int cnt = counts[min(int(m.y >> 24), nswarm - 1)];
+        if (cnt <= cap) continue;
+        const float q = float(double(cap) / double(cnt));
+        const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
+        if (u < q) {
+            xw[i].w = xw[i].w / q;
+            meta[i].z = m.z + 1u;
+        } else {
+            meta[i].z = PCL_DEAD_CTR;
         }
     }
 }

@@ -268,6 +268,52 @@ class MultiPopulation:
         key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
         _lib.check(_lib.lib().pcl_roulette(self.ctx, key, float(pkeep)), self.ctx, "pcl_roulette")
 
+    def roulette_swarms(self, particle, pkeep):
+        """Per-swarm roulette! (pcl_roulette_swarms): keep probability pkeep[s]
+        for swarm s; entries >= 1 leave a swarm untouched."""
+        key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        q = np.ascontiguousarray(np.asarray(pkeep, dtype=float))
+        _lib.check(_lib.lib().pcl_roulette_swarms(self.ctx, key, len(q), _lib.dptr(q)), self.ctx,
+                   "pcl_roulette_swarms")
+
+    def swarm_counts(self, particle, nswarm: int | None = None) -> np.ndarray:
+        """Live particles of each swarm (pcl_swarm_counts); with one swarm,
+        the whole population."""
+        key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
+        ns = nswarm or max(1, getattr(self, "nswarm", 1))
+        out = np.zeros(ns, dtype=np.int64)
+        _lib.check(_lib.lib().pcl_swarm_counts(self.ctx, key, ns, _lib.i64ptr(out)), self.ctx, "pcl_swarm_counts")
+        return out
+
+    def set_swarm_cap(self, cap: int, particles=(Electron,)):
+        """Device RouletteCallback per swarm (pcl_set_swarm_cap): after every
+        launch group of run!, each swarm of the given species with n > cap
+        live particles gets roulette!(cap / n).  cap = 0 turns it off."""
+        for sp in particles:
+            key = SPECIES_BY_NAME[sp] if isinstance(sp, str) else int(sp)
+            _lib.check(_lib.lib().pcl_set_swarm_cap(self.ctx, key, int(cap)), self.ctx, "pcl_set_swarm_cap")
+
+    def cap_swarms(self, cap: int, particles=(Electron, Photon, Positron)):
+        """Hold every swarm of a batched context at `cap` live particles per
+        species now: swarms above it get roulette!(cap / n), weights
+        compensating, then the population is repacked.  Returns the per-swarm
+        live counts before the cap."""
+        out = {}
+        cut = False
+        for sp in particles:
+            pop = self.index.get(sp)
+            if pop is None or pop.tally_only or pop.max_particles == 0:
+                continue
+            n = self.swarm_counts(sp, self.nswarm).astype(float)
+            out[sp] = n.copy()
+            q = np.where(n > cap, cap / np.maximum(n, 1), 1.0)
+            if np.any(q < 1.0):
+                self.roulette_swarms(sp, q)
+                cut = True
+        if cut:
+            _lib.check(_lib.lib().pcl_compact(self.ctx), self.ctx, "pcl_compact")
+        return out
+
     def split(self, particle, p: float):
         """split!(p, popl) (population.jl:318-335) on the device."""
         key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)

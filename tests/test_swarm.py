@@ -288,3 +288,54 @@ def test_lxcat_swarm_parity(pcl, oracle, gpu, lxcat_file):
                                      rtol=1e-5, stol=2e-4)
     assert rep["ok"], str(rep)
     mp.close()
+
+
+@pytest.mark.gpu
+def test_swarm_cap(pcl, gpu):
+    """cap_swarms: swarms above the cap are rouletted to it (weights scaled by
+    1 / pkeep), swarms below are untouched."""
+    b = _batch(pcl)
+    for k in range(2):
+        pcl.advance(b.mpopl, b.pusher, (k + 1) * b.dt)
+    m0 = b.mpopl.swarm_moments(pcl.Electron, len(b.E))
+    cap = int(np.median(m0[:, 0]))
+    before = b.mpopl.cap_swarms(cap, particles=(pcl.Electron,))
+    m1 = b.mpopl.swarm_moments(pcl.Electron, len(b.E))
+    for s in range(len(b.E)):
+        n0, w0 = m0[s, 0], m0[s, 1]
+        if n0 <= cap:
+            assert m1[s, 0] == n0 and m1[s, 1] == pytest.approx(w0, rel=1e-6)
+        else:
+            q = cap / n0
+            assert abs(m1[s, 0] - cap) < 5 * np.sqrt(n0 * q * (1 - q)) + 1
+            assert abs(m1[s, 1] - w0) < 6 * np.sqrt(n0 * (1 - q) / q) + 1
+    b.mpopl.close()
+
+
+@pytest.mark.gpu
+def test_device_swarm_cap(pcl, gpu):
+    """set_swarm_cap (per-swarm counts and roulette on the device after each
+    launch group of run!) removes and reweights exactly the particles that
+    the host-driven cap_swarms does after the same steps."""
+    a, b = _batch(pcl), _batch(pcl)
+    for q in (a, b):
+        for k in range(2):
+            pcl.advance(q.mpopl, q.pusher, (k + 1) * q.dt)
+    n0 = a.mpopl.swarm_counts(pcl.Electron)
+    np.testing.assert_array_equal(n0, b.mpopl.swarm_moments(pcl.Electron, len(b.E))[:, 0].astype(np.int64))
+    cap = int(np.median(n0))
+    pcl.run(a.mpopl, a.pusher, 3 * a.dt, a.dt)
+    before = a.mpopl.cap_swarms(cap, particles=(pcl.Electron,))
+    b.mpopl.set_swarm_cap(cap)
+    pcl.run(b.mpopl, b.pusher, 3 * b.dt, b.dt)
+    pcl.lib().pcl_compact(b.mpopl.ctx)
+    assert np.any(before[pcl.Electron] > cap)
+    na, nb = a.mpopl.swarm_counts(pcl.Electron), b.mpopl.swarm_counts(pcl.Electron)
+    np.testing.assert_array_equal(na, nb)
+    for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
+        ga, gb = a.mpopl.get(sp).particles(), b.mpopl.get(sp).particles()
+        for u, v in zip(_by_sid(ga), _by_sid(gb)):
+            np.testing.assert_array_equal(u, v)
+        np.testing.assert_array_equal(ga.w[np.argsort(ga.sid)], gb.w[np.argsort(gb.sid)])
+    a.mpopl.close()
+    b.mpopl.close()
