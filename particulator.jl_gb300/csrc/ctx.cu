@@ -12,6 +12,7 @@
 #include "device.cuh"
 #include "physconst.h"
 #include "../../include/particulator_gb300.h"
+#include "mlp.cuh"
 
 extern "C" int pcl_ratebound_split(int, int, int, int, double, const double*, double, double*, double*);
 
@@ -20,7 +21,8 @@ cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream
 cudaError_t prepare_step(int minb, size_t smem, bool general, bool event, bool learn);
 __global__ void k_learn_hist(StepArgs A, int species, int j, int kind, int nT, long long per_T, int nbins,
                              float hmin, float hmax, unsigned long long sid_base, unsigned int* hist);
-__global__ void k_learn_x(const float4* ps, const float4* m2, long long n, float* X);
+__global__ void k_learn_x(const float4* ps, const float4* m2, const unsigned long long* n_dev, long long cap,
+                          float* X);
 __global__ void k_roulette(float4* xw, uint4* meta, long long n, float pkeep, uint32_t k0, uint32_t k1,
                            unsigned long long* dead);
 __global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, uint32_t k0,
@@ -32,10 +34,11 @@ __global__ void k_swarm_count(const uint4* meta, const unsigned long long* nslot
 __global__ void k_roulette_cap(float4* xw, uint4* meta, const unsigned long long* nslots, long long slot_cap,
                                const unsigned int* counts, int nswarm, unsigned long long cap, uint32_t k0,
                                uint32_t k1);
-__global__ void k_learn_pick(const float4* m2, long long n, const float* Yk, long long stride, LearnPick which,
-                             float* Y);
+__global__ void k_learn_pick(const float4* m2, const unsigned long long* n_dev, long long cap, const float* Yk,
+                             long long stride, LearnPick which, float* Y);
 namespace mlp {
-cudaError_t infer(void* handle, const float* X, long long n, float* Y, cudaStream_t stream);
+cudaError_t infer_multi(void* const* handles, int nnets, const float* X, const unsigned long long* n_dev,
+                        long long cap, float* Y, long long ystride, cudaStream_t stream);
 }
 __global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long cap2);
 __global__ void k_begin_spill(Control* ctl, unsigned long long* in_n, unsigned long long* out_n);
@@ -178,6 +181,7 @@ struct Ctx {
     struct GraphEntry { std::vector<unsigned char> key; cudaGraphExec_t exec; };
     std::vector<GraphEntry> graphs;
     unsigned long long* h_spn = nullptr;  // pinned mirror of d_spn
+    unsigned long long* h_lqn = nullptr;  // pinned mirror of d_lqn
     long long graph_launches = 0;
     // instrumentation
     cudaEvent_t ev_k0 = nullptr, ev_k1 = nullptr, ev_t0 = nullptr, ev_t1 = nullptr;
@@ -645,6 +649,54 @@ static int compact_all(Ctx* c) {
     return PCL_OK;
 }
 
+// The learned-sampler round, enqueued with no host read-back (so that it can
+// be captured): the networks answer every collision suspended in queue 0 by
+// the step and its two spill passes (network inputs, one batched tensor-core
+// forward pass per attached network, the pick of each collision's network),
+// then a resume pass finishes those collisions and carries the particles to
+// the end of the launch, appending its overflow children to spill queue 1
+// after what the spill passes left there, and two more spill passes drain
+// it.  Every count is read on the device; the resume pass and the passes
+// after it use the table sampler for any further collision (no suspension).
+static cudaError_t enqueue_learned_round(Ctx* c, double dt, int nsteps, int minb, int threads, size_t smem) {
+    const int g = int(std::max<long long>(1, std::min<long long>((c->lq_cap + 255) / 256, 2ll * c->sm_count)));
+    const unsigned long long* nq = c->d_lqn;   // queue 0
+    k_learn_x<<<g, 256, 0, c->stream>>>(c->lq_ps[0], c->lq_m2[0], nq, c->lq_cap, c->lq_x);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = mlp::infer_multi(c->nets.data(), int(c->nets.size()), c->lq_x, nq, c->lq_cap, c->lq_yk, c->lq_cap,
+                             c->stream);
+    if (e != cudaSuccess) return e;
+    k_learn_pick<<<g, 256, 0, c->stream>>>(c->lq_m2[0], nq, c->lq_cap, c->lq_yk, c->lq_cap, c->pick, c->lq_y);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, nullptr, nullptr);   // work head only
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    StepArgs R = make_args(c, dt, nsteps, 2, 0);   // spill output: queue 1
+    set_lq(R, c, 1, 0);
+    R.lq_out_n = nullptr;
+    // queue-driven passes take any grid: one block per SM
+    if ((e = launch_step(minb, c->sm_count, threads, smem, c->stream, R)) != cudaSuccess) return e;
+    for (int in = 1, pass = 0; pass < 2; ++pass, in = 1 - in) {
+        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + in, c->d_spn + (1 - in));
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        StepArgs P = make_args(c, dt, nsteps, 1, in);
+        P.lq_out_n = nullptr;
+        if ((e = launch_step(minb, c->sm_count, threads, smem, c->stream, P)) != cudaSuccess) return e;
+    }
+    c->launches += 8 + ((long long)c->nets.size() + mlp::kMaxNets - 1) / mlp::kMaxNets;
+    return cudaSuccess;
+}
+
+// Statistics of the learned round of the last launch group (queue 0's count
+// read back with the control block).
+static void count_learned(Ctx* c) {
+    const long long m = std::min<long long>((long long)c->h_lqn[0], c->lq_cap);
+    if (m > 0) {
+        c->learn_rounds += 1;
+        c->learn_suspended += m;
+    }
+}
+
 // One launch group as a CUDA graph: prologue, step kernel, two spill passes
 // (each a no-op when its queue is empty), the compaction when due, and the
 // read-back of the control block and spill counts.  Graphs are cached by the
@@ -657,7 +709,12 @@ static int run_group_graph(Ctx* c, const StepArgs& A, const StepArgs& P0, const 
         key.insert(key.end(), b, b + n);
     };
     put(&A, sizeof(A)); put(&P0, sizeof(P0)); put(&P1, sizeof(P1));
-    int hdr[4] = {minb, grid, threads, C ? 1 : 0};
+    int hdr[4] = {minb, grid, threads, (C ? 1 : 0) | (c->learn_on ? 2 : 0)};
+    if (c->learn_on) {   // the learned round's networks and their pick table
+        put(c->nets.data(), c->nets.size() * sizeof(void*));
+        put(&c->pick, sizeof(c->pick));
+        put(&c->lq_cap, sizeof(c->lq_cap));
+    }
     put(hdr, sizeof(hdr)); put(&smem, sizeof(smem));
     if (C) put(C, sizeof(*C));
     long long caps[3] = {c->sp[0].cap, c->sp[1].cap, c->sp[2].cap};
@@ -685,9 +742,15 @@ static int run_group_graph(Ctx* c, const StepArgs& A, const StepArgs& P0, const 
         k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 0, c->d_spn + 1);
         q(cudaGetLastError());
         q(launch_step(minb, grid, threads, smem, c->stream, P1));
+        const long long l0 = c->launches;
+        if (c->learn_on) q(enqueue_learned_round(c, A.dt, A.nsteps, minb, threads, smem));
+        c->launches = l0;   // counted per replay below
         if (C) q(enqueue_compact(c, *C));
         q(cudaMemcpyAsync(c->h_ctl, c->d_ctl, sizeof(Control), cudaMemcpyDeviceToHost, c->stream));
         q(cudaMemcpyAsync(c->h_spn, c->d_spn, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+        if (c->learn_on)
+            q(cudaMemcpyAsync(c->h_lqn, c->d_lqn, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                              c->stream));
         cudaGraph_t g = nullptr;
         cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
         if (e == cudaSuccess) e = e2;
@@ -703,7 +766,8 @@ static int run_group_graph(Ctx* c, const StepArgs& A, const StepArgs& P0, const 
     CK(cudaGraphLaunch(exec, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->graph_launches += 1;
-    c->launches += C ? 11 : 8;
+    c->launches += (C ? 11 : 8) +
+                   (c->learn_on ? 8 + ((long long)c->nets.size() + mlp::kMaxNets - 1) / mlp::kMaxNets : 0);
     return PCL_OK;
 }
 
@@ -729,51 +793,8 @@ static int drain_spills(Ctx* c, double dt, int nsteps, int threads, size_t smem,
     return fail(c, PCL_ERR_TIMEOUT, "spill passes did not drain");
 }
 
-// Learned-sampler round: the networks answer every collision suspended by
-// the launch (one batched tensor-core forward pass per attached network), a
-// resume pass finishes them and carries the particles to the end of the
-// launch, then the spill passes drain.  The resume pass and its spill passes
-// use the table sampler for any further collision of those particles in the
-// same launch (kLearnRounds = 1: one host round trip per launch).
-constexpr int kLearnRounds = 1;
-
-static int learned_rounds(Ctx* c, double dt, int nsteps, int threads, size_t smem, bool* ran) {
-    int lin = 0;
-    for (int round = 0; round < kLearnRounds; ++round) {
-        unsigned long long n = 0;
-        CK(d2h(c, &n, c->d_lqn + lin, sizeof(n)));
-        if (n == 0) return PCL_OK;
-        *ran = true;
-        const long long m = std::min<long long>((long long)n, c->lq_cap);
-        const int grid = int(std::max<long long>(1, std::min<long long>((m + 255) / 256, 4ll * c->sm_count)));
-        k_learn_x<<<grid, 256, 0, c->stream>>>(c->lq_ps[lin], c->lq_m2[lin], m, c->lq_x);
-        CK(cudaGetLastError());
-        for (size_t k = 0; k < c->nets.size(); ++k)
-            CK(mlp::infer(c->nets[k], c->lq_x, m, c->lq_yk + k * c->lq_cap, c->stream));
-        k_learn_pick<<<grid, 256, 0, c->stream>>>(c->lq_m2[lin], m, c->lq_yk, c->lq_cap, c->pick, c->lq_y);
-        CK(cudaGetLastError());
-        CK(cudaMemsetAsync(c->d_lqn + (1 - lin), 0, sizeof(unsigned long long), c->stream));
-        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 0, c->d_spn + 1);  // head 0, spill queue 1 empty
-        StepArgs R = make_args(c, dt, nsteps, 2, 0);
-        set_lq(R, c, 1 - lin, lin);
-        const bool last = round + 1 == kLearnRounds;
-        if (last) R.lq_out_n = nullptr;   // no further suspension
-        // a grid sized to the suspended collisions (8 warps of 32 per CTA)
-        const int rgrid = int(std::min<long long>(grid_blocks(c), std::max<long long>(1, (m + 255) / 256)));
-        CK(launch_step(blocks_per_sm(c), rgrid, threads, smem, c->stream, R));
-        c->launches += 4 + (long long)c->nets.size();
-        c->learn_rounds += 1;
-        c->learn_suspended += m;
-        bool dummy = false;
-        int rc = drain_spills(c, dt, nsteps, threads, smem, 1, last ? -1 : 1 - lin, &dummy, nullptr);
-        if (rc) return rc;
-        lin = 1 - lin;
-    }
-    return PCL_OK;
-}
-
 // One launch of `nsteps` steps of length dt (seconds), plus spill passes and,
-// with a learned sampler attached, the learned rounds.
+// with a learned sampler attached, the learned round.
 static int launch_steps(Ctx* c, double dt_si, int nsteps) {
     int rc = build_blob(c);
     if (rc) return rc;
@@ -800,16 +821,30 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
         if (due) { flip_buffers(c); compacted = true; }
         pending0 = c->h_spn[1];  // the two in-graph passes leave the last queue written in 1
     } else {
+        const int minb = blocks_per_sm(c);
         k_begin<<<1, 64, 0, c->stream>>>(c->d_ctl, c->sp[0].cap, c->sp[1].cap, c->sp[2].cap);
         CK(cudaMemsetAsync(c->d_spn, 0, 2 * sizeof(unsigned long long), c->stream));
         if (c->learn_on) CK(cudaMemsetAsync(c->d_lqn, 0, 2 * sizeof(unsigned long long), c->stream));
         CK(cudaEventRecord(c->ev_k0, c->stream));
-        CK(launch_step(blocks_per_sm(c), grid_blocks(c), threads, smem, c->stream, A));
+        CK(launch_step(minb, grid_blocks(c), threads, smem, c->stream, A));
         CK(cudaEventRecord(c->ev_k1, c->stream));
         c->launches += 2;
-        if ((rc = readback(c))) return rc;
-        CK(d2h(c, &pending0, c->d_spn + 1, sizeof(pending0)));
+        if (c->learn_on) {   // the graph's sequence: two spill passes, then the learned round
+            StepArgs P0 = make_args(c, dt, nsteps, 1, 1), P1 = make_args(c, dt, nsteps, 1, 0);
+            k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 1, c->d_spn + 0);
+            CK(launch_step(minb, grid_blocks(c), threads, smem, c->stream, P0));
+            k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 0, c->d_spn + 1);
+            CK(launch_step(minb, grid_blocks(c), threads, smem, c->stream, P1));
+            c->launches += 4;
+            CK(enqueue_learned_round(c, dt, nsteps, minb, threads, smem));
+            CK(cudaMemcpyAsync(c->h_lqn, c->d_lqn, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                               c->stream));
+        }
+        CK(cudaMemcpyAsync(c->h_spn, c->d_spn, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, c->stream));
+        if ((rc = readback(c))) return rc;   // the one synchronisation of the group
+        pending0 = c->h_spn[1];
     }
+    if (c->learn_on) count_learned(c);
     {
         float ms = 0.0f;
         CK(cudaEventElapsedTime(&ms, c->ev_k0, c->ev_k1));
@@ -823,8 +858,8 @@ static int launch_steps(Ctx* c, double dt_si, int nsteps) {
         }
         c->k_bytes += 48.0 * nstart + 48.0 * nout + 4.0 * ndead;
     }
-    if ((rc = drain_spills(c, dt, nsteps, threads, smem, 1, 0, &host_passes, &pending0))) return rc;
-    if (c->learn_on && (rc = learned_rounds(c, dt, nsteps, threads, smem, &host_passes))) return rc;
+    // leftovers of the in-group passes (rare): host-driven passes, table sampler only
+    if ((rc = drain_spills(c, dt, nsteps, threads, smem, 1, -1, &host_passes, &pending0))) return rc;
     // the last read-back holds the final counters unless host passes ran after it
     if (host_passes && (rc = readback(c))) return rc;
     if (c->h_ctl->timeout) return fail(c, PCL_ERR_TIMEOUT, "table staging wait timed out");
@@ -883,6 +918,7 @@ int pcl_create(const pcl_config* cfg, void** out) {
         cudaMalloc(&c->d_ctl, sizeof(Control)) != cudaSuccess ||
         cudaMallocHost(&c->h_ctl, sizeof(Control)) != cudaSuccess ||
         cudaMallocHost(&c->h_spn, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMallocHost(&c->h_lqn, 2 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&c->d_spn, 2 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&c->d_nnew, 3 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&c->d_mom, 16 * sizeof(double)) != cudaSuccess ||
@@ -912,6 +948,7 @@ void pcl_destroy(void* ctx) {
     cudaFree(c->d_tile_off); cudaFree(c->d_nnew); cudaFree(c->d_mom); cudaFree(c->d_scr); cudaFree(c->d_swcnt);
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
     if (c->h_spn) cudaFreeHost(c->h_spn);
+    if (c->h_lqn) cudaFreeHost(c->h_lqn);
     free_lq(c);
     cudaFree(c->d_wall_xw); cudaFree(c->d_wall_pt); cudaFree(c->d_wall_meta); cudaFree(c->d_wall_n);
     for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);

@@ -77,6 +77,7 @@ static int ensure_batch(Handle* h, long long n) {
 
 static int set_attrs(Handle* h) {
     MCK(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kFwdSmem)));
+    MCK(cudaFuncSetAttribute(k_mlp_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kInferSmem)));
     MCK(cudaFuncSetAttribute(k_mlp_bwd_a, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBwdASmem)));
     MCK(cudaFuncSetAttribute(k_mlp_bwd_w, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kBwdWSmem)));
     return PCL_OK;
@@ -89,7 +90,8 @@ static int forward(Handle* h, const float* X, long long n, float* Y, const float
     long long ntiles = (n + kH - 1) / kH;
     int grid = int(std::min<long long>(ntiles, 2ll * h->sm_count));
     if (grid < 1) return PCL_OK;
-    k_mlp_forward<<<grid, 128, kFwdSmem, h->stream>>>(net_of(h), X, n, Y, h->tb, T, h->G, h->d_loss, h->d_err);
+    k_mlp_forward<<<grid, 128, kFwdSmem, h->stream>>>(net_of(h), X, n, Y, h->tb, T, h->G, h->d_loss, h->d_err,
+                                                      nullptr);
     MCK(cudaGetLastError());
     return PCL_OK;
 }
@@ -127,16 +129,28 @@ static uint64_t splitmix(uint64_t& s) {
     return z ^ (z >> 31);
 }
 
-// Batched inference on device arrays, on the caller's stream (the step's
-// learned rounds).  The handle's kernels attributes are set at creation.
-cudaError_t infer(void* handle, const float* X, long long n, float* Y, cudaStream_t stream) {
-    Handle* h = static_cast<Handle*>(handle);
-    if (n <= 0) return cudaSuccess;
-    long long ntiles = (n + kH - 1) / kH;
-    int grid = int(std::min<long long>(ntiles, 2ll * h->sm_count));
-    k_mlp_forward<<<grid, 128, kFwdSmem, stream>>>(net_of(h), X, n, Y, TrainBuf{}, nullptr, nullptr, nullptr,
-                                                     h->d_err);
-    return cudaGetLastError();
+// Several networks on the same rows, min(cap, *n_dev) of them, the count read
+// on the device (no host read-back, so the launch can sit in a captured
+// graph): network k writes Y + k * ystride.  One launch per kMaxNets
+// networks, a grid of at most one block per SM per network walking the tiles.
+cudaError_t infer_multi(void* const* handles, int nnets, const float* X, const unsigned long long* n_dev,
+                        long long cap, float* Y, long long ystride, cudaStream_t stream) {
+    if (cap <= 0 || nnets <= 0) return cudaSuccess;
+    const Handle* h0 = static_cast<const Handle*>(handles[0]);
+    long long ntiles = (cap + kH - 1) / kH;
+    int gx = int(std::min<long long>(ntiles, (long long)h0->sm_count));
+    for (int k0 = 0; k0 < nnets; k0 += kMaxNets) {
+        NetSet ns{};
+        const int m = std::min(kMaxNets, nnets - k0);
+        for (int i = 0; i < m; ++i) {
+            ns.net[i] = net_of(static_cast<const Handle*>(handles[k0 + i]));
+            ns.Y[i] = Y + (long long)(k0 + i) * ystride;
+        }
+        k_mlp_infer<<<dim3(gx, m), kInferThreads, kInferSmem, stream>>>(ns, X, cap, n_dev, h0->d_err);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace mlp
@@ -231,7 +245,8 @@ int pcl_mlp_forward(void* mh, int64_t n, const float* x, float* y) {
     int rc = ensure_batch(h, n);
     if (rc) return rc;
     MCK(cudaMemcpyAsync(h->X, x, sizeof(float) * 2 * n, cudaMemcpyHostToDevice, h->stream));
-    if ((rc = forward(h, h->X, n, h->Y, nullptr))) return rc;
+    void* one[1] = {h};   // the inference kernel of the step's learned round
+    MCK(infer_multi(one, 1, h->X, nullptr, n, h->Y, n, h->stream));
     MCK(cudaMemcpyAsync(y, h->Y, sizeof(float) * n, cudaMemcpyDeviceToHost, h->stream));
     return check_err(h);
 }

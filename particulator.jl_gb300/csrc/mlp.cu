@@ -214,11 +214,18 @@ __device__ __forceinline__ bool mma_sync(Smem& s, uint32_t d, const unsigned cha
 }
 
 // ------------------------------------------------------------------ forward --
-// One row per thread.  Inference (T == nullptr): Y[row] = net(X[row]).
+// One row per thread.  Inference (T == nullptr): Y[row] = net(X[row]), over
+// min(n, *n_dev) rows when n_dev is given (a count written on the device;
+// blocks without a tile then return before touching tensor memory).
 // Training: keeps the activations in tb, accumulates the mean-squared-error
 // loss and the gradients of the output layer and of b3, and writes dz3.
 __global__ void __launch_bounds__(128, 1) k_mlp_forward(Net net, const float* X, long long n, float* Y, TrainBuf tb,
-                                                        const float* T, float* G, double* loss, int* err) {
+                                                        const float* T, float* G, double* loss, int* err,
+                                                        const unsigned long long* n_dev) {
+    if (n_dev) {
+        n = min(n, (long long)*n_dev);
+        if ((long long)blockIdx.x * kH >= n) return;
+    }
     extern __shared__ unsigned char raw[];
     Smem s = carve(raw, 3);
     unsigned char* sA = s.base;
@@ -328,6 +335,81 @@ __global__ void __launch_bounds__(128, 1) k_mlp_forward(Net net, const float* X,
             atomicAdd(loss, double(r_b4[2]) / double(n));
         }
     }
+}
+
+// ---------------------------------------------------------------- infer --
+// Inference of up to kMaxNets networks on the same rows, one network per
+// blockIdx.y, over min(cap, *n_dev) rows.  512 threads per 128-row tile:
+// thread t owns row t % 128 (its warp reads tensor-memory lanes
+// 32 (w % 4) .. 32 (w % 4) + 31) and the 32 columns of quarter q = t / 128 in
+// every layer, so each row's GELUs are spread over four warps; the output
+// layer's four partial sums are added in quarter order in shared memory.
+__device__ __forceinline__ void load_tile_q(unsigned char* tile, const __nv_bfloat16* W) {
+    const int r = threadIdx.x & (kH - 1), q0 = 4 * (threadIdx.x >> 7);
+    const uint4* row = reinterpret_cast<const uint4*>(W + (size_t)r * kH);
+#pragma unroll
+    for (int q = q0; q < q0 + 4; ++q) *reinterpret_cast<uint4*>(tile + toff(r, 8 * q)) = row[q];
+}
+
+__global__ void __launch_bounds__(kInferThreads, 1) k_mlp_infer(NetSet ns, const float* X, long long cap,
+                                                                 const unsigned long long* n_dev, int* err) {
+    const long long n = n_dev ? min(cap, (long long)*n_dev) : cap;
+    const long long ntiles = (n + kH - 1) / kH;
+    if ((long long)blockIdx.x >= ntiles) return;   // whole block: before any barrier or tensor memory
+    extern __shared__ unsigned char raw[];
+    Smem s = carve(raw, 3);
+    unsigned char* sA = s.base;
+    unsigned char* sW2 = s.base + kTileBytes;
+    unsigned char* sW3 = s.base + 2 * kTileBytes;
+    const Net net = ns.net[blockIdx.y];
+    float* Y = ns.Y[blockIdx.y];
+    const int t = threadIdx.x;
+    const int r = t & (kH - 1);            // row within the tile
+    const int c0 = 32 * (t >> 7);          // first column of this thread's quarter
+    load_tile_q(sW2, net.W2);
+    load_tile_q(sW3, net.W3);
+    uint32_t tbase = setup(s);
+    uint32_t ph = 0;
+    const float* P = net.P;
+    const uint32_t lane_off = uint32_t(((t >> 5) & 3) * 32) << 16;
+    float* part = s.red;                   // [4][128] output-layer partial sums
+    bool ok = true;
+    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const long long row = tile * kH + r;
+        const bool valid = row < n;
+        const float x0 = valid ? X[2 * row] : 0.0f, x1 = valid ? X[2 * row + 1] : 0.0f;
+        for (int c = c0; c < c0 + 32; c += 8) {
+            float h[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                h[i] = gelu(fmaf(P[oW1 + 2 * (c + i)], x0, fmaf(P[oW1 + 2 * (c + i) + 1], x1, P[ob1 + c + i])));
+            st_row8(sA, r, c, h);
+        }
+        ok = mma_sync(s, tbase, sA, sW2, false, ph, err);
+        if (!ok) break;
+        {
+            float v[32];
+            tmem_ld32(tbase + lane_off + c0, v);
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = gelu(v[i] + P[ob2 + c0 + i]);
+#pragma unroll
+            for (int i = 0; i < 32; i += 8) st_row8(sA, r, c0 + i, v + i);
+        }
+        ok = mma_sync(s, tbase + 128, sA, sW3, false, ph, err);
+        if (!ok) break;
+        {
+            float v[32];
+            tmem_ld32(tbase + lane_off + 128 + c0, v);
+            float y = 0.0f;
+#pragma unroll
+            for (int i = 0; i < 32; ++i) y = fmaf(P[ow4 + c0 + i], gelu(v[i] + P[ob3 + c0 + i]), y);
+            part[(t >> 7) * kH + r] = y;
+        }
+        __syncthreads();
+        if (t < kH && valid) Y[row] = P[ob4] + part[r] + part[kH + r] + part[2 * kH + r] + part[3 * kH + r];
+        // the next tile writes `part` only after two more block barriers (in mma_sync)
+    }
+    teardown(tbase);
 }
 
 // ------------------------------------------------------- backward (rows) --

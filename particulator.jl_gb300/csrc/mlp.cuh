@@ -43,7 +43,7 @@ struct TrainBuf {
 constexpr int kTileBytes = kH * kH * 2;
 
 __global__ void k_mlp_forward(Net net, const float* X, long long n, float* Y, TrainBuf tb, const float* T,
-                              float* G, double* loss, int* err);
+                              float* G, double* loss, int* err, const unsigned long long* n_dev);
 __global__ void k_mlp_bwd_a(Net net, const float* X, long long n, TrainBuf tb, float* G, int* err);
 __global__ void k_mlp_bwd_w(long long n, TrainBuf tb, float* G, int* err);
 __global__ void k_mlp_adam(float* P, const float* G, float* M, float* V, __nv_bfloat16* W2, __nv_bfloat16* W3,
@@ -52,7 +52,18 @@ __global__ void k_mlp_sync_bf16(const float* P, __nv_bfloat16* W2, __nv_bfloat16
 __global__ void k_mlp_gather(const float* Xall, const float* Tall, long long nall, float* X, float* T, int B,
                              uint32_t key0, uint32_t key1, uint32_t step);
 
+// Several networks evaluated on the same inputs in one launch (blockIdx.y =
+// network): the step's learned round.
+constexpr int kMaxNets = 8;
+struct NetSet {
+    Net net[kMaxNets];
+    float* Y[kMaxNets];
+};
+constexpr int kInferThreads = 512;   // 4 column quarters x 128 rows
+__global__ void k_mlp_infer(NetSet ns, const float* X, long long cap, const unsigned long long* n_dev, int* err);
+
 constexpr size_t kFwdSmem = 3 * kTileBytes + 1024 + 3 * kH * 4 + 64;
+constexpr size_t kInferSmem = 3 * kTileBytes + 1024 + 4 * kH * 4 + 64;
 constexpr size_t kBwdASmem = 3 * kTileBytes + 1024 + 4 * kH * 4 + 64;
 constexpr size_t kBwdWSmem = 4 * kTileBytes + 1024 + 64;
 

@@ -1117,6 +1117,9 @@ __device__ __forceinline__ void load_slot(Lane& L, const float4* xw, const float
 // is unchanged.
 template <int MINB, bool GENERAL, bool EVENT, bool LEARN>
 __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
+    // a queue pass over an empty queue has nothing to stage, run or tally
+    if (A.spill_mode == 1 && *A.sp_in_n == 0) return;
+    if (LEARN && A.spill_mode == 2 && *A.lq_in_n == 0) return;
     extern __shared__ __align__(16) unsigned char smem[];
     const int nwarps = blockDim.x >> 5;
     const int warp = threadIdx.x >> 5;
@@ -1484,7 +1487,10 @@ __global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long 
 // Spill-pass prologue: the spill queue written by the previous pass becomes
 // the input of the next.
 __global__ void k_begin_spill(Control* ctl, unsigned long long* in_n, unsigned long long* out_n) {
-    if (threadIdx.x == 0) { *out_n = 0; ctl->head = 0; }
+    if (threadIdx.x == 0) {   // out_n == nullptr: the pass appends to a queue that keeps its contents
+        if (out_n) *out_n = 0;
+        ctl->head = 0;
+    }
     (void)in_n;
 }
 
@@ -1944,7 +1950,9 @@ __global__ void k_learn_hist(StepArgs A, int species, int j, int kind, int nT, l
 }
 
 // Network inputs of the suspended collisions: (a, 2u - 1).
-__global__ void k_learn_x(const float4* ps, const float4* m2, long long n, float* X) {
+__global__ void k_learn_x(const float4* ps, const float4* m2, const unsigned long long* n_dev, long long cap,
+                          float* X) {
+    const long long n = min((long long)*n_dev, cap);   // the queue counter can pass its capacity
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float4 b = ps[i];
         float4 q = m2[i];
@@ -1956,8 +1964,9 @@ __global__ void k_learn_x(const float4* ps, const float4* m2, long long n, float
 
 // Output of the network attached to each suspended collision's process:
 // Y[i] = Yk[which[species][j] * stride + i].
-__global__ void k_learn_pick(const float4* m2, long long n, const float* Yk, long long stride, LearnPick which,
-                             float* Y) {
+__global__ void k_learn_pick(const float4* m2, const unsigned long long* n_dev, long long cap, const float* Yk,
+                             long long stride, LearnPick which, float* Y) {
+    const long long n = min((long long)*n_dev, cap);
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         uint32_t pk = __float_as_uint(m2[i].w);
         int sp = int(pk & 3u), j = int((pk >> 8) & 15u);
