@@ -288,6 +288,16 @@ int pcl_set_swarms(void* ctx, int nswarm, const double* E, const double* Fdt, do
 /* Per-swarm FP64 moments of one species: out[6*s + q] = {live, sum w,
  * sum w E (J), sum w z, sum w z^2, sum w (x^2 + y^2)} (m). */
 int pcl_swarm_moments(void* ctx, int species, int nswarm, double* out);
+/* Energy spectrum of the live particles of one species, as the reference's
+ * scripts compute it with StatsBase.fit(Histogram, E, edges, weights(w))
+ * (scripts/beam.jl:137-147, scripts/swarm.jl:149-158): counts[i] and
+ * weights[i] (sum of w) over edges[i] <= E < edges[i+1], kinetic energies in
+ * J, edges strictly increasing (2 <= nedges <= PCL_MAX_HIST_EDGES); energies
+ * outside [edges[0], edges[nedges-1]) are not counted.  swarm >= 0 (batched
+ * contexts) keeps that swarm only; -1 takes every particle. */
+#define PCL_MAX_HIST_EDGES 4097
+int pcl_energy_histogram(void* ctx, int species, int swarm, int nedges, const double* edges, int64_t* counts,
+                         double* weights);
 /* Live particles of each swarm of one species (out[s], s < nswarm; with
  * nswarm = 1 the whole population). */
 int pcl_swarm_counts(void* ctx, int species, int nswarm, int64_t* out);

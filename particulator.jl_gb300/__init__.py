@@ -19,7 +19,7 @@ from .forcing import (HomogeneousField, DoubleLayerField, StepField, ConfinedDou
                       NullForcing, CombinedForcing, RK2Pusher)
 from .population import (ElectronState, PhotonState, PositronState, ParticleArrays, Population, MultiPopulation,
                          init, advance, run, nparticles, nactives, weight, meanenergy, maxenergy, spread, posvar,
-                         repack, droplow, kinenergy, AbstractCallback, VoidCallback, CombinedCallback,
+                         spectrum, repack, droplow, kinenergy, AbstractCallback, VoidCallback, CombinedCallback,
                          CollisionCounter, PopulationTargetCallback, ParticleCountCallback, WallCallback,
                          RouletteCallback, SplitCallback)
 from . import workloads, learned

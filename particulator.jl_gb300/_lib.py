@@ -116,6 +116,7 @@ _SIGS = {
     "pcl_set_swarms": (C.c_int, [C.c_void_p, C.c_int, _P(_d), _P(_d), _d]),
     "pcl_swarm_moments": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_d)]),
     "pcl_swarm_counts": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_i64)]),
+    "pcl_energy_histogram": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _P(_d), _P(_i64), _P(_d)]),
     "pcl_set_swarm_cap": (C.c_int, [C.c_void_p, C.c_int, _i64]),
     "pcl_upload": (C.c_int, [C.c_void_p, C.c_int, _i64, _P(_d), _P(_d), _P(_d), _P(_d), _P(_d), _P(_u64),
                              _u64]),

@@ -34,6 +34,9 @@ __global__ void k_swarm_count(const uint4* meta, const unsigned long long* nslot
 __global__ void k_roulette_cap(float4* xw, uint4* meta, const unsigned long long* nslots, long long slot_cap,
                                const unsigned int* counts, int nswarm, unsigned long long cap, uint32_t k0,
                                uint32_t k1);
+__global__ void k_energy_hist(const float4* xw, const float4* ps, const uint4* meta, const unsigned long long* nslots,
+                              long long cap, int species, int swarm, const double* edges, int nb,
+                              unsigned long long* counts, double* wsum);
 __global__ void k_learn_pick(const float4* m2, const unsigned long long* n_dev, long long cap, const float* Yk,
                              long long stride, LearnPick which, float* Y);
 namespace mlp {
@@ -1302,6 +1305,52 @@ int pcl_swarm_moments(void* ctx, int species, int nswarm, double* out) {
     CK(cudaMemcpyAsync(out, d, sizeof(double) * len, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     for (int k = 0; k < nswarm; ++k) out[6 * k + 2] = e_to_si(out[6 * k + 2]);
+    return PCL_OK;
+}
+
+int pcl_energy_histogram(void* ctx, int species, int swarm, int nedges, const double* edges, int64_t* counts,
+                         double* weights) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !edges || !counts || !weights) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    if (nedges < 2 || nedges > PCL_MAX_HIST_EDGES) return fail(c, PCL_ERR_INVALID, "nedges out of range");
+    if (swarm < -1 || swarm >= std::max(1, c->nswarm) || (swarm >= 0 && c->nswarm == 0))
+        return fail(c, PCL_ERR_INVALID, "swarm out of range");
+    std::vector<double> ed(nedges);
+    for (int i = 0; i < nedges; ++i) {
+        if (!(std::isfinite(edges[i]) && edges[i] >= 0.0) || (i > 0 && !(edges[i] > edges[i - 1])))
+            return fail(c, PCL_ERR_INVALID, "edges must be finite, >= 0 and strictly increasing");
+        ed[i] = e_to_dev(edges[i]);
+    }
+    const int nb = nedges - 1;
+    SpeciesState& S = c->sp[species];
+    CK(cudaSetDevice(c->device));
+    std::vector<unsigned long long> hc(nb, 0ull);
+    std::vector<double> hw(nb, 0.0);
+    if (S.cap > 0) {
+        // scratch: counts [nb] (u64), weights [nb], edges [nb + 1]
+        if ((rc = ensure_scratch(c, sizeof(double) * (3 * size_t(nb) + 1)))) return rc;
+        unsigned long long* dc = static_cast<unsigned long long*>(c->d_scr);
+        double* dw = reinterpret_cast<double*>(dc + nb);
+        double* de = dw + nb;
+        CK(cudaMemcpyAsync(de, ed.data(), sizeof(double) * nedges, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaMemsetAsync(dc, 0, 2 * sizeof(double) * nb, c->stream));
+        const size_t smem = sizeof(double) * (2 * size_t(nb) + 1) + sizeof(unsigned int) * nb;
+        CK(cudaFuncSetAttribute(k_energy_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(sizeof(double) * (2 * PCL_MAX_HIST_EDGES) + 4 * PCL_MAX_HIST_EDGES)));
+        const int grid = int(std::min<long long>((S.cap + 255) / 256, 2ll * c->sm_count));
+        k_energy_hist<<<grid, 256, smem, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], &c->d_ctl->n[species],
+                                                      S.cap, species, swarm, de, nb, dc, dw);
+        CK(cudaGetLastError());
+        CK(cudaMemcpyAsync(hc.data(), dc, sizeof(unsigned long long) * nb, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(hw.data(), dw, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    for (int i = 0; i < nb; ++i) {
+        counts[i] = (int64_t)hc[i];
+        weights[i] = hw[i];
+    }
     return PCL_OK;
 }
 

@@ -1625,6 +1625,51 @@ __global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta,
     }
 }
 
+// Energy spectrum of the live particles, as the reference's scripts build one
+// with StatsBase.fit(Histogram, E, edges[, weights]) (scripts/beam.jl:137-147,
+// scripts/swarm.jl:149-158): bin i counts edges[i] <= E < edges[i+1] (device
+// energy units, FP64 from the FP32 momentum); energies outside
+// [edges[0], edges[nb]) are not counted.  swarm >= 0 keeps the particles of
+// that swarm (top 8 bits of the stream id) only.  Per-block shared bins, one
+// global atomic per non-empty bin.
+__global__ void k_energy_hist(const float4* xw, const float4* ps, const uint4* meta, const unsigned long long* nslots,
+                              long long cap, int species, int swarm, const double* edges, int nb,
+                              unsigned long long* counts, double* wsum) {
+    extern __shared__ double hsh[];
+    double* se = hsh;                 // [nb + 1] edges
+    double* sw = hsh + nb + 1;        // [nb] weights
+    unsigned int* sc = reinterpret_cast<unsigned int*>(sw + nb);   // [nb] counts
+    for (int i = threadIdx.x; i <= nb; i += blockDim.x) se[i] = edges[i];
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) { sw[i] = 0.0; sc[i] = 0u; }
+    __syncthreads();
+    const long long n = min((long long)*nslots, cap);
+    const double lo = se[0], hi = se[nb];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const uint4 m = meta[i];
+        if (m.z == PCL_DEAD_CTR) continue;
+        if (swarm >= 0 && int(m.y >> 24) != swarm) continue;
+        const float4 b = ps[i];
+        const double p2 = double(b.x) * b.x + double(b.y) * b.y + double(b.z) * b.z;
+        const double E = (species == PCL_PHOTON) ? sqrt(p2) : p2 / (sqrt(1.0 + p2) + 1.0);
+        if (!(E >= lo && E < hi)) continue;
+        int a = 0, z = nb;            // se[a] <= E < se[z]
+        while (z - a > 1) {
+            const int mid = (a + z) >> 1;
+            if (E >= se[mid]) a = mid; else z = mid;
+        }
+        atomicAdd(&sc[a], 1u);
+        atomicAdd(&sw[a], double(xw[i].w));
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+        if (sc[i]) {
+            atomicAdd(&counts[i], (unsigned long long)sc[i]);
+            atomicAdd(&wsum[i], sw[i]);
+        }
+    }
+}
+
 // FP64 moments per swarm of a batched context: out[sw][6] = {live, sum w,
 // sum w E, sum w z, sum w z^2, sum w x^2 + y^2}; lanes of one warp are grouped
 // by swarm before the atomics.

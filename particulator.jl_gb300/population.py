@@ -125,6 +125,20 @@ class Population:
         _lib.check(_lib.lib().pcl_moments(self.ctx, self.particle, _lib.dptr(out)), self.ctx, "pcl_moments")
         return out
 
+    def energy_histogram(self, edges, swarm: int = -1):
+        """Device histogram of the live particles' kinetic energies (J) over
+        `edges` (pcl_energy_histogram): (counts, summed weights) per bin
+        edges[i] <= E < edges[i+1], as StatsBase.fit(Histogram, ...) in the
+        reference's scripts.  swarm >= 0 keeps one swarm of a batch."""
+        e = np.ascontiguousarray(np.asarray(edges, dtype=float))
+        nb = len(e) - 1
+        counts = np.zeros(max(nb, 0), dtype=np.int64)
+        w = np.zeros(max(nb, 0))
+        _lib.check(_lib.lib().pcl_energy_histogram(self.ctx, self.particle, int(swarm), len(e), _lib.dptr(e),
+                                                   _lib.i64ptr(counts), _lib.dptr(w)), self.ctx,
+                   "pcl_energy_histogram")
+        return counts, w
+
     def particles(self) -> ParticleArrays:
         """Download the live particles (SI)."""
         L = _lib.lib()
@@ -627,6 +641,16 @@ def meanenergy(pop: Population) -> float:
     """meanenergy (population.jl:152-166)."""
     m = pop.moments()
     return float(m[1] / m[0]) if m[0] else math.nan
+
+
+def spectrum(pop: Population, edges, n: float = 1.0, weighted: bool = True, swarm: int = -1) -> np.ndarray:
+    """Energy spectrum per unit energy as plotspec builds it (scripts/beam.jl:137-147
+    unweighted, scripts/swarm.jl:149-158 weighted): the histogram over `edges`
+    (J) normalised as StatsBase.normalize(mode=:density), i.e. divided by the
+    bin widths, then divided by n (e.g. the number of primaries)."""
+    counts, w = pop.energy_histogram(edges, swarm)
+    h = w if weighted else counts.astype(float)
+    return h / np.diff(np.asarray(edges, dtype=float)) / n
 
 
 def maxenergy(pop: Population) -> float:

@@ -361,3 +361,40 @@ def test_moments_match_download(pcl, gpu, air):
         np.testing.assert_allclose(m[2:5], (a.w[:, None] * a.x).sum(0), rtol=1e-5, atol=1e-12)
         assert abs(pcl.meanenergy(pop) - (a.w * E).sum() / a.w.sum()) <= 1e-5 * pcl.meanenergy(pop)
     mp.close()
+
+
+@pytest.mark.gpu
+def test_energy_histogram(pcl, gpu, air):
+    """pcl_energy_histogram against numpy on the downloaded particles: counts
+    and summed weights per bin edges[i] <= E < edges[i+1] (StatsBase.fit
+    semantics), equal except for particles within 1e-9 of an edge."""
+    rng = np.random.default_rng(21)
+    n = 200_000
+    E0 = 10 ** rng.uniform(3.5, 7.5, n) * pcl.co.eV
+    p = pcl.workloads.isotropic(n, 1e6 * pcl.co.eV, rng)
+    p *= (pcl.momentum_norm_from_kin(pcl.Electron, E0) / np.linalg.norm(p, axis=1))[:, None]
+    w = rng.uniform(0.5, 2.0, n)
+    arr = pcl.ParticleArrays(np.zeros((n, 3)), p, w, np.zeros(n))
+    mp = pcl.MultiPopulation(
+        ("electron", pcl.Population(n, arr, air["tabs"][0], air["cuts"][0], particle=pcl.Electron)), seed=3)
+    pop = mp.get(pcl.Electron)
+    g = pop.particles()
+    E = pcl.kinenergy(pcl.Electron, g.p)
+    for edges in (10 ** np.linspace(4, 7, 201) * pcl.co.eV, np.array([0.0, 1e5 * pcl.co.eV]),
+                  np.sort(rng.uniform(1e4, 1e7, 4097)) * pcl.co.eV):
+        counts, wsum = pop.energy_histogram(edges)
+        b = np.searchsorted(edges, E, side="right") - 1
+        ok = (b >= 0) & (b < len(edges) - 1)
+        ref_c = np.bincount(b[ok], minlength=len(edges) - 1)
+        ref_w = np.bincount(b[ok], weights=g.w[ok], minlength=len(edges) - 1)
+        k = np.searchsorted(edges, E)
+        lo, hi = edges[np.clip(k - 1, 0, len(edges) - 1)], edges[np.clip(k, 0, len(edges) - 1)]
+        near = (np.abs(E - lo) <= 1e-9 * E) | (np.abs(E - hi) <= 1e-9 * E)
+        slack = int(near.sum())
+        assert np.abs(counts - ref_c).sum() <= 2 * slack, (np.abs(counts - ref_c).sum(), slack)
+        np.testing.assert_allclose(wsum, ref_w, rtol=1e-9, atol=2.0 * slack + 1e-9)
+    dens = pcl.spectrum(pop, edges, n=10.0)
+    np.testing.assert_allclose(dens * np.diff(edges) * 10.0, wsum, rtol=1e-12)
+    with pytest.raises(Exception):
+        pop.energy_histogram(np.array([1.0, 0.5]))
+    mp.close()

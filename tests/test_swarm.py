@@ -339,3 +339,29 @@ def test_device_swarm_cap(pcl, gpu):
         np.testing.assert_array_equal(ga.w[np.argsort(ga.sid)], gb.w[np.argsort(gb.sid)])
     a.mpopl.close()
     b.mpopl.close()
+
+
+@pytest.mark.gpu
+def test_swarm_energy_histogram(pcl, gpu):
+    """Per-swarm spectra (pcl_energy_histogram with a swarm): each swarm's
+    counts and weights are those of its particles, and they sum to the whole."""
+    b = _batch(pcl)
+    for k in range(3):
+        pcl.advance(b.mpopl, b.pusher, (k + 1) * b.dt)
+    pop = b.mpopl.get(pcl.Electron)
+    g = pop.particles()
+    E = pcl.kinenergy(pcl.Electron, g.p)
+    sw = (g.sid >> np.uint64(56)).astype(int)
+    edges = 10 ** np.linspace(3.5, 7.5, 65) * pcl.co.eV
+    call, wall = pop.energy_histogram(edges)
+    tot_c, tot_w = np.zeros_like(call), np.zeros_like(wall)
+    for s in range(len(b.E)):
+        c, w = pop.energy_histogram(edges, swarm=s)
+        m = sw == s
+        ref = np.histogram(E[m], bins=edges)[0]
+        assert np.abs(c - ref).sum() <= 2, (s, c, ref)
+        tot_c += c
+        tot_w += w
+    np.testing.assert_array_equal(tot_c, call)
+    np.testing.assert_allclose(tot_w, wall, rtol=1e-12)
+    b.mpopl.close()
