@@ -316,8 +316,8 @@ def run_learned(args, pcl):
         pos = pcl.learned.table_positions(et, kind)
         targets = pos if kind == pcl.learned.LEARN_SB else pos[:1]   # Moller: one network for both Z
         for j in targets:
-            net, loss = pcl.learned.train_sampler(mp, pcl.Electron, j, kind, samples=1e8, nT=1024, Q=1024,
-                                                  steps=8000, batch=8192, lr=2e-3, seed=j)
+            net, loss = pcl.learned.train_sampler(mp, pcl.Electron, j, kind, samples=args.train_samples, nT=1024,
+                                                  Q=1024, steps=args.train_steps, batch=8192, lr=2e-3, seed=j)
             nets.append((j, kind, loss))
             for q in (pos if kind == pcl.learned.LEARN_MOLLER else [j]):
                 attach.append((q, kind, net))
@@ -363,7 +363,8 @@ def run_learned(args, pcl):
             "dtype": "f32+bf16", "data": "synthetic",
             "config": {"workload": "rrea-air-0.5MVm-16M-learned", "seed_electrons": args.n, "dt_s": 1e-12,
                        "networks": [{"table_position": j, "kind": k, "train_loss": l} for j, k, l in nets],
-                       "training_s": t_train, "training_samples_per_network": 1e8},
+                       "training_s": t_train, "training_samples_per_network": args.train_samples,
+                       "training_steps": args.train_steps},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                          "peak_kind": peak_kind, "traffic": None, "kernel": "k_step"},
             "learned": {"collisions_per_step": r["learned_collisions"] / args.steps,
@@ -603,6 +604,8 @@ def main():
     ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned", "plain", "reid", "mlp"])
     ap.add_argument("--nswarm", type=int, default=256)
     ap.add_argument("--tune-steps", type=int, default=512)
+    ap.add_argument("--train-samples", type=float, default=1e8, help="learned form: training samples per network")
+    ap.add_argument("--train-steps", type=int, default=8000, help="learned form: Adam steps per network")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
