@@ -594,6 +594,7 @@ def main():
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--n", type=int, default=1 << 24, help="seed electrons")
     ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-chunks", type=int, default=8, help="pipeline chunks of pcl_advance_host")
     ap.add_argument("--cpu-sample", type=int, default=1 << 21)
     ap.add_argument("--cpu-steps", type=int, default=48)
     ap.add_argument("--no-e2e", action="store_true")
@@ -664,42 +665,26 @@ def main():
     try:
         if args.no_e2e:
             raise RuntimeError("skipped (--no-e2e)")
-        import torch
-        caps = [mp.get(s).max_particles for s in (0, 1, 2)]
-        host = []
-        for s in (0, 1, 2):
-            xw = torch.empty((caps[s], 4), dtype=torch.float32).pin_memory()
-            ps = torch.empty((caps[s], 4), dtype=torch.float32).pin_memory()
-            meta = torch.empty((caps[s], 4), dtype=torch.int32).pin_memory()
-            pk = pcl._lib.Packed(C.cast(xw.data_ptr(), C.POINTER(C.c_float)),
-                                 C.cast(ps.data_ptr(), C.POINTER(C.c_float)),
-                                 C.cast(meta.data_ptr(), C.POINTER(C.c_uint32)))
-            host.append((xw, ps, meta, pk))
-        ns = []
-        for s in (0, 1, 2):
-            n = C.c_int64(caps[s])
-            pcl._lib.check(L.pcl_download_packed(ctx, s, C.byref(n), C.byref(host[s][3])), ctx)
-            ns.append(n.value)
+        # the population lives in pinned host buffers: every step uploads it,
+        # advances it and downloads it (pcl_advance_host, chunked pipeline)
+        host = mp.packed_buffers(pinned=True)
+        ns = mp.download_packed(host)
+        period = 8
         tal_a = mp.tallies()
         h2d = d2h = 0
         L.pcl_timer_start(ctx)
-        for _ in range(args.e2e_steps):
-            for s in (0, 1, 2):
-                pcl._lib.check(L.pcl_upload_packed(ctx, s, ns[s], C.byref(host[s][3])), ctx)
-                h2d += 48 * ns[s]
+        for k in range(args.e2e_steps):
             t += dt
-            pcl.advance(mp, pusher, t)
-            for s in (0, 1, 2):
-                n = C.c_int64(caps[s])
-                pcl._lib.check(L.pcl_download_packed(ctx, s, C.byref(n), C.byref(host[s][3])), ctx)
-                ns[s] = n.value
-                d2h += 48 * n.value
+            h2d += 48 * sum(ns)
+            ns = mp.advance_host(t, host, ns, nchunks=args.e2e_chunks, compact=(k % period == period - 1))
+            d2h += 48 * sum(ns)
         ms2 = C.c_double()
         L.pcl_timer_stop(ctx, C.byref(ms2))
         tal_b = mp.tallies()
         e_el = _barrier_max(ms2.value / 1e3, ws)
         e2e = {"value": (tal_b.particle_steps - tal_a.particle_steps) * ws / e_el, "unit": UNIT,
-               "h2d_bytes_per_step": int(h2d / args.e2e_steps), "d2h_bytes_per_step": int(d2h / args.e2e_steps)}
+               "h2d_bytes_per_step": int(h2d / args.e2e_steps), "d2h_bytes_per_step": int(d2h / args.e2e_steps),
+               "api": "pcl_advance_host", "chunks": args.e2e_chunks, "host_buffers": "pinned"}
     except Exception as ex:  # pragma: no cover
         e2e = {"value": None, "unit": UNIT, "error": str(ex)[:200], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     # ---- CPU baseline (rank 0, N = 1)

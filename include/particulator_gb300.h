@@ -335,6 +335,21 @@ int pcl_download_packed(void* ctx, int species, int64_t* n, pcl_packed* host);
  * below their cut.  tfinal must be > the context time. */
 int pcl_advance(void* ctx, double tfinal);
 
+/* advance! of populations that live in host memory (packed layout, one
+ * pcl_packed per species): the result equals pcl_upload_packed(in[s]) for
+ * every species, pcl_advance(tfinal), pcl_download_packed(out[s]) - slots
+ * updated in place with removed particles marked dead (ctr 0xFFFFFFFF), the
+ * step's secondaries appended after n_in[s] - but runs as a pipeline: the
+ * work is cut into `nchunks` (1-64) ranges, each uploaded on one copy stream,
+ * stepped by a population launch over its range, and downloaded on another
+ * copy stream while later ranges are still uploading or stepping.
+ * compact != 0 repacks the population on the device (repack!,
+ * population.jl:229-259) before it is downloaded (no download overlap that
+ * step).  in and out may be the same buffers; n_out[s] <= out_cap[s] or
+ * PCL_ERR_CAPACITY.  Host buffers should be pinned. */
+int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_packed* in, int64_t* n_out,
+                     pcl_packed* out, const int64_t* out_cap, int nchunks, int compact);
+
 /* run!(mpopl, pusher, tfinal, dt, callback) (run.jl:1-29) with the device-side
  * PopulationTargetCallback / CollisionCounter.  Steps of dt until tfinal, the
  * target or max_steps; fills *out. */

@@ -123,6 +123,8 @@ _SIGS = {
     "pcl_download": (C.c_int, [C.c_void_p, C.c_int, _P(_i64), _P(_d), _P(_d), _P(_d), _P(_d), _P(_d),
                                _P(_u64), _P(_u32)]),
     "pcl_upload_packed": (C.c_int, [C.c_void_p, C.c_int, _i64, _P(Packed)]),
+    "pcl_advance_host": (C.c_int, [C.c_void_p, _d, _P(_i64), _P(Packed), _P(_i64), _P(Packed), _P(_i64), C.c_int,
+                                   C.c_int]),
     "pcl_download_packed": (C.c_int, [C.c_void_p, C.c_int, _P(_i64), _P(Packed)]),
     "pcl_advance": (C.c_int, [C.c_void_p, _d]),
     "pcl_run": (C.c_int, [C.c_void_p, _d, _d, _P(RunOpts), _P(Tallies)]),

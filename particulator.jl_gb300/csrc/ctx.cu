@@ -19,6 +19,8 @@ extern "C" int pcl_ratebound_split(int, int, int, int, double, const double*, do
 namespace pcl {
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A);
 cudaError_t prepare_step(int minb, size_t smem, bool general, bool event, bool learn);
+cudaError_t launch_step_prepared(int minb, int grid, int threads, size_t smem, cudaStream_t stream,
+                                 const StepArgs& A);
 __global__ void k_learn_hist(StepArgs A, int species, int j, int kind, int nT, long long per_T, int nbins,
                              float hmin, float hmax, unsigned long long sid_base, unsigned int* hist);
 __global__ void k_learn_x(const float4* ps, const float4* m2, const unsigned long long* n_dev, long long cap,
@@ -151,6 +153,12 @@ struct Ctx {
     size_t scr_bytes = 0;
     unsigned int* d_swcnt = nullptr;       // [3][256] live particles per swarm
     long long swarm_cap[3] = {0, 0, 0};    // pcl_set_swarm_cap, 0 = off
+    // pcl_advance_host: copy streams and per-chunk events
+    cudaStream_t s_h2d = nullptr, s_d2h = nullptr, s_cmp = nullptr;
+    std::vector<cudaEvent_t> io_ev;        // [2 * chunks]: uploaded, stepped
+    std::vector<cudaEvent_t> io_tev;       // [2 * chunks]: timing of each chunk's launch
+    cudaEvent_t io_join = nullptr;
+    unsigned long long* d_heads = nullptr; // [64] work counters of the chunk launches
     // accumulated host state
     double t = 0.0;
     long long steps = 0;
@@ -475,6 +483,7 @@ static StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, int sp_
     A.sp_in_n = c->d_spn + sp_in;
     A.sp_out_n = c->d_spn + sp_out;
     A.ctl = c->d_ctl;
+    A.head = &c->d_ctl->head;
     A.blob = c->d_blob;
     for (size_t b = 0; b < c->sb.size(); ++b) A.sb_data[b] = c->sb[b].d_data;
     A.key0 = uint32_t(c->cfg.seed);
@@ -952,6 +961,13 @@ void pcl_destroy(void* ctx) {
     if (c->h_ctl) cudaFreeHost(c->h_ctl);
     if (c->h_spn) cudaFreeHost(c->h_spn);
     if (c->h_lqn) cudaFreeHost(c->h_lqn);
+    for (cudaEvent_t e : c->io_ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->io_tev) cudaEventDestroy(e);
+    if (c->io_join) cudaEventDestroy(c->io_join);
+    if (c->s_h2d) cudaStreamDestroy(c->s_h2d);
+    if (c->s_d2h) cudaStreamDestroy(c->s_d2h);
+    if (c->s_cmp) cudaStreamDestroy(c->s_cmp);
+    cudaFree(c->d_heads);
     free_lq(c);
     cudaFree(c->d_wall_xw); cudaFree(c->d_wall_pt); cudaFree(c->d_wall_meta); cudaFree(c->d_wall_n);
     for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
@@ -1510,6 +1526,185 @@ int pcl_download_packed(void* ctx, int species, int64_t* n, pcl_packed* host) {
     }
     CK(cudaStreamSynchronize(c->stream));
     *n = slots;
+    return PCL_OK;
+}
+
+// Slots [a, b) of each species covered by concatenated indices [g0, g1) of
+// the species ranges n[0], n[1], n[2] (the step kernel's work order).
+static void chunk_ranges(const long long n[3], long long g0, long long g1, long long a[3], long long b[3]) {
+    long long base = 0;
+    for (int s = 0; s < 3; ++s) {
+        a[s] = std::min(std::max(g0 - base, 0ll), n[s]);
+        b[s] = std::min(std::max(g1 - base, 0ll), n[s]);
+        base += n[s];
+    }
+}
+
+static cudaError_t copy_slots(const SpeciesState& S, const pcl_packed& h, long long a, long long b, bool up,
+                              cudaStream_t st) {
+    if (b <= a) return cudaSuccess;
+    const size_t n = size_t(b - a);
+    cudaError_t e;
+    if (up) {
+        e = cudaMemcpyAsync(S.xw[S.cur] + a, reinterpret_cast<const float4*>(h.xw) + a, 16 * n,
+                            cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(S.ps[S.cur] + a, reinterpret_cast<const float4*>(h.ps) + a, 16 * n,
+                                cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(S.meta[S.cur] + a, reinterpret_cast<const uint4*>(h.meta) + a, 16 * n,
+                                cudaMemcpyHostToDevice, st);
+    } else {
+        e = cudaMemcpyAsync(reinterpret_cast<float4*>(h.xw) + a, S.xw[S.cur] + a, 16 * n, cudaMemcpyDeviceToHost,
+                            st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(reinterpret_cast<float4*>(h.ps) + a, S.ps[S.cur] + a, 16 * n,
+                                cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(reinterpret_cast<uint4*>(h.meta) + a, S.meta[S.cur] + a, 16 * n,
+                                cudaMemcpyDeviceToHost, st);
+    }
+    return e;
+}
+
+int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_packed* in, int64_t* n_out,
+                     pcl_packed* out, const int64_t* out_cap, int nchunks, int compact) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || !n_in || !in || !n_out || !out || !out_cap) return PCL_ERR_INVALID;
+    if (!(tfinal > c->t)) return fail(c, PCL_ERR_INVALID, "tfinal must exceed the current time");
+    if (nchunks < 1 || nchunks > 64) return fail(c, PCL_ERR_INVALID, "nchunks must be in [1, 64]");
+    bool any = false;
+    long long n[3];
+    for (int s = 0; s < 3; ++s) {
+        SpeciesState& S = c->sp[s];
+        any = any || S.set;
+        n[s] = (S.set && S.cap > 0) ? (long long)n_in[s] : 0;
+        if (n[s] < 0 || n[s] > S.cap) return fail(c, PCL_ERR_CAPACITY, "input exceeds capacity");
+        if (n[s] > 0 && (!in[s].xw || !in[s].ps || !in[s].meta || !out[s].xw || !out[s].ps || !out[s].meta))
+            return fail(c, PCL_ERR_INVALID, "null particle arrays");
+    }
+    if (!any) return fail(c, PCL_ERR_STATE, "no species set");
+    CK(cudaSetDevice(c->device));
+    int rc = build_blob(c);
+    if (rc || (rc = ensure_spill(c)) || (rc = ensure_lq(c))) return rc;
+    if (!c->s_h2d) CK(cudaStreamCreateWithFlags(&c->s_h2d, cudaStreamNonBlocking));
+    if (!c->s_d2h) CK(cudaStreamCreateWithFlags(&c->s_d2h, cudaStreamNonBlocking));
+    if (!c->s_cmp) CK(cudaStreamCreateWithFlags(&c->s_cmp, cudaStreamNonBlocking));
+    if (!c->io_join) CK(cudaEventCreateWithFlags(&c->io_join, cudaEventDisableTiming));
+    if (!c->d_heads) CK(cudaMalloc(&c->d_heads, 64 * sizeof(unsigned long long)));
+    while ((int)c->io_ev.size() < 2 * nchunks) {
+        cudaEvent_t e;
+        CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->io_ev.push_back(e);
+        CK(cudaEventCreate(&e));
+        c->io_tev.push_back(e);
+    }
+    const double dt_si = tfinal - c->t;
+    const double dt = t_to_dev(dt_si);
+    const int threads = block_threads(c);
+    const size_t smem = step_smem_bytes(int(c->blob.size()), threads, c->cfg.classic_step == 0);
+    const int minb = blocks_per_sm(c);
+    // slot counts, then the step prologue (k_begin takes n_start from them)
+    unsigned long long nn[3] = {(unsigned long long)n[0], (unsigned long long)n[1], (unsigned long long)n[2]};
+    for (int s = 0; s < 3; ++s)
+        CK(cudaMemcpyAsync(&c->d_ctl->n[s], &nn[s], sizeof(nn[s]), cudaMemcpyHostToDevice, c->stream));
+    c->launch_t0.push_back(c->t);
+    k_begin<<<1, 64, 0, c->stream>>>(c->d_ctl, c->sp[0].cap, c->sp[1].cap, c->sp[2].cap);
+    CK(cudaMemsetAsync(c->d_spn, 0, 2 * sizeof(unsigned long long), c->stream));
+    if (c->learn_on) CK(cudaMemsetAsync(c->d_lqn, 0, 2 * sizeof(unsigned long long), c->stream));
+    CK(cudaMemsetAsync(c->d_heads, 0, 64 * sizeof(unsigned long long), c->stream));
+    CK(cudaStreamSynchronize(c->stream));   // the host counts above are stack memory
+    // pipeline: upload chunk i (copy stream) -> step chunk i (a launch over its
+    // range with its own work counter, on two alternating compute streams, so
+    // that the tail of one launch overlaps the next) -> download chunk i's
+    // slots, updated in place (copy stream), unless the population is
+    // compacted afterwards.  Launches of different chunks touch disjoint
+    // slots; appends, spills and tallies are atomic.
+    {
+        const StepArgs A0 = make_args(c, dt, 1, 0, 0);
+        CK(prepare_step(minb, smem, A0.general != 0, A0.event != 0, A0.learn != 0));
+    }
+    const long long G = n[0] + n[1] + n[2];
+    const long long cs = std::max<long long>(1, (G + nchunks - 1) / nchunks);
+    int nch = int((G + cs - 1) / cs);
+    for (int i = 0; i < nch; ++i) {
+        const long long g0 = i * cs, g1 = std::min(G, g0 + cs);
+        long long a[3], b[3];
+        chunk_ranges(n, g0, g1, a, b);
+        cudaEvent_t up = c->io_ev[2 * i], done = c->io_ev[2 * i + 1];
+        for (int s = 0; s < 3; ++s) CK(copy_slots(c->sp[s], in[s], a[s], b[s], true, c->s_h2d));
+        CK(cudaEventRecord(up, c->s_h2d));
+        cudaStream_t cs_i = (i & 1) ? c->s_cmp : c->stream;
+        CK(cudaStreamWaitEvent(cs_i, up, 0));
+        StepArgs A = make_args(c, dt, 1, 0, 0);
+        A.g_lo = g0;
+        A.g_hi = g1;
+        A.head = c->d_heads + i;
+        CK(cudaEventRecord(c->io_tev[2 * i], cs_i));
+        CK(launch_step_prepared(minb, grid_blocks(c), threads, smem, cs_i, A));
+        CK(cudaEventRecord(c->io_tev[2 * i + 1], cs_i));
+        c->launches += 1;
+        CK(cudaEventRecord(done, cs_i));
+        if (!compact) {
+            CK(cudaStreamWaitEvent(c->s_d2h, done, 0));
+            for (int s = 0; s < 3; ++s) CK(copy_slots(c->sp[s], out[s], a[s], b[s], false, c->s_d2h));
+        }
+    }
+    // both compute streams joined, then the spill passes and the learned
+    // round, as in a launch group
+    CK(cudaEventRecord(c->io_join, c->s_cmp));
+    CK(cudaStreamWaitEvent(c->stream, c->io_join, 0));
+    {
+        StepArgs P0 = make_args(c, dt, 1, 1, 1), P1 = make_args(c, dt, 1, 1, 0);
+        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 1, c->d_spn + 0);
+        CK(launch_step(minb, grid_blocks(c), threads, smem, c->stream, P0));
+        k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + 0, c->d_spn + 1);
+        CK(launch_step(minb, grid_blocks(c), threads, smem, c->stream, P1));
+        c->launches += 4;
+        if (c->learn_on) {
+            CK(enqueue_learned_round(c, dt, 1, minb, threads, smem));
+            CK(cudaMemcpyAsync(c->h_lqn, c->d_lqn, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                               c->stream));
+        }
+        CK(cudaMemcpyAsync(c->h_spn, c->d_spn, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           c->stream));
+        if ((rc = readback(c))) return rc;
+        if (c->learn_on) count_learned(c);
+        for (int i = 0; i < nch; ++i) {   // step-kernel time of the chunk launches
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, c->io_tev[2 * i], c->io_tev[2 * i + 1]));
+            c->k_ms += ms;
+            c->k_launches += 1;
+        }
+        unsigned long long pending = c->h_spn[1];
+        bool host_passes = false;
+        if ((rc = drain_spills(c, dt, 1, threads, smem, 1, -1, &host_passes, &pending))) return rc;
+        if (host_passes && (rc = readback(c))) return rc;
+    }
+    if (c->h_ctl->timeout) return fail(c, PCL_ERR_TIMEOUT, "table staging wait timed out");
+    c->t = tfinal;
+    c->steps += 1;
+    c->particle_steps += (long long)c->h_ctl->live_start[0];
+    for (int s = 0; s < 3; ++s) c->live[s] = (long long)c->h_ctl->live_end[0][s];
+    if (c->h_ctl->err[PCL_E_CAPACITY] > 0) return fail(c, PCL_ERR_CAPACITY, "population capacity exceeded");
+    if (compact) {
+        if ((rc = compact_all(c)) || (rc = readback(c))) return rc;
+        for (int s = 0; s < 3; ++s) n[s] = 0;   // everything is downloaded below
+    } else {
+        c->steps_since_compact += 1;
+    }
+    // the rest: appended secondaries (or the whole compacted population)
+    long long nf[3];
+    for (int s = 0; s < 3; ++s) {
+        nf[s] = (c->sp[s].set && c->sp[s].cap > 0) ? std::min<long long>((long long)c->h_ctl->n[s], c->sp[s].cap) : 0;
+        if (nf[s] > out_cap[s]) {
+            CK(cudaStreamSynchronize(c->s_d2h));
+            return fail(c, PCL_ERR_CAPACITY, "output arrays too small");
+        }
+    }
+    for (int s = 0; s < 3; ++s) CK(copy_slots(c->sp[s], out[s], n[s], nf[s], false, c->s_d2h));
+    CK(cudaStreamSynchronize(c->s_d2h));
+    for (int s = 0; s < 3; ++s) n_out[s] = nf[s];
     return PCL_OK;
 }
 

@@ -148,6 +148,10 @@ struct StepArgs {
     int general;    // a position-dependent field or a wall is set: the general step kernel runs
     int event;      // the event step kernel runs (parked collisions in full-warp batches)
     int learn;      // learned samplers attached: the kernel with suspend/resume runs
+    // population launches over part of the work: concatenated indices
+    // [g_lo, g_hi) of the species ranges (g_hi == 0: all of them)
+    long long g_lo, g_hi;
+    unsigned long long* head;   // work counter of this launch (the control block's, or a chunk's own)
 };
 
 // Network index of each (species, table position) with a learned sampler (-1: none).

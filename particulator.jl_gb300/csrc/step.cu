@@ -1176,6 +1176,11 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
         nsp1 = (long long)ctl->n_start[1];
         total = nsp0 + nsp1 + (long long)ctl->n_start[2];
     }
+    long long g0 = 0;   // a population launch over part of the work: indices g0 + [0, total)
+    if (!A.spill_mode && A.g_hi > 0) {
+        g0 = min(A.g_lo, total);
+        total = min(A.g_hi, total) - g0;
+    }
     const long long nwarps_grid = (long long)gridDim.x * nwarps;
 
     long long cur = 0, end = 0;  // warp-private chunk (uniform)
@@ -1236,11 +1241,11 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 if (cur >= end) {
                     long long base = 0, len = 0;
                     if (lane == 0) {
-                        long long done_est = (long long)(*(volatile unsigned long long*)&ctl->head);
+                        long long done_est = (long long)(*(volatile unsigned long long*)A.head);
                         long long rem = total - done_est;
                         long long chunk = rem / (4 * nwarps_grid);
                         chunk = chunk < 32 ? 32 : (chunk > 1024 ? 1024 : chunk);
-                        base = (long long)atomicAdd(&ctl->head, (unsigned long long)chunk);
+                        base = (long long)atomicAdd(A.head, (unsigned long long)chunk);
                         len = (base < total) ? min(chunk, total - base) : 0;
                     }
                     base = __shfl_sync(FULL, base, 0);
@@ -1253,7 +1258,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 int tk = min(avail, nn);
                 int rk = __popc(need & lt);
                 if (!has && rk < tk) {
-                    long long v = cur + rk;
+                    long long v = g0 + cur + rk;
                     if (LEARN && A.spill_mode == 2) {
                         float4 a = A.lq_in_xw[v], b = A.lq_in_ps[v];
                         uint4 m1 = A.lq_in_m1[v];
@@ -1460,6 +1465,14 @@ cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream
         if (e != cudaSuccess) return e;
     }
     kern<<<grid, threads, smem, stream>>>(A);
+    return cudaGetLastError();
+}
+
+// Launch without touching the kernel's attributes (prepare_step ran first):
+// setting an attribute between launches of a pipeline can hold the host back.
+cudaError_t launch_step_prepared(int minb, int grid, int threads, size_t smem, cudaStream_t stream,
+                                 const StepArgs& A) {
+    step_kernel(minb, A.general != 0, A.event != 0, A.learn != 0)<<<grid, threads, smem, stream>>>(A);
     return cudaGetLastError();
 }
 

@@ -333,6 +333,64 @@ class MultiPopulation:
         key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
         _lib.check(_lib.lib().pcl_split(self.ctx, key, float(p)), self.ctx, "pcl_split")
 
+    def packed_buffers(self, pinned: bool = False):
+        """Host buffers in the packed device layout for every species, sized to
+        its capacity: [(xw float32 [cap, 4], ps float32 [cap, 4], meta uint32
+        [cap, 4])] (page-locked through torch when pinned=True)."""
+        bufs = []
+        for s in (Electron, Photon, Positron):
+            pop = self.index.get(s)
+            cap = 0 if (pop is None or pop.tally_only) else pop.max_particles
+            if pinned:
+                import torch
+                mk = [torch.empty((cap, 4), dtype=torch.float32).pin_memory(),
+                      torch.empty((cap, 4), dtype=torch.float32).pin_memory(),
+                      torch.empty((cap, 4), dtype=torch.int32).pin_memory()]
+                bufs.append((mk[0].numpy(), mk[1].numpy(), mk[2].numpy().view(np.uint32), mk))
+            else:
+                bufs.append((np.zeros((cap, 4), np.float32), np.zeros((cap, 4), np.float32),
+                             np.zeros((cap, 4), np.uint32), None))
+        return bufs
+
+    @staticmethod
+    def _packed(b):
+        return _lib.Packed(b[0].ctypes.data_as(C.POINTER(C.c_float)), b[1].ctypes.data_as(C.POINTER(C.c_float)),
+                           b[2].ctypes.data_as(C.POINTER(C.c_uint32)))
+
+    def download_packed(self, bufs):
+        """pcl_download_packed of every species into `bufs`; returns the slot counts."""
+        ns = []
+        for s in (Electron, Photon, Positron):
+            n = C.c_int64(len(bufs[s][0]))
+            if len(bufs[s][0]):
+                _lib.check(_lib.lib().pcl_download_packed(self.ctx, s, C.byref(n), C.byref(self._packed(bufs[s]))),
+                           self.ctx, "pcl_download_packed")
+            else:
+                n.value = 0
+            ns.append(int(n.value))
+        return ns
+
+    def upload_packed(self, bufs, ns):
+        for s in (Electron, Photon, Positron):
+            if len(bufs[s][0]):
+                _lib.check(_lib.lib().pcl_upload_packed(self.ctx, s, int(ns[s]), C.byref(self._packed(bufs[s]))),
+                           self.ctx, "pcl_upload_packed")
+
+    def advance_host(self, tfinal: float, bufs, ns, out=None, nchunks: int = 8, compact: bool = False):
+        """advance! of host-resident populations (pcl_advance_host): bufs[s]
+        hold ns[s] slots of species s in the packed layout; the stepped
+        populations are written to `out` (default: in place).  Returns the
+        slot counts after the step."""
+        out = bufs if out is None else out
+        inp = (_lib.Packed * 3)(*[self._packed(b) for b in bufs])
+        outp = (_lib.Packed * 3)(*[self._packed(b) for b in out])
+        n_in = (C.c_int64 * 3)(*[int(x) for x in ns])
+        n_out = (C.c_int64 * 3)()
+        caps = (C.c_int64 * 3)(*[len(b[0]) for b in out])
+        _lib.check(_lib.lib().pcl_advance_host(self.ctx, float(tfinal), n_in, inp, n_out, outp, caps, int(nchunks),
+                                               int(bool(compact))), self.ctx, "pcl_advance_host")
+        return [int(n_out[s]) for s in range(3)]
+
     def set_learned(self, particle, proc_index: int, kind: int, net=None):
         """Attach (net) or detach (None) a learned sampler for one table
         position (pcl_set_learned)."""
