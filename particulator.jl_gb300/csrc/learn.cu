@@ -85,13 +85,12 @@ static int set_attrs(Handle* h) {
 
 Net net_of(const Handle* h) { return Net{h->P, h->W2, h->W3}; }
 
-// forward launch (inference when T == nullptr)
+// training forward launch (targets T)
 static int forward(Handle* h, const float* X, long long n, float* Y, const float* T) {
     long long ntiles = (n + kH - 1) / kH;
     int grid = int(std::min<long long>(ntiles, 2ll * h->sm_count));
     if (grid < 1) return PCL_OK;
-    k_mlp_forward<<<grid, 128, kFwdSmem, h->stream>>>(net_of(h), X, n, Y, h->tb, T, h->G, h->d_loss, h->d_err,
-                                                      nullptr);
+    k_mlp_forward<<<grid, 128, kFwdSmem, h->stream>>>(net_of(h), X, n, Y, h->tb, T, h->G, h->d_loss, h->d_err);
     MCK(cudaGetLastError());
     return PCL_OK;
 }

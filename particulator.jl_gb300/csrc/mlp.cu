@@ -214,18 +214,12 @@ __device__ __forceinline__ bool mma_sync(Smem& s, uint32_t d, const unsigned cha
 }
 
 // ------------------------------------------------------------------ forward --
-// One row per thread.  Inference (T == nullptr): Y[row] = net(X[row]), over
-// min(n, *n_dev) rows when n_dev is given (a count written on the device;
-// blocks without a tile then return before touching tensor memory).
-// Training: keeps the activations in tb, accumulates the mean-squared-error
-// loss and the gradients of the output layer and of b3, and writes dz3.
+// One row per thread.  Training forward pass (inference runs k_mlp_infer):
+// keeps the activations in tb, accumulates the mean-squared-error loss and the
+// gradients of the output layer and of b3, and writes dz3; Y (optional)
+// receives the outputs.
 __global__ void __launch_bounds__(128, 1) k_mlp_forward(Net net, const float* X, long long n, float* Y, TrainBuf tb,
-                                                        const float* T, float* G, double* loss, int* err,
-                                                        const unsigned long long* n_dev) {
-    if (n_dev) {
-        n = min(n, (long long)*n_dev);
-        if ((long long)blockIdx.x * kH >= n) return;
-    }
+                                                        const float* T, float* G, double* loss, int* err) {
     extern __shared__ unsigned char raw[];
     Smem s = carve(raw, 3);
     unsigned char* sA = s.base;

@@ -43,7 +43,7 @@ struct TrainBuf {
 constexpr int kTileBytes = kH * kH * 2;
 
 __global__ void k_mlp_forward(Net net, const float* X, long long n, float* Y, TrainBuf tb, const float* T,
-                              float* G, double* loss, int* err, const unsigned long long* n_dev);
+                              float* G, double* loss, int* err);
 __global__ void k_mlp_bwd_a(Net net, const float* X, long long n, TrainBuf tb, float* G, int* err);
 __global__ void k_mlp_bwd_w(long long n, TrainBuf tb, float* G, int* err);
 __global__ void k_mlp_adam(float* P, const float* G, float* M, float* V, __nv_bfloat16* W2, __nv_bfloat16* W3,
