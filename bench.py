@@ -698,7 +698,7 @@ def main():
     errs = {pcl._lib.ERROR_NAMES[q]: int(tal1.errors[q]) for q in range(8) if tal1.errors[q]}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
+                "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / (args.steps * K), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "rrea-air-0.5MVm-16M", "seed_electrons": args.n, "dt_s": dt,
                            "steps_per_launch": K, "blocks_per_sm": (args.bps or 4) if args.classic else 3,
