@@ -441,3 +441,31 @@ def test_advance_host_equals_upload_advance_download(pcl, gpu, nchunks):
     assert [list(r) for r in ta.collisions] == [list(r) for r in tb.collisions]
     a.mpopl.close()
     b.mpopl.close()
+
+
+@pytest.mark.gpu
+def test_device_cap_equals_roulette_callback(pcl, gpu):
+    """pcl_set_swarm_cap on a context without swarms is RouletteCallback(m)
+    (callback.jl:210-227) on the device: after the same steps it keeps and
+    reweights exactly the particles the host-driven callback keeps."""
+    a = pcl.workloads.avalanche(n=40_000, seed=6, capacity=1 << 18)
+    b = pcl.workloads.avalanche(n=40_000, seed=6, capacity=1 << 18)
+    m = 30_000
+    cb = pcl.RouletteCallback(m)
+    b.mpopl.set_swarm_cap(m, particles=(pcl.Electron, pcl.Photon, pcl.Positron))
+    for k in range(2):
+        t = (k + 1) * a.dt
+        pcl.run(a.mpopl, a.pusher, t, a.dt)
+        cb.onstep(a.mpopl, t)
+        pcl.run(b.mpopl, b.pusher, t, b.dt)
+    pcl.lib().pcl_compact(b.mpopl.ctx)
+    ne = pcl.nactives(b.mpopl.get(pcl.Electron))
+    assert abs(ne - m) < 5 * np.sqrt(m) + 1
+    for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
+        ga, gb = a.mpopl.get(sp).particles(), b.mpopl.get(sp).particles()
+        oa, ob = np.argsort(ga.sid), np.argsort(gb.sid)
+        np.testing.assert_array_equal(ga.sid[oa], gb.sid[ob])
+        np.testing.assert_array_equal(ga.w[oa], gb.w[ob])
+        np.testing.assert_array_equal(ga.p[oa], gb.p[ob])
+    a.mpopl.close()
+    b.mpopl.close()
