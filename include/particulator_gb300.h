@@ -346,7 +346,9 @@ int pcl_advance(void* ctx, double tfinal);
  * compact != 0 repacks the population on the device (repack!,
  * population.jl:229-259) before it is downloaded (no download overlap that
  * step).  in and out may be the same buffers; n_out[s] <= out_cap[s] or
- * PCL_ERR_CAPACITY.  Host buffers should be pinned. */
+ * PCL_ERR_CAPACITY, returned after the step (the context holds the stepped
+ * population; pcl_download_packed reads it into larger arrays).  No copy is
+ * in flight when the call returns.  Host buffers should be pinned. */
 int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_packed* in, int64_t* n_out,
                      pcl_packed* out, const int64_t* out_cap, int nchunks, int compact);
 

@@ -1585,6 +1585,17 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
     }
     if (!any) return fail(c, PCL_ERR_STATE, "no species set");
     CK(cudaSetDevice(c->device));
+    // every return, error or not, leaves no copy into or out of the caller's
+    // buffers in flight
+    struct Drain {
+        Ctx* c;
+        ~Drain() {
+            if (c->s_h2d) cudaStreamSynchronize(c->s_h2d);
+            if (c->s_d2h) cudaStreamSynchronize(c->s_d2h);
+            if (c->s_cmp) cudaStreamSynchronize(c->s_cmp);
+            cudaStreamSynchronize(c->stream);
+        }
+    } drain{c};
     int rc = build_blob(c);
     if (rc || (rc = ensure_spill(c)) || (rc = ensure_lq(c))) return rc;
     if (!c->s_h2d) CK(cudaStreamCreateWithFlags(&c->s_h2d, cudaStreamNonBlocking));
@@ -1697,10 +1708,7 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
     long long nf[3];
     for (int s = 0; s < 3; ++s) {
         nf[s] = (c->sp[s].set && c->sp[s].cap > 0) ? std::min<long long>((long long)c->h_ctl->n[s], c->sp[s].cap) : 0;
-        if (nf[s] > out_cap[s]) {
-            CK(cudaStreamSynchronize(c->s_d2h));
-            return fail(c, PCL_ERR_CAPACITY, "output arrays too small");
-        }
+        if (nf[s] > out_cap[s]) return fail(c, PCL_ERR_CAPACITY, "output arrays too small");
     }
     for (int s = 0; s < 3; ++s) CK(copy_slots(c->sp[s], out[s], n[s], nf[s], false, c->s_d2h));
     CK(cudaStreamSynchronize(c->s_d2h));
