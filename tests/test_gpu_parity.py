@@ -469,3 +469,45 @@ def test_device_cap_equals_roulette_callback(pcl, gpu):
         np.testing.assert_array_equal(ga.p[oa], gb.p[ob])
     a.mpopl.close()
     b.mpopl.close()
+
+
+def _subset(a, m):
+    return type(a)(**{f: getattr(a, f)[m] for f in ("x", "p", "w", "t", "s", "sid", "ctr")})
+
+
+def test_full_size_subset_parity(pcl, oracle, gpu, air):
+    """The bench workload at full size: 2^24 electrons at 1 MeV, isotropic,
+    stepped twice on the device; a random 4096 of them stepped by the oracle
+    from the same state.  A particle's step depends only on its own state and
+    stream, so the subset and all its secondaries must match the oracle as in
+    the small cases (draw counts, stream ids, momenta to 1e-5)."""
+    n = 1 << 24
+    rng = np.random.Generator(np.random.Philox(0))
+    p = pcl.workloads.isotropic(n, 1e6 * pcl.co.eV, rng)
+    arr = pcl.ParticleArrays(np.zeros((n, 3)), p, np.ones(n), np.zeros(n))
+    del p
+    mp = pcl.MultiPopulation(
+        ("electron", pcl.Population(n + n // 8, arr, air["tabs"][0], air["cuts"][0], particle=pcl.Electron)),
+        ("photon", pcl.Population(1 << 20, [], air["tabs"][1], air["cuts"][1], particle=pcl.Photon)),
+        ("positron", pcl.Population(1 << 16, [], air["tabs"][2], air["cuts"][2], particle=pcl.Positron)), seed=0)
+    del arr
+    pusher = _pusher(pcl, air)
+    g0 = mp.get(pcl.Electron).particles()
+    assert len(g0.w) == n
+    sel = np.sort(rng.choice(n, 4096, replace=False))
+    W = oracle.OracleWorld(0, air["tabs"], air["cuts"], pusher)
+    W.upload(pcl.Electron, _subset(g0, sel))
+    del g0
+    dt = 1e-12
+    for k in range(2):
+        pcl.advance(mp, pusher, (k + 1) * dt)
+        W.advance((k + 1) * dt, 8)
+    t = mp.tallies()
+    assert t.live[0] > n * 0.99 and not any(t.errors), (list(t.live), list(t.errors))
+    for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
+        o = W.download(sp)
+        g = mp.get(sp).particles()
+        gs = _subset(g, np.isin(g.sid, o.sid))
+        rep = oracle.compare_populations(gs, o, sp, rtol=RTOL, stol=2 * RTOL)
+        assert rep["ok"], str(rep)
+    mp.close()
