@@ -1184,7 +1184,11 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     const long long nwarps_grid = (long long)gridDim.x * nwarps;
 
     long long cur = 0, end = 0;  // warp-private chunk (uniform)
-    bool input_done = false;
+    // small work (less than 32 slots per warp of the grid): only the first
+    // warps of every block take input, so the particles spread over the SMs
+    // instead of filling the first blocks to reach the work counter
+    const long long per_block = (total + 32ll * gridDim.x - 1) / (32ll * gridDim.x);
+    bool input_done = per_block < nwarps && warp >= max(per_block, 1ll);
     Lane L;
     L.slot = -1; L.alive = false; L.rvalid = false;
     bool has = false;
