@@ -137,8 +137,11 @@ __device__ __forceinline__ uint32_t next_bits(Lane& L, uint32_t k0, uint32_t k1)
     return v;
 }
 
+// (2 (v >> 9) + 1) 2^-24, in (0, 1), without an integer-to-float conversion:
+// 1 + (v >> 9) 2^-23 is built in the mantissa, subtracting 1 is exact, and so is
+// adding 2^-24 (the result has at most 24 significant bits).
 __device__ __forceinline__ float bits_to_u(uint32_t v) {
-    return __uint2float_rn(((v >> 9) << 1) | 1u) * 5.9604644775390625e-8f;  // 2^-24
+    return __fadd_rn(__fsub_rn(__uint_as_float(0x3f800000u | (v >> 9)), 1.0f), 5.9604644775390625e-8f);
 }
 
 __device__ __forceinline__ float U(Lane& L, const KCtx& K) {
