@@ -21,6 +21,7 @@
 #ifndef PARTICULATOR_GB300_H
 #define PARTICULATOR_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -351,6 +352,16 @@ int pcl_advance(void* ctx, double tfinal);
  * in flight when the call returns.  Host buffers should be pinned. */
 int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_packed* in, int64_t* n_out,
                      pcl_packed* out, const int64_t* out_cap, int nchunks, int compact);
+/* Page-lock (and release) caller-owned host memory so that the copies of
+ * pcl_advance_host / pcl_upload_packed / pcl_download_packed from it run
+ * asynchronously at full link speed (cudaHostRegister / cudaHostUnregister on
+ * the current device; bytes > 0). */
+int pcl_host_register(void* ptr, size_t bytes);
+int pcl_host_unregister(void* ptr);
+/* Page-locked host memory allocated by CUDA (cudaHostAlloc), for hosts that
+ * can wrap a foreign buffer (Julia unsafe_wrap, numpy); *ptr = NULL on failure. */
+int pcl_host_alloc(void** ptr, size_t bytes);
+int pcl_host_free(void* ptr);
 
 /* run!(mpopl, pusher, tfinal, dt, callback) (run.jl:1-29) with the device-side
  * PopulationTargetCallback / CollisionCounter.  Steps of dt until tfinal, the

@@ -125,6 +125,10 @@ _SIGS = {
     "pcl_upload_packed": (C.c_int, [C.c_void_p, C.c_int, _i64, _P(Packed)]),
     "pcl_advance_host": (C.c_int, [C.c_void_p, _d, _P(_i64), _P(Packed), _P(_i64), _P(Packed), _P(_i64), C.c_int,
                                    C.c_int]),
+    "pcl_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "pcl_host_unregister": (C.c_int, [C.c_void_p]),
+    "pcl_host_alloc": (C.c_int, [_P(C.c_void_p), C.c_size_t]),
+    "pcl_host_free": (C.c_int, [C.c_void_p]),
     "pcl_download_packed": (C.c_int, [C.c_void_p, C.c_int, _P(_i64), _P(Packed)]),
     "pcl_advance": (C.c_int, [C.c_void_p, _d]),
     "pcl_run": (C.c_int, [C.c_void_p, _d, _d, _P(RunOpts), _P(Tallies)]),

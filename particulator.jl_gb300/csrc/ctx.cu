@@ -1716,6 +1716,31 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
     return PCL_OK;
 }
 
+int pcl_host_register(void* ptr, size_t bytes) {
+    if (!ptr || bytes == 0) return PCL_ERR_INVALID;
+    return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? PCL_OK : PCL_ERR_CUDA;
+}
+
+int pcl_host_unregister(void* ptr) {
+    if (!ptr) return PCL_ERR_INVALID;
+    return cudaHostUnregister(ptr) == cudaSuccess ? PCL_OK : PCL_ERR_CUDA;
+}
+
+int pcl_host_alloc(void** ptr, size_t bytes) {
+    if (!ptr) return PCL_ERR_INVALID;
+    *ptr = nullptr;
+    if (bytes == 0) return PCL_ERR_INVALID;
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) return PCL_ERR_CUDA;
+    *ptr = p;
+    return PCL_OK;
+}
+
+int pcl_host_free(void* ptr) {
+    if (!ptr) return PCL_ERR_INVALID;
+    return cudaFreeHost(ptr) == cudaSuccess ? PCL_OK : PCL_ERR_CUDA;
+}
+
 int pcl_advance(void* ctx, double tfinal) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c) return PCL_ERR_INVALID;

@@ -156,6 +156,61 @@ class Population:
         return ParticleArrays(x[:m], p[:m], w[:m], t[:m], s[:m], sid[:m], ctr[:m])
 
 
+class PinnedBlock:
+    """numpy arrays in one page-locked block allocated by CUDA
+    (pcl_host_alloc), freed when the last array viewing it is collected."""
+
+    def __init__(self, shapes_dtypes):
+        sizes = [int(np.prod(sh)) * np.dtype(dt).itemsize for sh, dt in shapes_dtypes]
+        offs = np.cumsum([0] + [(z + 4095) // 4096 * 4096 for z in sizes])
+        self.ptr = C.c_void_p()
+        rc = _lib.lib().pcl_host_alloc(C.byref(self.ptr), C.c_size_t(max(int(offs[-1]), 1)))
+        if rc != 0:
+            raise RuntimeError(f"pcl_host_alloc failed ({rc})")
+        raw = (C.c_uint8 * int(offs[-1])).from_address(self.ptr.value)
+        raw._owner = self   # every view keeps the block (and so the memory) alive
+        base = np.frombuffer(raw, dtype=np.uint8)
+        self.arrays = tuple(base[o:o + z].view(dt).reshape(sh)
+                            for o, z, (sh, dt) in zip(offs[:-1], sizes, shapes_dtypes))
+        for a in self.arrays:
+            a[...] = 0
+
+    def __del__(self):
+        try:
+            if self.ptr:
+                _lib.lib().pcl_host_free(self.ptr)
+                self.ptr = C.c_void_p()
+        except Exception:
+            pass
+
+
+class PinnedHost:
+    """Page-locks numpy arrays for asynchronous copies (pcl_host_register) and
+    releases them when collected."""
+
+    def __init__(self, arrays):
+        self.ptrs = []
+        self.arrays = arrays
+        for a in arrays:
+            if a.nbytes:
+                rc = _lib.lib().pcl_host_register(C.c_void_p(a.ctypes.data), C.c_size_t(a.nbytes))
+                if rc != 0:
+                    self.release()
+                    raise RuntimeError(f"pcl_host_register failed ({rc})")
+                self.ptrs.append(a.ctypes.data)
+
+    def release(self):
+        for p in self.ptrs:
+            _lib.lib().pcl_host_unregister(C.c_void_p(p))
+        self.ptrs = []
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
 class MultiPopulation:
     """MultiPopulation(:electron => ..., :photon => ..., :positron => ...)
     (mixed_population.jl:4-12).  Owns one device context; configuration
@@ -336,17 +391,15 @@ class MultiPopulation:
     def packed_buffers(self, pinned: bool = False):
         """Host buffers in the packed device layout for every species, sized to
         its capacity: [(xw float32 [cap, 4], ps float32 [cap, 4], meta uint32
-        [cap, 4])] (page-locked through torch when pinned=True)."""
+        [cap, 4], owner)]; pinned=True places them in page-locked memory
+        (pcl_host_alloc), freed when `owner` is collected."""
         bufs = []
         for s in (Electron, Photon, Positron):
             pop = self.index.get(s)
             cap = 0 if (pop is None or pop.tally_only) else pop.max_particles
-            if pinned:
-                import torch
-                mk = [torch.empty((cap, 4), dtype=torch.float32).pin_memory(),
-                      torch.empty((cap, 4), dtype=torch.float32).pin_memory(),
-                      torch.empty((cap, 4), dtype=torch.int32).pin_memory()]
-                bufs.append((mk[0].numpy(), mk[1].numpy(), mk[2].numpy().view(np.uint32), mk))
+            if pinned and cap:
+                blk = PinnedBlock([((cap, 4), np.float32), ((cap, 4), np.float32), ((cap, 4), np.uint32)])
+                bufs.append(blk.arrays + (blk,))
             else:
                 bufs.append((np.zeros((cap, 4), np.float32), np.zeros((cap, 4), np.float32),
                              np.zeros((cap, 4), np.uint32), None))

@@ -417,7 +417,7 @@ def test_advance_host_equals_upload_advance_download(pcl, gpu, nchunks):
     same number), with and without the device repack."""
     a = pcl.workloads.avalanche(n=60_000, seed=4, capacity=1 << 18)
     b = pcl.workloads.avalanche(n=60_000, seed=4, capacity=1 << 18)
-    ba, bb = a.mpopl.packed_buffers(), b.mpopl.packed_buffers()
+    ba, bb = a.mpopl.packed_buffers(pinned=(nchunks == 8)), b.mpopl.packed_buffers()
     na, nb = a.mpopl.download_packed(ba), b.mpopl.download_packed(bb)
     for k in range(3):
         t = (k + 1) * a.dt
