@@ -130,7 +130,7 @@ def _profile_traffic():
 
 
 def build_workload(pcl, n_seed: int, seed: int, device: int, steps_per_launch: int = 1, blocks_per_sm: int = 0,
-                   classic_step: bool = False):
+                   classic_step: bool = False, use_graph: bool = False):
     co = pcl.co
     comp = pcl.workloads.air_composition()
     dt = 1e-12
@@ -149,7 +149,7 @@ def build_workload(pcl, n_seed: int, seed: int, device: int, steps_per_launch: i
         ("photon", pcl.Population(cap_g, [], gt, 5e3 * co.eV, particle=pcl.Photon)),
         ("positron", pcl.Population(cap_p, [], pt, 1e4 * co.eV, particle=pcl.Positron)),
         seed=seed, device=device, steps_per_launch=steps_per_launch, blocks_per_sm=blocks_per_sm,
-        classic_step=classic_step)
+        classic_step=classic_step, use_graph=use_graph)
     mp.set_pusher(pusher)
     return mp, pusher, dt, dict(tables=(et, gt, pt), cl=cl, comp=comp)
 
@@ -308,7 +308,8 @@ def run_learned(args, pcl):
     L = pcl.lib()
     co = pcl.co
     t_train0 = time.perf_counter()
-    mp, pusher, dt, extra = build_workload(pcl, args.n, seed=0, device=0, blocks_per_sm=args.bps)
+    mp, pusher, dt, extra = build_workload(pcl, args.n, seed=0, device=0, blocks_per_sm=args.bps,
+                                           use_graph=bool(args.graph))
     et = extra["tables"][0]
     nets = []
     attach = []
@@ -353,7 +354,8 @@ def run_learned(args, pcl):
                              rounds=int(s1[1] - s0[1]), kbytes=kb.value, kms=kms.value, kl=kl.value)
         mp.close()
         if form == "plain":
-            mp, pusher, dt, extra = build_workload(pcl, args.n, seed=0, device=0, blocks_per_sm=args.bps)
+            mp, pusher, dt, extra = build_workload(pcl, args.n, seed=0, device=0, blocks_per_sm=args.bps,
+                                                   use_graph=bool(args.graph))
     r, p0 = results["learned"], results["plain"]
     peak, peak_kind = _peaks()
     achieved = (r["kbytes"] / max(r["kl"], 1)) / (r["kms"] / max(r["kl"], 1) / 1e3) / 1e9
@@ -602,6 +604,7 @@ def main():
     ap.add_argument("--steps-per-launch", type=int, default=1)
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
     ap.add_argument("--classic", type=int, default=0, help="1: classic step kernel (lanes collide in place)")
+    ap.add_argument("--graph", type=int, default=0, help="1: launch groups replayed from CUDA graphs")
     ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned", "plain", "reid", "mlp"])
     ap.add_argument("--nswarm", type=int, default=256)
     ap.add_argument("--tune-steps", type=int, default=512)
@@ -628,7 +631,7 @@ def main():
     L = pcl.lib()
     mp, pusher, dt, extra = build_workload(pcl, args.n, seed=rank, device=local,
                                            steps_per_launch=args.steps_per_launch, blocks_per_sm=args.bps,
-                                           classic_step=bool(args.classic))
+                                           classic_step=bool(args.classic), use_graph=bool(args.graph))
     ctx = mp.ctx
     K = args.steps_per_launch
     # ---- warm-up
@@ -701,7 +704,8 @@ def main():
                 "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / (args.steps * K), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "rrea-air-0.5MVm-16M", "seed_electrons": args.n, "dt_s": dt,
-                           "steps_per_launch": K, "blocks_per_sm": (args.bps or 4) if args.classic else 3,
+                           "steps_per_launch": K, "graph": bool(args.graph),
+                           "blocks_per_sm": (args.bps or 4) if args.classic else 3,
                            "step_kernel": "classic" if args.classic else "event", "live_at_end": list(tal1.live),
                            "l2": "inputs larger than L2 (population > 800 MB)", "parallelism": f"replicas{ws}"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
