@@ -1051,6 +1051,20 @@ __device__ void collide(Lane& L, const KCtx& K, const SpeciesHdr& S) {
             if (nu > xi) break;
             xi -= nu;
         }
+        if (j < S.nproc && S.proc[j].kind == PCL_PROC_REL_COULOMB && !(LEARN && S.proc[j].learn)) {
+            // elastic: |p| and so E are unchanged, and setr! (collisions.jl:63-74)
+            // evaluates the rate bound on the interval and basis already at hand
+            atomicAdd(&K.tal[T_COLL + 16 * L.species + j], 1u);
+            s_coulomb(L, K, S.proc[j]);
+            float rb = cheb_dot(K.blob + S.rb_off + i * S.order, t, S.order);
+            if (S.rbB_off >= 0) rb += K.blob[K.H->swarm_off + 4 * L.sw + 3] * cheb_dot(K.blob + S.rbB_off + i * S.order, t, S.order);
+            if (!(rb > 0.0f)) {
+                if (S.nproc > 0) err(K, PCL_E_NEG_RATE);
+                rb = 0.0f;
+            }
+            L.r = rb;
+            return;
+        }
     }
     if (j == S.nproc) {  // NullOutcome (collisions.jl:83-88)
         atomicAdd(&K.tal[T_NULL + L.species], 1u);
