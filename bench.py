@@ -642,7 +642,9 @@ def main():
     L.pcl_sync(ctx)
     tal0 = mp.tallies()
     L.pcl_kernel_stats(ctx, None, None, None, None, 1)
-    # ---- timed region: device-resident steps
+    # ---- timed region: device-resident steps, a device synchronisation and a
+    # barrier on both sides
+    L.pcl_sync(ctx)
     _barrier(ws)
     with Clocks(local) as clk:
         L.pcl_timer_start(ctx)
@@ -651,6 +653,8 @@ def main():
             pcl.run(mp, pusher, t, dt) if K > 1 else pcl.advance(mp, pusher, t)
         ms = C.c_double()
         L.pcl_timer_stop(ctx, C.byref(ms))
+    L.pcl_sync(ctx)
+    _barrier(ws)
     tal1 = mp.tallies()
     kms = C.c_double(); kl = C.c_int64(); nl = C.c_int64(); kb = C.c_double()
     L.pcl_kernel_stats(ctx, C.byref(kms), C.byref(kl), C.byref(nl), C.byref(kb), 1)
