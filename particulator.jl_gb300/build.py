@@ -21,7 +21,8 @@ LIB_PATH = os.path.join(BUILD, LIB_NAME)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3"]
-SOURCES = ["step.cu", "ctx.cu", "noalloc.cu", "mlp.cu", "learn.cu", "tables.cpp"]
+SOURCES = ["step.cu", "ctx.cu", "ctx_popops.cu", "ctx_hostio.cu", "ctx_learn.cu", "noalloc.cu", "mlp.cu", "learn.cu",
+           "tables.cpp"]
 
 
 def _nvcc() -> str:
