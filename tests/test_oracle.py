@@ -122,3 +122,61 @@ def test_field_shapes(pcl):
     pusher = pcl.RK2Pusher(pcl.CombinedForcing(pcl.ElectromagneticField(pcl.StepField(0, (0, 0, 1), (0, 0, 2)),
                                                                         pcl.HomogeneousField((0, 0, 0)))))
     assert pusher.device_efield()[0] == 2 and np.all(pusher.device_forcing()[0] == 0)
+
+
+def _electrons(pcl, oracle, n, seed=3):
+    rng = np.random.default_rng(seed)
+    E = np.exp(rng.uniform(np.log(2e4), np.log(1e7), n)) * pcl.co.eV
+    p = pcl.workloads.isotropic(n, 1.0, rng)
+    p *= (pcl.momentum_norm_from_kin(pcl.Electron, E) / np.linalg.norm(p, axis=1))[:, None]
+    return oracle.Arrays(np.zeros((n, 3)), p, np.ones(n), np.zeros(n), -np.log(rng.random(n)),
+                         np.arange(n, dtype=np.uint64), np.zeros(n, np.uint32))
+
+
+def _world(pcl, oracle, air, seed=5):
+    return oracle.OracleWorld(seed, air["tabs"], air["cuts"], pcl.workloads.pusher((0.0, 0.0, -5e5), cl=air["cl"]))
+
+
+def test_oracle_roulette(pcl, oracle, air):
+    """roulette!(q, popl) (population.jl:291-311) in the oracle: a live particle
+    stays with probability q (one draw of its stream) with weight w / q, else it
+    is removed; the choice belongs to the particle's stream, not to the order."""
+    n, q = 20000, 0.3
+    arr = _electrons(pcl, oracle, n)
+    W = _world(pcl, oracle, air)
+    W.upload(pcl.Electron, arr)
+    W.roulette(pcl.Electron, q)
+    d = W.download(pcl.Electron)
+    assert abs(len(d.w) - q * n) < 5 * np.sqrt(n * q * (1 - q))
+    np.testing.assert_allclose(d.w, 1.0 / q, rtol=1e-12)
+    assert np.all(d.ctr == 1)                       # one draw per particle
+    assert abs(d.w.sum() - n) < 6 * np.sqrt(n * (1 - q) / q)
+    # the same particles in reverse order keep the same stream ids
+    rev = oracle.Arrays(*(getattr(arr, f)[::-1].copy() for f in ("x", "p", "w", "t", "s", "sid", "ctr")))
+    W2 = _world(pcl, oracle, air)
+    W2.upload(pcl.Electron, rev)
+    W2.roulette(pcl.Electron, q)
+    np.testing.assert_array_equal(np.sort(W2.download(pcl.Electron).sid), np.sort(d.sid))
+
+
+def test_oracle_split(pcl, oracle, air):
+    """split!(p, popl) (population.jl:318-335) in the oracle: every live
+    particle's weight becomes w / (1 + p) and Poisson(p) copies of its state
+    are added with fresh stream ids; the expected total weight is unchanged."""
+    n, mu = 20000, 0.7
+    arr = _electrons(pcl, oracle, n)
+    W = _world(pcl, oracle, air)
+    W.upload(pcl.Electron, arr)
+    W.split(pcl.Electron, mu)
+    d = W.download(pcl.Electron)
+    np.testing.assert_allclose(d.w, 1.0 / (1.0 + mu), rtol=1e-12)
+    parent = np.isin(d.sid, arr.sid)
+    assert parent.sum() == n                         # every parent stays
+    ncopy = int((~parent).sum())
+    assert abs(ncopy - mu * n) < 5 * np.sqrt(mu * n)
+    assert len(np.unique(d.sid)) == len(d.sid)       # copies get distinct stream ids
+    assert abs(d.w.sum() - n) < 5 * np.sqrt(mu * n) / (1 + mu)
+    # a copy carries its parent's momentum
+    pn = np.linalg.norm(arr.p, axis=1)
+    cn = np.linalg.norm(d.p[~parent], axis=1)
+    assert np.all(np.isin(np.round(cn / pn.max(), 12), np.round(pn / pn.max(), 12)))
