@@ -180,3 +180,31 @@ def test_oracle_split(pcl, oracle, air):
     pn = np.linalg.norm(arr.p, axis=1)
     cn = np.linalg.norm(d.p[~parent], axis=1)
     assert np.all(np.isin(np.round(cn / pn.max(), 12), np.round(pn / pn.max(), 12)))
+
+
+def test_oracle_wall_records(pcl, oracle, air):
+    """WallCallback{P}(coord, v, drop) (callback.jl:146-184) in the oracle: a
+    particle crossing z = v upwards is recorded at the plane (lincomb of its
+    old and new states) and, with drop, leaves the population; a record's
+    time lies inside the step."""
+    n, zw, dt = 4000, 2e-5, 25e-12
+    rng = np.random.default_rng(9)
+    E = np.exp(rng.uniform(np.log(1e5), np.log(1e7), n)) * pcl.co.eV
+    p = np.zeros((n, 3))
+    p[:, 2] = pcl.momentum_norm_from_kin(pcl.Electron, E)        # along +z
+    x = np.zeros((n, 3))
+    x[:, 2] = rng.uniform(0.0, zw, n)                          # below the wall
+    arr = oracle.Arrays(x, p, np.ones(n), np.zeros(n), -np.log(rng.random(n)), np.arange(n, dtype=np.uint64),
+                        np.zeros(n, np.uint32))
+    W = _world(pcl, oracle, air, seed=8)
+    W.upload(pcl.Electron, arr)
+    W.set_wall(pcl.Electron, 2, zw, drop=True)
+    W.advance(dt, 4)
+    sp, sid, xr, pr, wr, tr = W.get_wall()
+    assert len(sid) > n // 4
+    assert np.all(sp == pcl.Electron)
+    np.testing.assert_allclose(xr[:, 2], zw, rtol=1e-12, atol=1e-18)
+    assert np.all((tr >= 0.0) & (tr <= dt * (1 + 1e-12)))
+    live = W.download(pcl.Electron)
+    assert not np.any(np.isin(live.sid, sid))                  # dropped at the wall
+    assert np.all(live.x[:, 2] <= zw * (1 + 1e-12))            # nobody above it
