@@ -130,7 +130,7 @@ def _profile_traffic():
 
 
 def build_workload(pcl, n_seed: int, seed: int, device: int, steps_per_launch: int = 1, blocks_per_sm: int = 0,
-                   classic_step: bool = False, use_graph: bool = False):
+                   classic_step: bool = False, use_graph: bool = False, compaction_period: int = 0):
     co = pcl.co
     comp = pcl.workloads.air_composition()
     dt = 1e-12
@@ -149,7 +149,7 @@ def build_workload(pcl, n_seed: int, seed: int, device: int, steps_per_launch: i
         ("photon", pcl.Population(cap_g, [], gt, 5e3 * co.eV, particle=pcl.Photon)),
         ("positron", pcl.Population(cap_p, [], pt, 1e4 * co.eV, particle=pcl.Positron)),
         seed=seed, device=device, steps_per_launch=steps_per_launch, blocks_per_sm=blocks_per_sm,
-        classic_step=classic_step, use_graph=use_graph)
+        classic_step=classic_step, use_graph=use_graph, compaction_period=compaction_period)
     mp.set_pusher(pusher)
     return mp, pusher, dt, dict(tables=(et, gt, pt), cl=cl, comp=comp)
 
@@ -605,6 +605,7 @@ def main():
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
     ap.add_argument("--classic", type=int, default=0, help="1: classic step kernel (lanes collide in place)")
     ap.add_argument("--graph", type=int, default=0, help="1: launch groups replayed from CUDA graphs")
+    ap.add_argument("--compaction-period", type=int, default=0, help="steps between repacks (0: the library's 8)")
     ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned", "plain", "reid", "mlp"])
     ap.add_argument("--nswarm", type=int, default=256)
     ap.add_argument("--tune-steps", type=int, default=512)
@@ -631,7 +632,8 @@ def main():
     L = pcl.lib()
     mp, pusher, dt, extra = build_workload(pcl, args.n, seed=rank, device=local,
                                            steps_per_launch=args.steps_per_launch, blocks_per_sm=args.bps,
-                                           classic_step=bool(args.classic), use_graph=bool(args.graph))
+                                           classic_step=bool(args.classic), use_graph=bool(args.graph),
+                                           compaction_period=args.compaction_period)
     ctx = mp.ctx
     K = args.steps_per_launch
     # ---- warm-up
@@ -709,6 +711,7 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": {"workload": "rrea-air-0.5MVm-16M", "seed_electrons": args.n, "dt_s": dt,
                            "steps_per_launch": K, "graph": bool(args.graph),
+                           "compaction_period": args.compaction_period or 8,
                            "blocks_per_sm": (args.bps or 4) if args.classic else 3,
                            "step_kernel": "classic" if args.classic else "event", "live_at_end": list(tal1.live),
                            "l2": "inputs larger than L2 (population > 800 MB)", "parallelism": f"replicas{ws}"},
