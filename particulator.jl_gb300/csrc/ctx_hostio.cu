@@ -185,8 +185,12 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
         any = any || S.set;
         n[s] = (S.set && S.cap > 0) ? (long long)n_in[s] : 0;
         if (n[s] < 0 || n[s] > S.cap) return fail(c, PCL_ERR_CAPACITY, "input exceeds capacity");
-        if (n[s] > 0 && (!in[s].xw || !in[s].ps || !in[s].meta || !out[s].xw || !out[s].ps || !out[s].meta))
-            return fail(c, PCL_ERR_INVALID, "null particle arrays");
+        if (n[s] > 0 && (!in[s].xw || !in[s].ps || !in[s].meta))
+            return fail(c, PCL_ERR_INVALID, "null input arrays");
+        // a species may gain secondaries in the step even if it starts empty
+        if (out_cap[s] < 0 || (out_cap[s] > 0 && (!out[s].xw || !out[s].ps || !out[s].meta)))
+            return fail(c, PCL_ERR_INVALID, "null or negative-size output arrays");
+        if (out_cap[s] < n[s]) return fail(c, PCL_ERR_CAPACITY, "output arrays smaller than the input");
     }
     if (!any) return fail(c, PCL_ERR_STATE, "no species set");
     CK(cudaSetDevice(c->device));

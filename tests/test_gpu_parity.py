@@ -421,6 +421,9 @@ def test_advance_host_equals_upload_advance_download(pcl, gpu, nchunks):
     if nchunks == 3:   # existing arrays page-locked in place (pcl_host_register)
         pins = [pcl.population.PinnedHost(x[:3]) for x in ba]
     na, nb = a.mpopl.download_packed(ba), b.mpopl.download_packed(bb)
+    small = [(x[0][:10], x[1][:10], x[2][:10], None) for x in ba]
+    with pytest.raises(Exception):      # output arrays smaller than the input: refused before any work
+        a.mpopl.advance_host(a.dt, ba, na, out=small, nchunks=nchunks)
     for k in range(3):
         t = (k + 1) * a.dt
         compact = k == 1
