@@ -408,6 +408,12 @@ int pcl_test_sampler(void* ctx, int species, int proc_index, int64_t n, const do
                      const uint64_t* sid, double* out_p, double* out_s, int32_t* out_kind,
                      uint32_t* out_ctr);
 
+/* Test hook of failure detection: a kernel waits, with the bounded wait every
+ * device wait of the library uses and a limit of max_iters polls (1 .. 2^20),
+ * on an mbarrier that nothing ever completes.  Returns PCL_ERR_TIMEOUT with
+ * the context left usable (the flag is cleared). */
+int pcl_test_timeout(void* ctx, int max_iters);
+
 /* ---- compaction without device allocation --------------------------------
  * No counterpart in the reference: an extra entry point for callers that
  * cannot call cudaMalloc (a host whose memory pool owns the device, code on a

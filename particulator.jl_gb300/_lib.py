@@ -129,6 +129,7 @@ _SIGS = {
     "pcl_host_unregister": (C.c_int, [C.c_void_p]),
     "pcl_host_alloc": (C.c_int, [_P(C.c_void_p), C.c_size_t]),
     "pcl_host_free": (C.c_int, [C.c_void_p]),
+    "pcl_test_timeout": (C.c_int, [C.c_void_p, C.c_int]),
     "pcl_download_packed": (C.c_int, [C.c_void_p, C.c_int, _P(_i64), _P(Packed)]),
     "pcl_advance": (C.c_int, [C.c_void_p, _d]),
     "pcl_run": (C.c_int, [C.c_void_p, _d, _d, _P(RunOpts), _P(Tallies)]),

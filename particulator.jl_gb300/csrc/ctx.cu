@@ -1087,6 +1087,22 @@ int pcl_sync(void* ctx) {
     return PCL_OK;
 }
 
+int pcl_test_timeout(void* ctx, int max_iters) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c || max_iters < 1 || max_iters > (1 << 20)) return PCL_ERR_INVALID;
+    CK(cudaSetDevice(c->device));
+    k_test_wait<<<1, 64, 0, c->stream>>>(c->d_ctl, max_iters);
+    CK(cudaGetLastError());
+    int rc = readback(c);
+    if (rc) return rc;
+    if (c->h_ctl->timeout) {   // the context stays usable: clear the flag, report the status
+        CK(cudaMemsetAsync(&c->d_ctl->timeout, 0, sizeof(c->d_ctl->timeout), c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        return fail(c, PCL_ERR_TIMEOUT, "bounded wait gave up (test hook)");
+    }
+    return PCL_OK;
+}
+
 int pcl_timer_start(void* ctx) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c) return PCL_ERR_INVALID;

@@ -47,6 +47,7 @@ cudaError_t infer_multi(void* const* handles, int nnets, const float* X, const u
                         long long cap, float* Y, long long ystride, cudaStream_t stream);
 }
 __global__ void k_begin(Control* ctl, long long cap0, long long cap1, long long cap2);
+__global__ void k_test_wait(Control* ctl, int max_iters);
 __global__ void k_begin_spill(Control* ctl, unsigned long long* in_n, unsigned long long* out_n);
 
 __global__ void k_compact_count(CompactArgs C);

@@ -1083,6 +1083,22 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
 
+// Wait for phase `parity` of the mbarrier at shared address `bar`, at most
+// `max_iters` polls (each a try_wait plus a short sleep); false on timeout.
+// Every mbarrier wait of the step kernels goes through here.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, int max_iters) {
+    uint32_t done = 0;
+    for (int it = 0; it < max_iters && !done; ++it) {
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (!done) __nanosleep(64);
+    }
+    return done != 0;
+}
+
 // Copy the table blob into shared memory with one bulk asynchronous copy
 // (cp.async.bulk, completion on an mbarrier).  Bounded wait; false on timeout.
 __device__ bool stage_blob(void* dst, const void* src, int bytes, unsigned long long* mbar) {
@@ -1102,16 +1118,22 @@ __device__ bool stage_blob(void* dst, const void* src, int bytes, unsigned long 
             "l"(src), "r"(bytes), "r"(bar)
             : "memory");
     }
-    uint32_t done = 0;
-    for (int it = 0; it < (1 << 22) && !done; ++it) {
-        asm volatile(
-            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-            : "=r"(done)
-            : "r"(bar), "r"(0u)
-            : "memory");
-        if (!done) __nanosleep(64);
+    return mbar_wait_bounded(bar, 0u, 1 << 22);
+}
+
+// Test hook of the bounded wait: every thread waits on an mbarrier that no
+// thread and no copy ever arrives on, with a limit of `max_iters` polls, and
+// the timeout is recorded in the control block as a staging timeout would be.
+__global__ void k_test_wait(Control* ctl, int max_iters) {
+    __shared__ unsigned long long bar;
+    const uint32_t b = static_cast<uint32_t>(__cvta_generic_to_shared(&bar));
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(b), "r"(1) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    return done != 0;
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(b, 0u, max_iters);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicExch(&ctl->timeout, 1);
 }
 
 // Load particle data of an input slot.

@@ -519,3 +519,18 @@ def test_full_size_subset_parity(pcl, oracle, gpu, air):
         rep = oracle.compare_populations(gs, o, sp, rtol=RTOL, stol=2 * RTOL)
         assert rep["ok"], str(rep)
     mp.close()
+
+
+def test_bounded_wait_times_out_and_context_survives(pcl, gpu, air):
+    """Failure detection without a fault: a device wait that nothing completes
+    gives up at its poll limit, the call returns PCL_ERR_TIMEOUT, and the same
+    context then steps as usual."""
+    mp = _mixed(pcl, air, n=(1024, 256, 128), seed=12)
+    L = pcl.lib()
+    assert L.pcl_test_timeout(mp.ctx, 0) == pcl._lib.PCL_ERR_INVALID
+    assert L.pcl_test_timeout(mp.ctx, 2000) == pcl._lib.PCL_ERR_TIMEOUT
+    assert b"bounded wait" in L.pcl_last_error(mp.ctx)
+    pcl.advance(mp, _pusher(pcl, air), 1e-12)
+    t = mp.tallies()
+    assert t.steps == 1 and t.particle_steps > 0
+    mp.close()
