@@ -442,6 +442,7 @@ class MultiPopulation:
         caps = (C.c_int64 * 3)(*[len(b[0]) for b in out])
         _lib.check(_lib.lib().pcl_advance_host(self.ctx, float(tfinal), n_in, inp, n_out, outp, caps, int(nchunks),
                                                int(bool(compact))), self.ctx, "pcl_advance_host")
+        self.t = float(tfinal)
         return [int(n_out[s]) for s in range(3)]
 
     def set_learned(self, particle, proc_index: int, kind: int, net=None):
