@@ -208,3 +208,20 @@ def test_oracle_wall_records(pcl, oracle, air):
     live = W.download(pcl.Electron)
     assert not np.any(np.isin(live.sid, sid))                  # dropped at the wall
     assert np.all(live.x[:, 2] <= zw * (1 + 1e-12))            # nobody above it
+
+
+def test_spectrum_normalisation(pcl):
+    """spectrum() divides the histogram by the bin widths and by n, as plotspec
+    does with StatsBase.normalize(mode = :density) (scripts/beam.jl:137-147);
+    weighted uses the summed weights, unweighted the counts."""
+    edges = np.array([1.0, 2.0, 4.0, 8.0])
+
+    class FakePop:
+        def energy_histogram(self, e, swarm=-1):
+            assert np.array_equal(e, edges) and swarm == 3
+            return np.array([4, 6, 8]), np.array([2.0, 3.0, 16.0])
+
+    w = pcl.spectrum(FakePop(), edges, n=2.0, swarm=3)
+    np.testing.assert_allclose(w, [2.0 / 1 / 2, 3.0 / 2 / 2, 16.0 / 4 / 2])
+    c = pcl.spectrum(FakePop(), edges, n=1.0, weighted=False, swarm=3)
+    np.testing.assert_allclose(c, [4.0, 3.0, 2.0])
