@@ -35,6 +35,13 @@ def test_no_device_means_status_not_crash(pcl):
     cfg = pcl._lib.Config()
     assert L.pcl_create(C.byref(cfg), C.byref(h)) == pcl._lib.PCL_ERR_CUDA
     assert L.pcl_advance(None, 1.0) == pcl._lib.PCL_ERR_INVALID
+    # page-locked host memory needs the runtime too: a status, never a crash
+    p = C.c_void_p()
+    assert L.pcl_host_alloc(C.byref(p), 4096) == pcl._lib.PCL_ERR_CUDA and not p.value
+    assert L.pcl_host_alloc(None, 4096) == pcl._lib.PCL_ERR_INVALID
+    buf = (C.c_uint8 * 4096)()
+    assert L.pcl_host_register(buf, 4096) == pcl._lib.PCL_ERR_CUDA
+    assert L.pcl_host_register(None, 4096) == pcl._lib.PCL_ERR_INVALID
 
 
 def test_builder_argument_checks(pcl):
