@@ -556,7 +556,6 @@ def run_mlp(args, pcl):
     (tcgen05 128 x 128 layers, 32768 tiles) and training steps of 8192 rows.
     FLOPs per row: 2 (2 x 128 + 2 x 128 x 128 + 128) = 66,304 forward."""
     L = pcl.lib()
-    import ctypes as Cc
     n = 1 << 22
     net = pcl.SamplerNet(seed=1)
     rng = np.random.default_rng(0)
