@@ -5,15 +5,21 @@ runaway electrons in air (N2/O2 0.79/0.21, 1 atm, 293 K) at E = 0.5 MV/m,
 electrons / photons / positrons tracked through Moller, Seltzer-Berger,
 screened Coulomb, Compton, photoelectric, Bethe-Heitler, Bhabha and
 annihilation with continuum losses below 10 keV (photon cut 5 keV),
-dt = 1 ps.  The population starts from 2^24 electrons at 1 MeV with isotropic
-directions (Philox seed 0); warm-up steps let secondaries appear, then K
-steps are timed.  A "step" is one advance! + droplow! over every particle.
+dt = 1 ps.  The population is 2^24 particles drawn (Philox seed = rank) from
+the recipe of the grown avalanche: the state that 10^4 seed electrons at 1 MeV
+reach when the electron count hits its target (PopulationTargetCallback),
+with that state's e- / gamma / e+ fractions, spectra and angular
+distributions (particulator.jl_gb300/data/grow_rrea.py writes the recipe).
+A "step" is one advance! + droplow! over every particle.
 
 Metric: particle-steps/s (live particles at step start x steps / time).
 `value` times the device-resident step (CUDA events on the library's
 stream); `e2e` times the same steps through the C ABI with the population
-copied in from and out to pinned host buffers every step.
-Inputs (16 M x 48 B = 805 MB) are far larger than L2 (129 MB).
+copied in from and out to pinned host buffers every step.  The same line
+carries the batched form (256 swarms in one context against 256 sequential
+plain contexts) and the learned form (network samplers against the plain
+form on the same state).  Inputs (16 M x 48 B = 805 MB) are far larger than
+L2 (129 MB).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 """
@@ -116,96 +122,103 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def _profile_traffic():
-    """DRAM bytes per k_step launch from the committed ncu summary, scaled
-    to the bench workload (see profiles/k_step_rrea.md), or None."""
-    path = os.path.join(ROOT, "profiles", "k_step_rrea.md")
-    if not os.path.exists(path):
-        return None
-    with open(path) as f:
-        for line in f:
-            if line.startswith("traffic_bytes_per_slot:"):
-                return float(line.split(":", 1)[1].strip())
-    return None
+# DRAM bytes (read + write) per slot of one k_step launch, from one ncu
+# capture (dram__bytes_read.sum + dram__bytes_write.sum) of the event kernel on
+# a 4 M-particle draw of the same mixed state at the commit named beside it;
+# scaled to a launch by the slots it processes.  None: not captured for the
+# current kernel, and the line says so.
+K_STEP_DRAM_BYTES_PER_SLOT = None
+K_STEP_DRAM_CAPTURE = None
+
+WORKLOAD = "rrea-air-0.5MVm-mixed-16M"
 
 
-def build_workload(pcl, n_seed: int, seed: int, device: int, steps_per_launch: int = 1, blocks_per_sm: int = 0,
+def workload_config(n: int, ws: int) -> dict:
+    """The workload keys both arms report (the GPU arm adds its launch shape
+    and results outside this dict)."""
+    return {"workload": WORKLOAD, "particles": n, "field_V_m": 5e5, "dt_s": 1e-12,
+            "state": "grown mixed e-/gamma/e+ avalanche (recipe rrea_mixed_0.5MVm.json), Philox seed = rank",
+            "l2": "inputs larger than L2 (population > 800 MB)", "parallelism": f"replicas{ws}"}
+
+
+def build_workload(pcl, n: int, seed: int, device: int, steps_per_launch: int = 1, blocks_per_sm: int = 0,
                    classic_step: bool = False, use_graph: bool = False, compaction_period: int = 0):
-    co = pcl.co
-    comp = pcl.workloads.air_composition()
-    dt = 1e-12
-    efield = 5e5
-    et, gt, pt = pcl.workloads.beam_tables(comp, efield, dt)
-    cl = pcl.workloads.air_continuum_loss(comp)
-    pusher = pcl.workloads.pusher((0.0, 0.0, -efield), cl=cl)
-    rng = np.random.Generator(np.random.Philox(seed))
-    p = pcl.workloads.isotropic(n_seed, 1e6 * co.eV, rng)
-    arr = pcl.ParticleArrays(np.zeros((n_seed, 3)), p, np.ones(n_seed), np.zeros(n_seed))
-    cap_e = int(n_seed * 1.25) + (1 << 16)
-    cap_g = max(1 << 20, n_seed // 4)
-    cap_p = max(1 << 16, n_seed // 64)
-    mp = pcl.MultiPopulation(
-        ("electron", pcl.Population(cap_e, arr, et, 1e4 * co.eV, particle=pcl.Electron)),
-        ("photon", pcl.Population(cap_g, [], gt, 5e3 * co.eV, particle=pcl.Photon)),
-        ("positron", pcl.Population(cap_p, [], pt, 1e4 * co.eV, particle=pcl.Positron)),
-        seed=seed, device=device, steps_per_launch=steps_per_launch, blocks_per_sm=blocks_per_sm,
-        classic_step=classic_step, use_graph=use_graph, compaction_period=compaction_period)
-    mp.set_pusher(pusher)
-    return mp, pusher, dt, dict(tables=(et, gt, pt), cl=cl, comp=comp)
+    wl = pcl.workloads.rrea_mixed(n, seed=seed, device=device, steps_per_launch=steps_per_launch,
+                                  blocks_per_sm=blocks_per_sm, classic_step=classic_step, use_graph=use_graph,
+                                  compaction_period=compaction_period)
+    wl.mpopl.set_pusher(wl.pusher)
+    et = wl.mpopl.get(pcl.Electron).collisions
+    return wl.mpopl, wl.pusher, wl.dt, dict(tables=(et,))
 
 
-def cpu_reference(pcl, n_sample: int, steps: int, threads: int, seed: int = 0):
-    """The oracle (C++ Float64 restatement of the reference step) on a bounded
-    sample of the workload: n_sample electrons, `steps` steps of 1 ps."""
-    from oracle.harness import Arrays, OracleWorld
-    co = pcl.co
-    comp = pcl.workloads.air_composition()
+def _build_oracle():
+    sys.path.insert(0, ROOT)
+    from oracle import build as obuild
+    obuild.build_oracle(verbose=False)
+
+
+def cpu_reference(n_sample: int, steps: int, warmup: int, threads: int, seed: int = 0):
+    """The oracle (C++ Float64 restatement of the reference step, tables from
+    the numpy restatement of its init path; the GPU library is not loaded) on
+    a bounded sample of the workload: n_sample particles drawn from the same
+    grown-state recipe, `warmup` untimed steps of 1 ps, then `steps` timed
+    ones.  Returns (particle-steps/s, seconds, particle-steps, live counts)."""
+    import __graft_entry__ as graft
+    graft.load_package()      # pure-Python parts only (recipe, descriptors)
+    import particulator_gb300 as pcl
+    from oracle.harness import Arrays
+    from oracle import reference_world as rw
+    W, tabs, cuts, pusher = rw.avalanche_world(seed)
+    st = pcl.workloads.rrea_mixed_state(n_sample, seed=seed)
+    rng = np.random.Generator(np.random.Philox(seed + 1000))
+    base = 0
+    for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
+        a = st[sp]
+        m = len(a.w)
+        if m:
+            W.upload(sp, Arrays(a.x, a.p, a.w, a.t, -np.log(rng.random(m)), np.arange(base, base + m, dtype=np.uint64),
+                                np.zeros(m, np.uint32)))
+        base += m
     dt = 1e-12
-    et, gt, pt = pcl.workloads.beam_tables(comp, 5e5, dt)
-    cl = pcl.workloads.air_continuum_loss(comp)
-    pusher = pcl.workloads.pusher((0.0, 0.0, -5e5), cl=cl)
-    cuts = {pcl.Electron: 1e4 * co.eV, pcl.Photon: 5e3 * co.eV, pcl.Positron: 1e4 * co.eV}
-    W = OracleWorld(seed, {pcl.Electron: et, pcl.Photon: gt, pcl.Positron: pt}, cuts, pusher)
-    rng = np.random.Generator(np.random.Philox(seed))
-    p = pcl.workloads.isotropic(n_sample, 1e6 * co.eV, rng)
-    s = -np.log(rng.random(n_sample))
-    W.upload(pcl.Electron, Arrays(np.zeros((n_sample, 3)), p, np.ones(n_sample), np.zeros(n_sample), s,
-                                  np.arange(n_sample, dtype=np.uint64), np.zeros(n_sample, np.uint32)))
-    W.advance(dt, threads)  # warm-up step
+    t = 0.0
+    for _ in range(warmup):
+        t += dt
+        W.advance(t, threads)
     psteps = 0
     t0 = time.perf_counter()
-    for k in range(steps):
-        live = sum(len(W.download(sp).w) for sp in (0, 1, 2))
-        W.advance((k + 2) * dt, threads)
-        psteps += live
+    for _ in range(steps):
+        psteps += sum(int(lib_count(W, sp)) for sp in (0, 1, 2))
+        t += dt
+        W.advance(t, threads)
     el = time.perf_counter() - t0
-    return psteps / el, el, psteps
+    live = [int(lib_count(W, sp)) for sp in (0, 1, 2)]
+    return psteps / el, el, psteps, live, rw.library_loaded()
+
+
+def lib_count(W, sp):
+    from oracle.harness import lib as olib
+    return olib().orc_count(W.h, int(sp))
 
 
 def run_reference(args):
+    """The CPU reference arm: the oracle on all host threads, on a bounded
+    sample of the same workload; only the oracle library is built or loaded."""
     ws, rank = _dist()
     if rank != 0:
         return 0
-    import __graft_entry__ as graft
-    graft.build()
-    pcl = graft.load_package()
+    _build_oracle()
     threads = os.cpu_count() or 1
-    n_sample = args.cpu_sample
-    values = []
-    for k in range(args.warmup + args.steps):
-        v, el, ps = cpu_reference(pcl, n_sample, 2, threads, seed=k)
-        if k >= args.warmup:
-            values.append((v, el, ps))
-    tot_ps = sum(v[2] for v in values)
-    tot_t = sum(v[1] for v in values)
-    val = tot_ps / tot_t
-    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot_t / args.steps,
+    v, el, ps, live, loaded = cpu_reference(args.cpu_sample, args.steps, args.warmup, threads)
+    sample = (f"{args.cpu_sample} particles drawn from the grown-state recipe (seed 0), {args.warmup} warm-up + "
+              f"{args.steps} timed steps of 1 ps ({ps} particle-steps, {el:.1f} s), C++ Float64 oracle, "
+              f"tables from the numpy restatement")
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "rrea-air-0.5MVm-16M", "sample": f"{n_sample} e- at 1 MeV isotropic, 2 steps of 1 ps per bench step"},
-            "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{n_sample} electrons x 2 steps per bench step, C++ Float64 oracle"},
-            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": workload_config(args.n, 1),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "live_at_end": live, "gpu_library_loaded": bool(loaded)}
     print(json.dumps(line))
     return 0
 
@@ -293,9 +306,8 @@ def run_swarms(args, pcl):
                                                                              np.maximum(mom[:, 0], 1)))},
             "batched_over_sequential": v_b / (ps_s / el_s),
             "cpu_baseline": None, "gpu_launches": int(nl.value), "clocks": clk.summary()}
-    print(json.dumps(line))
     mp.close()
-    return 0
+    return line
 
 
 def run_learned(args, pcl):
@@ -308,7 +320,7 @@ def run_learned(args, pcl):
     L = pcl.lib()
     co = pcl.co
     t_train0 = time.perf_counter()
-    mp, pusher, dt, extra = build_workload(pcl, args.n, seed=0, device=0, blocks_per_sm=args.bps,
+    mp, pusher, dt, extra = build_workload(pcl, args.learned_n, seed=0, device=0, blocks_per_sm=args.bps,
                                            use_graph=bool(args.graph))
     et = extra["tables"][0]
     nets = []
@@ -354,7 +366,7 @@ def run_learned(args, pcl):
                              rounds=int(s1[1] - s0[1]), kbytes=kb.value, kms=kms.value, kl=kl.value)
         mp.close()
         if form == "plain":
-            mp, pusher, dt, extra = build_workload(pcl, args.n, seed=0, device=0, blocks_per_sm=args.bps,
+            mp, pusher, dt, extra = build_workload(pcl, args.learned_n, seed=0, device=0, blocks_per_sm=args.bps,
                                                    use_graph=bool(args.graph))
     r, p0 = results["learned"], results["plain"]
     peak, peak_kind = _peaks()
@@ -363,7 +375,7 @@ def run_learned(args, pcl):
             "value": r["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": r["ms"] / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+bf16", "data": "synthetic",
-            "config": {"workload": "rrea-air-0.5MVm-16M-learned", "seed_electrons": args.n, "dt_s": 1e-12,
+            "config": {"workload": "rrea-air-0.5MVm-mixed-16M-learned", "particles": args.learned_n, "dt_s": 1e-12,
                        "networks": [{"table_position": j, "kind": k, "train_loss": l} for j, k, l in nets],
                        "training_s": t_train, "training_samples_per_network": args.train_samples,
                        "training_steps": args.train_steps},
@@ -375,8 +387,7 @@ def run_learned(args, pcl):
                       "live": p0["live"]},
             "learned_over_plain": r["value"] / p0["value"],
             "cpu_baseline": None, "gpu_launches": r["launches"], "clocks": r["clocks"]}
-    print(json.dumps(line))
-    return 0
+    return line
 
 
 def _oracle_world(pcl, seed, tabs, cuts, pusher, tally_only=()):
@@ -587,19 +598,39 @@ def run_mlp(args, pcl):
     return 0
 
 
+def _printing(fn):
+    def wrap(args, pcl):
+        print(json.dumps(fn(args, pcl)))
+        return 0
+    return wrap
+
+
+def _form_summary(line: dict, plain_value: float) -> dict:
+    """The sub-object of the default line for one other form."""
+    keep = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "dtype", "config", "roofline",
+            "gpu_launches", "clocks")
+    out = {k: line[k] for k in keep if k in line}
+    for k in ("sequential_plain", "batched_over_sequential", "plain", "learned_over_plain", "learned"):
+        if k in line:
+            out[k] = line[k]
+    out["over_plain_16M_line"] = line["value"] / plain_value if plain_value else None
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300")
-    ap.add_argument("--n", type=int, default=1 << 24, help="seed electrons")
+    ap.add_argument("--n", type=int, default=1 << 24, help="particles drawn from the grown-state recipe")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--e2e-chunks", type=int, default=8, help="pipeline chunks of pcl_advance_host")
     ap.add_argument("--cpu-sample", type=int, default=1 << 21)
-    ap.add_argument("--cpu-steps", type=int, default=48)
+    ap.add_argument("--cpu-steps", type=int, default=40)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched and learned sub-objects")
     ap.add_argument("--steps-per-launch", type=int, default=1)
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
     ap.add_argument("--classic", type=int, default=0, help="1: classic step kernel (lanes collide in place)")
@@ -608,21 +639,20 @@ def main():
     ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned", "plain", "reid", "mlp"])
     ap.add_argument("--nswarm", type=int, default=256)
     ap.add_argument("--tune-steps", type=int, default=512)
+    ap.add_argument("--learned-n", type=int, default=1 << 24, help="learned form: particles")
     ap.add_argument("--train-samples", type=float, default=1e8, help="learned form: training samples per network")
     ap.add_argument("--train-steps", type=int, default=8000, help="learned form: Adam steps per network")
     args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
     if args.workload != "rrea16M":
-        if args.warmup < 3:
-            args.warmup = 3
         import __graft_entry__ as graft
         graft.build()
-        fn = {"swarms": run_swarms, "learned": run_learned, "plain": run_plain, "reid": run_reid,
-              "mlp": run_mlp}[args.workload]
+        fn = {"swarms": _printing(run_swarms), "learned": _printing(run_learned), "plain": run_plain,
+              "reid": run_reid, "mlp": run_mlp}[args.workload]
         return fn(args, graft.load_package())
-    if args.warmup < 3:
-        args.warmup = 3
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     import __graft_entry__ as graft
@@ -635,6 +665,7 @@ def main():
                                            compaction_period=args.compaction_period)
     ctx = mp.ctx
     K = args.steps_per_launch
+    live_start = list(mp.tallies().live)
     # ---- warm-up
     t = 0.0
     for _ in range(args.warmup):
@@ -666,8 +697,7 @@ def main():
     peak, peak_kind = _peaks()
     achieved = (kb.value / max(kl.value, 1)) / (kms.value / max(kl.value, 1) / 1e3) / 1e9
     slots_per_launch = (kb.value / max(kl.value, 1)) / 96.0
-    tps = _profile_traffic()
-    traffic = tps * slots_per_launch if tps else None
+    traffic = K_STEP_DRAM_BYTES_PER_SLOT * slots_per_launch if K_STEP_DRAM_BYTES_PER_SLOT else None
     # ---- end to end through the C ABI with pinned host buffers
     e2e = None
     try:
@@ -692,35 +722,48 @@ def main():
         e_el = _barrier_max(ms2.value / 1e3, ws)
         e2e = {"value": (tal_b.particle_steps - tal_a.particle_steps) * ws / e_el, "unit": UNIT,
                "h2d_bytes_per_step": int(h2d / args.e2e_steps), "d2h_bytes_per_step": int(d2h / args.e2e_steps),
-               "api": "pcl_advance_host", "chunks": args.e2e_chunks, "host_buffers": "pinned"}
+               "api": "pcl_advance_host", "chunks": args.e2e_chunks, "host_buffers": "pinned",
+               "steps": args.e2e_steps}
+        del host
     except Exception as ex:  # pragma: no cover
         e2e = {"value": None, "unit": UNIT, "error": str(ex)[:200], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
-    # ---- CPU baseline (rank 0, N = 1)
+    errs = {pcl._lib.ERROR_NAMES[q]: int(tal1.errors[q]) for q in range(8) if tal1.errors[q]}
+    live_end = list(tal1.live)
+    mp.close()
+    # ---- CPU baseline (rank 0, N = 1): the oracle on a bounded sample
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, el, ps = cpu_reference(pcl, args.cpu_sample, args.cpu_steps, threads)
+        v, el, ps, _, _ = cpu_reference(args.cpu_sample, args.cpu_steps, 1, threads)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{args.cpu_sample} e- at 1 MeV isotropic, {args.cpu_steps} steps of 1 ps after 1 warm-up "
-                         f"({ps} particle-steps, {el:.1f} s), C++ Float64 oracle"}
-    errs = {pcl._lib.ERROR_NAMES[q]: int(tal1.errors[q]) for q in range(8) if tal1.errors[q]}
+               "sample": f"{args.cpu_sample} particles drawn from the grown-state recipe, 1 warm-up + "
+                         f"{args.cpu_steps} timed steps of 1 ps ({ps} particle-steps, {el:.1f} s), C++ Float64 "
+                         f"oracle"}
+    forms = {}
+    if rank == 0 and ws == 1 and not args.no_forms:
+        for name, fn in (("batched", run_swarms), ("learned", run_learned)):
+            try:
+                forms[name] = _form_summary(fn(args, pcl), value)
+            except Exception as ex:  # pragma: no cover
+                forms[name] = {"value": None, "error": str(ex)[:300]}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / (args.steps * K), "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-                "config": {"workload": "rrea-air-0.5MVm-16M", "seed_electrons": args.n, "dt_s": dt,
-                           "steps_per_launch": K, "graph": bool(args.graph),
-                           "compaction_period": args.compaction_period or 8,
-                           "blocks_per_sm": (args.bps or 4) if args.classic else 3,
-                           "step_kernel": "classic" if args.classic else "event", "live_at_end": list(tal1.live),
-                           "l2": "inputs larger than L2 (population > 800 MB)", "parallelism": f"replicas{ws}"},
+                "config": workload_config(args.n, ws),
+                "run": {"steps_per_launch": K, "graph": bool(args.graph),
+                        "compaction_period": args.compaction_period or 8,
+                        "blocks_per_sm": (args.bps or 4) if args.classic else 3,
+                        "step_kernel": "classic" if args.classic else "event",
+                        "live_at_start": live_start, "live_at_end": live_end},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "peak_kind": peak_kind,
-                             "traffic": traffic, "kernel": "k_step"},
+                             "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                             "traffic_source": K_STEP_DRAM_CAPTURE, "kernel": "k_step",
+                             "bytes_per_particle_step": 96},
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(nl.value), "clocks": clk.summary(),
                 "errors": errs}
+        line.update(forms)
         print(json.dumps(line))
-    mp.close()
     return 0
 
 

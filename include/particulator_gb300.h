@@ -352,6 +352,22 @@ int pcl_advance(void* ctx, double tfinal);
  * in flight when the call returns.  Host buffers should be pinned. */
 int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_packed* in, int64_t* n_out,
                      pcl_packed* out, const int64_t* out_cap, int nchunks, int compact);
+/* How pcl_advance_host moves the population over the CPU-GPU link (no
+ * counterpart in the reference, whose populations never leave host memory):
+ * PCL_HOST_IO_COPY: the chunked copy-engine pipeline above.
+ * PCL_HOST_IO_DIRECT: one launch of the step kernel reads every input slot
+ *   from the caller's page-locked arrays and writes every result (updated
+ *   slots, dead marks, appended secondaries) to the output arrays over the
+ *   link, with no copies (the context's device copy is written as well);
+ *   nchunks is ignored.  The arrays must be page-locked (pcl_host_alloc,
+ *   pcl_host_register, cudaHostAlloc) and usable by the device, else
+ *   PCL_ERR_INVALID.  A compacting step (compact != 0) downloads the
+ *   compacted population with copies as in the other mode.
+ * PCL_HOST_IO_AUTO (default): DIRECT where the arrays allow it, else COPY. */
+#define PCL_HOST_IO_AUTO   0
+#define PCL_HOST_IO_COPY   1
+#define PCL_HOST_IO_DIRECT 2
+int pcl_set_host_io(void* ctx, int mode);
 /* Page-lock (and release) caller-owned host memory so that the copies of
  * pcl_advance_host / pcl_upload_packed / pcl_download_packed from it run
  * asynchronously at full link speed (cudaHostRegister / cudaHostUnregister on
@@ -365,7 +381,11 @@ int pcl_host_free(void* ptr);
 
 /* run!(mpopl, pusher, tfinal, dt, callback) (run.jl:1-29) with the device-side
  * PopulationTargetCallback / CollisionCounter.  Steps of dt until tfinal, the
- * target or max_steps; fills *out. */
+ * target or max_steps; fills *out.  The target is tested after every step, as
+ * run! does: with steps_per_launch > 1 the launches shrink near the target
+ * (to one step until a per-step change has been seen, then to the steps the
+ * fastest change seen so far needs, with a margin), so the run stops on the
+ * same step as with one step per launch. */
 int pcl_run(void* ctx, double tfinal, double dt, const pcl_run_opts* opts, pcl_tallies* out);
 
 /* Counters, population statistics and maintenance. */
@@ -425,8 +445,11 @@ int pcl_test_timeout(void* ctx, int max_iters);
  * static device array of PCL_NOALLOC_SCRATCH_BYTES that every GPU loading the
  * library keeps until exit; n above PCL_NOALLOC_MAX_SLOTS returns
  * PCL_ERR_CAPACITY.  All calls share that array, so calls that overlap on the
- * GPU race.  The first call on each device looks up the array's address;
- * make it before any stream capture.  `stream` is a cudaStream_t (NULL =
+ * GPU race.  The input and output buffers must not overlap (an in-place
+ * call would race between tiles): overlapping ranges return PCL_ERR_INVALID.
+ * The first call on each device looks up the array's address and caches it
+ * for the life of the process; make it before any stream capture, and do not
+ * call this after cudaDeviceReset.  `stream` is a cudaStream_t (NULL =
  * default stream).  Context-free errors: pcl_last_error(NULL). */
 #define PCL_NOALLOC_MAX_SLOTS (1 << 25)
 #define PCL_NOALLOC_SCRATCH_BYTES 196864

@@ -39,6 +39,8 @@ def lib():
         L.orc_set_wall.argtypes = [C.c_void_p, C.c_int, C.c_int, _d, C.c_int]
         L.orc_roulette.argtypes = [C.c_void_p, C.c_int, _d]
         L.orc_split.argtypes = [C.c_void_p, C.c_int, _d]
+        L.orc_poisson_inv.argtypes = [_d, _d]
+        L.orc_poisson_inv.restype = C.c_int
         L.orc_get_wall.argtypes = [C.c_void_p, _P(C.c_int32), _P(C.c_uint64), _P(_d), _P(_d), _P(_d), _P(_d)]
         L.orc_get_wall.restype = C.c_int64
         L.orc_set_linear_table.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _d, _d, _P(_d), _P(_d),

@@ -271,7 +271,7 @@ static inline int precheb(double x, int k, double xmax, int n, double* t, bool& 
     return i;
 }
 
-// ratebound (collision_table.jl:293-305) and setr! (collisions.jl:63-74)
+// ratebound (collision_table.jl:94-106) and setr! (collisions.jl:63-74)
 static double setr(Walker& Wk, int species) {
     const Species& S = Wk.W->sp[species];
     double eng = kinenergy(species, Wk.P->p);
@@ -907,7 +907,7 @@ static void do_one_collision(Walker& Wk, int species, SpawnBuf& out) {
     const Table& T = S.tab;
     uint32_t ctr0 = L.ctr;
     int j = 0;
-    if (T.linear) {  // rate(::CollisionTable, j, pre) (collision_table.jl:249-256)
+    if (T.linear) {  // rate(::CollisionTable, j, pre) (collision_table.jl:53-57)
         double w;
         bool oor = false;
         int i = indweight(T, eng, w, oor);
@@ -1182,6 +1182,18 @@ int orc_roulette(void* w, int species, double pkeep) {
     return 0;
 }
 
+// Poisson(p) by inversion for split!, the pmf summed in Float64 from exp(-p)
+// as the device does it (p rounded to FP32 first; at most 1024 copies)
+static int poisson_inv(float pf, float u) {
+    int k = 0;
+    const double pd = double(pf);
+    double P = std::exp(-pd), F = P;
+    while (double(u) > F && k < 1024) { ++k; P = P * (pd / double(k)); F = F + P; }
+    return k;
+}
+
+int orc_poisson_inv(double p, double u) { return poisson_inv(float(p), float(u)); }
+
 int orc_split(void* w, int species, double p) {
     World* W = static_cast<World*>(w);
     auto& v = W->sp[species].parts;
@@ -1194,15 +1206,14 @@ int orc_split(void* w, int species, double p) {
         const uint32_t ctr0 = v[i].ctr;
         v[i].ctr += 1;
         const float u = float(double(((word >> 9) << 1) | 1u) * 5.9604644775390625e-8);
-        // Poisson(p) by inversion, in FP32 as the device does it
-        int k = 0;
-        float P = std::exp(-pf), F = P;
-        while (u > F && k < 1024) { ++k; P *= pf / float(k); F += P; }
+        const int k = poisson_inv(pf, u);
         for (int j = 0; j < k; ++j) {
             uint32_t a = ctr0, b = uint32_t(v[i].sid), c2 = uint32_t(v[i].sid >> 32), d = 2u + uint32_t(j >> 1);
             philox(a, b, c2, d, W->k0, W->k1);
             Part q = v[i];
             q.sid = (j & 1) ? (uint64_t(c2) | (uint64_t(d) << 32)) : (uint64_t(a) | (uint64_t(b) << 32));
+            if (W->nswarm > 0)   // the copy stays in its parent's swarm (top 8 bits of the stream id)
+                q.sid = (q.sid & 0x00FFFFFFFFFFFFFFull) | (v[i].sid & 0xFF00000000000000ull);
             q.ctr = 0;
             v.push_back(q);
         }

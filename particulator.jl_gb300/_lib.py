@@ -21,6 +21,7 @@ PCL_ERR_CAPACITY = -3
 PCL_ERR_UNSUPPORTED = -4
 PCL_ERR_STATE = -5
 PCL_ERR_TIMEOUT = -6
+HOST_IO_AUTO, HOST_IO_COPY, HOST_IO_DIRECT = 0, 1, 2
 PCL_ERR_NUMERIC = -7
 NOALLOC_MAX_SLOTS = 1 << 25
 
@@ -158,6 +159,7 @@ _SIGS = {
     "pcl_set_learned": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "pcl_autotune": (C.c_int, [C.c_void_p, _d, _i32, _P(TuneResult)]),
     "pcl_set_launch": (C.c_int, [C.c_void_p, _i32, _i32, _i32, _i32]),
+    "pcl_set_host_io": (C.c_int, [C.c_void_p, C.c_int]),
     "pcl_learn_stats": (C.c_int, [C.c_void_p, _P(_i64), _P(_i64)]),
     "pcl_learn_data": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, _u64,
                                  _P(C.c_float), _P(C.c_float), _P(_i64)]),

@@ -253,6 +253,13 @@ PCL_INTERNAL StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, i
         A.xw[s] = S.xw[S.cur];
         A.ps[s] = S.ps[S.cur];
         A.meta[s] = S.meta[S.cur];
+        A.in_xw[s] = c->hin_xw[s] ? c->hin_xw[s] : A.xw[s];
+        A.in_ps[s] = c->hin_ps[s] ? c->hin_ps[s] : A.ps[s];
+        A.in_meta[s] = c->hin_meta[s] ? c->hin_meta[s] : A.meta[s];
+        A.hx_xw[s] = c->hx_xw[s];
+        A.hx_ps[s] = c->hx_ps[s];
+        A.hx_meta[s] = c->hx_meta[s];
+        A.hx_cap[s] = c->hx_cap[s];
         A.cap[s] = S.cap;
         A.hist_n[s] = S.hist_n;
         A.hist_w[s] = S.hist_w;
@@ -934,13 +941,45 @@ int pcl_run(void* ctx, double tfinal, double dt, const pcl_run_opts* opts, pcl_t
     // tolerance, so that accumulated rounding of the clock never adds a step
     const long long total = (long long)std::ceil((tfinal - c->t) / dt - 1e-6);
     long long done = 0;
+    const bool target = opts && opts->target_species >= 0 && opts->target_species < 3;
+    double g_ext = 0.0;   // largest (ismax) or smallest per-step live ratio of the target species so far
     while (done < total) {
         // advance!, droplow!, onstep (population target)
         int ns = int(std::min<long long>(K, total - done));
         if (opts && opts->max_steps > 0) ns = int(std::min<long long>(ns, opts->max_steps - done));
         if (ns <= 0) break;
+        if (target && ns > 1) {
+            // run.jl:6-27 tests the target after every step.  A launch of ns
+            // steps can only stop at its end, so near the target the launches
+            // shrink: ns is the number of steps that the fastest per-step change
+            // seen so far, with a margin, needs to reach the target (one step
+            // until a change has been seen).
+            const double live = double(c->live[opts->target_species]), n = double(opts->target_n);
+            int m = 1;
+            if (g_ext > 0.0) {
+                if (opts->target_ismax) {
+                    const double g = std::max(g_ext, 1.0) * 1.01;
+                    m = (g_ext <= 1.0) ? ns : int(std::floor(std::log(n / (1.05 * live + 1.0)) / std::log(g)));
+                } else {
+                    const double g = std::min(g_ext, 1.0) * 0.99;
+                    m = (g_ext >= 1.0) ? ns
+                                       : int(std::floor(std::log((0.95 * live) / std::max(n, 0.5)) / -std::log(g)));
+                }
+            }
+            ns = std::max(1, std::min(ns, m));
+        }
+        const long long live0 = target ? c->live[opts->target_species] : 0;
         int rc = launch_steps(c, dt, ns);
         if (rc || (rc = apply_swarm_caps(c))) return rc;
+        if (target) {
+            double prev = double(std::max<long long>(live0, 1));
+            for (int k = 0; k < ns; ++k) {
+                const double cur = double(c->h_ctl->live_end[k][opts->target_species]);
+                const double r = std::max(cur, 1.0) / prev;
+                g_ext = (g_ext == 0.0) ? r : (opts->target_ismax ? std::max(g_ext, r) : std::min(g_ext, r));
+                prev = std::max(cur, 1.0);
+            }
+        }
         done += ns;
         if (done == total && std::fabs(c->t - tfinal) < 1e-6 * dt) c->t = tfinal;
         if (opts && opts->target_species >= 0 && opts->target_species < 3) {

@@ -172,6 +172,27 @@ static cudaError_t copy_slots(const SpeciesState& S, const pcl_packed& h, long l
     return e;
 }
 
+// Device-usable address of page-locked host memory (nullptr: not page-locked
+// or not reachable by the device).  Clears the error a failed query leaves.
+static void* device_view(const void* p) {
+    if (!p) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    return at.devicePointer;
+}
+
+int pcl_set_host_io(void* ctx, int mode) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    if (mode < PCL_HOST_IO_AUTO || mode > PCL_HOST_IO_DIRECT) return fail(c, PCL_ERR_INVALID, "host i/o mode");
+    c->host_io = mode;
+    return PCL_OK;
+}
+
 int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_packed* in, int64_t* n_out,
                      pcl_packed* out, const int64_t* out_cap, int nchunks, int compact) {
     Ctx* c = static_cast<Ctx*>(ctx);
@@ -194,8 +215,24 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
     }
     if (!any) return fail(c, PCL_ERR_STATE, "no species set");
     CK(cudaSetDevice(c->device));
-    // every return, error or not, leaves no copy into or out of the caller's
-    // buffers in flight
+    // host-direct mode: every array the kernels would touch must be page-locked
+    // and usable by the device
+    bool direct = c->host_io != PCL_HOST_IO_COPY;
+    void* hv[3][6] = {};
+    for (int s = 0; s < 3 && direct; ++s) {
+        if (n[s] > 0) {
+            hv[s][0] = device_view(in[s].xw); hv[s][1] = device_view(in[s].ps); hv[s][2] = device_view(in[s].meta);
+            direct = hv[s][0] && hv[s][1] && hv[s][2];
+        }
+        if (direct && out_cap[s] > 0) {
+            hv[s][3] = device_view(out[s].xw); hv[s][4] = device_view(out[s].ps); hv[s][5] = device_view(out[s].meta);
+            direct = hv[s][3] && hv[s][4] && hv[s][5];
+        }
+    }
+    if (c->host_io == PCL_HOST_IO_DIRECT && !direct)
+        return fail(c, PCL_ERR_INVALID, "host-direct mode needs page-locked arrays the device can use");
+    // every return, error or not, leaves no copy or kernel using the caller's
+    // buffers in flight, and the host-direct pointers cleared
     struct Drain {
         Ctx* c;
         ~Drain() {
@@ -203,6 +240,11 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
             if (c->s_d2h) cudaStreamSynchronize(c->s_d2h);
             if (c->s_cmp) cudaStreamSynchronize(c->s_cmp);
             cudaStreamSynchronize(c->stream);
+            for (int s = 0; s < 3; ++s) {
+                c->hin_xw[s] = nullptr; c->hin_ps[s] = nullptr; c->hin_meta[s] = nullptr;
+                c->hx_xw[s] = nullptr; c->hx_ps[s] = nullptr; c->hx_meta[s] = nullptr;
+                c->hx_cap[s] = 0;
+            }
         }
     } drain{c};
     int rc = build_blob(c);
@@ -246,7 +288,30 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
     }
     const long long G = n[0] + n[1] + n[2];
     const long long cs = std::max<long long>(1, (G + nchunks - 1) / nchunks);
-    int nch = int((G + cs - 1) / cs);
+    int nch = direct ? 0 : int((G + cs - 1) / cs);
+    if (direct) {
+        // one population launch over everything, reading the host slots and
+        // writing results to the host arrays; the spill passes and the learned
+        // round below append there too
+        for (int s = 0; s < 3; ++s) {
+            if (n[s] > 0) {
+                c->hin_xw[s] = static_cast<const float4*>(hv[s][0]);
+                c->hin_ps[s] = static_cast<const float4*>(hv[s][1]);
+                c->hin_meta[s] = static_cast<const uint4*>(hv[s][2]);
+            }
+            if (out_cap[s] > 0) {
+                c->hx_xw[s] = static_cast<float4*>(hv[s][3]);
+                c->hx_ps[s] = static_cast<float4*>(hv[s][4]);
+                c->hx_meta[s] = static_cast<uint4*>(hv[s][5]);
+                c->hx_cap[s] = out_cap[s];
+            }
+        }
+        StepArgs A = make_args(c, dt, 1, 0, 0);
+        CK(cudaEventRecord(c->io_tev[0], c->stream));
+        CK(launch_step_prepared(minb, grid_blocks(c), threads, smem, c->stream, A));
+        CK(cudaEventRecord(c->io_tev[1], c->stream));
+        c->launches += 1;
+    }
     for (int i = 0; i < nch; ++i) {
         const long long g0 = i * cs, g1 = std::min(G, g0 + cs);
         long long a[3], b[3];
@@ -290,7 +355,7 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
                            c->stream));
         if ((rc = readback(c))) return rc;
         if (c->learn_on) count_learned(c);
-        for (int i = 0; i < nch; ++i) {   // step-kernel time of the chunk launches
+        for (int i = 0; i < std::max(nch, direct ? 1 : 0); ++i) {   // step-kernel time of the launches
             float ms = 0.0f;
             CK(cudaEventElapsedTime(&ms, c->io_tev[2 * i], c->io_tev[2 * i + 1]));
             c->k_ms += ms;
@@ -307,19 +372,22 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
     c->particle_steps += (long long)c->h_ctl->live_start[0];
     for (int s = 0; s < 3; ++s) c->live[s] = (long long)c->h_ctl->live_end[0][s];
     if (c->h_ctl->err[PCL_E_CAPACITY] > 0) return fail(c, PCL_ERR_CAPACITY, "population capacity exceeded");
+    long long from[3] = {n[0], n[1], n[2]};   // slots the host arrays do not hold yet
     if (compact) {
         if ((rc = compact_all(c)) || (rc = readback(c))) return rc;
-        for (int s = 0; s < 3; ++s) n[s] = 0;   // everything is downloaded below
+        for (int s = 0; s < 3; ++s) from[s] = 0;   // everything is downloaded below
     } else {
         c->steps_since_compact += 1;
     }
-    // the rest: appended secondaries (or the whole compacted population)
+    // the rest: appended secondaries (or the whole compacted population); in
+    // host-direct mode the kernels wrote the appended slots to the host already
     long long nf[3];
     for (int s = 0; s < 3; ++s) {
         nf[s] = (c->sp[s].set && c->sp[s].cap > 0) ? std::min<long long>((long long)c->h_ctl->n[s], c->sp[s].cap) : 0;
         if (nf[s] > out_cap[s]) return fail(c, PCL_ERR_CAPACITY, "output arrays too small");
+        if (direct && !compact) from[s] = nf[s];
     }
-    for (int s = 0; s < 3; ++s) CK(copy_slots(c->sp[s], out[s], n[s], nf[s], false, c->s_d2h));
+    for (int s = 0; s < 3; ++s) CK(copy_slots(c->sp[s], out[s], from[s], nf[s], false, c->s_d2h));
     CK(cudaStreamSynchronize(c->s_d2h));
     for (int s = 0; s < 3; ++s) n_out[s] = nf[s];
     return PCL_OK;

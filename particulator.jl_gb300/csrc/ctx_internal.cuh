@@ -28,8 +28,8 @@ __global__ void k_learn_x(const float4* ps, const float4* m2, const unsigned lon
                           float* X);
 __global__ void k_roulette(float4* xw, uint4* meta, long long n, float pkeep, uint32_t k0, uint32_t k1,
                            unsigned long long* dead);
-__global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, uint32_t k0,
-                        uint32_t k1, unsigned long long* nslots, unsigned long long* lost);
+__global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, double e,
+                        int nswarm, uint32_t k0, uint32_t k1, unsigned long long* nslots, unsigned long long* lost);
 __global__ void k_roulette_swarms(float4* xw, uint4* meta, long long n, const float* pkeep, int nswarm, uint32_t k0,
                                   uint32_t k1, unsigned long long* dead);
 __global__ void k_swarm_count(const uint4* meta, const unsigned long long* nslots, long long cap, int nswarm,
@@ -161,6 +161,17 @@ struct Ctx {
     std::vector<cudaEvent_t> io_tev;       // [2 * chunks]: timing of each chunk's launch
     cudaEvent_t io_join = nullptr;
     unsigned long long* d_heads = nullptr; // [64] work counters of the chunk launches
+    int host_io = PCL_HOST_IO_AUTO;        // pcl_set_host_io
+    // host-direct mode, set for the duration of one pcl_advance_host call:
+    // population launches read these host slots and every slot write is
+    // repeated to hx_* (device-usable pointers of the caller's page-locked arrays)
+    const float4* hin_xw[3] = {nullptr, nullptr, nullptr};
+    const float4* hin_ps[3] = {nullptr, nullptr, nullptr};
+    const uint4* hin_meta[3] = {nullptr, nullptr, nullptr};
+    float4* hx_xw[3] = {nullptr, nullptr, nullptr};
+    float4* hx_ps[3] = {nullptr, nullptr, nullptr};
+    uint4* hx_meta[3] = {nullptr, nullptr, nullptr};
+    long long hx_cap[3] = {0, 0, 0};
     // accumulated host state
     double t = 0.0;
     long long steps = 0;

@@ -76,9 +76,10 @@ int pcl_split(void* ctx, int species, double p) {
     CK(cudaMallocAsync(&lost, sizeof(unsigned long long), c->stream));
     CK(cudaMemsetAsync(lost, 0, sizeof(unsigned long long), c->stream));
     const int grid = int(std::min<long long>((n + 255) / 256, 8ll * c->sm_count));
-    k_split<<<grid, 256, 0, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], n, S.cap, float(p),
-                                         uint32_t(c->cfg.seed), uint32_t(c->cfg.seed >> 32), &c->d_ctl->n[species],
-                                         lost);
+    const float pf = float(p);
+    k_split<<<grid, 256, 0, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], n, S.cap, pf,
+                                         std::exp(-double(pf)), c->nswarm, uint32_t(c->cfg.seed),
+                                         uint32_t(c->cfg.seed >> 32), &c->d_ctl->n[species], lost);
     CK(cudaGetLastError());
     unsigned long long hl = 0;
     CK(cudaMemcpyAsync(&hl, lost, sizeof(hl), cudaMemcpyDeviceToHost, c->stream));

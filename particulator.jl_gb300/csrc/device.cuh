@@ -114,6 +114,18 @@ struct StepArgs {
     float4* ps[3];
     uint4*  meta[3];
     long long cap[3];
+    // where population launches read their input slots: the population arrays
+    // above, or (host-direct mode of pcl_advance_host) the caller's page-locked
+    // host arrays, read over the CPU-GPU link
+    const float4* in_xw[3];
+    const float4* in_ps[3];
+    const uint4*  in_meta[3];
+    // host-direct mode: every slot write (update, dead mark, append) is also
+    // made to these host arrays, for slots below hx_cap (nullptr: none)
+    float4* hx_xw[3];
+    float4* hx_ps[3];
+    uint4*  hx_meta[3];
+    long long hx_cap[3];
     // spill queues: the kernel reads `sp_in` (spill mode) and writes `sp_out`
     float4* sp_in_xw; float4* sp_in_ps; uint4* sp_in_meta;
     float4* sp_out_xw; float4* sp_out_ps; uint4* sp_out_meta;

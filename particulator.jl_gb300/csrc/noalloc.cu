@@ -19,7 +19,17 @@
 //
 // Set-up: the first call on each device looks up the array's device address
 // with cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture.
+// first call before any stream capture.  The cache assumes that the device's
+// primary context lives until the process exits: after cudaDeviceReset the
+// cached address would name memory of the destroyed context.
+//
+// The input and output buffers must not overlap: the scatter of one tile
+// writes below its own input range while other tiles may still read there, so
+// an in-place call would race.  Overlapping ranges are refused.
+//
+// Launch errors are read from each launch's own return code
+// (cudaLaunchKernel), so an error left pending by earlier, unrelated work on
+// the thread is neither reported as this call's nor cleared by it.
 #include <cuda_runtime.h>
 #include <mutex>
 #include <string>
@@ -78,6 +88,10 @@ static int scratch_address(unsigned char** out) {
 
 const char* noalloc_last_error() { return g_err.c_str(); }
 
+static bool ranges_overlap(const unsigned char* a, const unsigned char* b, size_t len) {
+    return a < b + len && b < a + len;
+}
+
 }  // namespace pcl
 
 using namespace pcl;
@@ -94,6 +108,27 @@ extern "C" int pcl_compact_noalloc(int64_t n, const float* xw, const float* ps, 
         g_err = "pcl_compact_noalloc: " + std::to_string(n) + " slots exceed PCL_NOALLOC_MAX_SLOTS (" +
                 std::to_string(kMaxSlots) + "); use pcl_compact";
         return PCL_ERR_CAPACITY;
+    }
+    if (n > 0) {
+        const size_t b16 = size_t(n) * 16;
+        const unsigned char* in_lo[3] = {reinterpret_cast<const unsigned char*>(xw),
+                                         reinterpret_cast<const unsigned char*>(ps),
+                                         reinterpret_cast<const unsigned char*>(meta)};
+        const unsigned char* out_lo[3] = {reinterpret_cast<const unsigned char*>(out_xw),
+                                          reinterpret_cast<const unsigned char*>(out_ps),
+                                          reinterpret_cast<const unsigned char*>(out_meta)};
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b)
+                if (ranges_overlap(out_lo[a], in_lo[b], b16) || (a < b && ranges_overlap(out_lo[a], out_lo[b], b16))) {
+                    g_err = "pcl_compact_noalloc: input and output buffers overlap (in-place compaction races)";
+                    return PCL_ERR_INVALID;
+                }
+        const unsigned char* nb = reinterpret_cast<const unsigned char*>(n_out);
+        for (int a = 0; a < 3; ++a)
+            if (nb + sizeof(int64_t) > out_lo[a] && out_lo[a] + b16 > nb) {
+                g_err = "pcl_compact_noalloc: n_out lies inside an output buffer";
+                return PCL_ERR_INVALID;
+            }
     }
     unsigned char* base = nullptr;
     int rc = scratch_address(&base);
@@ -114,14 +149,20 @@ extern "C" int pcl_compact_noalloc(int64_t n, const float* xw, const float* ps, 
     C.n_out = dn_out;
     int nt = int(n > 0 ? (n + kTile - 1) / kTile : 1);
     C.ntiles_max = nt;
-    k_noalloc_set_n<<<1, 32, 0, s>>>(dn, n);
-    dim3 g(nt, 1);
-    k_compact_count<<<g, 256, 0, s>>>(C);
-    k_compact_scan<<<1, 1024, 0, s>>>(C);
-    k_compact_scatter<<<g, 256, 0, s>>>(C);
-    cudaError_t e = cudaGetLastError();
+    long long nv = n;
+    void* set_args[2] = {&dn, &nv};
+    void* c_args[1] = {&C};
+    const dim3 g(nt, 1);
+    cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(k_noalloc_set_n), dim3(1), dim3(32), set_args, 0, s);
+    if (e == cudaSuccess)
+        e = cudaLaunchKernel(reinterpret_cast<const void*>(k_compact_count), g, dim3(256), c_args, 0, s);
+    if (e == cudaSuccess)
+        e = cudaLaunchKernel(reinterpret_cast<const void*>(k_compact_scan), dim3(1), dim3(1024), c_args, 0, s);
+    if (e == cudaSuccess)
+        e = cudaLaunchKernel(reinterpret_cast<const void*>(k_compact_scatter), g, dim3(256), c_args, 0, s);
     if (e == cudaSuccess) e = cudaMemcpyAsync(n_out, dn_out, sizeof(int64_t), cudaMemcpyDeviceToDevice, s);
     if (e != cudaSuccess) {
+        cudaGetLastError();   // this call's own launch error: not left for the caller's next check
         g_err = std::string("pcl_compact_noalloc: ") + cudaGetErrorString(e);
         return PCL_ERR_CUDA;
     }

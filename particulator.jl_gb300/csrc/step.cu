@@ -230,7 +230,7 @@ __device__ __forceinline__ int lin_index(const SpeciesHdr& S, const KCtx& K, flo
 __device__ __forceinline__ float setr(const SpeciesHdr& S, const KCtx& K, float E, int sw) {
     if (E < S.cut) return 0.0f;
     float rb;
-    if (S.table_kind == 1) {  // ratebound(::CollisionTable) (collision_table.jl:231-242)
+    if (S.table_kind == 1) {  // ratebound(::CollisionTable) (collision_table.jl:32-43)
         float w;
         int i = lin_index(S, K, E, w);
         const float* b = K.blob + S.rb_off + i;
@@ -606,7 +606,7 @@ __device__ __forceinline__ void sb_tail(Lane& L, const KCtx& K, float E, float k
 
 // seltzer.jl:67-122 with the photon angle of util.jl:143-159.  The inverse-CDF
 // lookup reproduces the reference's interpolation weights as written
-// (seltzer.jl:278-284, off-diagonal corners included).
+// (seltzer.jl:114-118, off-diagonal corners included).
 __device__ PCL_RARE void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
     const SBHdr& T = K.H->sb[P.sb];
     const float* data = K.A->sb_data[P.sb];
@@ -1029,7 +1029,7 @@ __device__ void collide(Lane& L, const KCtx& K, const SpeciesHdr& S) {
     if (!(E >= S.cut)) return;
     const uint32_t ctr0 = L.ctr;
     int j = 0;
-    if (S.table_kind == 1) {  // rate(::CollisionTable, j, pre) (collision_table.jl:249-256)
+    if (S.table_kind == 1) {  // rate(::CollisionTable, j, pre) (collision_table.jl:53-57)
         float w;
         int i = lin_index(S, K, E, w);
         float xi = U(L, K) * L.r;
@@ -1147,6 +1147,19 @@ __device__ __forceinline__ void load_slot(Lane& L, const float4* xw, const float
     L.sid_lo = m.x; L.sid_hi = m.y; L.ctr = m.z;
     L.th = -__uint_as_float(m.w);  // + dt by the caller (t_off <= 0 is time still owed)
     L.tlo = 0.0f;
+}
+
+// A slot of the population written at the end of a particle's launch, and in
+// host-direct mode the same slot of the caller's host arrays.
+__device__ __forceinline__ void put_slot(const StepArgs& A, int sp, long long slot, float4 a, float4 b, uint4 m) {
+    A.xw[sp][slot] = a;
+    A.ps[sp][slot] = b;
+    A.meta[sp][slot] = m;
+    if (A.hx_xw[sp] && slot < A.hx_cap[sp]) {
+        A.hx_xw[sp][slot] = a;
+        A.hx_ps[sp][slot] = b;
+        A.hx_meta[sp][slot] = m;
+    }
 }
 
 // ------------------------------------------------------------ the step ---
@@ -1334,11 +1347,18 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         else if (v < nsp0 + nsp1) { sp = 1; sl = v - nsp0; }
                         else { sp = 2; sl = v - nsp0 - nsp1; }
                         L.species = sp;
-                        load_slot(L, A.xw[sp], A.ps[sp], A.meta[sp], sl);
+                        load_slot(L, A.in_xw[sp], A.in_ps[sp], A.in_meta[sp], sl);
                         dd_add(L.th, L.tlo, dt_hi, dt_lo);
                         L.slot = int(sl);
                         L.k = 0;
                         has = (L.ctr != PCL_DEAD_CTR);
+                        // host-direct mode: a slot read dead from the host is dead in
+                        // the device copy (which may hold an older particle there)
+                        // and in the output arrays (which may differ from the input)
+                        if (!has && A.hx_meta[sp]) {
+                            A.meta[sp][sl].z = PCL_DEAD_CTR;
+                            if (sl < A.hx_cap[sp]) A.hx_meta[sp][sl].z = PCL_DEAD_CTR;
+                        }
                         if (has) atomicAdd(&tal[T_LSTART + 0], 1u);
                     }
                     if (has && !(LEARN && A.spill_mode == 2)) {
@@ -1443,9 +1463,8 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
             if (grp & (1u << lane)) {
                 long long slot = (long long)base + __popc(grp & lt);
                 if (slot < A.cap[lsp]) {
-                    A.xw[lsp][slot] = make_float4(L.x, L.y, L.z, L.w);
-                    A.ps[lsp][slot] = make_float4(L.px, L.py, L.pz, L.s);
-                    A.meta[lsp][slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-dd_val(L.th, L.tlo)));
+                    put_slot(A, lsp, slot, make_float4(L.x, L.y, L.z, L.w), make_float4(L.px, L.py, L.pz, L.s),
+                             make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-dd_val(L.th, L.tlo))));
                 } else {
                     err(K, PCL_E_CAPACITY);
                 }
@@ -1453,12 +1472,11 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
             am &= ~grp;
         }
         if (fin == 1 && L.slot >= 0) {
-            const int sp = L.species;
-            A.xw[sp][L.slot] = make_float4(L.x, L.y, L.z, L.w);
-            A.ps[sp][L.slot] = make_float4(L.px, L.py, L.pz, L.s);
-            A.meta[sp][L.slot] = make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-dd_val(L.th, L.tlo)));
+            put_slot(A, L.species, L.slot, make_float4(L.x, L.y, L.z, L.w), make_float4(L.px, L.py, L.pz, L.s),
+                     make_uint4(L.sid_lo, L.sid_hi, L.ctr, __float_as_uint(-dd_val(L.th, L.tlo))));
         } else if (fin == 2 && L.slot >= 0) {
             A.meta[L.species][L.slot].z = PCL_DEAD_CTR;
+            if (A.hx_meta[L.species] && L.slot < A.hx_cap[L.species]) A.hx_meta[L.species][L.slot].z = PCL_DEAD_CTR;
             atomicAdd(&tal[T_DEAD + L.species], 1u);
         }
         if (fin) has = false;
@@ -1959,12 +1977,17 @@ __global__ void k_roulette_cap(float4* xw, uint4* meta, const unsigned long long
 
 // split! (population.jl:318-335): divide a live particle's weight by 1 + p and
 // add Poisson(p) copies of it (number by inversion with one draw from its
-// stream; the reference draws it from Distributions.jl).  Copy j gets the
-// stream id of words (2(j%2), 2(j%2)+1) of Philox block (ctr, sid, 2 + j/2) of
-// its parent and a fresh counter; x, p, w, s and the step clock are copied.
-__global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, uint32_t k0,
-                        uint32_t k1, unsigned long long* nslots, unsigned long long* lost) {
-    const float e = expf(-p);
+// stream; the reference draws it from Distributions.jl).  The inversion sums
+// the pmf in Float64 from e = exp(-p) (computed on the host), with
+// correctly rounded operations that the compiler cannot contract, so the sum
+// passes every uniform below 1 and matches a host computation bit for bit.
+// Copy j gets the stream id of words (2(j%2), 2(j%2)+1) of Philox block
+// (ctr, sid, 2 + j/2) of its parent and a fresh counter; in swarm mode
+// (nswarm > 0) its top 8 bits stay the parent's swarm, as for any secondary.
+// x, p, w, s and the step clock are copied.
+__global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, double e,
+                        int nswarm, uint32_t k0, uint32_t k1, unsigned long long* nslots, unsigned long long* lost) {
+    const double pd = double(p);
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         uint4 m = meta[i];
@@ -1976,13 +1999,19 @@ __global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long l
         const uint32_t ctr0 = m.z;
         meta[i].z = m.z + 1u;
         int k = 0;
-        float P = e, F = e;
-        while (u > F && k < 1024) { ++k; P *= p / float(k); F += P; }
+        double P = e, F = e;
+        const double ud = double(u);
+        while (ud > F && k < 1024) {
+            ++k;
+            P = __dmul_rn(P, __ddiv_rn(pd, double(k)));
+            F = __dadd_rn(F, P);
+        }
         const float4 b = ps[i];
         for (int j = 0; j < k; ++j) {
             uint32_t c0 = ctr0, c1 = m.x, c2 = m.y, c3 = 2u + uint32_t(j >> 1);
             philox4x32_10(c0, c1, c2, c3, k0, k1);
             uint32_t lo = (j & 1) ? c2 : c0, hi = (j & 1) ? c3 : c1;
+            if (nswarm > 0) hi = (hi & 0x00FFFFFFu) | (m.y & 0xFF000000u);
             const unsigned long long q = atomicAdd(nslots, 1ull);
             if ((long long)q < cap) {
                 xw[q] = a;

@@ -52,7 +52,7 @@ def binding_energies(Z: int) -> np.ndarray:
 
 def sandia(Z: int):
     """Left energies (J) and coefficients [n][4] (m^2 J^i per atom) as built by
-    PhotoElectric(T, Z) (photo_electric.jl:163-176)."""
+    PhotoElectric(T, Z) (photo_electric.jl:19-31)."""
     rows = SANDIA_TABLE[Z]
     A = Z / Z_TO_A_RATIO[Z]
     s = (co.kilo * co.eV) ** np.arange(1, 5)

@@ -445,6 +445,13 @@ class MultiPopulation:
         self.t = float(tfinal)
         return [int(n_out[s]) for s in range(3)]
 
+    def set_host_io(self, mode: int):
+        """How advance_host moves the population over the CPU-GPU link
+        (pcl_set_host_io): 0 auto (direct where the arrays allow), 1 copy
+        pipeline, 2 direct (the step kernel reads and writes the page-locked
+        host arrays)."""
+        _lib.check(_lib.lib().pcl_set_host_io(self.ctx, int(mode)), self.ctx, "pcl_set_host_io")
+
     def set_learned(self, particle, proc_index: int, kind: int, net=None):
         """Attach (net) or detach (None) a learned sampler for one table
         position (pcl_set_learned)."""

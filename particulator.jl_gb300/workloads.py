@@ -6,6 +6,8 @@ coefficient of every atomic process is the atom density 2 n_X2.
 """
 from __future__ import annotations
 
+import json
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -140,6 +142,87 @@ def avalanche(n: int = 10000, kin: float = 1 * MEV, efield: float = 5e5, dt: flo
     mp = MultiPopulation(("electron", electrons), ("photon", photons), ("positron", positrons), seed=seed, **cfg)
     cl = air_continuum_loss(comp, Tcut=cut_e)
     return Workload(mp, pusher((0.0, 0.0, -efield), cl=cl), dt, 1.0, "rrea-air-0.5MVm")
+
+
+RREA_STATE_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "rrea_mixed_0.5MVm.json")
+_RECIPES = {}
+
+
+def rrea_recipe(path: str | None = None) -> dict:
+    """The recipe of the grown mixed avalanche at 0.5 MV/m (written by
+    data/grow_rrea.py): per-species fractions and (log10 E, cos theta_z)
+    histograms of the state reached from 10^4 seed electrons."""
+    path = path or RREA_STATE_PATH
+    if path not in _RECIPES:
+        with open(path) as f:
+            _RECIPES[path] = json.load(f)
+    return _RECIPES[path]
+
+
+def rrea_species_counts(n_total: int, path: str | None = None):
+    """Particles per species (electron, photon, positron) for a sample of
+    n_total: each species' share of the grown state, rounded down, the
+    remainder to the electrons."""
+    rec = rrea_recipe(path)
+    fr = [rec["species"][k]["fraction"] for k in ("electron", "photon", "positron")]
+    counts = [0, int(n_total * fr[1]), int(n_total * fr[2])]
+    counts[0] = int(n_total) - counts[1] - counts[2]
+    return counts
+
+
+def rrea_mixed_state(n_total: int, seed: int = 0, path: str | None = None) -> dict:
+    """n_total particles drawn from the grown avalanche's recipe (Philox
+    seed): species in the recorded fractions, each particle's cell of the
+    (log10 E, cos theta_z) histogram drawn by its count, E and cos theta
+    uniform within the cell, azimuth uniform, positions normal with the
+    recorded mean and spread, weight 1, t = 0; no energy below the species'
+    cut.  Returns {species: ParticleArrays}."""
+    rec = rrea_recipe(path)
+    rng = np.random.Generator(np.random.Philox(seed))
+    le = np.asarray(rec["log10_energy_eV_edges"])
+    ce = np.asarray(rec["cos_theta_z_edges"])
+    out = {}
+    for sp, name, m in zip((Electron, Photon, Positron), ("electron", "photon", "positron"),
+                           rrea_species_counts(n_total, path)):
+        d = rec["species"][name]
+        cells = np.asarray(d["cells"], dtype=np.int64).reshape(-1, 3)
+        if m == 0 or len(cells) == 0:
+            out[sp] = ParticleArrays.empty()
+            continue
+        w = cells[:, 2].astype(np.float64)
+        cdf = np.cumsum(w)
+        idx = np.minimum(np.searchsorted(cdf, rng.random(m) * cdf[-1], side="right"), len(cells) - 1)
+        iE, ic = cells[idx, 0], cells[idx, 1]
+        # within a cell, energies start at the species' cut (the state has none below it)
+        lo = np.maximum(le[iE], np.log10(rec["growth"]["cuts_eV"][name]))
+        lg = lo + rng.random(m) * (le[iE + 1] - lo)
+        cz = ce[ic] + rng.random(m) * (ce[ic + 1] - ce[ic])
+        phi = 2 * np.pi * rng.random(m)
+        pn = momentum_norm_from_kin(sp, 10.0 ** lg * co.eV)
+        st = np.sqrt(np.maximum(0.0, 1 - cz * cz))
+        p = np.stack([st * np.cos(phi), st * np.sin(phi), cz], axis=1) * pn[:, None]
+        x = np.asarray(d["x_mean_m"]) + rng.standard_normal((m, 3)) * np.asarray(d["x_std_m"])
+        out[sp] = ParticleArrays(x, p, np.ones(m), np.zeros(m))
+    return out
+
+
+def rrea_mixed(n_total: int = 1 << 24, seed: int = 0, dt: float = 1e-12, efield: float = 5e5,
+               path: str | None = None, tables=None, **cfg) -> Workload:
+    """The mixed avalanche at 0.5 MV/m started from n_total particles drawn
+    from the grown state's recipe (rrea_mixed_state): the 2^24-particle point
+    of the avalanche with its grown e- / gamma / e+ mix and spectra.
+    Capacities leave room for the growth of a few hundred steps."""
+    comp = air_composition()
+    et, gt, pt = tables if tables is not None else beam_tables(comp, efield, dt)
+    st = rrea_mixed_state(n_total, seed, path)
+    ne, ng, npos = (len(st[s]) for s in (Electron, Photon, Positron))
+    mp = MultiPopulation(
+        ("electron", Population(int(ne * 1.25) + (1 << 16), st[Electron], et, 10 * KEV, particle=Electron)),
+        ("photon", Population(int(ng * 1.25) + (1 << 20), st[Photon], gt, 5 * KEV, particle=Photon)),
+        ("positron", Population(int(npos * 1.5) + (1 << 16), st[Positron], pt, 10 * KEV, particle=Positron)),
+        seed=seed, **cfg)
+    cl = air_continuum_loss(comp)
+    return Workload(mp, pusher((0.0, 0.0, -efield), cl=cl), dt, 1.0, "rrea-air-0.5MVm-mixed")
 
 
 def reid_table(density: float, emax: float = 8.0 * co.eV, n: int = 4001, mass_ratio: float = 4e-3):

@@ -409,17 +409,27 @@ def _live_sorted(b, n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("nchunks", [1, 3, 8])
-def test_advance_host_equals_upload_advance_download(pcl, gpu, nchunks):
-    """pcl_advance_host (chunked uploads, range launches and downloads on
-    three streams) gives the particles of pcl_upload_packed + pcl_advance +
-    pcl_download_packed, bit for bit (matched by stream id; dead slots in the
-    same number), with and without the device repack."""
+@pytest.mark.parametrize("nchunks,mode", [(1, "auto"), (3, "auto"), (8, "auto"), (8, "copy"), (3, "direct")])
+def test_advance_host_equals_upload_advance_download(pcl, gpu, nchunks, mode):
+    """pcl_advance_host gives the particles of pcl_upload_packed + pcl_advance
+    + pcl_download_packed, bit for bit (matched by stream id; dead slots in the
+    same number), with and without the device repack, in both of its modes:
+    the copy pipeline (chunked uploads, range launches and downloads on three
+    streams; pageable arrays, or page-locked ones with the mode forced) and
+    host-direct (the step kernel reads and writes the page-locked arrays over
+    the link; the default for page-locked arrays)."""
     a = pcl.workloads.avalanche(n=60_000, seed=4, capacity=1 << 18)
     b = pcl.workloads.avalanche(n=60_000, seed=4, capacity=1 << 18)
     ba, bb = a.mpopl.packed_buffers(pinned=(nchunks == 8)), b.mpopl.packed_buffers()
     if nchunks == 3:   # existing arrays page-locked in place (pcl_host_register)
         pins = [pcl.population.PinnedHost(x[:3]) for x in ba]
+    a.mpopl.set_host_io({"auto": 0, "copy": 1, "direct": 2}[mode])
+    if nchunks == 1:   # pageable arrays: host-direct mode is refused
+        b.mpopl.set_host_io(2)
+        nb0 = b.mpopl.download_packed(bb)
+        with pytest.raises(Exception):
+            b.mpopl.advance_host(b.dt, bb, nb0)
+        b.mpopl.set_host_io(0)
     na, nb = a.mpopl.download_packed(ba), b.mpopl.download_packed(bb)
     small = [(x[0][:10], x[1][:10], x[2][:10], None) for x in ba]
     with pytest.raises(Exception):      # output arrays smaller than the input: refused before any work
@@ -484,36 +494,36 @@ def _subset(a, m):
 
 
 def test_full_size_subset_parity(pcl, oracle, gpu, air):
-    """The bench workload at full size: 2^24 electrons at 1 MeV, isotropic,
-    stepped twice on the device; a random 4096 of them stepped by the oracle
-    from the same state.  A particle's step depends only on its own state and
-    stream, so the subset and all its secondaries must match the oracle as in
-    the small cases (draw counts, stream ids, momenta to 1e-5)."""
+    """The bench workload at full size: 2^24 particles drawn from the grown
+    mixed e-/gamma/e+ state, stepped twice on the device; a random 4096 of
+    them, across the three species (2800 electrons, 512 positrons, photons
+    for the rest), stepped by the oracle from the same state.  A particle's
+    step depends only on its own state and stream, so the subset and all its
+    secondaries must match the oracle as in the small cases (draw counts,
+    stream ids, momenta to 1e-5)."""
     n = 1 << 24
-    rng = np.random.Generator(np.random.Philox(0))
-    p = pcl.workloads.isotropic(n, 1e6 * pcl.co.eV, rng)
-    arr = pcl.ParticleArrays(np.zeros((n, 3)), p, np.ones(n), np.zeros(n))
-    del p
-    mp = pcl.MultiPopulation(
-        ("electron", pcl.Population(n + n // 8, arr, air["tabs"][0], air["cuts"][0], particle=pcl.Electron)),
-        ("photon", pcl.Population(1 << 20, [], air["tabs"][1], air["cuts"][1], particle=pcl.Photon)),
-        ("positron", pcl.Population(1 << 16, [], air["tabs"][2], air["cuts"][2], particle=pcl.Positron)), seed=0)
-    del arr
-    pusher = _pusher(pcl, air)
-    g0 = mp.get(pcl.Electron).particles()
-    assert len(g0.w) == n
-    sel = np.sort(rng.choice(n, 4096, replace=False))
+    wl = pcl.workloads.rrea_mixed(n, seed=0, tables=(air["tabs"][0], air["tabs"][1], air["tabs"][2]))
+    mp, pusher = wl.mpopl, _pusher(pcl, air)
+    g0 = {sp: mp.get(sp).particles() for sp in (0, 1, 2)}
+    assert sum(len(g0[sp].w) for sp in g0) == n
+    assert min(len(g0[sp].w) for sp in g0) > 1000
+    rng = np.random.Generator(np.random.Philox(1))
+    npos = len(g0[2].w)
+    share = {0: 2800, 1: 4096 - 2800 - min(npos, 512), 2: min(npos, 512)}
     W = oracle.OracleWorld(0, air["tabs"], air["cuts"], pusher)
-    W.upload(pcl.Electron, _subset(g0, sel))
+    for sp in (0, 1, 2):
+        sel = np.sort(rng.choice(len(g0[sp].w), share[sp], replace=False))
+        W.upload(sp, _subset(g0[sp], sel))
     del g0
     dt = 1e-12
     for k in range(2):
         pcl.advance(mp, pusher, (k + 1) * dt)
         W.advance((k + 1) * dt, 8)
     t = mp.tallies()
-    assert t.live[0] > n * 0.99 and not any(t.errors), (list(t.live), list(t.errors))
+    assert sum(t.live) > n * 0.99 and not any(t.errors), (list(t.live), list(t.errors))
     for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
         o = W.download(sp)
+        assert len(o.w) > 0.9 * share[sp]
         g = mp.get(sp).particles()
         gs = _subset(g, np.isin(g.sid, o.sid))
         rep = oracle.compare_populations(gs, o, sp, rtol=RTOL, stol=2 * RTOL)
@@ -534,3 +544,70 @@ def test_bounded_wait_times_out_and_context_survives(pcl, gpu, air):
     t = mp.tallies()
     assert t.steps == 1 and t.particle_steps > 0
     mp.close()
+
+
+def _pick_target(counts, rising):
+    """A target whose first crossing in `counts` (per step) clears the
+    neighbouring values by a few particles, so that tie-affected lineages
+    (a few particles) cannot move the stop step."""
+    c = np.asarray(counts)
+    for k in range(2, len(c)):
+        before = c[:k].max() if rising else c[:k].min()
+        if rising and c[k] - before >= 5:
+            return int(before + 3), k
+        if not rising and before - c[k] >= 5:
+            return int(before - 3), k
+    return None, None
+
+
+@pytest.mark.parametrize("kind", ["grow", "decay"])
+def test_population_target_stop(pcl, oracle, gpu, air, kind):
+    """PopulationTargetCallback{S}(n, ismax) (callback.jl:253-267) through
+    pcl_run: run! (run.jl:1-29) stops after the first step on which the
+    species reaches the target.  The oracle, stepped one step at a time,
+    gives the step and the live counts; the device must stop on the same step
+    with the same populations, with one step per launch and with eight (the
+    launches shrink near the target)."""
+    dt, nsteps = 25e-12, 30
+    rising = kind == "grow"
+    sp = pcl.Electron if rising else pcl.Photon
+    mp0 = _mixed(pcl, air, n=(2048, 2048, 256), seed=70 if rising else 71)
+    pusher = _pusher(pcl, air, E=2e6)
+    W = _oracle_from(oracle, pcl, mp0, air, pusher)
+    init = {k: mp0.get(k).particles() for k in (0, 1, 2)}
+    mp0.close()
+    counts = []
+    for k in range(nsteps):
+        W.advance((k + 1) * dt, 4)
+        counts.append(len(W.download(sp).w))
+    target, k_stop = _pick_target(counts, rising)
+    assert target is not None, counts
+    W = _oracle_from_arrays(oracle, pcl, init, air, pusher, seed=70 if rising else 71)
+    for k in range(k_stop + 1):
+        W.advance((k + 1) * dt, 4)
+    states = {}
+    for K in (1, 8):
+        # the same initial state (the set-up is deterministic), launched K steps at a time
+        mp = _mixed(pcl, air, n=(2048, 2048, 256), seed=70 if rising else 71, steps_per_launch=K)
+        cb = pcl.PopulationTargetCallback(sp, target, ismax=rising)
+        tal = pcl.run(mp, pusher, nsteps * dt, dt, cb)
+        assert tal.steps == k_stop + 1, (K, tal.steps, k_stop + 1, counts, target)
+        live = tal.live[sp]
+        assert (live >= target) if rising else (live <= target), (live, target)
+        for q in (0, 1, 2):
+            rep = oracle.compare_populations(mp.get(q).particles(), W.download(q), q, rtol=3 * RTOL,
+                                             stol=2 * RTOL * 25 / 3)
+            assert rep["ok"], (K, q, str(rep))
+        states[K] = [mp.get(q).particles() for q in (0, 1, 2)]
+        mp.close()
+    for a, b in zip(states[1], states[8]):      # the launch shape does not change the physics
+        oa, ob = np.argsort(a.sid), np.argsort(b.sid)
+        np.testing.assert_array_equal(a.sid[oa], b.sid[ob])
+        np.testing.assert_array_equal(a.p[oa], b.p[ob])
+
+
+def _oracle_from_arrays(oracle, pcl, arrays, air, pusher, seed):
+    W = oracle.OracleWorld(seed, air["tabs"], air["cuts"], pusher)
+    for k, a in arrays.items():
+        W.upload(k, a)
+    return W

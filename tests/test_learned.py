@@ -93,7 +93,7 @@ def test_learned_matches_table(pcl, setup, which):
     each decade of the trained range, and chi^2 per bin near 1.
 
     Single energies are reported, not held to 1 %: with the reference's
-    swapped-corner interpolation weights (seltzer.jl:278-284, reproduced) the
+    swapped-corner interpolation weights (seltzer.jl:114-118, reproduced) the
     bremsstrahlung table sampler's distribution is piecewise constant in T
     (the pcum fraction picks the energy row), with steps at the 57 grid
     energies that a smooth network averages over."""
@@ -166,8 +166,13 @@ def test_step_with_learned_samplers(pcl, air, setup):
         mp.close()
     (t0, k0, s0, e0), (t1, k1, s1, e1) = runs
     assert s0 == (0, 0) and s1[0] > 1000 and s1[1] >= 1, s1
+    # 3 sigma: Poisson counts, and the two-sample KS critical value at a
+    # two-sided 0.27 % (the runs share the initial state and most draws, which
+    # only makes them closer than independent samples)
     for sp in (pcl.Electron, pcl.Photon):
         a, b = t0.spawned[sp], t1.spawned[sp]
-        assert abs(a - b) < 5 * np.sqrt(a + b) + 10, (sp, a, b)
-    assert _ks(np.log(k0), np.log(k1)) < 5 * np.sqrt(2.0 / min(len(k0), len(k1))) + 0.01
+        assert abs(a - b) <= 3 * np.sqrt(a + b), (sp, a, b)
+    n0, n1 = len(k0), len(k1)
+    c3 = np.sqrt(-0.5 * np.log(0.0027 / 2))
+    assert _ks(np.log(k0), np.log(k1)) <= c3 * np.sqrt((n0 + n1) / (n0 * n1))
     assert e1[5] == 0 and e1[6] == 0, e1   # no capacity or kinematics errors

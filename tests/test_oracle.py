@@ -182,6 +182,21 @@ def test_oracle_split(pcl, oracle, air):
     assert np.all(np.isin(np.round(cn / pn.max(), 12), np.round(pn / pn.max(), 12)))
 
 
+def test_split_poisson_inversion_is_bounded(oracle):
+    """The Poisson inversion of split! (the device's arithmetic, restated in the
+    oracle) sums the pmf in Float64, so even the largest uniform the streams
+    produce, 1 - 2^-24, gives a copy count near p rather than the 1024-copy
+    cap; small uniforms give 0 copies and the median is near p."""
+    L = oracle.lib()
+    umax = 1.0 - 2.0 ** -24
+    for p in np.concatenate([np.linspace(0.0, 64.0, 257), [3.0, 0.3, 1e-3, 63.999]]):
+        k = L.orc_poisson_inv(float(p), umax)
+        assert k <= p + 10 * np.sqrt(p) + 10, (p, k)
+        assert L.orc_poisson_inv(float(p), 2.0 ** -25) <= (0 if p < 1e-7 else max(1, p))
+        med = L.orc_poisson_inv(float(p), 0.5)
+        assert abs(med - p) <= 1, (p, med)
+
+
 def test_oracle_wall_records(pcl, oracle, air):
     """WallCallback{P}(coord, v, drop) (callback.jl:146-184) in the oracle: a
     particle crossing z = v upwards is recorded at the plane (lincomb of its

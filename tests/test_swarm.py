@@ -93,7 +93,9 @@ def test_swarm_parity(pcl, oracle, gpu, reid):
 def test_swarm_observables_fp32_vs_fp64(pcl, oracle, gpu, reid):
     """Drift velocity, mean energy and longitudinal diffusion of the FP32 device
     against the Float64 oracle from the same initial swarm and streams, after
-    the swarm relaxes: within the combined statistical error (4 sigma)."""
+    the swarm relaxes: within 3 sigma of the combined statistical error of
+    two independent swarms of this size (the shared streams only make the two
+    closer)."""
     N, tab = reid
     EN = 12.0
     pusher = _pusher(pcl, N, EN)
@@ -115,14 +117,20 @@ def test_swarm_observables_fp32_vs_fp64(pcl, oracle, gpu, reid):
     o = W.download(pcl.Electron)
     Eg, Eo = pcl.kinenergy(0, g.p), pcl.kinenergy(0, o.p)
     se = np.hypot(Eg.std() / np.sqrt(len(Eg)), Eo.std() / np.sqrt(len(Eo)))
-    assert abs(Eg.mean() - Eo.mean()) < 4 * se + 1e-3 * Eo.mean(), (Eg.mean() / EV, Eo.mean() / EV)
+    assert abs(Eg.mean() - Eo.mean()) <= 3 * se, (Eg.mean() / EV, Eo.mean() / EV, se / EV)
     Wg = np.polyfit(tt, zg, 1)[0]
     Wo = np.polyfit(tt, zo, 1)[0]
     assert Wg > 0 and Wo > 0
+    # drift: the mean velocity's standard error
     vz_sd = np.hypot(np.std(g.p[:, 2]), np.std(o.p[:, 2])) / pcl.co.electron_mass / np.sqrt(n)
-    assert abs(Wg - Wo) < 4 * vz_sd + 0.02 * Wo, (Wg, Wo)
-    Dg, Do = np.var(g.x[:, 2]), np.var(o.x[:, 2])
-    assert abs(Dg - Do) < 0.1 * Do, (Dg, Do)
+    assert abs(Wg - Wo) <= 3 * vz_sd, (Wg, Wo, vz_sd)
+
+    # spread along z: the sample variance's standard error, sqrt((m4 - var^2) / n)
+    def var_se(z):
+        d = z - z.mean()
+        return np.var(z), np.sqrt(max(np.mean(d ** 4) - np.var(z) ** 2, 0.0) / len(z))
+    (Dg, sg), (Do, so) = var_se(g.x[:, 2]), var_se(o.x[:, 2])
+    assert abs(Dg - Do) <= 3 * np.hypot(sg, so), (Dg, Do, sg, so)
     mp.close()
 
 
@@ -187,6 +195,44 @@ def test_batched_oracle_parity(pcl, oracle, gpu):
     W.set_swarms(tabs, Evec, pcl.co.elementary_charge * b.E * b.dt, safety=1.15)
     W.upload(pcl.Electron, b.mpopl.get(pcl.Electron).particles())
     for k in range(4):
+        pcl.advance(b.mpopl, b.pusher, (k + 1) * b.dt)
+        W.advance((k + 1) * b.dt, 4)
+    for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
+        rep = oracle.compare_populations(b.mpopl.get(sp).particles(), W.download(sp), sp, rtol=3e-5, stol=1e-4)
+        assert rep["ok"], (sp, str(rep))
+    b.mpopl.close()
+
+
+@pytest.mark.gpu
+def test_split_keeps_swarm(pcl, oracle, gpu):
+    """split! in swarm mode: every copy stays in its parent's swarm (top 8
+    bits of the stream id), so each swarm's count grows by its own copies; the
+    copies and weights equal the oracle's, and the next steps still match."""
+    b = _batch(pcl)
+    et, gt, pt = b.tables
+    tabs = {pcl.Electron: et, pcl.Photon: gt, pcl.Positron: pt}
+    W = oracle.OracleWorld(5, tabs, {pcl.Electron: 10e3 * EV, pcl.Photon: 5e3 * EV, pcl.Positron: 10e3 * EV},
+                           b.pusher)
+    Evec = np.zeros((len(b.E), 3))
+    Evec[:, 2] = -b.E
+    W.set_swarms(tabs, Evec, pcl.co.elementary_charge * b.E * b.dt, safety=1.15)
+    W.upload(pcl.Electron, b.mpopl.get(pcl.Electron).particles())
+    for k in range(2):
+        pcl.advance(b.mpopl, b.pusher, (k + 1) * b.dt)
+        W.advance((k + 1) * b.dt, 4)
+    nsw = len(b.E)
+    n0 = b.mpopl.swarm_counts(pcl.Electron)
+    mu = 0.6
+    b.mpopl.split(pcl.Electron, mu)
+    W.split(pcl.Electron, mu)
+    n1 = b.mpopl.swarm_counts(pcl.Electron)
+    g = b.mpopl.get(pcl.Electron).particles()
+    assert np.all((g.sid >> np.uint64(56)) < nsw)
+    for s in range(nsw):
+        assert abs((n1[s] - n0[s]) - mu * n0[s]) < 5 * np.sqrt(mu * n0[s]) + 2, (s, n0[s], n1[s])
+    rep = oracle.compare_populations(g, W.download(pcl.Electron), pcl.Electron, rtol=3e-5, stol=1e-4)
+    assert rep["ok"], str(rep)
+    for k in range(2, 4):
         pcl.advance(b.mpopl, b.pusher, (k + 1) * b.dt)
         W.advance((k + 1) * b.dt, 4)
     for sp in (pcl.Electron, pcl.Photon, pcl.Positron):

@@ -70,3 +70,57 @@ def test_compact_noalloc_matches_compact(pcl, gpu, air):
     assert rc == pcl._lib.PCL_ERR_CAPACITY
     assert b"PCL_NOALLOC_MAX_SLOTS" in L.pcl_last_error(None)
     mp.close()
+
+
+def test_compact_noalloc_many_scan_chunks(pcl, gpu, air):
+    """More than 1024 tiles of 2048 slots, so the tile-offset scan runs over
+    several chunks of its block: 3,000,000 slots of synthetic records, about a
+    third of them dead, compacted by the allocation-free entry point (twice in
+    a row) and by pcl_compact through a context; the two must agree bit for
+    bit.  Overlapping input and output buffers are refused."""
+    import torch
+    L = pcl.lib()
+    n = 3_000_000
+    assert (n + 2047) // 2048 > 1024
+    rng = np.random.default_rng(5)
+    xw = rng.standard_normal((n, 4)).astype(np.float32)
+    ps = rng.standard_normal((n, 4)).astype(np.float32)
+    meta = rng.integers(0, 1 << 32, size=(n, 4), dtype=np.uint64).astype(np.uint32)
+    meta[:, 2] = rng.integers(0, 1000, size=n, dtype=np.uint32)
+    dead = rng.random(n) < 0.35
+    meta[dead, 2] = 0xFFFFFFFF
+    live = int((~dead).sum())
+    dev = torch.device("cuda", 0)
+    t_in = [torch.from_numpy(a.view(np.int32)).to(dev) for a in (xw, ps, meta)]
+    outs = []
+    for _ in range(2):                           # two calls in a row
+        t_out = [torch.full((n, 4), -7, dtype=torch.int32, device=dev) for _ in range(3)]
+        n_out = torch.zeros(1, dtype=torch.int64, device=dev)
+        rc = L.pcl_compact_noalloc(n, *[t.data_ptr() for t in t_in], *[t.data_ptr() for t in t_out],
+                                   n_out.data_ptr(), None)
+        assert rc == 0, L.pcl_last_error(None)
+        torch.cuda.synchronize()
+        assert int(n_out.item()) == live
+        outs.append([t[:live].cpu().numpy() for t in t_out])
+    # the allocating entry point on the same records
+    mp = pcl.MultiPopulation(("electron", pcl.Population(n, [], air["tabs"][pcl.Electron], air["cuts"][pcl.Electron],
+                                                         particle=pcl.Electron)), seed=5, compaction_period=1000)
+    bufs = [(xw, ps, meta, None), (np.zeros((0, 4), np.float32),) * 3 + (None,),
+            (np.zeros((0, 4), np.float32),) * 3 + (None,)]
+    mp.upload_packed(bufs, [n, 0, 0])
+    pcl.repack(mp.get(pcl.Electron))
+    back = [(np.zeros((n, 4), np.float32), np.zeros((n, 4), np.float32), np.zeros((n, 4), np.uint32), None),
+            bufs[1], bufs[2]]
+    ns = mp.download_packed(back)
+    assert ns[0] == live
+    for oxw, ops, ometa in outs:
+        assert np.array_equal(oxw.view(np.float32), back[0][0][:live])
+        assert np.array_equal(ops.view(np.float32), back[0][1][:live])
+        assert np.array_equal(ometa.view(np.uint32), back[0][2][:live])
+    # in place (or any overlap of an output with an input) is refused before any launch
+    n_out = torch.zeros(1, dtype=torch.int64, device=dev)
+    ptrs = [t.data_ptr() for t in t_in]
+    rc = L.pcl_compact_noalloc(n, *ptrs, *ptrs, n_out.data_ptr(), None)
+    assert rc == pcl._lib.PCL_ERR_INVALID
+    assert b"overlap" in L.pcl_last_error(None)
+    mp.close()
