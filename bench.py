@@ -470,6 +470,82 @@ def _swarm_obs(t, z, zz, E):
     return float(W), float(D), float(np.mean(E))
 
 
+REID_EN = (1.0, 3.0, 12.0, 24.0, 48.0)
+REID_GROUPS = 8
+
+
+def _reid_group_obs(snaps, groups):
+    """Swarm observables of a run and their statistical errors by batch means:
+    snaps = [(t, z, E, g)] with per-particle z (m), E (J) and group index g;
+    the observables of each of `groups` groups (drift = slope of <z>, D_L =
+    slope of var z / 2, mean energy over the snapshots), the value of the
+    whole run, and its standard error std(groups) / sqrt(groups)."""
+    t = np.array([q[0] for q in snaps])
+    out = {}
+    for name in ("W_m_s", "DL_m2_s", "mean_energy_eV"):
+        out[name] = []
+    per = []
+    for gsel in [None] + list(range(groups)):
+        zm, zv, em = [], [], []
+        for _, z, E, g in snaps:
+            m = slice(None) if gsel is None else (g == gsel)
+            zz = z[m]
+            zm.append(zz.mean()); zv.append(zz.var()); em.append(E[m].mean())
+        W = np.polyfit(t, zm, 1)[0]
+        D = np.polyfit(t, zv, 1)[0] / 2
+        per.append((W, D, np.mean(em) / 1.6021766208e-19))
+    per = np.array(per)
+    res = {}
+    for k, name in enumerate(("W_m_s", "DL_m2_s", "mean_energy_eV")):
+        res[name] = float(per[0, k])
+        res[name + "_se"] = float(per[1:, k].std(ddof=1) / np.sqrt(groups))
+    return res
+
+
+def run_reid_fp64(args, pcl):
+    """The Float64 side of the Reid precision study, on the host cores only:
+    the oracle (C++ Float64, all host threads) runs an independent swarm of
+    args.reid_fp64_n electrons (Maxwellian, 1 eV mean; numpy Philox seed
+    1002) at each E/N with the device run's schedule (1000 relaxation steps,
+    2000 measured, a snapshot every 100), and reports each observable with
+    its batch-means standard error over 8 groups of electrons."""
+    from oracle.harness import Arrays, OracleWorld
+    threads = os.cpu_count() or 1
+    dt = 1e-12
+    relax, meas, every = 1000, 2000, 100
+    n = args.reid_fp64_n
+    N = 2.504e25
+    tab = pcl.workloads.reid_table(N)
+    rows = []
+    el_all = 0.0
+    for EN in REID_EN:
+        pusher = pcl.workloads.pusher((0.0, 0.0, -EN * pcl.co.Td * N))
+        rng = np.random.Generator(np.random.Philox(1002))
+        kT = 2.0 / 3.0 * 1.0 * pcl.co.eV
+        p = rng.normal(scale=np.sqrt(pcl.co.electron_mass * kT), size=(n, 3))
+        W = OracleWorld(2, {pcl.Electron: tab}, {pcl.Electron: 0.0}, pusher)
+        W.upload(pcl.Electron, Arrays(np.zeros((n, 3)), p, np.ones(n), np.zeros(n), -np.log(rng.random(n)),
+                                      np.arange(n, dtype=np.uint64), np.zeros(n, np.uint32)))
+        snaps = []
+        c0 = time.perf_counter()
+        for blk in range((relax + meas) // every):
+            for i in range(every):
+                W.advance((blk * every + i + 1) * dt, threads)
+            if (blk + 1) * every > relax:
+                o = W.download(pcl.Electron)
+                snaps.append(((blk + 1) * every * dt, o.x[:, 2].copy(), pcl.kinenergy(0, o.p),
+                              (o.sid % REID_GROUPS).astype(int)))
+        el = time.perf_counter() - c0
+        el_all += el
+        rows.append(dict({"EN_Td": EN, "electrons": n, "seconds": el}, **_reid_group_obs(snaps, REID_GROUPS)))
+    line = {"metric": "Reid ramp swarm observables, Float64 oracle (host cores)", "unit": "particle-steps/s",
+            "value": n * (relax + meas) * len(REID_EN) / el_all, "cores": threads, "data": "synthetic",
+            "config": {"workload": "reid-ramp-fp64", "electrons": n, "dt_s": dt, "relax_steps": relax,
+                       "measured_steps": meas, "groups": REID_GROUPS}, "observables": rows}
+    print(json.dumps(line))
+    return 0
+
+
 def run_reid(args, pcl):
     """Reid's ramp model gas at E/N = 1, 3, 12, 24, 48 Td: 2^20 electrons
     (Maxwellian, 1 eV mean, Philox seed 2), dt = 1 ps, 1000 relaxation steps
@@ -503,8 +579,11 @@ def run_reid(args, pcl):
         t = 0.0
         gt, gz, gzz, gE = [], [], [], []
         ot, oz, ozz, oE = [], [], [], []
+        snaps = []
         pz_g, pz_o, pE_g, pE_o = [], [], [], []
         tal0 = mp.tallies()
+        seg = C.c_double()
+        dev_ms = 0.0
         with Clocks(0) as clk:
             L.pcl_timer_start(mp.ctx)
             for blk in range((relax + meas) // every):
@@ -513,12 +592,19 @@ def run_reid(args, pcl):
                 if (blk + 1) * every > relax:
                     m = e.moments()
                     gt.append(t1); gz.append(m[4] / m[0]); gzz.append(m[7] / m[0]); gE.append(m[1] / m[0])
-            ms = C.c_double()
-            L.pcl_timer_stop(mp.ctx, C.byref(ms))
+                    if args.reid_groups:   # every particle, for the batch-means errors (outside the device time)
+                        L.pcl_timer_stop(mp.ctx, C.byref(seg))
+                        dev_ms += seg.value
+                        q = e.particles()
+                        snaps.append((t1, q.x[:, 2].copy(), pcl.kinenergy(0, q.p),
+                                      (q.sid % REID_GROUPS).astype(int)))
+                        L.pcl_timer_start(mp.ctx)
+            L.pcl_timer_stop(mp.ctx, C.byref(seg))
+            dev_ms += seg.value
         clk_all = clk.summary()
         tal1 = mp.tallies()
         total_ps += tal1.particle_steps - tal0.particle_steps
-        total_ms += ms.value
+        total_ms += dev_ms
         # oracle: the first nsub electrons, same streams
         c0 = time.perf_counter()
         for blk in range((relax + meas) // every):
@@ -542,6 +628,7 @@ def run_reid(args, pcl):
         Wg, Dg, Eg = _swarm_obs(gt, gz, gzz, gE)
         Wo, Do, Eo_ = _swarm_obs(ot, oz, ozz, oE)
         rows.append({"EN_Td": EN, "gpu": {"W_m_s": Wg, "DL_m2_s": Dg, "mean_energy_eV": Eg / pcl.co.eV},
+                     "gpu_batch_means": _reid_group_obs(snaps, REID_GROUPS) if snaps else None,
                      "oracle_fp64_4096": {"W_m_s": Wo, "DL_m2_s": Do, "mean_energy_eV": Eo_ / pcl.co.eV},
                      "paired_rel_diff": {"mean_energy": float(dE), "mean_z": float(dz)},
                      "oracle_ties": int(W.counters()["ties"])})
@@ -598,6 +685,78 @@ def run_mlp(args, pcl):
     return 0
 
 
+def run_kernels(args, pcl):
+    """Every kernel of the path besides the step, once each on the 16 M
+    mixed state (inputs larger than L2), timed with CUDA events on the
+    context's stream around its ABI call: algorithmic bytes (or FLOPs) per call
+    and the achieved rate against the measured peaks."""
+    L = pcl.lib()
+    peak, peak_kind = _peaks()
+    mp, pusher, dt, extra = build_workload(pcl, args.n, seed=0, device=0)
+    for k in range(args.warmup):
+        pcl.advance(mp, pusher, (k + 1) * dt)
+    L.pcl_sync(mp.ctx)
+    tal = mp.tallies()
+    n_slots = [int(v) for v in tal.n]
+    n_live = [int(v) for v in tal.live]
+    E, G, P = pcl.Electron, pcl.Photon, pcl.Positron
+    rows = []
+
+    def timed(name, kernels, nbytes, fn, reps=3):
+        best = 1e30
+        for _ in range(reps):
+            L.pcl_timer_start(mp.ctx)
+            fn()
+            ms = C.c_double()
+            L.pcl_timer_stop(mp.ctx, C.byref(ms))
+            best = min(best, ms.value)
+        gbs = nbytes / (best / 1e3) / 1e9
+        rows.append({"op": name, "kernels": kernels, "ms": best, "bytes": nbytes, "GB_s": gbs, "frac": gbs / peak})
+
+    edges = np.geomspace(1e3, 1e9, 257) * pcl.co.eV
+    timed("moments (electrons)", "k_moments", 48 * n_slots[E], lambda: mp.get(E).moments())
+    timed("energy histogram (electrons, 256 bins)", "k_energy_hist", 48 * n_slots[E],
+          lambda: mp.get(E).energy_histogram(edges))
+    timed("swarm counts (electrons, one swarm)", "k_swarm_count", 16 * n_slots[E], lambda: mp.swarm_counts(E, 1))
+    timed("swarm moments (electrons, one swarm)", "k_swarm_moments + k_swarm_reduce", 48 * n_slots[E],
+          lambda: mp.swarm_moments(E, 1))
+    timed("roulette (photons, keep 0.9999)", "k_roulette", 16 * n_slots[G], lambda: mp.roulette(G, 0.9999), reps=1)
+    tal = mp.tallies()
+    n_slots = [int(v) for v in tal.n]
+    n_live = [int(v) for v in tal.live]
+    cbytes = sum(16 * n_slots[q] + 48 * n_slots[q] + 48 * n_live[q] for q in range(3))
+    timed("repack (all species)", "k_compact_count + k_compact_scan + k_compact_scatter", cbytes,
+          lambda: L.pcl_compact(mp.ctx), reps=1)
+    mp.close()
+    # the network kernels (FLOPs): inference of 4 M rows, training steps of 8192 rows
+    net = pcl.SamplerNet(seed=1)
+    nrow = 1 << 22
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1, 1, (nrow, 2)).astype(np.float32)
+    net.forward(x)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        net.forward(x)
+    fwd_s = (time.perf_counter() - t0) / 3
+    flops_row = 2.0 * (2 * 128 + 2 * 128 * 128 + 128)
+    t = (np.sin(3 * x[:, 0]) * x[:, 1]).astype(np.float32)
+    steps = 300
+    t1 = time.perf_counter()
+    net.train(x[: 1 << 20], t[: 1 << 20], steps=steps, batch=8192, lr=1e-3, seed=0)
+    tr_s = (time.perf_counter() - t1) / steps
+    net.close()
+    line = {"metric": "achieved HBM GB/s of the kernels beside the step (CUDA events around each ABI call)",
+            "unit": "GB/s", "peak": peak, "peak_kind": peak_kind, "data": "synthetic",
+            "config": {"workload": WORKLOAD, "particles": args.n, "slots": n_slots, "live": n_live},
+            "ops": rows,
+            "network": {"inference_rows": nrow, "inference_s_incl_host_copies": fwd_s,
+                        "inference_TFLOP_s_incl_host_copies": nrow * flops_row / fwd_s / 1e12,
+                        "train_step_s (8192 rows, forward + backward + Adam)": tr_s,
+                        "train_TFLOP_s": 3 * 8192 * flops_row / tr_s / 1e12}}
+    print(json.dumps(line))
+    return 0
+
+
 def _printing(fn):
     def wrap(args, pcl):
         print(json.dumps(fn(args, pcl)))
@@ -636,10 +795,13 @@ def main():
     ap.add_argument("--classic", type=int, default=0, help="1: classic step kernel (lanes collide in place)")
     ap.add_argument("--graph", type=int, default=0, help="1: launch groups replayed from CUDA graphs")
     ap.add_argument("--compaction-period", type=int, default=0, help="steps between repacks (0: the library's 8)")
-    ap.add_argument("--workload", default="rrea16M", choices=["rrea16M", "swarms", "learned", "plain", "reid", "mlp"])
+    ap.add_argument("--workload", default="rrea16M",
+                    choices=["rrea16M", "swarms", "learned", "plain", "reid", "reid-fp64", "mlp", "kernels"])
     ap.add_argument("--nswarm", type=int, default=256)
     ap.add_argument("--tune-steps", type=int, default=512)
     ap.add_argument("--learned-n", type=int, default=1 << 24, help="learned form: particles")
+    ap.add_argument("--reid-groups", type=int, default=0, help="reid: batch-means errors from particle snapshots")
+    ap.add_argument("--reid-fp64-n", type=int, default=1 << 17, help="reid-fp64: electrons of the Float64 run")
     ap.add_argument("--train-samples", type=float, default=1e8, help="learned form: training samples per network")
     ap.add_argument("--train-steps", type=int, default=8000, help="learned form: Adam steps per network")
     args = ap.parse_args()
@@ -647,11 +809,15 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "reid-fp64":   # host cores only: the oracle, no GPU library
+        _build_oracle()
+        import __graft_entry__ as graft
+        return run_reid_fp64(args, graft.load_package())
     if args.workload != "rrea16M":
         import __graft_entry__ as graft
         graft.build()
         fn = {"swarms": _printing(run_swarms), "learned": _printing(run_learned), "plain": run_plain,
-              "reid": run_reid, "mlp": run_mlp}[args.workload]
+              "reid": run_reid, "mlp": run_mlp, "kernels": run_kernels}[args.workload]
         return fn(args, graft.load_package())
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -703,27 +869,39 @@ def main():
     try:
         if args.no_e2e:
             raise RuntimeError("skipped (--no-e2e)")
-        # the population lives in pinned host buffers: every step uploads it,
-        # advances it and downloads it (pcl_advance_host, chunked pipeline)
+        # the population lives in pinned host buffers: every step reads it from
+        # there and writes it back (pcl_advance_host), in the library's default
+        # mode (the copy pipeline: chunked copy-engine uploads and downloads
+        # around range launches) and, for comparison, host-direct (the step
+        # kernel reads and writes the page-locked arrays over the CPU-GPU link)
         host = mp.packed_buffers(pinned=True)
         ns = mp.download_packed(host)
         period = 8
-        tal_a = mp.tallies()
-        h2d = d2h = 0
-        L.pcl_timer_start(ctx)
-        for k in range(args.e2e_steps):
-            t += dt
-            h2d += 48 * sum(ns)
-            ns = mp.advance_host(t, host, ns, nchunks=args.e2e_chunks, compact=(k % period == period - 1))
-            d2h += 48 * sum(ns)
-        ms2 = C.c_double()
-        L.pcl_timer_stop(ctx, C.byref(ms2))
-        tal_b = mp.tallies()
-        e_el = _barrier_max(ms2.value / 1e3, ws)
-        e2e = {"value": (tal_b.particle_steps - tal_a.particle_steps) * ws / e_el, "unit": UNIT,
-               "h2d_bytes_per_step": int(h2d / args.e2e_steps), "d2h_bytes_per_step": int(d2h / args.e2e_steps),
-               "api": "pcl_advance_host", "chunks": args.e2e_chunks, "host_buffers": "pinned",
-               "steps": args.e2e_steps}
+        modes = {}
+        for mode, name in ((pcl._lib.HOST_IO_AUTO, "default"), (pcl._lib.HOST_IO_DIRECT, "direct")):
+            mp.set_host_io(mode)
+            tal_a = mp.tallies()
+            h2d = d2h = 0
+            L.pcl_timer_start(ctx)
+            for k in range(args.e2e_steps):
+                t += dt
+                h2d += 48 * sum(ns)
+                ns = mp.advance_host(t, host, ns, nchunks=args.e2e_chunks, compact=(k % period == period - 1))
+                d2h += 48 * sum(ns)
+            ms2 = C.c_double()
+            L.pcl_timer_stop(ctx, C.byref(ms2))
+            tal_b = mp.tallies()
+            e_el = _barrier_max(ms2.value / 1e3, ws)
+            modes[name] = {"value": (tal_b.particle_steps - tal_a.particle_steps) * ws / e_el,
+                           "ms_per_step": 1e3 * e_el / args.e2e_steps,
+                           "h2d_bytes_per_step": int(h2d / args.e2e_steps),
+                           "d2h_bytes_per_step": int(d2h / args.e2e_steps)}
+        mp.set_host_io(pcl._lib.HOST_IO_AUTO)
+        d = modes["default"]
+        e2e = {"value": d["value"], "unit": UNIT, "h2d_bytes_per_step": d["h2d_bytes_per_step"],
+               "d2h_bytes_per_step": d["d2h_bytes_per_step"], "ms_per_step": d["ms_per_step"],
+               "api": "pcl_advance_host", "mode": "copy pipeline (the default)", "chunks": args.e2e_chunks,
+               "host_buffers": "pinned", "steps": args.e2e_steps, "host_direct": modes["direct"]}
         del host
     except Exception as ex:  # pragma: no cover
         e2e = {"value": None, "unit": UNIT, "error": str(ex)[:200], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}

@@ -363,7 +363,10 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
  *   pcl_host_register, cudaHostAlloc) and usable by the device, else
  *   PCL_ERR_INVALID.  A compacting step (compact != 0) downloads the
  *   compacted population with copies as in the other mode.
- * PCL_HOST_IO_AUTO (default): DIRECT where the arrays allow it, else COPY. */
+ * PCL_HOST_IO_AUTO (default): the faster of the two on GB300, COPY (a step of
+ *   16.8 M particles: 6.8 ms against 11.9 ms for DIRECT; SM loads and copy
+ *   engines reach the same link rates, and DIRECT exposes the link's latency
+ *   to every particle load of the step kernel). */
 #define PCL_HOST_IO_AUTO   0
 #define PCL_HOST_IO_COPY   1
 #define PCL_HOST_IO_DIRECT 2
@@ -526,6 +529,19 @@ int pcl_set_learned(void* ctx, int species, int proc_index, int kind, void* mlp)
  * Energies outside the kind's domain give no rows; *nrows = rows written. */
 int pcl_learn_data(void* ctx, int species, int proc_index, int kind, int nT, int64_t per_T, int Q, uint64_t seed,
                    float* x_out, float* t_out, int64_t* nrows);
+/* Measurement hook (no counterpart in the reference): the cost of one
+ * secondary-energy draw, table sampler against network.  n primaries
+ * (1 .. 2^26) at E_i = 10^(4 + 4 (i + 1/2) / n) eV; the table path draws
+ * k / T (PCL_LEARN_SB) or eps (PCL_LEARN_MOLLER) with the table sampler of
+ * proc_index (seltzer.jl:97-122, moller.jl:64-87; one kernel); the network path
+ * draws one uniform per primary, evaluates mlp on the tensor cores and maps its
+ * output to the same quantity (three kernels).  Each path runs reps (1 .. 100)
+ * times on the context's stream, timed with CUDA events; *ms_table / *ms_net
+ * = the fastest repetition.  out_table / out_net (n floats) receive the draws
+ * and draws_table (n) the uniforms the table sampler used per primary (the
+ * network path uses one); each may be NULL. */
+int pcl_time_energy_draw(void* ctx, int species, int proc_index, int kind, void* mlp, int64_t n, int reps,
+                         double* ms_table, double* ms_net, float* out_table, float* out_net, uint32_t* draws_table);
 /* Collisions answered by a network and rounds run since the context was made. */
 int pcl_learn_stats(void* ctx, int64_t* suspended, int64_t* rounds);
 

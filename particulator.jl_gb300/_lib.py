@@ -160,6 +160,8 @@ _SIGS = {
     "pcl_autotune": (C.c_int, [C.c_void_p, _d, _i32, _P(TuneResult)]),
     "pcl_set_launch": (C.c_int, [C.c_void_p, _i32, _i32, _i32, _i32]),
     "pcl_set_host_io": (C.c_int, [C.c_void_p, C.c_int]),
+    "pcl_time_energy_draw": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, _i64, C.c_int, _P(_d),
+                                       _P(_d), _P(C.c_float), _P(C.c_float), _P(C.c_uint32)]),
     "pcl_learn_stats": (C.c_int, [C.c_void_p, _P(_i64), _P(_i64)]),
     "pcl_learn_data": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _i64, C.c_int, _u64,
                                  _P(C.c_float), _P(C.c_float), _P(_i64)]),

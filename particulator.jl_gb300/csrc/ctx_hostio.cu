@@ -217,7 +217,7 @@ int pcl_advance_host(void* ctx, double tfinal, const int64_t* n_in, const pcl_pa
     CK(cudaSetDevice(c->device));
     // host-direct mode: every array the kernels would touch must be page-locked
     // and usable by the device
-    bool direct = c->host_io != PCL_HOST_IO_COPY;
+    bool direct = c->host_io == PCL_HOST_IO_DIRECT;
     void* hv[3][6] = {};
     for (int s = 0; s < 3 && direct; ++s) {
         if (n[s] > 0) {

@@ -42,6 +42,10 @@ __global__ void k_energy_hist(const float4* xw, const float4* ps, const uint4* m
                               unsigned long long* counts, double* wsum);
 __global__ void k_learn_pick(const float4* m2, const unsigned long long* n_dev, long long cap, const float* Yk,
                              long long stride, LearnPick which, float* Y);
+__global__ void k_draw_table(StepArgs A, int species, int j, int kind, long long n, unsigned long long sid_base,
+                             float* out, uint32_t* draws);
+__global__ void k_draw_net_x(long long n, unsigned long long sid_base, uint32_t k0, uint32_t k1, float* X);
+__global__ void k_draw_net_map(StepArgs A, int species, int j, int kind, long long n, const float* Y, float* out);
 namespace mlp {
 cudaError_t infer_multi(void* const* handles, int nnets, const float* X, const unsigned long long* n_dev,
                         long long cap, float* Y, long long ystride, cudaStream_t stream);

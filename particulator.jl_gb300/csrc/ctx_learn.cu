@@ -72,6 +72,82 @@ int pcl_set_learned(void* ctx, int species, int proc_index, int kind, void* mlp)
     return ensure_lq(c);
 }
 
+int pcl_time_energy_draw(void* ctx, int species, int proc_index, int kind, void* mlp, int64_t n, int reps,
+                         double* ms_table, double* ms_net, float* out_table, float* out_net, uint32_t* draws_table) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    SpeciesState& S = c->sp[species];
+    if (proc_index < 0 || proc_index >= S.nproc) return fail(c, PCL_ERR_INVALID, "process index");
+    if (!mlp || n < 1 || n > (1ll << 26) || reps < 1 || reps > 100 || !ms_table || !ms_net)
+        return fail(c, PCL_ERR_INVALID, "time_energy_draw arguments");
+    if (!learn_kind_ok(S.procs[proc_index], kind))
+        return fail(c, PCL_ERR_UNSUPPORTED, "learned sampler kind does not match the process");
+    CK(cudaSetDevice(c->device));
+    if ((rc = build_blob(c))) return rc;
+    float *d_t = nullptr, *d_n = nullptr, *d_x = nullptr, *d_y = nullptr;
+    uint32_t* d_draws = nullptr;
+    unsigned long long* d_cnt = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    struct Free {
+        float **a, **b, **x, **y; uint32_t** d; unsigned long long** cnt; cudaEvent_t *e0, *e1; cudaStream_t s;
+        ~Free() {
+            cudaStreamSynchronize(s);
+            cudaFree(*a); cudaFree(*b); cudaFree(*x); cudaFree(*y); cudaFree(*d); cudaFree(*cnt);
+            if (*e0) cudaEventDestroy(*e0);
+            if (*e1) cudaEventDestroy(*e1);
+        }
+    } fr{&d_t, &d_n, &d_x, &d_y, &d_draws, &d_cnt, &e0, &e1, c->stream};
+    CK(cudaMalloc(&d_t, sizeof(float) * n));
+    CK(cudaMalloc(&d_n, sizeof(float) * n));
+    CK(cudaMalloc(&d_x, sizeof(float) * 2 * n));
+    CK(cudaMalloc(&d_y, sizeof(float) * n));
+    CK(cudaMalloc(&d_draws, sizeof(uint32_t) * n));
+    CK(cudaMalloc(&d_cnt, sizeof(unsigned long long)));
+    const unsigned long long nn = (unsigned long long)n;
+    CK(cudaMemcpy(d_cnt, &nn, sizeof(nn), cudaMemcpyHostToDevice));
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    StepArgs A = make_args(c, 0.0, 1, 0, 0);
+    const size_t smem = c->blob.size() + 16;
+    CK(cudaFuncSetAttribute(k_draw_table, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    CK(cudaFuncSetAttribute(k_draw_net_map, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+    const int grid = int(std::max<long long>(1, std::min<long long>((n + 255) / 256, 8ll * c->sm_count)));
+    const unsigned long long sid_t = 0xB1ull << 56, sid_n = 0xB2ull << 56;
+    double bt = 1e30, bn = 1e30;
+    for (int r = 0; r < reps; ++r) {
+        float ms = 0.0f;
+        CK(cudaEventRecord(e0, c->stream));
+        k_draw_table<<<grid, 256, smem, c->stream>>>(A, species, proc_index, kind, n, sid_t, d_t, d_draws);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(e1, c->stream));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        bt = std::min(bt, double(ms));
+        CK(cudaEventRecord(e0, c->stream));
+        k_draw_net_x<<<grid, 256, 0, c->stream>>>(n, sid_n, A.key0, A.key1, d_x);
+        CK(cudaGetLastError());
+        CK(mlp::infer_multi(&mlp, 1, d_x, d_cnt, n, d_y, n, c->stream));
+        k_draw_net_map<<<grid, 256, smem, c->stream>>>(A, species, proc_index, kind, n, d_y, d_n);
+        CK(cudaGetLastError());
+        CK(cudaEventRecord(e1, c->stream));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        bn = std::min(bn, double(ms));
+    }
+    if (out_table) CK(cudaMemcpy(out_table, d_t, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    if (out_net) CK(cudaMemcpy(out_net, d_n, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    if (draws_table) CK(cudaMemcpy(draws_table, d_draws, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost));
+    *ms_table = bt;
+    *ms_net = bn;
+    // a network whose tensor-core wait gave up flags its handle; report it here
+    float probe[2] = {0.0f, 0.0f}, py = 0.0f;
+    if (pcl_mlp_forward(mlp, 1, probe, &py) == PCL_ERR_TIMEOUT)
+        return fail(c, PCL_ERR_TIMEOUT, "network inference timed out");
+    return PCL_OK;
+}
+
 int pcl_learn_data(void* ctx, int species, int proc_index, int kind, int nT, int64_t per_T, int Q, uint64_t seed,
                    float* x_out, float* t_out, int64_t* nrows) {
     Ctx* c = static_cast<Ctx*>(ctx);

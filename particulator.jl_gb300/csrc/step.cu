@@ -524,8 +524,8 @@ __device__ __forceinline__ void moller_tail(Lane& L, const KCtx& K, float E, flo
     emit(L, K, PCL_ELECTRON, bx, by, bz, cs, 0, ctr0);
 }
 
-// moller.jl:13-37, 64-87
-__device__ void s_moller(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+// sample_secondary_energy(Moller) (moller.jl:64-87): eps by rejection
+__device__ __forceinline__ float moller_eps(Lane& L, const KCtx& K, const DevProc& P, float E) {
     const float e0 = P.p[0] / E;
     const float g = 1.0f + E;
     const float nrm = 4.0f / (9.0f * g * g - 10.0f * g + 5.0f);
@@ -541,7 +541,12 @@ __device__ void s_moller(Lane& L, const KCtx& K, const DevProc& P, float E, uint
         if (U(L, K) < gg) break;
         if (++it >= kRejectCap) { err(K, PCL_E_REJECT_CAP); break; }
     }
-    moller_tail(L, K, E, eps, ctr0);
+    return eps;
+}
+
+// moller.jl:13-37, 64-87
+__device__ void s_moller(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+    moller_tail(L, K, E, moller_eps(L, K, P, E), ctr0);
 }
 
 // rbeb.jl:54-80, 156-196
@@ -559,13 +564,16 @@ __device__ PCL_RARE void s_rbeb(Lane& L, const KCtx& K, const DevProc& P, float 
     const float A = -(1.0f + 2.0f * t1) / (t + 1.0f) / (op * op);
     const float C = logf(t1 * (t1 + 2.0f)) - bt2 - logf(2.0f * b1);
     const float M = b1 * b1 / (op * op);
-    const float ratio = (t + 1.0f) / (t - 1.0f);
-    const float pbn = 2.0f + 2.0f * C + (t + 1.0f) * (t + 1.0f) * M / 4.0f;
+    const float tm1 = t - 1.0f, tp1 = t + 1.0f;
+    const float pbn = 2.0f + 2.0f * C + tp1 * tp1 * M / 4.0f;
     float w = 0.0f;
     int it = 0;
     for (;;) {
         float u = U(L, K);
-        w = u / (ratio - u);
+        // w = u / (ratio - u) with ratio = (t + 1) / (t - 1) (rbeb.jl:175), in
+        // the form u (t - 1) / (t (1 - u) + 1 + u): for t = E / B in the
+        // millions ratio - u cancels to a few FP32 ulps, and 1 - u is exact
+        w = u * tm1 / (t * (1.0f - u) + (1.0f + u));
         float a1 = 1.0f / (w + 1.0f), a2 = 1.0f / (t - w);
         float pb = pbn * a1 * a1;
         float p0 = A * (a1 + a2) + ((a1 * a1 + a2 * a2) + M) + C * (a1 * a1 * a1 + a2 * a2 * a2);
@@ -604,10 +612,11 @@ __device__ __forceinline__ void sb_tail(Lane& L, const KCtx& K, float E, float k
     emit(L, K, PCL_PHOTON, gx, gy, gz, cs, 0, ctr0);
 }
 
-// seltzer.jl:67-122 with the photon angle of util.jl:143-159.  The inverse-CDF
-// lookup reproduces the reference's interpolation weights as written
-// (seltzer.jl:114-118, off-diagonal corners included).
-__device__ PCL_RARE void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+// sample_secondary_energy(SeltzerBerger) (seltzer.jl:97-122): the photon
+// energy k by the inverse-CDF lookup, which reproduces the reference's
+// interpolation weights as written (seltzer.jl:114-118, off-diagonal corners
+// included).
+__device__ __forceinline__ float sb_k(Lane& L, const KCtx& K, const DevProc& P, float E) {
     const SBHdr& T = K.H->sb[P.sb];
     const float* data = K.A->sb_data[P.sb];
     uint32_t bits = next_bits(L, K.A->key0, K.A->key1);
@@ -634,8 +643,12 @@ __device__ PCL_RARE void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E,
     float A = (xb - xa) * (y2 - y1);
     float S = u11 * (xb - x) * (y2 - y) + u12 * (x - xa) * (y2 - y) + u21 * (xb - x) * (y - y1) +
               u22 * (x - xa) * (y - y1);
-    float k = E * expf(S / A);
-    sb_tail(L, K, E, k, ctr0);
+    return E * expf(S / A);
+}
+
+// seltzer.jl:67-90: the photon energy, then its angle (util.jl:143-159)
+__device__ PCL_RARE void s_sb(Lane& L, const KCtx& K, const DevProc& P, float E, uint32_t ctr0) {
+    sb_tail(L, K, E, sb_k(L, K, P, E), ctr0);
 }
 
 // compton.jl:9-28, 119-144 (Compton and KleinNishinaCompton share the sampler)
@@ -1162,6 +1175,40 @@ __device__ __forceinline__ void put_slot(const StepArgs& A, int sp, long long sl
     }
 }
 
+// A photon taken from the input whose next collision falls beyond the end of
+// its step: the loop's sub-step (a straight flight of the rest of the step)
+// and step boundary (droplow! and, in a multi-step launch, setr! of the next
+// step), the same operations in the same order, done at once so that its lane
+// takes the next input in the same refill.  Returns 0 as soon as a collision
+// falls within the current step (the particle is then where a step boundary
+// left it, and the loop goes on from there), 1 when it survives the launch,
+// 2 when it is removed.
+template <bool GENERAL>
+__device__ __forceinline__ int photon_free_flight(Lane& L, const KCtx& K, const SpeciesHdr& S, int nsteps,
+                                                  float dt_hi, float dt_lo) {
+    for (;;) {
+        if (dd_val(L.th, L.tlo) > kEpsT) {
+            const float tnext = L.s / L.r;
+            if (__fadd_rn(__fsub_rn(L.th, tnext), L.tlo) > 0.0f) return 0;
+            const float h = dd_val(L.th, L.tlo);
+            L.s -= h * L.r;
+            push<GENERAL>(L, S, K, h);
+            L.th = 0.0f;
+            L.tlo = 0.0f;
+            L.nsub += 1;
+        }
+        const float E = kin_energy(L.species, L.px, L.py, L.pz);
+        if (E < S.cut) return 2;  // droplow! (population.jl:273-284)
+        atomicAdd(&K.tal[T_LEND + 3 * L.k + L.species], 1u);
+        if (L.k + 1 >= nsteps) return 1;
+        L.k += 1;
+        L.nsub = 0;
+        dd_add(L.th, L.tlo, dt_hi, dt_lo);
+        L.r = setr(S, K, E, L.sw);
+        atomicAdd(&K.tal[T_LSTART + L.k], 1u);
+    }
+}
+
 // ------------------------------------------------------------ the step ---
 // EVENT: colliding particles are parked in a per-warp stash and collided in
 // batches that fill the warp's free lanes (see the loop), instead of each lane
@@ -1365,6 +1412,25 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         L.rvalid = false; L.alive = true; L.nsub = 0;
                         L.sw = (H->nswarm > 0) ? min(int(L.sid_hi >> 24), H->nswarm - 1) : 0;
                         L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz), L.sw);
+                        // photons of the population: most fly through the whole step
+                        // without a collision; finish those here (no wall on photons)
+                        if (A.spill_mode == 0 && L.species == PCL_PHOTON &&
+                            (!GENERAL || H->sp[PCL_PHOTON].wall_coord < 0)) {
+                            const int f = photon_free_flight<GENERAL>(L, K, H->sp[PCL_PHOTON], nsteps, dt_hi, dt_lo);
+                            if (f == 1) {
+                                put_slot(A, PCL_PHOTON, L.slot, make_float4(L.x, L.y, L.z, L.w),
+                                         make_float4(L.px, L.py, L.pz, L.s),
+                                         make_uint4(L.sid_lo, L.sid_hi, L.ctr,
+                                                    __float_as_uint(-dd_val(L.th, L.tlo))));
+                                has = false;
+                            } else if (f == 2) {
+                                A.meta[PCL_PHOTON][L.slot].z = PCL_DEAD_CTR;
+                                if (A.hx_meta[PCL_PHOTON] && L.slot < A.hx_cap[PCL_PHOTON])
+                                    A.hx_meta[PCL_PHOTON][L.slot].z = PCL_DEAD_CTR;
+                                atomicAdd(&tal[T_DEAD + PCL_PHOTON], 1u);
+                                has = false;
+                            }
+                        }
                     }
                 }
                 cur += tk;
@@ -2102,6 +2168,79 @@ __global__ void k_learn_pick(const float4* m2, const unsigned long long* n_dev, 
         int sp = int(pk & 3u), j = int((pk >> 8) & 15u);
         int w = which.net[sp * 16 + j];
         Y[i] = Yk[(long long)max(w, 0) * stride + i];
+    }
+}
+
+// ------------------------------------------ energy-draw cost (test hook) --
+// The secondary-energy draw alone, for timing the table samplers against the
+// networks: primary i of n at E_i = 10^(4 + 4 (i + 1/2) / n) eV along z, with
+// stream id sid_base + i.
+__device__ __forceinline__ float draw_grid_energy(long long i, long long n) {
+    return exp10f(4.0f + 4.0f * (float(i) + 0.5f) / float(n)) / 510998.95f;
+}
+
+__device__ __forceinline__ void draw_lane(Lane& L, int species, unsigned long long sid, float E) {
+    L.x = L.y = L.z = 0.0f; L.w = 1.0f; L.th = 0.0f; L.tlo = 0.0f; L.k = 0; L.s = 0.0f;
+    L.px = 0.0f; L.py = 0.0f; L.pz = sqrtf(E * (E + 2.0f));
+    L.sid_lo = uint32_t(sid); L.sid_hi = uint32_t(sid >> 32); L.ctr = 0u; L.rvalid = false;
+    L.species = species; L.alive = true; L.slot = -1; L.nsub = 0; L.sw = 0; L.r = 0.0f;
+}
+
+// Table path: k / T (Seltzer-Berger) or eps (Moller) from the table sampler's
+// energy draw; draws[i] = uniforms it consumed.
+__global__ void k_draw_table(StepArgs A, int species, int j, int kind, long long n, unsigned long long sid_base,
+                             float* out, uint32_t* draws) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(smem + A.blob_bytes);
+    __shared__ uint32_t tal[T_WORDS];
+    for (int i = threadIdx.x; i < T_WORDS; i += blockDim.x) tal[i] = 0u;
+    bool ok = stage_blob(smem, A.blob, A.blob_bytes, mbar);
+    if (__syncthreads_or(!ok)) return;
+    KCtx K;
+    K.H = reinterpret_cast<const BlobHdr*>(smem); K.blob = reinterpret_cast<const float*>(smem); K.stk = nullptr;
+    K.top = nullptr; K.tal = tal; K.A = &A; K.cap = nullptr; K.ncap = nullptr;
+    const DevProc& P = K.H->sp[species].proc[j];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float E = draw_grid_energy(i, n);
+        Lane L;
+        draw_lane(L, species, sid_base + (unsigned long long)i, E);
+        out[i] = (kind == PCL_LEARN_SB) ? sb_k(L, K, P, E) / E : moller_eps(L, K, P, E);
+        draws[i] = L.ctr;
+    }
+}
+
+// Network path, before the network: its inputs (a, 2u - 1), one uniform each.
+__global__ void k_draw_net_x(long long n, unsigned long long sid_base, uint32_t k0, uint32_t k1, float* X) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float E = draw_grid_energy(i, n);
+        Lane L;
+        draw_lane(L, 0, sid_base + (unsigned long long)i, E);
+        const float u = bits_to_u(next_bits(L, k0, k1));
+        X[2 * i] = learn_a(E);
+        X[2 * i + 1] = 2.0f * u - 1.0f;
+    }
+}
+
+// Network path, after the network: its output mapped to k / T or eps as the
+// step's learned samplers map it (learned_outcome).
+__global__ void k_draw_net_map(StepArgs A, int species, int j, int kind, long long n, const float* Y, float* out) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    unsigned long long* mbar = reinterpret_cast<unsigned long long*>(smem + A.blob_bytes);
+    bool ok = stage_blob(smem, A.blob, A.blob_bytes, mbar);
+    if (__syncthreads_or(!ok)) return;
+    KCtx K;
+    K.H = reinterpret_cast<const BlobHdr*>(smem); K.blob = reinterpret_cast<const float*>(smem); K.stk = nullptr;
+    K.top = nullptr; K.tal = nullptr; K.A = &A; K.cap = nullptr; K.ncap = nullptr;
+    const DevProc& P = K.H->sp[species].proc[j];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float E = draw_grid_energy(i, n);
+        const float v = fminf(fmaxf(Y[i], 0.0f), 1.0f);
+        if (kind == PCL_LEARN_SB) {
+            out[i] = expf(fminf((1.0f - v) * sb_ymin(K, P, E), -1e-6f));
+        } else {
+            const float e0 = P.p[0] / E;
+            out[i] = e0 / (1.0f - v * (1.0f - 2.0f * e0));
+        }
     }
 }
 

@@ -447,9 +447,9 @@ class MultiPopulation:
 
     def set_host_io(self, mode: int):
         """How advance_host moves the population over the CPU-GPU link
-        (pcl_set_host_io): 0 auto (direct where the arrays allow), 1 copy
-        pipeline, 2 direct (the step kernel reads and writes the page-locked
-        host arrays)."""
+        (pcl_set_host_io): 0 the library's default (the copy pipeline), 1
+        copy pipeline, 2 direct (the step kernel reads and writes the
+        page-locked host arrays)."""
         _lib.check(_lib.lib().pcl_set_host_io(self.ctx, int(mode)), self.ctx, "pcl_set_host_io")
 
     def set_learned(self, particle, proc_index: int, kind: int, net=None):

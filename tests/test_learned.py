@@ -1,8 +1,8 @@
 """The learned inverse-CDF sampler: training data from the table samplers,
 networks trained on the GPU by the tensor-core kernels, their accuracy against
-the table samplers (KS distance and chi^2 on the physical variable), what the
-network saves over the rejection sampler, and the step with the networks
-attached against the plain step."""
+the table samplers (KS distance and chi^2 on the physical variable), the time
+and uniforms a draw costs with and without the network, and the step with the
+networks attached against the plain step."""
 import numpy as np
 import pytest
 
@@ -124,16 +124,37 @@ def test_learned_matches_table(pcl, setup, which):
     assert max(d[2] for d in decades) < KS_MAX, (loss, decades, single)
 
 
-def test_gain_over_rejection(pcl, setup):
-    """The Moller rejection sampler spends 2 draws per trial; the network
-    spends exactly one uniform per energy sample, with no loop."""
+def test_gain_over_table_sampler_timed(pcl, setup):
+    """What the trained network gains over the sampler it replaces, measured on
+    the GPU (pcl_time_energy_draw, CUDA events, fastest of 5): the time per
+    secondary-energy draw of 2^22 primaries spread over 1e4-1e8 eV, table
+    sampler (one kernel) against network (inputs, tensor-core inference,
+    output map), and the uniforms each draw consumes.  Both paths must give the
+    same distribution (KS < 1 %); the times and draws are reported, whichever
+    way they fall."""
+    import ctypes as C
     mp, et, sb, mo, nets = setup
-    _, draws = _table_samples(pcl, mp, mo[0], 1e6 * pcl.co.eV, 100_000, seed=9)
-    # draws = 2 k (trials) + 1 (phi) + 2 (s of both electrons)
-    trials = (draws.astype(np.float64) - 3) / 2
-    assert trials.mean() > 1.0 and np.all(trials >= 1)
-    learned_draws = 1 + 1 + 2   # u for the network, phi, two s
-    assert learned_draws < draws.mean()
+    L = pcl.lib()
+    n = 1 << 22
+    Tev = 10.0 ** (4.0 + 4.0 * (np.arange(n) + 0.5) / n)
+    report = {}
+    for which, j in (("sb", sb[0]), ("moller", mo[0])):
+        net, kind, _ = nets[j]
+        ms_t, ms_n = C.c_double(), C.c_double()
+        ot = np.zeros(n, np.float32); on = np.zeros(n, np.float32); dr = np.zeros(n, np.uint32)
+        rc = L.pcl_time_energy_draw(mp.ctx, pcl.Electron, j, kind, net.h, n, 5, C.byref(ms_t), C.byref(ms_n),
+                                    ot.ctypes.data_as(C.POINTER(C.c_float)), on.ctypes.data_as(C.POINTER(C.c_float)),
+                                    dr.ctypes.data_as(C.POINTER(C.c_uint32)))
+        assert rc == 0, L.pcl_last_error(mp.ctx)
+        ok = np.ones(n, bool) if which == "sb" else (et.proc[j].tcut / (Tev * pcl.co.eV) < 0.45)
+        ks = _ks(np.log(ot[ok]), np.log(on[ok]))
+        assert ks < KS_MAX, (which, ks)
+        assert np.all(dr >= 1) and (which == "sb" or dr.mean() > 2.0)
+        report[which] = {"ns_per_draw_table": 1e6 * ms_t.value / n, "ns_per_draw_network": 1e6 * ms_n.value / n,
+                         "network_over_table_time": ms_n.value / ms_t.value,
+                         "uniforms_per_draw_table": float(dr.mean()), "uniforms_per_draw_network": 1.0, "ks": ks}
+        assert np.isfinite(ms_t.value) and np.isfinite(ms_n.value) and ms_t.value > 0 and ms_n.value > 0
+    print("energy-draw cost", report)
 
 
 def test_step_with_learned_samplers(pcl, air, setup):
