@@ -1175,40 +1175,6 @@ __device__ __forceinline__ void put_slot(const StepArgs& A, int sp, long long sl
     }
 }
 
-// A photon taken from the input whose next collision falls beyond the end of
-// its step: the loop's sub-step (a straight flight of the rest of the step)
-// and step boundary (droplow! and, in a multi-step launch, setr! of the next
-// step), the same operations in the same order, done at once so that its lane
-// takes the next input in the same refill.  Returns 0 as soon as a collision
-// falls within the current step (the particle is then where a step boundary
-// left it, and the loop goes on from there), 1 when it survives the launch,
-// 2 when it is removed.
-template <bool GENERAL>
-__device__ __forceinline__ int photon_free_flight(Lane& L, const KCtx& K, const SpeciesHdr& S, int nsteps,
-                                                  float dt_hi, float dt_lo) {
-    for (;;) {
-        if (dd_val(L.th, L.tlo) > kEpsT) {
-            const float tnext = L.s / L.r;
-            if (__fadd_rn(__fsub_rn(L.th, tnext), L.tlo) > 0.0f) return 0;
-            const float h = dd_val(L.th, L.tlo);
-            L.s -= h * L.r;
-            push<GENERAL>(L, S, K, h);
-            L.th = 0.0f;
-            L.tlo = 0.0f;
-            L.nsub += 1;
-        }
-        const float E = kin_energy(L.species, L.px, L.py, L.pz);
-        if (E < S.cut) return 2;  // droplow! (population.jl:273-284)
-        atomicAdd(&K.tal[T_LEND + 3 * L.k + L.species], 1u);
-        if (L.k + 1 >= nsteps) return 1;
-        L.k += 1;
-        L.nsub = 0;
-        dd_add(L.th, L.tlo, dt_hi, dt_lo);
-        L.r = setr(S, K, E, L.sw);
-        atomicAdd(&K.tal[T_LSTART + L.k], 1u);
-    }
-}
-
 // ------------------------------------------------------------ the step ---
 // EVENT: colliding particles are parked in a per-warp stash and collided in
 // batches that fill the warp's free lanes (see the loop), instead of each lane
@@ -1412,25 +1378,6 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         L.rvalid = false; L.alive = true; L.nsub = 0;
                         L.sw = (H->nswarm > 0) ? min(int(L.sid_hi >> 24), H->nswarm - 1) : 0;
                         L.r = setr(H->sp[L.species], K, kin_energy(L.species, L.px, L.py, L.pz), L.sw);
-                        // photons of the population: most fly through the whole step
-                        // without a collision; finish those here (no wall on photons)
-                        if (A.spill_mode == 0 && L.species == PCL_PHOTON &&
-                            (!GENERAL || H->sp[PCL_PHOTON].wall_coord < 0)) {
-                            const int f = photon_free_flight<GENERAL>(L, K, H->sp[PCL_PHOTON], nsteps, dt_hi, dt_lo);
-                            if (f == 1) {
-                                put_slot(A, PCL_PHOTON, L.slot, make_float4(L.x, L.y, L.z, L.w),
-                                         make_float4(L.px, L.py, L.pz, L.s),
-                                         make_uint4(L.sid_lo, L.sid_hi, L.ctr,
-                                                    __float_as_uint(-dd_val(L.th, L.tlo))));
-                                has = false;
-                            } else if (f == 2) {
-                                A.meta[PCL_PHOTON][L.slot].z = PCL_DEAD_CTR;
-                                if (A.hx_meta[PCL_PHOTON] && L.slot < A.hx_cap[PCL_PHOTON])
-                                    A.hx_meta[PCL_PHOTON][L.slot].z = PCL_DEAD_CTR;
-                                atomicAdd(&tal[T_DEAD + PCL_PHOTON], 1u);
-                                has = false;
-                            }
-                        }
                     }
                 }
                 cur += tk;
@@ -1732,35 +1679,77 @@ __global__ void k_compact_scatter(CompactArgs C) {
 }
 
 // ------------------------------------------------------------- moments ---
-// FP64 weighted moments of the live particles (weight, meanenergy, spread,
-// posvar, maxenergy, nactives; population.jl:89-223).
+// Double-float accumulation (hi + lo, ~48-bit significand) on the FP32 pipes:
+// GB300 runs FP64 arithmetic at a small fraction of its FP32 rate, and a
+// reduction of FP32 state in plain FP64 per particle is bound by it.
+// (hi, lo) += a
+__device__ __forceinline__ void df_acc(float& hi, float& lo, float a) {
+    float s, e;
+    two_sum(hi, a, s, e);
+    e = __fadd_rn(e, lo);
+    fast_two_sum(s, e, hi, lo);
+}
+// (hi, lo) += a b, the product split exactly into p + pe (fma)
+__device__ __forceinline__ void df_acc_prod(float& hi, float& lo, float a, float b) {
+    const float p = __fmul_rn(a, b), pe = __fmaf_rn(a, b, -p);
+    float s, e;
+    two_sum(hi, p, s, e);
+    e = __fadd_rn(__fadd_rn(e, pe), lo);
+    fast_two_sum(s, e, hi, lo);
+}
+// (hi, lo) += (bh, bl)
+__device__ __forceinline__ void df_acc2(float& hi, float& lo, float bh, float bl) {
+    float s, e;
+    two_sum(hi, bh, s, e);
+    e = __fadd_rn(e, __fadd_rn(lo, bl));
+    fast_two_sum(s, e, hi, lo);
+}
+
+// Population moments (nactives, weight, meanenergy, spread, posvar;
+// population.jl:89-223): sum w, sum w E, sum w x, y, z, sum w x^2, y^2, z^2,
+// max E and the live count.  Per particle in FP32 (E = p^2 / (sqrt(1 + p^2)
+// + 1), the step's cancellation-free form, with IEEE square root and division;
+// products split exactly), summed per thread and per warp in double-float,
+// and across warps in FP64.
 __global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta, long long n, int species,
                           double* out) {
-    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    double emax = 0.0;
+    float hi[8] = {0, 0, 0, 0, 0, 0, 0, 0}, lo[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    float emax = 0.0f;
     unsigned long long live = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         uint4 m = meta[i];
         if (m.z == PCL_DEAD_CTR) continue;
-        float4 a = xw[i], b = ps[i];
-        double p2 = double(b.x) * b.x + double(b.y) * b.y + double(b.z) * b.z;
-        double E = (species == PCL_PHOTON) ? sqrt(p2) : p2 / (sqrt(1.0 + p2) + 1.0);
-        double w = a.w;
-        acc[0] += w; acc[1] += w * E;
-        acc[2] += w * a.x; acc[3] += w * a.y; acc[4] += w * a.z;
-        acc[5] += w * double(a.x) * a.x; acc[6] += w * double(a.y) * a.y; acc[7] += w * double(a.z) * a.z;
-        emax = fmax(emax, E);
+        const float4 a = xw[i], b = ps[i];
+        const float E = kin_energy_exact(species, b.x, b.y, b.z);
+        const float w = a.w;
+        df_acc(hi[0], lo[0], w);
+        df_acc_prod(hi[1], lo[1], w, E);
+        df_acc_prod(hi[2], lo[2], w, a.x);
+        df_acc_prod(hi[3], lo[3], w, a.y);
+        df_acc_prod(hi[4], lo[4], w, a.z);
+        const float c[3] = {a.x, a.y, a.z};
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {   // w c^2: c^2 = p + pe exactly, then w p exactly and w pe in FP32
+            const float p = __fmul_rn(c[q], c[q]), pe = __fmaf_rn(c[q], c[q], -p);
+            df_acc_prod(hi[5 + q], lo[5 + q], w, p);
+            df_acc(hi[5 + q], lo[5 + q], __fmul_rn(w, pe));
+        }
+        emax = fmaxf(emax, E);
         live += 1;
     }
     for (int o = 16; o; o >>= 1) {
-        for (int q = 0; q < 8; ++q) acc[q] += __shfl_xor_sync(0xffffffffu, acc[q], o);
-        emax = fmax(emax, __shfl_xor_sync(0xffffffffu, emax, o));
+        for (int q = 0; q < 8; ++q) {
+            const float bh = __shfl_xor_sync(0xffffffffu, hi[q], o), bl = __shfl_xor_sync(0xffffffffu, lo[q], o);
+            df_acc2(hi[q], lo[q], bh, bl);
+        }
+        emax = fmaxf(emax, __shfl_xor_sync(0xffffffffu, emax, o));
         live += __shfl_xor_sync(0xffffffffu, live, o);
     }
     if ((threadIdx.x & 31) == 0) {
-        for (int q = 0; q < 8; ++q) atomicAdd(&out[q], acc[q]);
-        atomicMax(reinterpret_cast<unsigned long long*>(&out[8]), (unsigned long long)__double_as_longlong(emax));
+        for (int q = 0; q < 8; ++q) atomicAdd(&out[q], double(hi[q]) + double(lo[q]));
+        atomicMax(reinterpret_cast<unsigned long long*>(&out[8]),
+                  (unsigned long long)__double_as_longlong(double(emax)));
         atomicAdd(reinterpret_cast<unsigned long long*>(&out[9]), live);
     }
 }
@@ -1768,8 +1757,8 @@ __global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta,
 // Energy spectrum of the live particles, as the reference's scripts build one
 // with StatsBase.fit(Histogram, E, edges[, weights]) (scripts/beam.jl:137-147,
 // scripts/swarm.jl:149-158): bin i counts edges[i] <= E < edges[i+1] (device
-// energy units, FP64 from the FP32 momentum); energies outside
-// [edges[0], edges[nb]) are not counted.  swarm >= 0 keeps the particles of
+// energy units, FP64 from the FP32 momentum, as the host computes it from the
+// downloaded state); energies outside [edges[0], edges[nb]) are not counted.  swarm >= 0 keeps the particles of
 // that swarm (top 8 bits of the stream id) only.  Per-block shared bins, one
 // global atomic per non-empty bin.
 __global__ void k_energy_hist(const float4* xw, const float4* ps, const uint4* meta, const unsigned long long* nslots,
@@ -1790,13 +1779,32 @@ __global__ void k_energy_hist(const float4* xw, const float4* ps, const uint4* m
         if (m.z == PCL_DEAD_CTR) continue;
         if (swarm >= 0 && int(m.y >> 24) != swarm) continue;
         const float4 b = ps[i];
-        const double p2 = double(b.x) * b.x + double(b.y) * b.y + double(b.z) * b.z;
-        const double E = (species == PCL_PHOTON) ? sqrt(p2) : p2 / (sqrt(1.0 + p2) + 1.0);
-        if (!(E >= lo && E < hi)) continue;
+        // the bin from the FP32 energy (GB300's FP64 rate is a small fraction
+        // of its FP32 rate); the FP64 energy decides whenever the FP32 one lies
+        // within 1e-6 (relative) of an edge it was compared with
+        const float Ef = kin_energy_exact(species, b.x, b.y, b.z);
+        const double Ed = double(Ef), tol = 1e-6 * Ed;
+        bool near = fabs(Ed - lo) <= tol || fabs(Ed - hi) <= tol;
         int a = 0, z = nb;            // se[a] <= E < se[z]
-        while (z - a > 1) {
-            const int mid = (a + z) >> 1;
-            if (E >= se[mid]) a = mid; else z = mid;
+        if (!near && (Ed >= lo && Ed < hi)) {
+            while (z - a > 1) {
+                const int mid = (a + z) >> 1;
+                const double d = Ed - se[mid];
+                near = near || fabs(d) <= tol;
+                if (d >= 0.0) a = mid; else z = mid;
+            }
+        } else if (!near) {
+            continue;                 // clearly outside [edges[0], edges[nb])
+        }
+        if (near) {
+            const double p2 = double(b.x) * b.x + double(b.y) * b.y + double(b.z) * b.z;
+            const double E = (species == PCL_PHOTON) ? sqrt(p2) : p2 / (sqrt(1.0 + p2) + 1.0);
+            if (!(E >= lo && E < hi)) continue;
+            a = 0; z = nb;
+            while (z - a > 1) {
+                const int mid = (a + z) >> 1;
+                if (E >= se[mid]) a = mid; else z = mid;
+            }
         }
         atomicAdd(&sc[a], 1u);
         atomicAdd(&sw[a], double(xw[i].w));
