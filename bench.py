@@ -124,11 +124,14 @@ def _peaks():
 
 # DRAM bytes (read + write) per slot of one k_step launch, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the event kernel on
-# a 4 M-particle draw of the same mixed state at the commit named beside it;
-# scaled to a launch by the slots it processes.  None: not captured for the
-# current kernel, and the line says so.
-K_STEP_DRAM_BYTES_PER_SLOT = None
-K_STEP_DRAM_CAPTURE = None
+# a 4 M-particle draw of the same mixed state at the commit named below (the
+# step kernel's source has not changed since); scaled to a launch by the slots
+# it processes: the reads grow in proportion, the writes are bounded by 48 B
+# per slot.
+K_STEP_DRAM_BYTES_PER_SLOT = 85.0
+K_STEP_DRAM_CAPTURE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 4th k_step launch of "
+                       "'bench.py --n 4194304 --steps 3 --warmup 3 --no-cpu --no-e2e --no-forms' at commit "
+                       "c0c1db4: 201.8 MB read + 154.6 MB written over 4.19 M slots")
 
 WORKLOAD = "rrea-air-0.5MVm-mixed-16M"
 

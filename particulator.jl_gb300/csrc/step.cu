@@ -1718,9 +1718,11 @@ __global__ void k_moments(const float4* xw, const float4* ps, const uint4* meta,
     unsigned long long live = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        uint4 m = meta[i];
-        if (m.z == PCL_DEAD_CTR) continue;
+        // the three records are loaded together, before the dead-slot test, so
+        // their latencies overlap
+        const uint4 m = meta[i];
         const float4 a = xw[i], b = ps[i];
+        if (m.z == PCL_DEAD_CTR) continue;
         const float E = kin_energy_exact(species, b.x, b.y, b.z);
         const float w = a.w;
         df_acc(hi[0], lo[0], w);
@@ -1766,19 +1768,21 @@ __global__ void k_energy_hist(const float4* xw, const float4* ps, const uint4* m
                               unsigned long long* counts, double* wsum) {
     extern __shared__ double hsh[];
     double* se = hsh;                 // [nb + 1] edges
-    double* sw = hsh + nb + 1;        // [nb] weights
+    double* sw = hsh + nb + 1;        // [nb] weights other than 1
     unsigned int* sc = reinterpret_cast<unsigned int*>(sw + nb);   // [nb] counts
+    unsigned int* s1 = sc + nb;       // [nb] counts of weight-1 particles (most populations)
     for (int i = threadIdx.x; i <= nb; i += blockDim.x) se[i] = edges[i];
-    for (int i = threadIdx.x; i < nb; i += blockDim.x) { sw[i] = 0.0; sc[i] = 0u; }
+    for (int i = threadIdx.x; i < nb; i += blockDim.x) { sw[i] = 0.0; sc[i] = 0u; s1[i] = 0u; }
     __syncthreads();
     const long long n = min((long long)*nslots, cap);
     const double lo = se[0], hi = se[nb];
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const uint4 m = meta[i];
+        const float4 b = ps[i];
+        const float w = xw[i].w;      // loaded with the others, so the latencies overlap
         if (m.z == PCL_DEAD_CTR) continue;
         if (swarm >= 0 && int(m.y >> 24) != swarm) continue;
-        const float4 b = ps[i];
         // the bin from the FP32 energy (GB300's FP64 rate is a small fraction
         // of its FP32 rate); the FP64 energy decides whenever the FP32 one lies
         // within 1e-6 (relative) of an edge it was compared with
@@ -1807,13 +1811,16 @@ __global__ void k_energy_hist(const float4* xw, const float4* ps, const uint4* m
             }
         }
         atomicAdd(&sc[a], 1u);
-        atomicAdd(&sw[a], double(xw[i].w));
+        // a weight of exactly 1 is counted in integers (a shared FP64 atomic is
+        // a compare-and-swap loop); other weights are summed in FP64
+        if (w == 1.0f) atomicAdd(&s1[a], 1u);
+        else atomicAdd(&sw[a], double(w));
     }
     __syncthreads();
     for (int i = threadIdx.x; i < nb; i += blockDim.x) {
         if (sc[i]) {
             atomicAdd(&counts[i], (unsigned long long)sc[i]);
-            atomicAdd(&wsum[i], sw[i]);
+            atomicAdd(&wsum[i], sw[i] + double(s1[i]));
         }
     }
 }
