@@ -793,7 +793,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and learned sub-objects")
-    ap.add_argument("--steps-per-launch", type=int, default=1)
+    ap.add_argument("--steps-per-launch", type=int, default=0,
+                    help="steps per launch of the timed run! (0: chosen by the library's autotuner)")
+    ap.add_argument("--tune-budget", type=int, default=256, help="steps the autotuner may use (untimed)")
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
     ap.add_argument("--classic", type=int, default=0, help="1: classic step kernel (lanes collide in place)")
     ap.add_argument("--graph", type=int, default=0, help="1: launch groups replayed from CUDA graphs")
@@ -829,29 +831,34 @@ def main():
     pcl = graft.load_package()
     L = pcl.lib()
     mp, pusher, dt, extra = build_workload(pcl, args.n, seed=rank, device=local,
-                                           steps_per_launch=args.steps_per_launch, blocks_per_sm=args.bps,
+                                           steps_per_launch=max(1, args.steps_per_launch), blocks_per_sm=args.bps,
                                            classic_step=bool(args.classic), use_graph=bool(args.graph),
                                            compaction_period=args.compaction_period)
     ctx = mp.ctx
-    K = args.steps_per_launch
     live_start = list(mp.tallies().live)
-    # ---- warm-up
+    # ---- warm-up: W steps, then (unless a launch shape is given) the
+    # library's autotuner, whose trials are real steps of the same run
     t = 0.0
     for _ in range(args.warmup):
-        t += dt * K
-        pcl.run(mp, pusher, t, dt) if K > 1 else pcl.advance(mp, pusher, t)
+        t += dt
+        pcl.advance(mp, pusher, t)
+    tune = None
+    if args.steps_per_launch == 0:
+        tune = mp.autotune(pusher, dt, steps=args.tune_budget)
+        t = mp.t
+    K = int(mp.config.steps_per_launch)
     L.pcl_sync(ctx)
     tal0 = mp.tallies()
     L.pcl_kernel_stats(ctx, None, None, None, None, 1)
-    # ---- timed region: device-resident steps, a device synchronisation and a
-    # barrier on both sides
+    # ---- timed region: K steps of run! (launch groups of the chosen shape), a
+    # device synchronisation and a barrier on both sides
     L.pcl_sync(ctx)
     _barrier(ws)
     with Clocks(local) as clk:
         L.pcl_timer_start(ctx)
-        for _ in range(args.steps):
-            t += dt * K
-            pcl.run(mp, pusher, t, dt) if K > 1 else pcl.advance(mp, pusher, t)
+        t_end = t + args.steps * dt
+        pcl.run(mp, pusher, t_end, dt)
+        t = t_end
         ms = C.c_double()
         L.pcl_timer_stop(ctx, C.byref(ms))
     L.pcl_sync(ctx)
@@ -860,11 +867,17 @@ def main():
     kms = C.c_double(); kl = C.c_int64(); nl = C.c_int64(); kb = C.c_double()
     L.pcl_kernel_stats(ctx, C.byref(kms), C.byref(kl), C.byref(nl), C.byref(kb), 1)
     psteps = tal1.particle_steps - tal0.particle_steps
+    assert tal1.steps - tal0.steps == args.steps, (tal1.steps, tal0.steps)
     elapsed = _barrier_max(ms.value / 1e3, ws)
     total_psteps = psteps * ws
     value = total_psteps / elapsed
     peak, peak_kind = _peaks()
-    achieved = (kb.value / max(kl.value, 1)) / (kms.value / max(kl.value, 1) / 1e3) / 1e9
+    # algorithmic bytes: 96 B per particle-step (48 B read + 48 B written per
+    # particle per step) over the step kernel's own time; with several steps
+    # per launch a particle stays in registers between its steps, and the
+    # bytes the kernel moves are its slots' 96 B once per launch
+    achieved = 96.0 * psteps / (kms.value / 1e3) / 1e9
+    moved = kb.value / (kms.value / 1e3) / 1e9
     slots_per_launch = (kb.value / max(kl.value, 1)) / 96.0
     traffic = K_STEP_DRAM_BYTES_PER_SLOT * slots_per_launch if K_STEP_DRAM_BYTES_PER_SLOT else None
     # ---- end to end through the C ABI with pinned host buffers
@@ -929,18 +942,23 @@ def main():
                 forms[name] = {"value": None, "error": str(ex)[:300]}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / (args.steps * K), "higher_is_better": True,
+                "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
                 "config": workload_config(args.n, ws),
-                "run": {"steps_per_launch": K, "graph": bool(args.graph),
-                        "compaction_period": args.compaction_period or 8,
-                        "blocks_per_sm": (args.bps or 4) if args.classic else 3,
-                        "step_kernel": "classic" if args.classic else "event",
+                "run": {"api": "run! (pcl_run) over the timed steps", "steps_per_launch": K,
+                        "graph": bool(mp.config.use_graph),
+                        "compaction_period": int(mp.config.compaction_period) or 8,
+                        "blocks_per_sm": int(mp.config.blocks_per_sm) or 3,
+                        "step_kernel": "classic" if mp.config.classic_step else "event",
+                        "launch_shape": "autotuned (pcl_autotune, untimed)" if tune else "given",
+                        "autotune": tune, "step_launches": int(kl.value),
                         "live_at_start": live_start, "live_at_end": live_end},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
                              "traffic_source": K_STEP_DRAM_CAPTURE, "kernel": "k_step",
-                             "bytes_per_particle_step": 96},
+                             "bytes_rule": "96 B per particle-step over the step kernel's time",
+                             "moved_GB_s": moved, "moved_rule": "96 B per slot per launch (once per "
+                             f"{K} steps) over the step kernel's time"},
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(nl.value), "clocks": clk.summary(),
                 "errors": errs}
         line.update(forms)

@@ -228,10 +228,12 @@ int pcl_energy_histogram(void* ctx, int species, int swarm, int nedges, const do
         double* de = dw + nb;
         CK(cudaMemcpyAsync(de, ed.data(), sizeof(double) * nedges, cudaMemcpyHostToDevice, c->stream));
         CK(cudaMemsetAsync(dc, 0, 2 * sizeof(double) * nb, c->stream));
-        // shared: edges [nb + 1] and weights [nb] (FP64), counts and weight-1 counts [nb] (u32)
-        const size_t smem = sizeof(double) * (2 * size_t(nb) + 1) + 2 * sizeof(unsigned int) * nb;
+        // shared: edges [nb + 1] and weights [nb] (FP64), counts and weight-1 counts [nb] (u32),
+        // FP32 edges [nb + 1]
+        const size_t smem = sizeof(double) * (2 * size_t(nb) + 1) + 2 * sizeof(unsigned int) * nb +
+                            sizeof(float) * (size_t(nb) + 1);
         CK(cudaFuncSetAttribute(k_energy_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(sizeof(double) * (2 * PCL_MAX_HIST_EDGES) + 8 * PCL_MAX_HIST_EDGES)));
+                                int(sizeof(double) * (2 * PCL_MAX_HIST_EDGES) + 12 * PCL_MAX_HIST_EDGES)));
         const long long bps = std::max<long long>(1, std::min<long long>(8, (200ll << 10) / (long long)smem));
         const int grid = int(std::min<long long>((S.cap + 255) / 256, bps * c->sm_count));
         k_energy_hist<<<grid, 256, smem, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], &c->d_ctl->n[species],

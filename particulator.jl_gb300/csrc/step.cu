@@ -1771,7 +1771,8 @@ __global__ void k_energy_hist(const float4* xw, const float4* ps, const uint4* m
     double* sw = hsh + nb + 1;        // [nb] weights other than 1
     unsigned int* sc = reinterpret_cast<unsigned int*>(sw + nb);   // [nb] counts
     unsigned int* s1 = sc + nb;       // [nb] counts of weight-1 particles (most populations)
-    for (int i = threadIdx.x; i <= nb; i += blockDim.x) se[i] = edges[i];
+    float* sf = reinterpret_cast<float*>(s1 + nb);                 // [nb + 1] edges rounded to FP32
+    for (int i = threadIdx.x; i <= nb; i += blockDim.x) { se[i] = edges[i]; sf[i] = float(edges[i]); }
     for (int i = threadIdx.x; i < nb; i += blockDim.x) { sw[i] = 0.0; sc[i] = 0u; s1[i] = 0u; }
     __syncthreads();
     const long long n = min((long long)*nslots, cap);
@@ -1783,19 +1784,21 @@ __global__ void k_energy_hist(const float4* xw, const float4* ps, const uint4* m
         const float w = xw[i].w;      // loaded with the others, so the latencies overlap
         if (m.z == PCL_DEAD_CTR) continue;
         if (swarm >= 0 && int(m.y >> 24) != swarm) continue;
-        // the bin from the FP32 energy (GB300's FP64 rate is a small fraction
-        // of its FP32 rate); the FP64 energy decides whenever the FP32 one lies
-        // within 1e-6 (relative) of an edge it was compared with
+        // the bin from the FP32 energy and FP32 edges (GB300's FP64 rate is a
+        // small fraction of its FP32 rate); the FP64 energy decides whenever
+        // the FP32 one lies within 1e-6 (relative) of an edge it was compared
+        // with, a margin far above both roundings
         const float Ef = kin_energy_exact(species, b.x, b.y, b.z);
-        const double Ed = double(Ef), tol = 1e-6 * Ed;
-        bool near = fabs(Ed - lo) <= tol || fabs(Ed - hi) <= tol;
+        const float tol = 1e-6f * Ef;
+        const float flo = sf[0], fhi = sf[nb];
+        bool near = fabsf(Ef - flo) <= tol || fabsf(Ef - fhi) <= tol;
         int a = 0, z = nb;            // se[a] <= E < se[z]
-        if (!near && (Ed >= lo && Ed < hi)) {
+        if (!near && (Ef >= flo && Ef < fhi)) {
             while (z - a > 1) {
                 const int mid = (a + z) >> 1;
-                const double d = Ed - se[mid];
-                near = near || fabs(d) <= tol;
-                if (d >= 0.0) a = mid; else z = mid;
+                const float d = Ef - sf[mid];
+                near = near || fabsf(d) <= tol;
+                if (d >= 0.0f) a = mid; else z = mid;
             }
         } else if (!near) {
             continue;                 // clearly outside [edges[0], edges[nb])
