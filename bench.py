@@ -130,7 +130,7 @@ def _peaks():
 # per slot.
 K_STEP_DRAM_BYTES_PER_SLOT = 85.0
 K_STEP_DRAM_CAPTURE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 4th k_step launch of "
-                       "'bench.py --n 4194304 --steps 3 --warmup 3 --no-cpu --no-e2e --no-forms' at commit "
+                       "'bench.py --n 4194304 --steps 3 --warmup 3 --steps-per-launch 1 --no-cpu --no-e2e --no-forms' at commit "
                        "c0c1db4: 201.8 MB read + 154.6 MB written over 4.19 M slots")
 
 WORKLOAD = "rrea-air-0.5MVm-mixed-16M"
@@ -782,7 +782,7 @@ def _form_summary(line: dict, plain_value: float) -> dict:
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=64)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--n", type=int, default=1 << 24, help="particles drawn from the grown-state recipe")
@@ -795,7 +795,7 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and learned sub-objects")
     ap.add_argument("--steps-per-launch", type=int, default=0,
                     help="steps per launch of the timed run! (0: chosen by the library's autotuner)")
-    ap.add_argument("--tune-budget", type=int, default=256, help="steps the autotuner may use (untimed)")
+    ap.add_argument("--tune-budget", type=int, default=1152, help="steps the autotuner may use (untimed)")
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
     ap.add_argument("--classic", type=int, default=0, help="1: classic step kernel (lanes collide in place)")
     ap.add_argument("--graph", type=int, default=0, help="1: launch groups replayed from CUDA graphs")
@@ -803,7 +803,7 @@ def main():
     ap.add_argument("--workload", default="rrea16M",
                     choices=["rrea16M", "swarms", "learned", "plain", "reid", "reid-fp64", "mlp", "kernels"])
     ap.add_argument("--nswarm", type=int, default=256)
-    ap.add_argument("--tune-steps", type=int, default=512)
+    ap.add_argument("--tune-steps", type=int, default=1152)
     ap.add_argument("--learned-n", type=int, default=1 << 24, help="learned form: particles")
     ap.add_argument("--reid-groups", type=int, default=0, help="reid: batch-means errors from particle snapshots")
     ap.add_argument("--reid-fp64-n", type=int, default=1 << 17, help="reid-fp64: electrons of the Float64 run")

@@ -1182,10 +1182,13 @@ int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* ou
     if (!any) return fail(c, PCL_ERR_STATE, "no species set");
     CK(cudaSetDevice(c->device));
     // step kernel: 0 = event, 2-4 = classic with that many blocks per SM
-    const int bps_c[] = {0, 2, 3, 4}, k_c[] = {1, 2, 4, 8, 16}, per_c[] = {2, 4, 8, 16, 32}, g_c[] = {0, 1};
-    const int ntrials = 4 + 5 + 5 + 2;
-    // steps per trial: a multiple of the largest steps-per-launch and period tried
-    int len = std::max(32, (steps_budget / ntrials) / 32 * 32);
+    const int bps_c[] = {0, 2, 3, 4}, k_c[] = {1, 2, 4, 8, 16, 32, 64}, per_c[] = {2, 4, 8, 16, 32}, g_c[] = {0, 1};
+    const int ntrials = 4 + 7 + 5 + 2;
+    // steps per trial: a multiple of the largest steps-per-launch tried (64),
+    // so that every trial is a whole number of launches; a budget below
+    // ntrials x 64 steps ends the search early (the candidates are tried in
+    // the order above)
+    int len = std::max(64, (steps_budget / ntrials) / 64 * 64);
     pcl_config best = c->cfg;
     best.blocks_per_sm = (c->cfg.classic_step == 0) ? 4 : blocks_per_sm(c);
     if (best.steps_per_launch < 1) best.steps_per_launch = 1;

@@ -172,10 +172,12 @@ def test_autotune_keeps_physics(pcl, gpu, air):
     where separate launches round it to FP32)."""
     pusher = _pusher(pcl, air, E=2e6)
     a = _mixed(pcl, air, n=(2048, 1024, 512), seed=21)
+    # a budget of 512 steps: 8 trials of 64 (the step kernels, then 1-8 steps
+    # per launch) before the budget ends the search
     r = a.autotune(pusher, 1e-12, steps=512)
-    assert r["blocks_per_sm"] in (0, 2, 3, 4) and r["steps_per_launch"] in (1, 2, 4, 8, 16)
+    assert r["blocks_per_sm"] in (0, 2, 3, 4) and r["steps_per_launch"] in (1, 2, 4, 8)
     assert r["compaction_period"] in (2, 4, 8, 16, 32) and r["use_graph"] in (0, 1)
-    assert r["trials"] == 16 and r["steps"] == 512 and r["rate"] > 0
+    assert r["trials"] == 8 and r["steps"] == 512 and r["rate"] > 0
     ta = a.tallies()
     assert ta.steps == 512
     b = _mixed(pcl, air, n=(2048, 1024, 512), seed=21)
