@@ -724,12 +724,25 @@ def run_kernels(args, pcl):
     timed("swarm moments (electrons, one swarm)", "k_swarm_moments + k_swarm_reduce", 48 * n_slots[E],
           lambda: mp.swarm_moments(E, 1))
     timed("roulette (photons, keep 0.9999)", "k_roulette", 16 * n_slots[G], lambda: mp.roulette(G, 0.9999), reps=1)
+    timed("per-swarm roulette (electrons, one swarm, keep 0.9999)", "k_roulette_swarms", 16 * n_slots[E],
+          lambda: mp.roulette_swarms(E, [0.9999]), reps=1)
+    timed("split (photons, 1 % copies)", "k_split", 16 * n_slots[G], lambda: mp.split(G, 0.01), reps=1)
     tal = mp.tallies()
     n_slots = [int(v) for v in tal.n]
     n_live = [int(v) for v in tal.live]
     cbytes = sum(16 * n_slots[q] + 48 * n_slots[q] + 48 * n_live[q] for q in range(3))
     timed("repack (all species)", "k_compact_count + k_compact_scan + k_compact_scatter", cbytes,
           lambda: L.pcl_compact(mp.ctx), reps=1)
+    # training data of a learned sampler: 2^22 draws of the Seltzer-Berger table
+    # sampler, histogrammed on the device (k_learn_hist)
+    et = mp.get(E).collisions
+    j = pcl.learned.table_positions(et, pcl.learned.LEARN_SB)[0]
+    L.pcl_timer_start(mp.ctx)
+    pcl.learned.learn_data(mp, E, j, pcl.learned.LEARN_SB, samples=float(1 << 22), nT=256, Q=256, seed=1)
+    lms = C.c_double()
+    L.pcl_timer_stop(mp.ctx, C.byref(lms))
+    rows.append({"op": "learned-sampler training data (2^22 table draws, 256 energies)",
+                 "kernels": "k_learn_hist", "ms": lms.value, "draws_per_s": (1 << 22) / (lms.value / 1e3)})
     mp.close()
     # the network kernels (FLOPs): inference of 4 M rows, training steps of 8192 rows
     net = pcl.SamplerNet(seed=1)
