@@ -133,6 +133,14 @@ K_STEP_DRAM_CAPTURE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 
                        "'bench.py --n 4194304 --steps 3 --warmup 3 --steps-per-launch 1 --no-cpu --no-e2e --no-forms' at commit "
                        "c0c1db4: 201.8 MB read + 154.6 MB written over 4.19 M slots")
 
+# Warp instructions per particle-step of the event step kernel on a 4 M draw
+# of the same state, by steps per launch (ncu smsp__inst_executed.sum of one
+# launch over its particle-steps; commits c0c1db4 and cb28eba, the kernel's
+# source unchanged between them), for the issue ceiling: 152 SMs x 4
+# schedulers x 2.07 GHz warp instructions per second.
+K_STEP_WARP_INST_PER_PSTEP = {1: 47.7, 16: 55.2, 64: 55.1}
+ISSUE_RATE = 152 * 4 * 2.07e9
+
 WORKLOAD = "rrea-air-0.5MVm-mixed-16M"
 
 
@@ -893,6 +901,11 @@ def main():
     moved = kb.value / (kms.value / 1e3) / 1e9
     slots_per_launch = (kb.value / max(kl.value, 1)) / 96.0
     traffic = K_STEP_DRAM_BYTES_PER_SLOT * slots_per_launch if K_STEP_DRAM_BYTES_PER_SLOT else None
+    # issue ceiling with the instruction count captured at the nearest launch shape
+    kq = min(K_STEP_WARP_INST_PER_PSTEP, key=lambda q: abs(np.log(q) - np.log(K)))
+    ceiling = ISSUE_RATE / K_STEP_WARP_INST_PER_PSTEP[kq]
+    issue = {"warp_inst_per_particle_step": K_STEP_WARP_INST_PER_PSTEP[kq], "captured_at_steps_per_launch": kq,
+             "ceiling": ceiling, "unit": UNIT, "frac": value / ws / ceiling}
     # ---- end to end through the C ABI with pinned host buffers
     e2e = None
     try:
@@ -972,6 +985,7 @@ def main():
                              "bytes_rule": "96 B per particle-step over the step kernel's time",
                              "moved_GB_s": moved, "moved_rule": "96 B per slot per launch (once per "
                              f"{K} steps) over the step kernel's time"},
+                "issue_roofline": issue,
                 "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(nl.value), "clocks": clk.summary(),
                 "errors": errs}
         line.update(forms)
