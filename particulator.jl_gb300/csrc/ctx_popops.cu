@@ -17,8 +17,9 @@ int pcl_roulette(void* ctx, int species, double pkeep) {
     SpeciesState& S = c->sp[species];
     long long n = 0;
     if (S.cap <= 0 || (rc = get_n(c, species, n)) || n == 0) return rc;
-    unsigned long long* killed = nullptr;
-    CK(cudaMallocAsync(&killed, sizeof(unsigned long long), c->stream));
+    // the removed count in the context's reusable scratch (no allocation per call)
+    if ((rc = ensure_scratch(c, 256))) return rc;
+    unsigned long long* killed = static_cast<unsigned long long*>(c->d_scr);
     CK(cudaMemsetAsync(killed, 0, sizeof(unsigned long long), c->stream));
     const int grid = int(std::min<long long>((n + 255) / 256, 8ll * c->sm_count));
     k_roulette<<<grid, 256, 0, c->stream>>>(S.xw[S.cur], S.meta[S.cur], n, float(pkeep), uint32_t(c->cfg.seed),
@@ -26,7 +27,6 @@ int pcl_roulette(void* ctx, int species, double pkeep) {
     CK(cudaGetLastError());
     unsigned long long hk = 0;
     CK(cudaMemcpyAsync(&hk, killed, sizeof(hk), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaFreeAsync(killed, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     c->live[species] = std::max<long long>(0, c->live[species] - (long long)hk);
     return PCL_OK;
@@ -72,8 +72,9 @@ int pcl_split(void* ctx, int species, double p) {
     SpeciesState& S = c->sp[species];
     long long n = 0;
     if (S.cap <= 0 || (rc = get_n(c, species, n)) || n == 0) return rc;
-    unsigned long long* lost = nullptr;
-    CK(cudaMallocAsync(&lost, sizeof(unsigned long long), c->stream));
+    // the lost count in the context's reusable scratch (no allocation per call)
+    if ((rc = ensure_scratch(c, 256))) return rc;
+    unsigned long long* lost = static_cast<unsigned long long*>(c->d_scr);
     CK(cudaMemsetAsync(lost, 0, sizeof(unsigned long long), c->stream));
     const int grid = int(std::min<long long>((n + 255) / 256, 8ll * c->sm_count));
     const float pf = float(p);
@@ -83,7 +84,6 @@ int pcl_split(void* ctx, int species, double p) {
     CK(cudaGetLastError());
     unsigned long long hl = 0;
     CK(cudaMemcpyAsync(&hl, lost, sizeof(hl), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaFreeAsync(lost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     long long nn = 0;
     if ((rc = get_n(c, species, nn))) return rc;
