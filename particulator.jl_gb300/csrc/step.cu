@@ -1841,6 +1841,17 @@ __global__ void k_swarm_moments(const float4* xw, const float4* ps, const uint4*
     const int len = 6 * nswarm;
     for (int i = threadIdx.x; i < len; i += blockDim.x) acc[i] = 0.0;
     __syncthreads();
+    // the warp's running sums of its current swarm, in double-float (a shared
+    // FP64 atomic is a compare-and-swap loop on GB300): flushed to shared
+    // memory when the swarm changes and at the end
+    float rh[6] = {0, 0, 0, 0, 0, 0}, rl[6] = {0, 0, 0, 0, 0, 0};
+    int cur = -1;
+    auto flush = [&]() {
+        if (cur >= 0 && (threadIdx.x & 31) == 0)
+            for (int q = 0; q < 6; ++q) atomicAdd(&acc[6 * cur + q], double(rh[q]) + double(rl[q]));
+        for (int q = 0; q < 6; ++q) { rh[q] = 0.0f; rl[q] = 0.0f; }
+        cur = -1;
+    };
     for (long long i0 = (long long)blockIdx.x * blockDim.x; i0 < n; i0 += (long long)gridDim.x * blockDim.x) {
         long long i = i0 + threadIdx.x;
         bool live = false;
@@ -1863,13 +1874,17 @@ __global__ void k_swarm_moments(const float4* xw, const float4* ps, const uint4*
         if (!act) continue;
         const int sw0 = __shfl_sync(FULL, sw, __ffs(act) - 1);
         if (__all_sync(FULL, !live || sw == sw0)) {
-            // the usual case (swarms are contiguous): one butterfly sum per value
+            // the usual case (swarms are contiguous): one butterfly sum per value,
+            // added to the warp's running sums
+            if (sw0 != cur) { flush(); cur = sw0; }
             for (int q = 0; q < 6; ++q) {
                 float t = v[q];
                 for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(FULL, t, o);
-                if ((threadIdx.x & 31) == 0) atomicAdd(&acc[6 * sw0 + q], double(t));
+                df_acc(rh[q], rl[q], t);
             }
-        } else if (live) {
+        } else {
+            flush();
+            if (!live) continue;
             unsigned grp = __match_any_sync(act, sw);
             int leader = __ffs(grp) - 1;
             for (int q = 0; q < 6; ++q) {
@@ -1879,6 +1894,7 @@ __global__ void k_swarm_moments(const float4* xw, const float4* ps, const uint4*
             }
         }
     }
+    flush();
     __syncthreads();
     for (int i = threadIdx.x; i < len; i += blockDim.x) partial[(size_t)blockIdx.x * len + i] = acc[i];
 }
