@@ -197,3 +197,46 @@ def test_step_with_learned_samplers(pcl, air, setup):
     c3 = np.sqrt(-0.5 * np.log(0.0027 / 2))
     assert _ks(np.log(k0), np.log(k1)) <= c3 * np.sqrt((n0 + n1) / (n0 * n1))
     assert e1[5] == 0 and e1[6] == 0, e1   # no capacity or kinematics errors
+
+
+def test_learned_multistep_launches(pcl, air, setup):
+    """The learned round with several steps per launch: a collision suspended
+    at any step of a launch is finished after the launch by the resume pass,
+    which carries the particle through the launch's remaining steps.  Eight
+    25-ps steps at 8 steps per launch leave the particles of one step per
+    launch (the same operations per particle; the launch shape only changes
+    the rounding of a step's sub-eps remainder, so a few particles may differ
+    in the last bits)."""
+    mp0, et, sb, mo, nets = setup
+    states, stats = [], []
+    for K in (1, 8):
+        rng = np.random.default_rng(43)
+        n = 1 << 16
+        p = pcl.workloads.isotropic(n, 1e6 * pcl.co.eV, rng)
+        arr = pcl.ParticleArrays(np.zeros((n, 3)), p, np.ones(n), np.zeros(n))
+        mp = pcl.MultiPopulation(
+            ("electron", pcl.Population(n * 2, arr, air["tabs"][0], air["cuts"][0], particle=pcl.Electron)),
+            ("photon", pcl.Population(n, [], air["tabs"][1], air["cuts"][1], particle=pcl.Photon)),
+            ("positron", pcl.Population(1 << 14, [], air["tabs"][2], air["cuts"][2], particle=pcl.Positron)),
+            seed=9, steps_per_launch=K)
+        for j in sb:
+            mp.set_learned(pcl.Electron, j, pcl.learned.LEARN_SB, nets[sb[0]][0])
+        for j in mo:
+            mp.set_learned(pcl.Electron, j, pcl.learned.LEARN_MOLLER, nets[mo[0]][0])
+        pusher = pcl.workloads.pusher((0.0, 0.0, -5e5), cl=air["cl"])
+        pcl.run(mp, pusher, 8 * 25e-12, 25e-12)
+        t = mp.tallies()
+        assert not any(t.errors[q] for q in (2, 3, 5, 6)), list(t.errors)
+        stats.append((mp.learn_stats(), list(t.live), [t.spawned[q] for q in range(3)]))
+        states.append([mp.get(q).particles() for q in (0, 1, 2)])
+        mp.close()
+    (s1, live1, sp1), (s8, live8, sp8) = stats
+    assert s1[0] > 100 and s8[0] > 100, (s1, s8)
+    assert s8[1] < s1[1]                       # one learned round per launch
+    for q in range(3):
+        assert abs(live1[q] - live8[q]) <= 2 + live1[q] // 1000, (live1, live8)
+        a, b = states[0][q], states[1][q]
+        common, ia, ib = np.intersect1d(a.sid, b.sid, return_indices=True)
+        assert len(common) >= 0.999 * max(len(a.sid), len(b.sid)) - 2
+        dp = np.linalg.norm(a.p[ia] - b.p[ib], axis=1) / np.maximum(np.linalg.norm(b.p[ib], axis=1), 1e-300)
+        assert np.mean(dp > 1e-4) <= 2e-3, np.sort(dp)[-5:]
