@@ -192,7 +192,7 @@ int pcl_swarm_moments(void* ctx, int species, int nswarm, double* out) {
     } else {
         CK(cudaMemsetAsync(part, 0, sizeof(double) * len * blocks, c->stream));
     }
-    k_swarm_reduce<<<(len + 255) / 256, 256, 0, c->stream>>>(part, blocks, len, d);
+    k_swarm_reduce<<<(len + 7) / 8, 256, 0, c->stream>>>(part, blocks, len, d);   // one warp per value
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(out, d, sizeof(double) * len, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));

