@@ -241,5 +241,6 @@ def test_learned_multistep_launches(pcl, air, setup):
         common, ia, ib = np.intersect1d(a.sid, b.sid, return_indices=True)
         assert len(common) >= 0.999 * max(len(a.sid), len(b.sid)) - 2
         dp = np.linalg.norm(a.p[ia] - b.p[ib], axis=1) / np.maximum(np.linalg.norm(b.p[ib], axis=1), 1e-300)
-        assert np.mean(dp > 1e-4) <= 5e-3, np.sort(dp)[-5:]
+        # drifted particles: a few per thousand, and at most two in a small species
+        assert np.count_nonzero(dp > 1e-4) <= 2 + 5e-3 * len(dp), np.sort(dp)[-5:]
         assert np.median(dp) == 0.0
