@@ -823,7 +823,7 @@ def main():
     ap.add_argument("--no-forms", action="store_true", help="skip the batched and learned sub-objects")
     ap.add_argument("--steps-per-launch", type=int, default=0,
                     help="steps per launch of the timed run! (0: chosen by the library's autotuner)")
-    ap.add_argument("--tune-budget", type=int, default=1152, help="steps the autotuner may use (untimed)")
+    ap.add_argument("--tune-budget", type=int, default=1344, help="steps the autotuner may use (untimed)")
     ap.add_argument("--bps", type=int, default=0, help="step-kernel blocks per SM (2, 3, 4)")
     ap.add_argument("--classic", type=int, default=0, help="1: classic step kernel (lanes collide in place)")
     ap.add_argument("--graph", type=int, default=0, help="1: launch groups replayed from CUDA graphs")
@@ -831,7 +831,7 @@ def main():
     ap.add_argument("--workload", default="rrea16M",
                     choices=["rrea16M", "swarms", "learned", "plain", "reid", "reid-fp64", "mlp", "kernels"])
     ap.add_argument("--nswarm", type=int, default=256)
-    ap.add_argument("--tune-steps", type=int, default=1152)
+    ap.add_argument("--tune-steps", type=int, default=1344)
     ap.add_argument("--learned-n", type=int, default=1 << 24, help="learned form: particles")
     ap.add_argument("--learned-spl", type=int, default=64, help="learned form: steps per launch (both forms)")
     ap.add_argument("--reid-groups", type=int, default=0, help="reid: batch-means errors from particle snapshots")

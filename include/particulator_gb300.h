@@ -465,11 +465,12 @@ int pcl_compact_noalloc(int64_t n, const float* xw, const float* ps, const uint3
  * depend on the launch parameters) while a coordinate search times candidate
  * launch shapes with CUDA events: step kernel {event, classic with 2, 3, 4
  * blocks per SM}, steps per launch {1, 2, 4, 8, 16, 32, 64}, compaction
- * period {2, 4, 8, 16, 32}, graph replay {0, 1}, in that order, each trial
- * max(64, steps_budget / 18 rounded down to a multiple of 64) steps, a whole
- * number of launches; the search stops when the budget is spent (a full
- * search takes 18 x 64 = 1152 steps).  The context keeps the fastest shape
- * (particle-steps per second). */
+ * period {2, 4, 8, 16, 32}, graph replay {0, 1}, in that order, then the
+ * other step kernels once more at the chosen shape (the best kernel depends
+ * on the steps per launch); each trial max(64, steps_budget / 21 rounded down
+ * to a multiple of 64) steps, a whole number of launches; the search stops
+ * when the budget is spent (a full search takes 21 x 64 = 1344 steps).  The
+ * context keeps the fastest shape (particle-steps per second). */
 typedef struct pcl_tune_result {
     int32_t blocks_per_sm, steps_per_launch, compaction_period, use_graph;   /* blocks_per_sm 0: event kernel */
     double  rate;              /* particle-steps per second of the kept shape */

@@ -1183,11 +1183,12 @@ int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* ou
     CK(cudaSetDevice(c->device));
     // step kernel: 0 = event, 2-4 = classic with that many blocks per SM
     const int bps_c[] = {0, 2, 3, 4}, k_c[] = {1, 2, 4, 8, 16, 32, 64}, per_c[] = {2, 4, 8, 16, 32}, g_c[] = {0, 1};
-    const int ntrials = 4 + 7 + 5 + 2;
+    const int ntrials = 4 + 7 + 5 + 2 + 3;
     // steps per trial: a multiple of the largest steps-per-launch tried (64),
     // so that every trial is a whole number of launches; a budget below
     // ntrials x 64 steps ends the search early (the candidates are tried in
-    // the order above)
+    // the order above, then the other step kernels once more at the chosen
+    // steps per launch, compaction period and graph setting)
     int len = std::max(64, (steps_budget / ntrials) / 64 * 64);
     pcl_config best = c->cfg;
     best.blocks_per_sm = (c->cfg.classic_step == 0) ? 4 : blocks_per_sm(c);
@@ -1237,6 +1238,16 @@ int pcl_autotune(void* ctx, double dt, int32_t steps_budget, pcl_tune_result* ou
     for (int v : per_c) { pcl_config q = after_k; q.compaction_period = v; if ((rc = consider(q))) return rc; }
     const pcl_config after_p = best;
     for (int v : g_c) { pcl_config q = after_p; q.use_graph = v; if ((rc = consider(q))) return rc; }
+    // the best kernel depends on the launch shape: a second pass over the others
+    const pcl_config after_g = best;
+    for (int v : bps_c) {
+        const bool same = (v == 0) ? after_g.classic_step == 0 : (after_g.classic_step != 0 && after_g.blocks_per_sm == v);
+        if (same) continue;
+        pcl_config q = after_g;
+        q.classic_step = (v == 0) ? 0 : 1;
+        q.blocks_per_sm = (v == 0) ? 4 : v;
+        if ((rc = consider(q))) return rc;
+    }
     c->cfg = best;
     if (out) {
         std::memset(out, 0, sizeof(*out));

@@ -39,7 +39,9 @@
 namespace pcl {
 
 constexpr int   kWarpStack   = 32;          // child-stack entries per warp
-constexpr int   kCollStash   = 64;          // event kernel: parked collisions per warp
+constexpr int   kCollStash   = 72;          // event kernel: per-warp entries, parked collisions from the
+                                            // bottom and held particles from the top
+constexpr int   kBatchMin    = 24;          // event kernel: free lanes that collide without the hold
 constexpr int   kRejectCap   = 10000;       // rejection-loop iteration cap
 constexpr int   kSubstepCap  = 1 << 20;     // sub-steps per particle per step
 constexpr float kEpsT        = 2.220446049250313e-7f;  // eps(Float64) s in ns (mixed_population.jl:66)
@@ -53,7 +55,8 @@ constexpr int T_DEAD = 54;             // [3]
 constexpr int T_ERR = 57;              // [8]
 constexpr int T_LEND = 65;             // [64][3]
 constexpr int T_LSTART = T_LEND + 3 * PCL_MAX_STEPS_PER_LAUNCH;  // [64]
-constexpr int T_WORDS = T_LSTART + PCL_MAX_STEPS_PER_LAUNCH;     // 321
+constexpr int T_FLY = T_LSTART + PCL_MAX_STEPS_PER_LAUNCH;       // [64] photon flights over whole steps (differences)
+constexpr int T_WORDS = T_FLY + PCL_MAX_STEPS_PER_LAUNCH;         // 385
 
 // ------------------------------------------------------------ Philox ----
 __device__ __forceinline__ void philox4x32_10(uint32_t& c0, uint32_t& c1, uint32_t& c2, uint32_t& c3,
@@ -1177,10 +1180,12 @@ __device__ __forceinline__ void put_slot(const StepArgs& A, int sp, long long sl
 
 // ------------------------------------------------------------ the step ---
 // EVENT: colliding particles are parked in a per-warp stash and collided in
-// batches that fill the warp's free lanes (see the loop), instead of each lane
-// colliding as soon as its push ends; each particle's sequence of operations
-// is unchanged.
-template <int MINB, bool GENERAL, bool EVENT, bool LEARN>
+// batches (the warp's free lanes, or, in MULTI, all 32 lanes with the lanes'
+// other particles held in the stash meanwhile; see the loop), instead of each
+// lane colliding as soon as its push ends; each particle's sequence of
+// operations is unchanged.  MULTI: the instance for launches of several steps
+// (the hold, guided chunks per species range, photon flights over whole steps).
+template <int MINB, bool GENERAL, bool EVENT, bool LEARN, bool MULTI>
 __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     // a queue pass over an empty queue has nothing to stage, run or tally
     if (A.spill_mode == 1 && *A.sp_in_n == 0) return;
@@ -1199,14 +1204,16 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     unsigned long long* mbar =
         reinterpret_cast<unsigned long long*>(reinterpret_cast<uintptr_t>(tal + T_WORDS + 8) & ~uintptr_t(7));
     // event kernel: collision stash after the mbarrier (16-B aligned), counters after it
+    // (parked collisions, then held particles, one of each per warp)
     float4* cs_all = reinterpret_cast<float4*>((reinterpret_cast<uintptr_t>(mbar + 1) + 15) & ~uintptr_t(15));
     int* cs_ns = reinterpret_cast<int*>(cs_all + size_t(nwarps) * kCollStash * 5);
     float4* cs = cs_all + size_t(warp) * kCollStash * 5;
     int* cs_n = cs_ns + warp;
+    int* hd_n = cs_ns + nwarps + warp;
 
     for (int i = threadIdx.x; i < T_WORDS; i += blockDim.x) tal[i] = 0u;
     if (lane == 0) tops[warp] = 0;
-    if (EVENT && lane == 0) *cs_n = 0;
+    if (EVENT && lane == 0) { *cs_n = 0; *hd_n = 0; }
     bool ok = stage_blob(smem, A.blob, A.blob_bytes, mbar);
     if (__syncthreads_or(!ok)) {
         if (threadIdx.x == 0) atomicExch(&A.ctl->timeout, 1);
@@ -1259,24 +1266,48 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     bool has = false;
 
     for (;;) {
-        // ---------------- event kernel: collide parked particles in the free
-        // lanes once the stash can fill all of them (or nothing else is left)
+        // ---------------- event kernel: collide parked particles in batches.
+        // Mode 1: the free lanes, when the stash fills at least kBatchMin of
+        // them (or all of them once the input is taken, or nothing else is
+        // left).  Mode 2: all 32 lanes, once 32 collisions are parked; the
+        // lanes' particles between collisions wait in the hold (the top of the
+        // stash) and refill free lanes before children and input do.
         if (EVENT) {
             const unsigned empty = __ballot_sync(FULL, !has);
             __syncwarp();
             const int nstash = *cs_n;
+            const int nh = MULTI ? *hd_n : 0;
             const int ne = __popc(empty);
             const bool drain = input_done && *K.top == 0;
-            if (ne > 0 && nstash > 0 && (nstash >= ne || drain)) {
-                const int take = min(ne, nstash);
-                const int rank = __popc(empty & lt);
+            int mode = 0;
+            if (!MULTI) {
+                if (ne > 0 && nstash > 0 && (nstash >= ne || drain)) mode = 1;
+            } else if (ne > 0 && nstash > 0 && ((nstash >= ne && (ne >= kBatchMin || input_done)) || drain)) {
+                mode = 1;
+            } else if (nstash >= 32 && nstash + nh + (32 - ne) <= kCollStash) {
+                mode = 2;
+            }
+            if (mode) {
+                int take, rank;
+                if (MULTI && mode == 2) {
+                    if (has) park_lane(L, cs + size_t(kCollStash - 1 - nh - __popc(~empty & lt)) * 5);
+                    has = false;
+                    take = 32;
+                    rank = lane;
+                } else {
+                    take = min(ne, nstash);
+                    rank = __popc(empty & lt);
+                }
                 if (!has && rank < take) {
                     unpark_lane(L, cs + size_t(nstash - 1 - rank) * 5);
                     has = true;
                     collide<LEARN>(L, K, H->sp[L.species]);
                 }
                 __syncwarp();
-                if (lane == 0) *cs_n = nstash - take;
+                if (lane == 0) {
+                    *cs_n = nstash - take;
+                    if (MULTI && mode == 2) *hd_n = nh + (32 - ne);
+                }
                 __syncwarp();
             }
         }
@@ -1284,6 +1315,21 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
         unsigned need = __ballot_sync(FULL, !has);
         if (need) {
             __syncwarp();
+            if (EVENT && MULTI) {  // held particles first (the newest at the lowest index)
+                const int nh = *hd_n;
+                if (nh > 0) {
+                    const int take = min(__popc(need), nh);
+                    const int rank = __popc(need & lt);
+                    if (!has && rank < take) {
+                        unpark_lane(L, cs + size_t(kCollStash - nh + rank) * 5);
+                        has = true;
+                    }
+                    __syncwarp();
+                    if (lane == 0) *hd_n = nh - take;
+                    __syncwarp();
+                    need = __ballot_sync(FULL, !has);
+                }
+            }
             int top = *K.top;
             if (top > kWarpStack) top = kWarpStack;
             int take = min(__popc(need), top);
@@ -1310,8 +1356,15 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 if (cur >= end) {
                     long long base = 0, len = 0;
                     if (lane == 0) {
+                        // guided chunks over what is left of the work or, in a
+                        // launch of several steps, of the current species' range
+                        // (the species differ in cost per slot: a range's last
+                        // chunks stay small whatever follows it)
                         long long done_est = (long long)(*(volatile unsigned long long*)A.head);
-                        long long rem = total - done_est;
+                        long long rend = total;
+                        if (MULTI && done_est < nsp0 - g0) rend = min(total, nsp0 - g0);
+                        else if (MULTI && done_est < nsp0 + nsp1 - g0) rend = min(total, nsp0 + nsp1 - g0);
+                        long long rem = rend - done_est;
                         long long chunk = rem / (4 * nwarps_grid);
                         chunk = chunk < 32 ? 32 : (chunk > 1024 ? 1024 : chunk);
                         base = (long long)atomicAdd(A.head, (unsigned long long)chunk);
@@ -1386,7 +1439,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
         }
         if (__ballot_sync(FULL, has) == 0u) {
             // no work in this warp; the stack is empty because it is drained first
-            if (input_done && (!EVENT || *cs_n == 0)) break;
+            if (input_done && (!EVENT || (*cs_n == 0 && (!MULTI || *hd_n == 0)))) break;
             continue;
         }
 
@@ -1434,21 +1487,45 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         L.nsub = 0;
                         dd_add(L.th, L.tlo, dt_hi, dt_lo);  // remainder below eps carries over (mixed_population.jl:65)
                         L.r = setr(S, K, E, L.sw);  // advance_init! of the next step
-                        atomicAdd(&tal[T_LSTART + L.k], 1u);
+                        if (MULTI && !GENERAL && L.species == PCL_PHOTON) {
+                            // A photon's collision-free whole steps in this
+                            // iteration, each exactly as its own iteration would
+                            // run it (the same clock decision, decrement, push and
+                            // clock reset): no force acts on it and its energy, so
+                            // its rate bound (setr!) and the droplow! outcome, do
+                            // not change in flight.  The step that collides, and
+                            // the launch's last step, are left to the loop.
+                            const int k0 = L.k;
+                            while (L.k + 1 < nsteps && dd_val(L.th, L.tlo) > kEpsT) {
+                                const float tn = L.s / L.r;
+                                if (__fadd_rn(__fsub_rn(L.th, tn), L.tlo) > 0.0f) break;
+                                const float hh = dd_val(L.th, L.tlo);
+                                L.s -= hh * L.r;
+                                push<false>(L, S, K, hh);
+                                L.th = 0.0f; L.tlo = 0.0f;
+                                dd_add(L.th, L.tlo, dt_hi, dt_lo);
+                                L.k += 1;
+                            }
+                            if (L.k > k0) {  // live at the end of steps k0 .. L.k - 1
+                                atomicAdd(&tal[T_FLY + k0], 1u);
+                                atomicAdd(&tal[T_FLY + L.k], 0xffffffffu);
+                            }
+                        }
                     }
                 }
             }
         }
 
         if (EVENT) {
-            // park the colliding particles; if the stash is full (possible with
-            // several steps per launch, where lanes keep particles across steps)
-            // the rest collide in place
+            // park the colliding particles; if the stash is full (its parked
+            // collisions and held particles; possible with several steps per
+            // launch, where lanes keep particles across steps) the rest collide
+            // in place
             const unsigned pm = __ballot_sync(FULL, park);
             if (pm) {
                 __syncwarp();
                 const int base = *cs_n;
-                const int space = kCollStash - base;
+                const int space = kCollStash - base - (MULTI ? *hd_n : 0);
                 const int rank = __popc(pm & lt);
                 if (park) {
                     if (rank < space) {
@@ -1497,8 +1574,24 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 
     // ---------------- flush block tallies
     __syncthreads();
+    // photons flown through whole steps: T_FLY is a difference array over the
+    // steps (+1 at the first step flown, -1 after the last; modulo 2^32)
+    for (int j = threadIdx.x; j < nsteps - 1; j += blockDim.x) {
+        uint32_t f = 0;
+        for (int k = 0; k <= j; ++k) f += tal[T_FLY + k];
+        tal[T_LEND + 3 * j + PCL_PHOTON] += f;
+    }
+    __syncthreads();
     for (int i = threadIdx.x; i < T_WORDS; i += blockDim.x) {
         uint32_t v = tal[i];
+        // the particles that start step k >= 1 of the launch are those that
+        // ended step k - 1 (every boundary but the last ends one step and
+        // starts the next); only loaded slots count at step 0
+        const int ks = i - T_LSTART;
+        if (ks >= 1) {
+            const int e = T_LEND + 3 * (ks - 1);
+            v = ks < nsteps ? tal[e] + tal[e + 1] + tal[e + 2] : 0u;
+        }
         if (!v) continue;
         unsigned long long vv = v;
         if (i < T_NULL) atomicAdd(&ctl->coll[i / 16][i % 16], vv);
@@ -1507,7 +1600,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
         else if (i < T_ERR) atomicAdd(&ctl->dead[i - T_DEAD], vv);
         else if (i < T_LEND) atomicAdd(&ctl->err[i - T_ERR], vv);
         else if (i < T_LSTART) atomicAdd(&ctl->live_end[(i - T_LEND) / 3][(i - T_LEND) % 3], vv);
-        else atomicAdd(&ctl->live_start[i - T_LSTART], vv);
+        else if (i < T_FLY) atomicAdd(&ctl->live_start[i - T_LSTART], vv);
     }
 }
 
@@ -1517,18 +1610,22 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 // kernel in 3 (its stash), each with or without the learned samplers'
 // suspend/resume (LEARN); the general kernel (position-dependent field, wall
 // crossings; learned samplers included) in 3, where it needs no register
-// spills.  Code a launch does not use stays out of its kernel.
-static void (*step_kernel(int minb, bool general, bool event, bool learn))(StepArgs) {
-    if (general) return event ? k_step<3, true, true, true> : k_step<3, true, false, true>;
-    if (learn) return event ? k_step<3, false, true, true> : k_step<3, true, false, true>;
-    if (event) return k_step<3, false, true, false>;
-    return (minb == 2)   ? k_step<2, false, false, false>
-           : (minb == 3) ? k_step<3, false, false, false>
-                         : k_step<4, false, false, false>;
+// spills; the event kernel has a second instance for launches of several
+// steps (MULTI).  Code a launch does not use stays out of its kernel.
+static void (*step_kernel(int minb, bool general, bool event, bool learn, bool multi))(StepArgs) {
+    if (general) return event ? k_step<3, true, true, true, false> : k_step<3, true, false, true, false>;
+    if (learn) {
+        if (!event) return k_step<3, true, false, true, false>;
+        return multi ? k_step<3, false, true, true, true> : k_step<3, false, true, true, false>;
+    }
+    if (event) return multi ? k_step<3, false, true, false, true> : k_step<3, false, true, false, false>;
+    return (minb == 2)   ? k_step<2, false, false, false, false>
+           : (minb == 3) ? k_step<3, false, false, false, false>
+                         : k_step<4, false, false, false, false>;
 }
 
 cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream_t stream, const StepArgs& A) {
-    void (*kern)(StepArgs) = step_kernel(minb, A.general != 0, A.event != 0, A.learn != 0);
+    void (*kern)(StepArgs) = step_kernel(minb, A.general != 0, A.event != 0, A.learn != 0, A.nsteps > 1);
     // the shared-memory attribute is set outside stream capture (prepare_step
     // runs first); during capture the launch is only recorded
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -1546,13 +1643,17 @@ cudaError_t launch_step(int minb, int grid, int threads, size_t smem, cudaStream
 // setting an attribute between launches of a pipeline can hold the host back.
 cudaError_t launch_step_prepared(int minb, int grid, int threads, size_t smem, cudaStream_t stream,
                                  const StepArgs& A) {
-    step_kernel(minb, A.general != 0, A.event != 0, A.learn != 0)<<<grid, threads, smem, stream>>>(A);
+    step_kernel(minb, A.general != 0, A.event != 0, A.learn != 0, A.nsteps > 1)<<<grid, threads, smem, stream>>>(A);
     return cudaGetLastError();
 }
 
 cudaError_t prepare_step(int minb, size_t smem, bool general, bool event, bool learn) {
-    return cudaFuncSetAttribute(step_kernel(minb, general, event, learn), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(smem));
+    for (bool multi : {false, true}) {
+        cudaError_t e = cudaFuncSetAttribute(step_kernel(minb, general, event, learn, multi),
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 // Launch prologue: snapshot the work space and clear per-launch counters.
@@ -2287,7 +2388,7 @@ __global__ void k_draw_net_map(StepArgs A, int species, int j, int kind, long lo
 size_t step_smem_bytes(int blob_bytes, int threads, bool event) {
     int nw = threads / 32;
     size_t b = size_t(blob_bytes) + size_t(nw) * kWarpStack * 3 * 16 + size_t(nw) * 4 + T_WORDS * 4 + 64;
-    if (event) b += 16 + size_t(nw) * kCollStash * 5 * 16 + size_t(nw) * 4;
+    if (event) b += 16 + size_t(nw) * kCollStash * 5 * 16 + size_t(nw) * 8;
     return (b + 15) & ~size_t(15);
 }
 

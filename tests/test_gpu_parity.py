@@ -94,6 +94,43 @@ def test_multistep_launch_matches_plain(pcl, oracle, gpu, air):
     mp.close()
 
 
+@pytest.mark.parametrize("spl", [4, 16])
+def test_photons_fly_through_launch(pcl, oracle, gpu, air, spl):
+    """Photons whose clock runs past the end of a multi-step launch fly through
+    its remaining steps in one push.  Their per-step live counts (the
+    particle-steps, built from them) equal those of one-step launches, the
+    photons equal those launches' photons to FP32 rounding, and the population
+    matches the oracle."""
+    pusher = _pusher(pcl, air)
+    runs = []
+    for k in (1, spl):
+        mp = _mixed(pcl, air, n=(512, 16384, 128), seed=31, steps_per_launch=k)
+        pcl.run(mp, pusher, 32e-12, 1e-12)
+        runs.append(mp)
+    a, b = runs
+    ta, tb = a.tallies(), b.tallies()
+    assert ta.steps == tb.steps == 32
+    assert abs(ta.particle_steps - tb.particle_steps) <= 2, (ta.particle_steps, tb.particle_steps)
+    assert ta.particle_steps > 30 * 16000
+    for q in range(3):
+        assert abs(ta.live[q] - tb.live[q]) <= 1, (list(ta.live), list(tb.live))
+    pa, pb = a.get(pcl.Photon).particles(), b.get(pcl.Photon).particles()
+    common, ia, ib = np.intersect1d(pa.sid, pb.sid, return_indices=True)
+    assert len(common) >= len(pa.sid) - 2
+    np.testing.assert_allclose(pb.x[ib], pa.x[ia], rtol=1e-5, atol=1e-9)
+    np.testing.assert_allclose(pb.s[ib], pa.s[ia], rtol=1e-4, atol=1e-6)
+    assert np.array_equal(pb.p[ib], pa.p[ia]) or np.mean(np.any(pb.p[ib] != pa.p[ia], axis=1)) < 1e-3
+    a.close()
+    # the same run against the oracle, step by step
+    mp = _mixed(pcl, air, n=(512, 16384, 128), seed=31, steps_per_launch=spl)
+    W = _oracle_from(oracle, pcl, mp, air, pusher)
+    pcl.run(mp, pusher, 8e-12, 1e-12)
+    for k in range(8):
+        W.advance((k + 1) * 1e-12, 4)
+    _check(pcl, oracle, mp, W, rtol=3 * RTOL)
+    mp.close(); b.close()
+
+
 def test_graph_matches_plain(pcl, gpu, air):
     """Launch groups replayed from CUDA graphs (prologue, step, device-gated
     spill passes, compaction inside the graph) give bit-identical particles and
@@ -554,8 +591,8 @@ def test_population_target_stop(pcl, oracle, gpu, air, kind):
     species reaches the target.  A run without a target gives the per-step
     counts and the target; the run with it must stop on the first step that
     reaches it, with one step per launch and with eight (the launches shrink
-    near the target), leave the same particles in both, and match the oracle
-    stepped as many steps."""
+    near the target), leave the same particles in both (momenta equal to FP32
+    rounding), and match the oracle stepped as many steps."""
     dt, nsteps = 5e-12, 40
     rising = kind == "grow"
     seed = 70 if rising else 71
@@ -599,7 +636,12 @@ def test_population_target_stop(pcl, oracle, gpu, air, kind):
             assert rep["ok"], (K, q, str(rep))
         states[K] = [mp.get(q).particles() for q in (0, 1, 2)]
         mp.close()
-    for a, b in zip(states[1], states[8]):      # the launch shape does not change the physics
+    # the launch shape does not change the physics: the same particles, with
+    # momenta equal up to FP32 rounding (a collision batched with the warp's
+    # other parked collisions or, when the stash is full, collided in place
+    # may round its inlined arithmetic differently)
+    for a, b in zip(states[1], states[8]):
         oa, ob = np.argsort(a.sid), np.argsort(b.sid)
         np.testing.assert_array_equal(a.sid[oa], b.sid[ob])
-        np.testing.assert_array_equal(a.p[oa], b.p[ob])
+        dp = np.abs(a.p[oa] - b.p[ob]).max(axis=1) / np.maximum(np.abs(b.p[ob]).max(axis=1), 1e-300)
+        assert dp.max(initial=0.0) < 1e-5 and np.mean(dp > 0) <= 2e-3, np.sort(dp)[-5:]

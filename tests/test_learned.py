@@ -243,4 +243,4 @@ def test_learned_multistep_launches(pcl, air, setup):
         dp = np.linalg.norm(a.p[ia] - b.p[ib], axis=1) / np.maximum(np.linalg.norm(b.p[ib], axis=1), 1e-300)
         # drifted particles: a few per thousand, and at most two in a small species
         assert np.count_nonzero(dp > 1e-4) <= 2 + 5e-3 * len(dp), np.sort(dp)[-5:]
-        assert np.median(dp) == 0.0
+        assert len(dp) == 0 or np.median(dp) == 0.0
