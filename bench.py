@@ -124,21 +124,21 @@ def _peaks():
 
 # DRAM bytes (read + write) per slot of one k_step launch, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the event kernel on
-# a 4 M-particle draw of the same mixed state at the commit named below (the
-# step kernel's source has not changed since); scaled to a launch by the slots
+# a 4 M-particle draw of the same mixed state at the commit named below;
+# scaled to a launch by the slots
 # it processes: the reads grow in proportion, the writes are bounded by 48 B
 # per slot.
 K_STEP_DRAM_BYTES_PER_SLOT = 85.0
 K_STEP_DRAM_CAPTURE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 4th k_step launch of "
                        "'bench.py --n 4194304 --steps 3 --warmup 3 --steps-per-launch 1 --no-cpu --no-e2e --no-forms' at commit "
-                       "c0c1db4: 201.8 MB read + 154.6 MB written over 4.19 M slots")
+                       "463b944: 201.8 MB read + 154.6 MB written over 4.19 M slots")
 
 # Warp instructions per particle-step of the event step kernel on a 4 M draw
 # of the same state, by steps per launch (ncu smsp__inst_executed.sum of one
-# launch over its particle-steps; commits c0c1db4 and cb28eba, the kernel's
-# source unchanged between them), for the issue ceiling: 152 SMs x 4
-# schedulers x 2.07 GHz warp instructions per second.
-K_STEP_WARP_INST_PER_PSTEP = {1: 47.7, 16: 55.2, 64: 55.1}
+# launch over its particle-steps, commit 463b944: the one-step instance, and
+# the multi-step instance at 64 steps per launch), for the issue ceiling:
+# 152 SMs x 4 schedulers x 2.07 GHz warp instructions per second.
+K_STEP_WARP_INST_PER_PSTEP = {1: 48.6, 64: 42.8}
 ISSUE_RATE = 152 * 4 * 2.07e9
 
 WORKLOAD = "rrea-air-0.5MVm-mixed-16M"
