@@ -1264,6 +1264,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     Lane L;
     L.slot = -1; L.alive = false; L.rvalid = false;
     bool has = false;
+    bool pend = false;  // event kernel: a collision that found the stash full, collided next
 
     for (;;) {
         // ---------------- event kernel: collide parked particles in batches.
@@ -1271,9 +1272,12 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
         // them (or all of them once the input is taken, or nothing else is
         // left).  Mode 2: all 32 lanes, once 32 collisions are parked; the
         // lanes' particles between collisions wait in the hold (the top of the
-        // stash) and refill free lanes before children and input do.
+        // stash) and refill free lanes before children and input do.  Lanes
+        // whose collision found the stash full collide here too, in their
+        // lane, before any other push (one call site of the samplers).
         if (EVENT) {
             const unsigned empty = __ballot_sync(FULL, !has);
+            const bool anyp = __any_sync(FULL, pend);
             __syncwarp();
             const int nstash = *cs_n;
             const int nh = MULTI ? *hd_n : 0;
@@ -1284,12 +1288,14 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 if (ne > 0 && nstash > 0 && (nstash >= ne || drain)) mode = 1;
             } else if (ne > 0 && nstash > 0 && ((nstash >= ne && (ne >= kBatchMin || input_done)) || drain)) {
                 mode = 1;
-            } else if (nstash >= 32 && nstash + nh + (32 - ne) <= kCollStash) {
+            } else if (!anyp && nstash >= 32 && nstash + nh + (32 - ne) <= kCollStash) {
                 mode = 2;
             }
-            if (mode) {
-                int take, rank;
-                if (MULTI && mode == 2) {
+            if (mode || anyp) {
+                int take = 0, rank = 0;
+                if (!mode) {
+                    // only the pending collisions
+                } else if (MULTI && mode == 2) {
                     if (has) park_lane(L, cs + size_t(kCollStash - 1 - nh - __popc(~empty & lt)) * 5);
                     has = false;
                     take = 32;
@@ -1298,13 +1304,18 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                     take = min(ne, nstash);
                     rank = __popc(empty & lt);
                 }
+                bool doit = pend;
                 if (!has && rank < take) {
                     unpark_lane(L, cs + size_t(nstash - 1 - rank) * 5);
                     has = true;
+                    doit = true;
+                }
+                if (doit) {
+                    pend = false;
                     collide<LEARN>(L, K, H->sp[L.species]);
                 }
                 __syncwarp();
-                if (lane == 0) {
+                if (lane == 0 && mode) {
                     *cs_n = nstash - take;
                     if (MULTI && mode == 2) *hd_n = nh + (32 - ne);
                 }
@@ -1519,8 +1530,8 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
         if (EVENT) {
             // park the colliding particles; if the stash is full (its parked
             // collisions and held particles; possible with several steps per
-            // launch, where lanes keep particles across steps) the rest collide
-            // in place
+            // launch, where lanes keep particles across steps) the rest stay
+            // in their lanes and collide at the start of the next iteration
             const unsigned pm = __ballot_sync(FULL, park);
             if (pm) {
                 __syncwarp();
@@ -1532,7 +1543,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         park_lane(L, cs + size_t(base + rank) * 5);
                         has = false;
                     } else {
-                        collide<LEARN>(L, K, H->sp[L.species]);
+                        pend = true;
                     }
                 }
                 __syncwarp();
