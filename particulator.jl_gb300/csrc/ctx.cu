@@ -474,8 +474,11 @@ PCL_INTERNAL cudaError_t enqueue_learned_round(Ctx* c, double dt, int nsteps, in
     StepArgs R = make_args(c, dt, nsteps, 2, 0);   // spill output: queue 1
     set_lq(R, c, 1, 0);
     R.lq_out_n = nullptr;
-    // queue-driven passes take any grid: one block per SM
-    if ((e = launch_step(minb, c->sm_count, threads, smem, c->stream, R)) != cudaSuccess) return e;
+    // queue-driven passes take any grid: one block per SM, or the persistent
+    // grid when the launch has several steps (the resumed particles then carry
+    // the rest of the launch's steps)
+    const int rgrid = nsteps > 1 ? grid_blocks(c) : c->sm_count;
+    if ((e = launch_step(minb, rgrid, threads, smem, c->stream, R)) != cudaSuccess) return e;
     for (int in = 1, pass = 0; pass < 2; ++pass, in = 1 - in) {
         k_begin_spill<<<1, 32, 0, c->stream>>>(c->d_ctl, c->d_spn + in, c->d_spn + (1 - in));
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
