@@ -128,17 +128,17 @@ def _peaks():
 # scaled to a launch by the slots
 # it processes: the reads grow in proportion, the writes are bounded by 48 B
 # per slot.
-K_STEP_DRAM_BYTES_PER_SLOT = 85.0
+K_STEP_DRAM_BYTES_PER_SLOT = 84.9
 K_STEP_DRAM_CAPTURE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 4th k_step launch of "
                        "'bench.py --n 4194304 --steps 3 --warmup 3 --steps-per-launch 1 --no-cpu --no-e2e --no-forms' at commit "
-                       "463b944: 201.8 MB read + 154.6 MB written over 4.19 M slots")
+                       "b3cc758: 201.8 MB read + 154.3 MB written over 4.19 M slots")
 
 # Warp instructions per particle-step of the event step kernel on a 4 M draw
 # of the same state, by steps per launch (ncu smsp__inst_executed.sum of one
-# launch over its particle-steps, commit 463b944: the one-step instance, and
+# launch over its particle-steps, commit b3cc758: the one-step instance, and
 # the multi-step instance at 64 steps per launch), for the issue ceiling:
 # 152 SMs x 4 schedulers x 2.07 GHz warp instructions per second.
-K_STEP_WARP_INST_PER_PSTEP = {1: 48.6, 64: 42.8}
+K_STEP_WARP_INST_PER_PSTEP = {1: 46.8, 64: 41.3}
 ISSUE_RATE = 152 * 4 * 2.07e9
 
 WORKLOAD = "rrea-air-0.5MVm-mixed-16M"
