@@ -120,6 +120,8 @@ typedef struct pcl_process {
 } pcl_process;
 
 /* ---- context configuration --------------------------------------------- */
+#define PCL_STASH_MAX 72   /* event kernel: collision-stash entries per warp */
+
 typedef struct pcl_config {
     uint64_t seed;             /* Philox4x32-10 key for every particle stream        */
     int32_t  device;           /* CUDA device ordinal                                 */
@@ -132,7 +134,10 @@ typedef struct pcl_config {
     int32_t  classic_step;     /* 0 (default): colliding particles are parked and collided in
                                   full-warp batches (event kernel, 3 blocks per SM); 1: each
                                   lane collides in place (blocks_per_sm applies)            */
-    int32_t  reserved[2];
+    int32_t  stash_entries;    /* event kernel: entries per warp of its collision stash in use
+                                  (0 = all PCL_STASH_MAX; fewer, so that collisions find it
+                                  full more often: the results do not depend on it)         */
+    int32_t  reserved;
 } pcl_config;
 
 /* ---- per-context tallies (FP64 / int64 on the device) -------------------- */

@@ -66,7 +66,7 @@ class Process(C.Structure):
 class Config(C.Structure):
     _fields_ = [("seed", _u64), ("device", _i32), ("block_size", _i32), ("grid_blocks", _i32),
                 ("steps_per_launch", _i32), ("compaction_period", _i32), ("use_graph", _i32),
-                ("blocks_per_sm", _i32), ("classic_step", _i32), ("reserved", _i32 * 2)]
+                ("blocks_per_sm", _i32), ("classic_step", _i32), ("stash_entries", _i32), ("reserved", _i32)]
 
 
 class Tallies(C.Structure):

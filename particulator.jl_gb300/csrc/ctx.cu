@@ -287,6 +287,7 @@ PCL_INTERNAL StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, i
     for (int s = 0; s < 3; ++s)
         if (c->sp[s].wall_coord >= 0 && c->wall_cap > 0) A.general = 1;
     A.event = (c->cfg.classic_step == 0) ? 1 : 0;
+    A.stash = c->cfg.stash_entries > 0 ? c->cfg.stash_entries : PCL_STASH_MAX;
     if (c->learn_on) {  // suspended collisions go to queue 0 unless set_lq says otherwise
         A.lq_out_xw = c->lq_xw[0]; A.lq_out_ps = c->lq_ps[0]; A.lq_out_m1 = c->lq_m1[0]; A.lq_out_m2 = c->lq_m2[0];
         A.lq_out_n = c->d_lqn;
@@ -721,6 +722,7 @@ int pcl_create(const pcl_config* cfg, void** out) {
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return PCL_ERR_CUDA;
     if (cfg->device < 0 || cfg->device >= ndev) return PCL_ERR_INVALID;
     if (cfg->steps_per_launch > PCL_MAX_STEPS_PER_LAUNCH) return PCL_ERR_INVALID;
+    if (cfg->stash_entries < 0 || cfg->stash_entries > PCL_STASH_MAX) return PCL_ERR_INVALID;
     Ctx* c = new Ctx();
     c->cfg = *cfg;
     c->device = cfg->device;

@@ -159,6 +159,7 @@ struct StepArgs {
     long long wall_cap;
     int general;    // a position-dependent field or a wall is set: the general step kernel runs
     int event;      // the event step kernel runs (parked collisions in full-warp batches)
+    int stash;      // event kernel: stash entries per warp in use (1 to PCL_STASH_MAX)
     int learn;      // learned samplers attached: the kernel with suspend/resume runs
     // population launches over part of the work: concatenated indices
     // [g_lo, g_hi) of the species ranges (g_hi == 0: all of them)

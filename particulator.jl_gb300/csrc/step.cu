@@ -39,7 +39,7 @@
 namespace pcl {
 
 constexpr int   kWarpStack   = 32;          // child-stack entries per warp
-constexpr int   kCollStash   = 72;          // event kernel: per-warp entries, parked collisions from the
+constexpr int   kCollStash   = PCL_STASH_MAX;  // event kernel: per-warp entries, parked collisions from the
                                             // bottom and held particles from the top
 constexpr int   kBatchMin    = 24;          // event kernel: free lanes that collide without the hold
 constexpr int   kRejectCap   = 10000;       // rejection-loop iteration cap
@@ -1305,7 +1305,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 if (ne > 0 && nstash > 0 && (nstash >= ne || drain)) mode = 1;
             } else if (ne > 0 && nstash > 0 && ((nstash >= ne && (ne >= kBatchMin || input_done)) || drain)) {
                 mode = 1;
-            } else if (!anyp && nstash >= 32 && nstash + nh + (32 - ne) <= kCollStash) {
+            } else if (!anyp && nstash >= 32 && nstash + nh + (32 - ne) <= A.stash) {
                 mode = 2;
             }
             if (mode || anyp) {
@@ -1548,12 +1548,15 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
             // park the colliding particles; if the stash is full (its parked
             // collisions and held particles; possible with several steps per
             // launch, where lanes keep particles across steps) the rest stay
-            // in their lanes and collide at the start of the next iteration
+            // in their lanes and collide at the start of the next iteration.
+            // A.stash entries are in use: parked collisions from the bottom,
+            // held particles from the top of all kCollStash, and together at
+            // most A.stash, so the two never meet
             const unsigned pm = __ballot_sync(FULL, park);
             if (pm) {
                 __syncwarp();
                 const int base = *cs_n;
-                const int space = kCollStash - base - (MULTI ? *hd_n : 0);
+                const int space = A.stash - base - (MULTI ? *hd_n : 0);
                 const int rank = __popc(pm & lt);
                 if (park) {
                     if (rank < space) {

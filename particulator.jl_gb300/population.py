@@ -218,7 +218,7 @@ class MultiPopulation:
 
     def __init__(self, *pairs, seed: int = 0, device: int = 0, steps_per_launch: int = 1,
                  compaction_period: int = 0, block_size: int = 0, grid_blocks: int = 0, blocks_per_sm: int = 0,
-                 use_graph: bool = False, classic_step: bool = False, **named):
+                 use_graph: bool = False, classic_step: bool = False, stash_entries: int = 0, **named):
         index = {}
         for name, pop in list(pairs) + list(named.items()):
             key = SPECIES_BY_NAME[name] if isinstance(name, str) else int(name)
@@ -234,6 +234,7 @@ class MultiPopulation:
         cfg.blocks_per_sm = blocks_per_sm
         cfg.use_graph = 1 if use_graph else 0
         cfg.classic_step = 1 if classic_step else 0
+        cfg.stash_entries = stash_entries
         self.config = cfg
         h = C.c_void_p()
         rc = _lib.lib().pcl_create(C.byref(cfg), C.byref(h))

@@ -131,6 +131,38 @@ def test_photons_fly_through_launch(pcl, oracle, gpu, air, spl):
     mp.close(); b.close()
 
 
+@pytest.mark.parametrize("spl", [1, 8])
+def test_full_stash_same_results(pcl, gpu, air, spl):
+    """A collision that finds its warp's stash full stays in its lane and
+    collides at the start of the next iteration.  With 8 or 40 of the stash's
+    entries in use that happens all the time (the full stash of 72 rarely
+    fills on these populations), and the particles and tallies are bit for bit
+    those of the full stash: where a particle collides changes the order of a
+    warp's work, not any particle's operations."""
+    pusher = _pusher(pcl, air, E=2e6)
+    runs = [_mixed(pcl, air, n=(8192, 2048, 1024), seed=14, steps_per_launch=spl, stash_entries=st)
+            for st in (0, 8, 40)]
+    for mp in runs:
+        pcl.run(mp, pusher, 8 * 25e-12, 25e-12)
+    ta = runs[0].tallies()
+    for b in runs[1:]:
+        tb = b.tallies()
+        assert tb.steps == ta.steps == 8
+        assert list(tb.live) == list(ta.live) and tb.particle_steps == ta.particle_steps
+        assert list(tb.spawned) == list(ta.spawned)
+        for q in range(3):
+            assert list(tb.collisions[q]) == list(ta.collisions[q])
+        for k in runs[0].index:
+            pa, pb = runs[0].get(k).particles(), b.get(k).particles()
+            oa, ob = np.argsort(pa.sid), np.argsort(pb.sid)
+            for f in ("sid", "ctr", "p", "x", "s", "w"):
+                np.testing.assert_array_equal(getattr(pb, f)[ob], getattr(pa, f)[oa])
+    for mp in runs:
+        mp.close()
+    with pytest.raises(pcl.PCLError):
+        _mixed(pcl, air, n=(64, 64, 64), seed=14, stash_entries=73)
+
+
 def test_graph_matches_plain(pcl, gpu, air):
     """Launch groups replayed from CUDA graphs (prologue, step, device-gated
     spill passes, compaction inside the graph) give bit-identical particles and
