@@ -204,6 +204,41 @@ def test_batched_oracle_parity(pcl, oracle, gpu):
 
 
 @pytest.mark.gpu
+def test_batched_multistep_launches(pcl, oracle, gpu):
+    """The batch at eight steps per launch (the multi-step kernel in swarm
+    mode: per-swarm field and rate bound, full-warp collide batches, photon
+    flights) equals eight one-step launches bit for bit and matches the
+    oracle."""
+    runs = []
+    for K in (1, 8):
+        b = _batch(pcl, steps_per_launch=K)
+        pcl.run(b.mpopl, b.pusher, 8 * b.dt, b.dt)
+        runs.append(b)
+    a, b = runs
+    assert a.mpopl.tallies().steps == b.mpopl.tallies().steps == 8
+    for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
+        for u, v in zip(_by_sid(a.mpopl.get(sp).particles()), _by_sid(b.mpopl.get(sp).particles())):
+            np.testing.assert_array_equal(u, v)
+    a.mpopl.close()
+    c = _batch(pcl, steps_per_launch=8)
+    et, gt, pt = c.tables
+    tabs = {pcl.Electron: et, pcl.Photon: gt, pcl.Positron: pt}
+    W = oracle.OracleWorld(5, tabs, {pcl.Electron: 10e3 * EV, pcl.Photon: 5e3 * EV, pcl.Positron: 10e3 * EV},
+                           c.pusher)
+    Evec = np.zeros((len(c.E), 3))
+    Evec[:, 2] = -c.E
+    W.set_swarms(tabs, Evec, pcl.co.elementary_charge * c.E * c.dt, safety=1.15)
+    W.upload(pcl.Electron, c.mpopl.get(pcl.Electron).particles())
+    pcl.run(c.mpopl, c.pusher, 4 * c.dt, c.dt)
+    for k in range(4):
+        W.advance((k + 1) * c.dt, 4)
+    for sp in (pcl.Electron, pcl.Photon, pcl.Positron):
+        rep = oracle.compare_populations(c.mpopl.get(sp).particles(), W.download(sp), sp, rtol=3e-5, stol=1e-4)
+        assert rep["ok"], (sp, str(rep))
+    b.mpopl.close(); c.mpopl.close()
+
+
+@pytest.mark.gpu
 def test_split_keeps_swarm(pcl, oracle, gpu):
     """split! in swarm mode: every copy stays in its parent's swarm (top 8
     bits of the stream id), so each swarm's count grows by its own copies; the
