@@ -1285,10 +1285,11 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 
     for (;;) {
         // ---------------- event kernel: collide parked particles in batches.
-        // Mode 1: the free lanes, when the stash fills at least kBatchMin of
-        // them (or all of them once the input is taken, or nothing else is
-        // left).  Mode 2: all 32 lanes, once 32 collisions are parked; the
-        // lanes' particles between collisions wait in the hold (the top of the
+        // Mode 1: the free lanes, once the stash can fill all of them (in the
+        // multi-step instance only when they are at least kBatchMin or the
+        // input is taken), or when nothing else is left.  Mode 2 (multi-step
+        // instance): all 32 lanes, once 32 collisions are parked; the lanes'
+        // particles between collisions wait in the hold (the top of the
         // stash) and refill free lanes before children and input do.  Lanes
         // whose collision found the stash full collide here too, in their
         // lane, before any other push (one call site of the samplers).
@@ -1339,7 +1340,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 __syncwarp();
             }
         }
-        // ---------------- refill idle lanes: children first, then input
+        // ---------------- refill idle lanes: held particles, children, then input
         unsigned need = __ballot_sync(FULL, !has);
         if (need) {
             __syncwarp();
