@@ -742,6 +742,14 @@ def run_kernels(args, pcl):
     timed("per-swarm roulette (electrons, one swarm, keep 0.9999)", "k_roulette_swarms", 16 * n_slots[E],
           lambda: mp.roulette_swarms(E, [0.9999]), reps=1)
     timed("split (photons, 1 % copies)", "k_split", 16 * n_slots[G], lambda: mp.split(G, 0.01), reps=1)
+    # the device per-swarm population cap (a RouletteCallback per swarm, applied
+    # after every launch group of run!): one step with the electrons' cap below
+    # their count, so that k_swarm_count and k_roulette_cap follow the step
+    t_cap = float(tal.t) + dt
+    mp.set_swarm_cap(int(0.9 * n_live[E]), particles=(E,))
+    timed("one step, then the per-swarm cap of the electrons (keep ~0.9)",
+          "k_step + k_swarm_count + k_roulette_cap", 0, lambda: pcl.run(mp, pusher, t_cap, dt), reps=1)
+    mp.set_swarm_cap(0, particles=(E,))
     tal = mp.tallies()
     n_slots = [int(v) for v in tal.n]
     n_live = [int(v) for v in tal.live]

@@ -2193,16 +2193,22 @@ __global__ void k_roulette_cap(float4* xw, uint4* meta, const unsigned long long
                                const unsigned int* counts, int nswarm, unsigned long long cap, uint32_t k0,
                                uint32_t k1) {
     const long long n = min((long long)*nslots, slot_cap);
+    // each swarm's keep probability once per block (an FP64 quotient, which
+    // GB300 runs at a small fraction of its FP32 rate); 2 = under the cap
+    __shared__ float qs[256];
     int over = 0;
-    for (int i = threadIdx.x; i < nswarm; i += blockDim.x) over |= (counts[i] > cap);
+    for (int i = threadIdx.x; i < nswarm; i += blockDim.x) {
+        const unsigned int cnt = counts[i];
+        over |= (cnt > cap);
+        qs[i] = (cnt > cap) ? float(double(cap) / double(cnt)) : 2.0f;
+    }
     if (!__syncthreads_or(over)) return;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         const uint4 m = meta[i];
         if (m.z == PCL_DEAD_CTR) continue;
-        const unsigned int cnt = counts[min(int(m.y >> 24), nswarm - 1)];
-        if (cnt <= cap) continue;
-        const float q = float(double(cap) / double(cnt));
+        const float q = qs[min(int(m.y >> 24), nswarm - 1)];
+        if (q > 1.0f) continue;
         const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
         if (u < q) {
             xw[i].w = xw[i].w / q;
