@@ -12,7 +12,7 @@ W3[128][128], b3[128], w4[128], b4 (33537 floats).
 from __future__ import annotations
 
 import numpy as np
-from scipy.special import erf
+from scipy.special import expit
 
 H = 128
 oW1, ob1 = 0, 2 * H
@@ -33,12 +33,19 @@ def bf16(a):
     return r.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+GELU_K = 2.0 * np.sqrt(2.0 / np.pi)
+GELU_A = 0.044715
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+    # the tanh form of GELU (Hendrycks and Gimpel 2016): 0.5 z (1 + tanh(u)),
+    # u = sqrt(2/pi) (z + 0.044715 z^3), written z sigmoid(2u)
+    return z * expit(GELU_K * (z + GELU_A * z ** 3))
 
 
 def dgelu(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
+    s = expit(GELU_K * (z + GELU_A * z ** 3))
+    return s + z * s * (1.0 - s) * GELU_K * (1.0 + 3.0 * GELU_A * z * z)
 
 
 def unpack(P):

@@ -116,9 +116,22 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+// GELU in its tanh form (Hendrycks and Gimpel, "Gaussian Error Linear Units",
+// 2016): 0.5 z (1 + tanh(sqrt(2/pi) (z + 0.044715 z^3))) = z sigmoid(v) with
+// v = 2 sqrt(2/pi) (z + 0.044715 z^3): one exponential and one fast quotient
+// per unit (v is clamped where sigmoid(v) is already 0 in FP32).
+constexpr float kGeluK = 1.5957691216057308f;   // 2 sqrt(2 / pi)
+constexpr float kGeluA = 0.044715f;
+__device__ __forceinline__ float gelu(float z) {
+    const float v = fmaxf(kGeluK * fmaf(kGeluA * z, z * z, z), -80.0f);
+    return __fdividef(z, 1.0f + __expf(-v));
+}
+// d/dz [z sigmoid(v)] = s + z s (1 - s) dv/dz, s = sigmoid(v), dv/dz = K (1 + 3 A z^2)
 __device__ __forceinline__ float dgelu(float z) {
-    return 0.5f * (1.0f + erff(z * 0.70710678118654752f)) + z * 0.39894228040143268f * expf(-0.5f * z * z);
+    const float z2 = z * z;
+    const float v = fmaxf(kGeluK * fmaf(kGeluA * z, z2, z), -80.0f);
+    const float s = __fdividef(1.0f, 1.0f + __expf(-v));
+    return fmaf(z * s * (1.0f - s), kGeluK * fmaf(3.0f * kGeluA, z2, 1.0f), s);
 }
 
 // warp-wide sum, added once to a shared-memory accumulator
