@@ -109,3 +109,57 @@ def test_continuum_loss_matches_restatement(pcl, comp):
     # restricted stopping power of 1 MeV electrons in air: ~0.16 MeV/m (below the 0.2 MeV/m total)
     f = cl.force_magnitude(pcl.Electron, 1e6 * co.eV) / (1e6 * co.eV)
     assert 0.12 < f < 0.2
+
+
+def test_moller_total_cs_integrates_the_differential(pcl):
+    """The Moller total cross section above the cut (moller.jl:40-56, a closed
+    form) equals the integral over eps = T2 / T in [tcut / T, 1/2] of the
+    published Moller differential cross section per atom,
+    2 pi r_e^2 Z / (beta^2 (gamma - 1)) [((gamma - 1) / gamma)^2
+    + (1 / eps) (1 / eps - (2 gamma - 1) / gamma^2)
+    + (1 / (1 - eps)) (1 / (1 - eps) - (2 gamma - 1) / gamma^2)],
+    integrated numerically here: a check of the restated closed form against
+    the physics it stands for, independent of any restatement."""
+    from scipy.integrate import quad
+    co = pcl.co
+    for Z in (7, 8):
+        for tcut_ev in (1e3, 1e4):
+            m = pcl.Moller(Z, tcut_ev * co.eV)
+            for T_ev in (2.5e3, 3e4, 1e6, 3e7, 1e9):
+                if tcut_ev / T_ev >= 0.5:
+                    continue
+                g = 1.0 + T_ev * co.eV / co.electron_mc2
+                b2 = (g * g - 1.0) / (g * g)
+                q = (2.0 * g - 1.0) / (g * g)
+                f = lambda e: ((g - 1.0) / g) ** 2 + (1.0 / e) * (1.0 / e - q) + (1.0 / (1.0 - e)) * (1.0 / (1.0 - e) - q)
+                integral, err = quad(f, tcut_ev / T_ev, 0.5, epsabs=0.0, epsrel=1e-12, limit=200)
+                want = 2.0 * np.pi * co.r_e ** 2 * Z * integral / (b2 * (g - 1.0))
+                got = pcl.totalcs(m, T_ev * co.eV)
+                assert abs(got - want) <= 1e-9 * want, (Z, tcut_ev, T_ev, got, want)
+
+
+def test_coulomb_total_cs_integrates_the_differential(pcl):
+    """The screened relativistic Coulomb total cross section
+    (relativistic_coulomb.jl:58-75, a closed form) equals pi r_e^2 Z^2 /
+    (beta^4 gamma^2) times the integral over x = sin^2(theta / 2) in [0, 1] of
+    (1 - beta^2 x) / (x + alpha)^2, the density its sampler draws from
+    (relativistic_coulomb.jl:27-52), integrated numerically here in
+    y = ln(x + alpha) (with the reference's 1e-4 eV added to the energy)."""
+    from scipy.integrate import quad
+    co = pcl.co
+    for Z in (7, 8):
+        c = pcl.RelativisticCoulomb(Z)
+        for K_ev in (1e2, 1e4, 1e6, 1e8):
+            K = K_ev * co.eV + 1e-4 * co.eV
+            mc2 = co.electron_mass * co.c ** 2
+            a = 1.3413 * Z ** (-1.0 / 3.0) * co.a_0
+            g = 1.0 + K / mc2
+            p = np.sqrt(K * (K + 2.0 * mc2)) / co.c
+            b = p / (g * co.electron_mass * co.c)
+            al = co.hbar ** 2 / (4.0 * p * p * a * a)
+            # y = ln(x + alpha) spreads the peak of width alpha at x = 0
+            integral, err = quad(lambda y: (1.0 - b * b * (np.exp(y) - al)) * np.exp(-y), np.log(al),
+                                 np.log1p(al), epsabs=0.0, epsrel=1e-12, limit=400)
+            want = np.pi * co.r_e ** 2 * Z ** 2 / (b ** 4 * g ** 2) * integral
+            got = pcl.totalcs(c, K_ev * co.eV)
+            assert abs(got - want) <= 1e-8 * want, (Z, K_ev, got, want)
