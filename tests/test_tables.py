@@ -163,3 +163,30 @@ def test_coulomb_total_cs_integrates_the_differential(pcl):
             want = np.pi * co.r_e ** 2 * Z ** 2 / (b ** 4 * g ** 2) * integral
             got = pcl.totalcs(c, K_ev * co.eV)
             assert abs(got - want) <= 1e-8 * want, (Z, K_ev, got, want)
+
+
+def test_bhabha_total_cs_integrates_the_differential(pcl):
+    """The Bhabha total cross section above the cut (bhaba.jl:34-48, a closed
+    form) equals the integral over eps in [tcut / T, 1] of the published
+    differential form 2 pi r_e^2 Z / (gamma - 1) [1 / (beta^2 eps^2) - B1 / eps
+    + B2 - B3 eps + B4 eps^2], y = 1 / (gamma + 1), B1 = 2 - y^2,
+    B2 = (1 - 2y)(3 + y^2), B3 = (1 - 2y)^2 + (1 - 2y)^3, B4 = (1 - 2y)^3,
+    integrated numerically here in ln(eps)."""
+    from scipy.integrate import quad
+    co = pcl.co
+    for Z in (7, 8):
+        for tcut_ev in (1e3, 1e4):
+            b = pcl.Bhabha(Z, tcut_ev * co.eV)
+            for T_ev in (2e4, 3e5, 1e7, 1e9):
+                g = 1.0 + T_ev * co.eV / co.electron_mc2
+                b2 = (g * g - 1.0) / (g * g)
+                y = 1.0 / (g + 1.0)
+                u = 1.0 - 2.0 * y
+                B1, B2, B3, B4 = 2.0 - y * y, u * (3.0 + y * y), u * u + u ** 3, u ** 3
+                f = lambda e: 1.0 / (b2 * e * e) - B1 / e + B2 - B3 * e + B4 * e * e
+                # in t = ln(eps), so that the 1 / eps^2 peak at the cut is resolved
+                integral, err = quad(lambda t: f(np.exp(t)) * np.exp(t), np.log(tcut_ev / T_ev), 0.0,
+                                     epsabs=0.0, epsrel=1e-12, limit=200)
+                want = 2.0 * np.pi * co.r_e ** 2 * Z * integral / (g - 1.0)
+                got = pcl.totalcs(b, T_ev * co.eV)
+                assert abs(got - want) <= 1e-9 * want, (Z, tcut_ev, T_ev, got, want)
