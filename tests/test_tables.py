@@ -190,3 +190,25 @@ def test_bhabha_total_cs_integrates_the_differential(pcl):
                 want = 2.0 * np.pi * co.r_e ** 2 * Z * integral / (g - 1.0)
                 got = pcl.totalcs(b, T_ev * co.eV)
                 assert abs(got - want) <= 1e-9 * want, (Z, tcut_ev, T_ev, got, want)
+
+
+def test_klein_nishina_total_cs_integrates_the_differential(pcl):
+    """The Klein-Nishina total cross section (compton.jl:34-47, a closed form)
+    equals Z times the Klein-Nishina differential cross section per electron,
+    d sigma / d Omega = (r_e^2 / 2) P^2 (P + 1 / P - sin^2 theta) with
+    P = 1 / (1 + k (1 - cos theta)), k = E / (m_e c^2), integrated over the
+    sphere numerically here."""
+    from scipy.integrate import quad
+    co = pcl.co
+    for Z in (7, 8):
+        c = pcl.KleinNishinaCompton(Z)
+        for E_ev in (1e3, 1e5, 1e6, 1e8):
+            k = E_ev * co.eV / co.electron_mc2
+
+            def f(mu):
+                P = 1.0 / (1.0 + k * (1.0 - mu))
+                return P * P * (P + 1.0 / P - (1.0 - mu * mu))
+            integral, err = quad(f, -1.0, 1.0, epsabs=0.0, epsrel=1e-12, limit=200)
+            want = Z * 2.0 * np.pi * 0.5 * co.r_e ** 2 * integral
+            got = pcl.totalcs(c, E_ev * co.eV)
+            assert abs(got - want) <= 1e-7 * want, (Z, E_ev, got, want)
