@@ -47,6 +47,71 @@ def test_moller_conserves_energy(pcl, world, air):
     assert np.all(ok[:, 0] == pcl.Electron) and np.all(ok[:, 1] == pcl.Electron)
 
 
+def _ks(samples, cdf):
+    x = np.sort(samples)
+    n = len(x)
+    F = cdf(x)
+    return max(np.max(np.arange(1, n + 1) / n - F), np.max(F - np.arange(n) / n))
+
+
+def test_moller_sampler_follows_the_differential(pcl, world, air):
+    """The oracle's Moller secondary energies (moller.jl:64-87) at 30 keV (the
+    10 keV cut at a third of T, where the whole shape matters) follow the
+    published Moller differential cross section on [tcut / T, 1/2]
+    (normalised; its integral is the closed form of moller.jl:40-56):
+    Kolmogorov-Smirnov distance within the 0.1 % critical value (0.006
+    against 0.0098 at 40 000 samples; a pure 1 / eps^2 law is at 0.039)."""
+    W, _ = world
+    tab = air["tabs"][pcl.Electron]
+    j = [type(q).__name__ for q in tab.proc].index("Moller")
+    n = 40000
+    T = 3e4 * pcl.co.eV
+    p = np.zeros((n, 3)); p[:, 2] = pcl.momentum_norm_from_kin(pcl.Electron, np.full(n, T))
+    op, os_, ok, oc, ot = W.sample(pcl.Electron, j, p, np.arange(n, dtype=np.uint64) + 77)
+    eps = _energy(pcl, pcl.Electron, op[:, 1]) / T
+    x = tab.proc[j].tcut / T
+    g = 1.0 + T / pcl.co.electron_mc2
+    q = (2.0 * g - 1.0) / (g * g)
+    c = ((g - 1.0) / g) ** 2
+
+    def prim(e):   # antiderivative of the bracket of the differential cross section
+        return c * e - 1.0 / e - q * np.log(e) + 1.0 / (1.0 - e) + q * np.log(1.0 - e)
+    cdf = lambda e: (prim(e) - prim(x)) / (prim(0.5) - prim(x))
+    assert _ks(eps, cdf) < 1.95 / np.sqrt(n)
+
+
+def test_coulomb_sampler_follows_the_differential(pcl, world, air):
+    """The oracle's screened relativistic Coulomb deflections
+    (relativistic_coulomb.jl:10-52) at 100 keV follow the density
+    (1 - beta^2 x) / (x + alpha)^2 in x = sin^2(theta / 2) on [0, 1]:
+    Kolmogorov-Smirnov distance within the 0.1 % critical value (0.0033
+    against 0.0098; a screening parameter alpha off by 10 % is at 0.023; the
+    beta^2 factor moves the distance by less than the noise)."""
+    W, _ = world
+    tab = air["tabs"][pcl.Electron]
+    j = [type(q).__name__ for q in tab.proc].index("RelativisticCoulomb")
+    Z = tab.proc[j].Z
+    n = 40000
+    T = 1e5 * pcl.co.eV
+    co = pcl.co
+    pn = pcl.momentum_norm_from_kin(pcl.Electron, np.full(n, T))
+    p = np.zeros((n, 3)); p[:, 2] = pn
+    op, os_, ok, oc, ot = W.sample(pcl.Electron, j, p, np.arange(n, dtype=np.uint64) + 99)
+    cth = op[:, 0, 2] / np.linalg.norm(op[:, 0], axis=1)
+    xs = 0.5 * (1.0 - cth)
+    a = 1.3413 * Z ** (-1.0 / 3.0) * co.a_0
+    mc2 = co.electron_mass * co.c ** 2
+    g = 1.0 + T / mc2
+    pm = pn[0]
+    b2 = (pm / (g * co.electron_mass * co.c)) ** 2
+    al = co.hbar ** 2 / (4.0 * pm * pm * a * a)
+
+    def prim(t):   # antiderivative of (1 - b2 t) / (t + al)^2
+        return -(1.0 + al * b2) / (t + al) - b2 * np.log(t + al)
+    cdf = lambda t: (prim(t) - prim(0.0)) / (prim(1.0) - prim(0.0))
+    assert _ks(xs, cdf) < 1.95 / np.sqrt(n)
+
+
 def test_bremsstrahlung_conserves_momentum(pcl, world, air):
     tab = air["tabs"][pcl.Electron]
     j = [type(q).__name__ for q in tab.proc].index("SeltzerBerger")
