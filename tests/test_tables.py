@@ -212,3 +212,36 @@ def test_klein_nishina_total_cs_integrates_the_differential(pcl):
             want = Z * 2.0 * np.pi * 0.5 * co.r_e ** 2 * integral
             got = pcl.totalcs(c, E_ev * co.eV)
             assert abs(got - want) <= 1e-7 * want, (Z, E_ev, got, want)
+
+
+def _rbeb_bracket(w, t, t1, b1, bt2):
+    """The bracket of the relativistic binary-encounter-Bethe differential
+    cross section in w = W / B (Kim, Santos and Parente, Phys. Rev. A 62,
+    052710 (2000); rbeb.jl:102-113)."""
+    return (b1 ** 2 / (1 + t1) ** 2 + 1 / (t - w) ** 2 + 1 / (1 + w) ** 2
+            - (1 + 2 * t1) * (1 / (t - w) + 1 / (1 + w)) / ((1 + t) * (1 + t1) ** 2)
+            + (1 / (t - w) ** 3 + 1 / (1 + w) ** 3) * (-bt2 - np.log(2 * b1) + np.log(bt2 / (1 - bt2))))
+
+
+def test_rbeb_total_cs_integrates_the_differential(pcl):
+    """The RBEB total ionization cross section (rbeb.jl:119-146, a closed form)
+    equals N times the integral of the RBEB differential cross section over
+    w = W / B in [0, (T / B - 1) / 2], integrated numerically here, for an N2
+    and an O2 orbital from 100 eV to 100 MeV."""
+    from scipy.integrate import quad
+    co = pcl.co
+    mc2 = co.electron_mc2
+    for B_ev, U_ev, N in ((15.58, 54.91, 2), (543.8, 796.2, 4)):
+        r = pcl.RBEB(B_ev * co.eV, U_ev * co.eV, N)
+        for T_ev in (1e2, 1e3, 1e4, 1e6, 1e8):
+            if T_ev <= B_ev:
+                continue
+            t1, b1, u1 = T_ev * co.eV / mc2, B_ev * co.eV / mc2, U_ev * co.eV / mc2
+            bt2, bb2, bu2 = (1 - 1 / (1 + t1) ** 2, 1 - 1 / (1 + b1) ** 2, 1 - 1 / (1 + u1) ** 2)
+            t = T_ev / B_ev
+            pref = 2 * co.a_0 ** 2 * np.pi * co.fine_structure ** 4 / (b1 * (bb2 + bt2 + bu2))
+            integral, err = quad(lambda y: _rbeb_bracket(np.expm1(y), t, t1, b1, bt2) * np.exp(y), 0.0,
+                                 np.log1p((t - 1) / 2), epsabs=0.0, epsrel=1e-12, limit=400)
+            want = N * pref * integral
+            got = pcl.totalcs(r, T_ev * co.eV)
+            assert abs(got - want) <= 1e-8 * want, (B_ev, T_ev, got, want)
