@@ -245,3 +245,25 @@ def test_rbeb_total_cs_integrates_the_differential(pcl):
             want = N * pref * integral
             got = pcl.totalcs(r, T_ev * co.eV)
             assert abs(got - want) <= 1e-8 * want, (B_ev, T_ev, got, want)
+
+
+def test_annihilation_total_cs_integrates_the_differential(pcl):
+    """The two-photon annihilation total cross section (anihilation.jl:24-32,
+    Heitler's closed form) equals Z pi r_e^2 / ((gamma + 1) (gamma^2 - 1)) times
+    the integral over the photon energy fraction eps in [eps_min, 1 - eps_min]
+    of S(eps) = -(gamma + 1)^2 + (gamma^2 + 4 gamma + 1) / eps - 1 / eps^2,
+    eps_min = (1 - sqrt((gamma - 1) / (gamma + 1))) / 2 (the differential form
+    of the GEANT4 Physics Reference Manual), integrated numerically here."""
+    from scipy.integrate import quad
+    co = pcl.co
+    for Z in (7, 8):
+        a = pcl.PositronAnihilation(Z)
+        for T_ev in (1e3, 1e5, 1e6, 1e8):
+            g = 1.0 + T_ev * co.eV / co.electron_mc2
+            e0 = 0.5 * (1.0 - np.sqrt((g - 1.0) / (g + 1.0)))
+            S = lambda e: -(g + 1.0) ** 2 + (g * g + 4.0 * g + 1.0) / e - 1.0 / (e * e)
+            integral, err = quad(lambda t: S(np.exp(t)) * np.exp(t), np.log(e0), np.log1p(-e0),
+                                 epsabs=0.0, epsrel=1e-12, limit=400)
+            want = Z * np.pi * co.r_e ** 2 * integral / ((g + 1.0) * (g * g - 1.0))
+            got = pcl.totalcs(a, T_ev * co.eV)
+            assert abs(got - want) <= 1e-8 * want, (Z, T_ev, got, want)
