@@ -796,6 +796,67 @@ def run_kernels(args, pcl):
     return 0
 
 
+def run_fields(args, pcl):
+    """The general step kernel (a position-dependent E of field.jl, a wall
+    record of WallCallback) on the 16 M mixed state, against the homogeneous
+    kernel on the same draw and launch shape (64 steps per launch, repack
+    every 8).  Each arm draws the same particles (Philox seed 0) into a fresh
+    context, runs W warm-up steps, then times `args.steps` steps of run! with
+    CUDA events on the context's stream; the wall arm's records are read back
+    inside the timed region, as run! does after every launch."""
+    L = pcl.lib()
+    E0 = (0.0, 0.0, -5e5)
+    zc = 191.0   # mean z of the grown state's electrons (m); spread 8.7 m
+    arms = (("homogeneous E (the headline kernel)", None, None),
+            ("DoubleLayerField over the whole population (same physics)", pcl.DoubleLayerField(-1e4, 1e4, E0), None),
+            ("StepField: E above the electrons' mean z, 0 below", pcl.StepField(zc, (0.0, 0.0, 0.0), E0), None),
+            ("ConfinedDoubleLayerField (40 m, 40 m, 200 m, 0.5 MV/m)",
+             pcl.ConfinedDoubleLayerField(40.0, 40.0, 200.0, -5e5), None),
+            ("DoubleLayerField over the upper half + WallCallback (electrons, z = 200 m, drop)",
+             pcl.DoubleLayerField(zc, 1e4, E0), (pcl.Electron, 3, 200.0)))
+    rows = []
+    with Clocks(0) as clk:
+        for name, field, wall in arms:
+            mp, pusher, dt, _ = build_workload(pcl, args.n, seed=0, device=0, steps_per_launch=64,
+                                               compaction_period=8)
+            if field is not None:
+                cl = pusher.device_forcing()[2]
+                pusher = pcl.RK2Pusher(pcl.CombinedForcing(
+                    pcl.ElectromagneticField(field, pcl.HomogeneousField((0.0, 0.0, 0.0))), cl))
+            cb = pcl.WallCallback(*wall) if wall is not None else None
+            pcl.run(mp, pusher, args.warmup * dt, dt, cb)
+            tal0 = mp.tallies()
+            L.pcl_sync(mp.ctx)
+            L.pcl_timer_start(mp.ctx)
+            pcl.run(mp, pusher, (args.warmup + args.steps) * dt, dt, cb)
+            ms = C.c_double()
+            L.pcl_timer_stop(mp.ctx, C.byref(ms))
+            tal1 = mp.tallies()
+            ps = tal1.particle_steps - tal0.particle_steps
+            nl = C.c_int64()
+            L.pcl_kernel_stats(mp.ctx, None, None, C.byref(nl), None, 1)
+            row = {"arm": name, "general_kernel": field is not None or wall is not None,
+                   "value": ps / (ms.value / 1e3), "ms_per_step": ms.value / args.steps,
+                   "particle_steps": int(ps), "live_at_end": [int(v) for v in tal1.live]}
+            if cb is not None:
+                row["wall_records"] = int(len(cb.states().w))
+            rows.append(row)
+            mp.close()
+    base = rows[0]["value"]
+    for r in rows:
+        r["over_homogeneous"] = r["value"] / base
+    line = {"metric": "particle-steps/s on 1 GB300 of the general step kernel (position-dependent E, wall "
+                      "records), mixed avalanche at 2^24 particles", "value": min(r["value"] for r in rows[1:]),
+            "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": WORKLOAD + " (field shapes of field.jl)", "particles": args.n,
+                       "steps_per_launch": 64, "compaction_period": 8,
+                       "l2": "inputs larger than L2 (population > 800 MB)"},
+            "value_is": "the slowest general-kernel arm", "arms": rows, "clocks": clk.summary()}
+    print(json.dumps(line))
+    return 0
+
+
 def _printing(fn):
     def wrap(args, pcl):
         print(json.dumps(fn(args, pcl)))
@@ -837,7 +898,7 @@ def main():
     ap.add_argument("--graph", type=int, default=0, help="1: launch groups replayed from CUDA graphs")
     ap.add_argument("--compaction-period", type=int, default=0, help="steps between repacks (0: the library's 8)")
     ap.add_argument("--workload", default="rrea16M",
-                    choices=["rrea16M", "swarms", "learned", "plain", "reid", "reid-fp64", "mlp", "kernels"])
+                    choices=["rrea16M", "swarms", "learned", "plain", "reid", "reid-fp64", "mlp", "kernels", "fields"])
     ap.add_argument("--nswarm", type=int, default=256)
     ap.add_argument("--tune-steps", type=int, default=1344)
     ap.add_argument("--learned-n", type=int, default=1 << 24, help="learned form: particles")
@@ -859,7 +920,8 @@ def main():
         import __graft_entry__ as graft
         graft.build()
         fn = {"swarms": _printing(run_swarms), "learned": _printing(run_learned), "plain": run_plain,
-              "reid": run_reid, "mlp": run_mlp, "kernels": run_kernels}[args.workload]
+              "reid": run_reid, "mlp": run_mlp, "kernels": run_kernels,
+              "fields": run_fields}[args.workload]
         return fn(args, graft.load_package())
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))

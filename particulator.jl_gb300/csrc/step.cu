@@ -312,9 +312,12 @@ template <bool GENERAL>
 __device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K, int sw, float x, float y, float z,
                                              float px, float py, float pz, float& bx, float& by, float& bz,
                                              float& fx, float& fy, float& fz) {
-    float p2 = px * px + py * py + pz * pz;
+    // Every product and sum below is rounded explicitly (no contraction left
+    // to the compiler), so that each instance of the step kernel, and each
+    // place it is inlined, gives the same bits.
+    float p2 = __fmaf_rn(pz, pz, __fmaf_rn(py, py, __fmul_rn(px, px)));
     float ig = rsqrtf(1.0f + p2);   // 1 / gamma
-    bx = px * ig; by = py * ig; bz = pz * ig;
+    bx = __fmul_rn(px, ig); by = __fmul_rn(py, ig); bz = __fmul_rn(pz, ig);
     const float q = S.charge;
     float ex, ey, ez;
     if (GENERAL) {
@@ -329,54 +332,62 @@ __device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K,
     }
     if (K.hasB) {
         const float* B = K.H->B;
-        fx = q * (ex + (by * B[2] - bz * B[1]));
-        fy = q * (ey + (bz * B[0] - bx * B[2]));
-        fz = q * (ez + (bx * B[1] - by * B[0]));
+        fx = __fmul_rn(q, __fadd_rn(ex, __fmaf_rn(by, B[2], -__fmul_rn(bz, B[1]))));
+        fy = __fmul_rn(q, __fadd_rn(ey, __fmaf_rn(bz, B[0], -__fmul_rn(bx, B[2]))));
+        fz = __fmul_rn(q, __fadd_rn(ez, __fmaf_rn(bx, B[1], -__fmul_rn(by, B[0]))));
     } else {  // the same values: adding the zero v x B term changes no finite component
-        fx = q * ex; fy = q * ey; fz = q * ez;
+        fx = __fmul_rn(q, ex); fy = __fmul_rn(q, ey); fz = __fmul_rn(q, ez);
     }
-    float f = cl_mag(S, K, __fdividef(p2 * ig, 1.0f + ig));
+    float f = cl_mag(S, K, __fdividef(__fmul_rn(p2, ig), 1.0f + ig));
     if (f != 0.0f && p2 > 0.0f) {
-        float c = f * rsqrtf(p2);
-        fx -= c * px; fy -= c * py; fz -= c * pz;
+        float c = __fmul_rn(f, rsqrtf(p2));
+        fx = __fmaf_rn(-c, px, fx); fy = __fmaf_rn(-c, py, fy); fz = __fmaf_rn(-c, pz, fz);
     }
 }
 
 // advance_particle(RK2Pusher, y, dt) (pusher.jl:41-63); photons move in a
-// straight line (photon.jl:46-52; both forcings vanish on photons).
+// straight line (photon.jl:46-52; both forcings vanish on photons).  Rounded
+// explicitly like lepton_force: a photon's flight over whole steps in the
+// multi-step instances and its steps in the loop give the same bits.
 template <bool GENERAL>
 __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K, float h) {
     if (L.species == PCL_PHOTON) {
-        float v = h * kCns * rsqrtf(L.px * L.px + L.py * L.py + L.pz * L.pz);
-        L.x += v * L.px; L.y += v * L.py; L.z += v * L.pz;
+        const float p2 = __fmaf_rn(L.pz, L.pz, __fmaf_rn(L.py, L.py, __fmul_rn(L.px, L.px)));
+        const float v = __fmul_rn(__fmul_rn(h, kCns), rsqrtf(p2));
+        L.x = __fmaf_rn(v, L.px, L.x); L.y = __fmaf_rn(v, L.py, L.y); L.z = __fmaf_rn(v, L.pz, L.z);
         return;
     }
     float b1x, b1y, b1z, f1x, f1y, f1z;
     lepton_force<GENERAL>(S, K, L.sw, L.x, L.y, L.z, L.px, L.py, L.pz, b1x, b1y, b1z, f1x, f1y, f1z);
-    const float h23 = h * (2.0f / 3.0f);
-    float qx = L.px + h23 * f1x, qy = L.py + h23 * f1y, qz = L.pz + h23 * f1z;
+    const float h23 = __fmul_rn(h, 2.0f / 3.0f);
+    const float qx = __fmaf_rn(h23, f1x, L.px), qy = __fmaf_rn(h23, f1y, L.py), qz = __fmaf_rn(h23, f1z, L.pz);
     // second stage at x + 2 dt v1 / 3 (only a position-dependent field reads it)
-    const float c23 = GENERAL ? h23 * kCns : 0.0f;
+    const float c23 = GENERAL ? __fmul_rn(h23, kCns) : 0.0f;
     float b2x, b2y, b2z, f2x, f2y, f2z;
-    lepton_force<GENERAL>(S, K, L.sw, L.x + c23 * b1x, L.y + c23 * b1y, L.z + c23 * b1z, qx, qy, qz, b2x, b2y, b2z,
-                          f2x, f2y, f2z);
-    const float hc = h * kCns;
-    L.x += hc * (0.25f * b1x + 0.75f * b2x);
-    L.y += hc * (0.25f * b1y + 0.75f * b2y);
-    L.z += hc * (0.25f * b1z + 0.75f * b2z);
-    L.px += h * (0.25f * f1x + 0.75f * f2x);
-    L.py += h * (0.25f * f1y + 0.75f * f2y);
-    L.pz += h * (0.25f * f1z + 0.75f * f2z);
+    lepton_force<GENERAL>(S, K, L.sw, __fmaf_rn(c23, b1x, L.x), __fmaf_rn(c23, b1y, L.y), __fmaf_rn(c23, b1z, L.z),
+                          qx, qy, qz, b2x, b2y, b2z, f2x, f2y, f2z);
+    const float hc = __fmul_rn(h, kCns);
+    L.x = __fmaf_rn(hc, __fmaf_rn(0.75f, b2x, __fmul_rn(0.25f, b1x)), L.x);
+    L.y = __fmaf_rn(hc, __fmaf_rn(0.75f, b2y, __fmul_rn(0.25f, b1y)), L.y);
+    L.z = __fmaf_rn(hc, __fmaf_rn(0.75f, b2z, __fmul_rn(0.25f, b1z)), L.z);
+    L.px = __fmaf_rn(h, __fmaf_rn(0.75f, f2x, __fmul_rn(0.25f, f1x)), L.px);
+    L.py = __fmaf_rn(h, __fmaf_rn(0.75f, f2y, __fmul_rn(0.25f, f1y)), L.py);
+    L.pz = __fmaf_rn(h, __fmaf_rn(0.75f, f2z, __fmul_rn(0.25f, f1z)), L.pz);
 }
 
-// push with the WallCallback's onadvance (callback.jl:167-184): a crossing of
+// The general kernel's push (one call site of push<true>, whose field
+// evaluations are the larger part of its code), with the WallCallback's
+// onadvance (callback.jl:167-184) when the species has a wall: a crossing of
 // the wall in the +axis direction records lincomb(new, old, w) (electron.jl:
 // 127-132), whose constructor draws s (one draw), and drops the particle if
-// the wall is set to.  t_in: sub-step start in ns since the launch start.
-__device__ __forceinline__ void push_wall(Lane& L, const SpeciesHdr& S, const KCtx& K, float h, float t_in) {
+// the wall is set to.  The sub-step starts (k + 1) dt - th in ns since the
+// launch start (dt_hi: dt in ns).
+__device__ __forceinline__ void push_general(Lane& L, const SpeciesHdr& S, const KCtx& K, float h, float dt_hi) {
     const float ox = L.x, oy = L.y, oz = L.z, opx = L.px, opy = L.py, opz = L.pz;
+    const float t_in = __fmaf_rn(float(L.k + 1), dt_hi, -dd_val(L.th, L.tlo));
     push<true>(L, S, K, h);
     const int q = S.wall_coord;
+    if (q < 0) return;
     const float o = (q == 0) ? ox : (q == 1 ? oy : oz);
     const float n = (q == 0) ? L.x : (q == 1 ? L.y : L.z);
     const float v = S.wall_v;
@@ -385,8 +396,10 @@ __device__ __forceinline__ void push_wall(Lane& L, const SpeciesHdr& S, const KC
     const StepArgs& A = *K.A;
     const unsigned long long r = atomicAdd(A.wall_n, 1ull);
     if ((long long)r < A.wall_cap) {
-        A.wall_xw[r] = make_float4(L.x * w + ox * u, L.y * w + oy * u, L.z * w + oz * u, L.w);
-        A.wall_pt[r] = make_float4(L.px * w + opx * u, L.py * w + opy * u, L.pz * w + opz * u, t_in + w * h);
+        A.wall_xw[r] = make_float4(__fmaf_rn(L.x, w, __fmul_rn(ox, u)), __fmaf_rn(L.y, w, __fmul_rn(oy, u)),
+                                   __fmaf_rn(L.z, w, __fmul_rn(oz, u)), L.w);
+        A.wall_pt[r] = make_float4(__fmaf_rn(L.px, w, __fmul_rn(opx, u)), __fmaf_rn(L.py, w, __fmul_rn(opy, u)),
+                                   __fmaf_rn(L.pz, w, __fmul_rn(opz, u)), __fmaf_rn(w, h, t_in));
         A.wall_meta[r] = make_uint4(L.sid_lo, L.sid_hi, uint32_t(L.species), A.ctl->launch_seq);
     } else {
         err(K, PCL_E_CAPACITY);
@@ -1486,8 +1499,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                 float h = coll ? tnext : dd_val(L.th, L.tlo);
                 if (!coll) L.s -= h * L.r;
                 if (!GENERAL) push<false>(L, S, K, h);
-                else if (S.wall_coord >= 0) push_wall(L, S, K, h, float(L.k + 1) * dt_hi - dd_val(L.th, L.tlo));
-                else push<true>(L, S, K, h);
+                else push_general(L, S, K, h, dt_hi);
                 if (coll) dd_add(L.th, L.tlo, -tnext, 0.0f);
                 else { L.th = 0.0f; L.tlo = 0.0f; }
                 L.nsub += 1;
@@ -1516,14 +1528,16 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         L.nsub = 0;
                         dd_add(L.th, L.tlo, dt_hi, dt_lo);  // remainder below eps carries over (mixed_population.jl:65)
                         L.r = setr(S, K, E, L.sw);  // advance_init! of the next step
-                        if (MULTI && !GENERAL && L.species == PCL_PHOTON) {
+                        if (MULTI && L.species == PCL_PHOTON && (!GENERAL || S.wall_coord < 0)) {
                             // A photon's collision-free whole steps in this
                             // iteration, each exactly as its own iteration would
                             // run it (the same clock decision, decrement, push and
                             // clock reset): no force acts on it and its energy, so
                             // its rate bound (setr!) and the droplow! outcome, do
-                            // not change in flight.  The step that collides, and
-                            // the launch's last step, are left to the loop.
+                            // not change in flight, whatever the field.  The step
+                            // that collides, the launch's last step, and every
+                            // step of photons with a wall (whose crossings are
+                            // recorded per sub-step) are left to the loop.
                             const int k0 = L.k;
                             while (L.k + 1 < nsteps && dd_val(L.th, L.tlo) > kEpsT) {
                                 const float tn = L.s / L.r;
@@ -1642,10 +1656,15 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
 // kernel in 3 (its stash), each with or without the learned samplers'
 // suspend/resume (LEARN); the general kernel (position-dependent field, wall
 // crossings; learned samplers included) in 3, where it needs no register
-// spills; the event kernel has a second instance for launches of several
-// steps (MULTI).  Code a launch does not use stays out of its kernel.
+// spills; the event kernels (plain, learned, general) have a second instance
+// for launches of several steps (MULTI).  Code a launch does not use stays out
+// of its kernel.
 static void (*step_kernel(int minb, bool general, bool event, bool learn, bool multi))(StepArgs) {
-    if (general) return event ? k_step<3, true, true, true, false> : k_step<3, true, false, true, false>;
+    if (general) {
+        if (!event) return k_step<3, true, false, true, false>;
+        if (learn) return multi ? k_step<3, true, true, true, true> : k_step<3, true, true, true, false>;
+        return multi ? k_step<3, true, true, false, true> : k_step<3, true, true, false, false>;
+    }
     if (learn) {
         if (!event) return k_step<3, true, false, true, false>;
         return multi ? k_step<3, false, true, true, true> : k_step<3, false, true, true, false>;

@@ -291,36 +291,44 @@ def test_position_dependent_fields(pcl, oracle, gpu, air, kind):
     mp.close()
 
 
-def test_general_kernel_multistep(pcl, gpu, air):
+@pytest.mark.parametrize("wall_species", ["electron", "photon"])
+def test_general_kernel_multistep(pcl, gpu, air, wall_species):
     """The general kernel (position-dependent field, wall records) with four
-    steps per launch equals one step per launch bit for bit: the particles and
-    the wall crossings (matched by stream id; their times, kept in FP32 from
-    the launch's start, to that rounding)."""
+    and eight steps per launch (its multi-step instance: collide batches with
+    the lanes' particles held, photon flights over collision-free whole steps
+    unless the photons have the wall) equals one step per launch bit for bit:
+    the particles and the wall crossings (matched by stream id; their times,
+    kept in FP32 from the launch's start, to that rounding)."""
     F = pcl.DoubleLayerField(-0.004, 0.004, (0.0, 0.0, -1.5e6))
     pusher = pcl.RK2Pusher(pcl.CombinedForcing(pcl.ElectromagneticField(F, pcl.HomogeneousField((0.0, 0.0, 0.0))),
                                                air["cl"]))
+    wsp = {"electron": pcl.Electron, "photon": pcl.Photon}[wall_species]
     out = []
-    for K in (1, 4):
+    for K in (1, 4, 8):
         rng = np.random.default_rng(41)
         arr = random_population(pcl, pcl.Electron, 4096, 1e4, 3e7, rng, spread_x=0.004)
+        ph = random_population(pcl, pcl.Photon, 4096, 1e4, 3e7, rng, spread_x=0.004)
         mp = pcl.MultiPopulation((pcl.Electron, pcl.Population(1 << 15, arr, air["tabs"][0], air["cuts"][0],
                                                               particle=pcl.Electron)),
-                                 (pcl.Photon, pcl.Population(1 << 15, [], air["tabs"][1], air["cuts"][1],
+                                 (pcl.Photon, pcl.Population(1 << 15, ph, air["tabs"][1], air["cuts"][1],
                                                              particle=pcl.Photon)), seed=41, steps_per_launch=K)
-        wall = pcl.WallCallback(pcl.Electron, 3, 0.002, drop=False)
+        wall = pcl.WallCallback(wsp, 3, 0.002, drop=False)
         pcl.run(mp, pusher, 8 * 5e-12, 5e-12, wall)
         out.append(([mp.get(q).particles() for q in (0, 1)], wall.states()))
         mp.close()
-    (pa, wa), (pb, wb) = out
-    for a, b in zip(pa, pb):
-        oa, ob = np.argsort(a.sid), np.argsort(b.sid)
-        for f in ("sid", "ctr", "p", "x", "s", "w"):
-            np.testing.assert_array_equal(getattr(b, f)[ob], getattr(a, f)[oa])
-    assert len(wa.w) > 50 and len(wa.w) == len(wb.w)
-    oa, ob = np.lexsort((wa.t, wa.sid)), np.lexsort((wb.t, wb.sid))
-    for f in ("sid", "x", "p", "w"):
-        np.testing.assert_array_equal(getattr(wb, f)[ob], getattr(wa, f)[oa])
-    np.testing.assert_allclose(wb.t[ob], wa.t[oa], rtol=0, atol=1e-17)
+    pa, wa = out[0]
+    assert len(wa.w) > 50
+    oa = np.lexsort((wa.t, wa.sid))
+    for pb, wb in out[1:]:
+        for a, b in zip(pa, pb):
+            ia, ib = np.argsort(a.sid), np.argsort(b.sid)
+            for f in ("sid", "ctr", "p", "x", "s", "w"):
+                np.testing.assert_array_equal(getattr(b, f)[ib], getattr(a, f)[ia])
+        assert len(wa.w) == len(wb.w)
+        ob = np.lexsort((wb.t, wb.sid))
+        for f in ("sid", "x", "p", "w"):
+            np.testing.assert_array_equal(getattr(wb, f)[ob], getattr(wa, f)[oa])
+        np.testing.assert_allclose(wb.t[ob], wa.t[oa], rtol=0, atol=1e-17)
 
 
 @pytest.mark.parametrize("drop", [True, False])
