@@ -742,6 +742,14 @@ def run_kernels(args, pcl):
     timed("per-swarm roulette (electrons, one swarm, keep 0.9999)", "k_roulette_swarms", 16 * n_slots[E],
           lambda: mp.roulette_swarms(E, [0.9999]), reps=1)
     timed("split (photons, 1 % copies)", "k_split", 16 * n_slots[G], lambda: mp.split(G, 0.01), reps=1)
+    # the function forms (roulette!(f, popl), split!(f, popl)): f of the
+    # kinetic energy as a 4096-node table; each live particle's momentum is
+    # read too (32 B per slot)
+    ftab = (pcl.ENERGY_TABLE_NODES, np.full(4096, 0.9999))
+    timed("roulette with f(E) (photons, 4096-node table, keep 0.9999)", "k_roulette_fn", 32 * n_slots[G],
+          lambda: mp.roulette(G, ftab), reps=1)
+    timed("split with f(E) (photons, 4096-node table, 1 % copies)", "k_split_fn", 32 * n_slots[G],
+          lambda: mp.split(G, (pcl.ENERGY_TABLE_NODES, np.full(4096, 0.01))), reps=1)
     # the device per-swarm population cap (a RouletteCallback per swarm, applied
     # after every launch group of run!): one step with the electrons' cap below
     # their count, so that k_swarm_count and k_roulette_cap follow the step

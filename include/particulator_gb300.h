@@ -256,6 +256,13 @@ int pcl_set_forcing(void* ctx, const double E[3], const double B[3], int cl_orde
  * v2y, v2z}, 3 ConfinedDoubleLayerField {sx, sy, sz, ez0}.  Evaluated at each
  * RK2 stage's position (pusher.jl:41-63).  Batched swarms keep their own
  * homogeneous fields. */
+/* RestrictedPusher{T}(p) / NullPusher (pusher.jl:67-76) and
+ * RestrictedForcing{T}(f) (pusher.jl:28-34), as species bit masks (bit s =
+ * 1 << species): `pushed`, the species that move at all (the others only
+ * advance their clocks, and still collide); `field`, those the EM field acts
+ * on; `loss`, those the continuum loss acts on.  7 = every species (the
+ * default). */
+int pcl_set_push_mask(void* ctx, int pushed, int field, int loss);
 int pcl_set_field(void* ctx, int kind, const double* params, int nparams);
 /* WallCallback{P}(coord, v, drop) (callback.jl:146-184): while advancing,
  * a particle of `species` crossing the plane x[coord] = v (coord 0-2; -1
@@ -276,6 +283,17 @@ int pcl_roulette(void* ctx, int species, double pkeep);
  * hold each swarm at a population cap. */
 int pcl_roulette_swarms(void* ctx, int species, int nswarm, const double* pkeep);
 int pcl_split(void* ctx, int species, double p);
+/* roulette!(f, popl) and split!(f, popl) (population.jl:291-305, 316-331)
+ * with f a function of the particle's kinetic energy, given as a table of n
+ * nodes (1 to 4096): energies in J, >= 0 and strictly increasing, and the
+ * keep probabilities (any finite value: <= 0 removes, >= 1 keeps and divides
+ * the weight by it, as rand() < p does) or the mean numbers of copies (in
+ * [0, 64]).  f(E) is linear in E between nodes and constant beyond the ends,
+ * evaluated on the device in FP64 from the particle's FP32 momentum.  A
+ * caller with f as code (a Julia closure) tabulates it first.  Draws and
+ * copies as for pcl_roulette / pcl_split. */
+int pcl_roulette_fn(void* ctx, int species, int n, const double* energy, const double* pkeep);
+int pcl_split_fn(void* ctx, int species, int n, const double* energy, const double* mean);
 int pcl_set_wall(void* ctx, int species, int coord, double v, int drop, int64_t capacity);
 int pcl_get_wall(void* ctx, int64_t* n, int32_t* species, uint64_t* sid, double* x, double* p, double* w,
                  double* t);

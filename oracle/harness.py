@@ -36,9 +36,12 @@ def lib():
         L.orc_set_sb.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _P(_d), _P(_d)]
         L.orc_set_swarms.argtypes = [C.c_void_p, C.c_int, _P(_d), _P(_d), _P(_d)]
         L.orc_set_field.argtypes = [C.c_void_p, C.c_int, _P(_d), C.c_int]
+        L.orc_set_push_mask.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
         L.orc_set_wall.argtypes = [C.c_void_p, C.c_int, C.c_int, _d, C.c_int]
         L.orc_roulette.argtypes = [C.c_void_p, C.c_int, _d]
         L.orc_split.argtypes = [C.c_void_p, C.c_int, _d]
+        L.orc_roulette_fn.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_d), C.POINTER(_d)]
+        L.orc_split_fn.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(_d), C.POINTER(_d)]
         L.orc_poisson_inv.argtypes = [_d, _d]
         L.orc_poisson_inv.restype = C.c_int
         L.orc_get_wall.argtypes = [C.c_void_p, _P(C.c_int32), _P(C.c_uint64), _P(_d), _P(_d), _P(_d), _P(_d)]
@@ -140,6 +143,7 @@ class OracleWorld:
         fp = np.ascontiguousarray(np.asarray(fparams, dtype=float)) if fparams else np.zeros(1)
         self._keep.append(fp)
         L.orc_set_field(self.h, int(kind), _p(fp), len(fparams))
+        L.orc_set_push_mask(self.h, *(int(m) for m in pusher.device_masks()))
 
     def set_swarms(self, tabs, E, Fdt, safety=1.15):
         """Swarm mode: per-swarm field E [n,3] (V/m) and the rate bound of the
@@ -159,10 +163,20 @@ class OracleWorld:
         lib().orc_set_swarms(self.h, len(Fdt), _p(E), _p(rbs[0]), _p(rbs[2]))
 
     def roulette(self, sp, pkeep):
-        lib().orc_roulette(self.h, int(sp), float(pkeep))
+        """pkeep: a number, or a table (energies in J, keep probabilities)."""
+        if np.ndim(pkeep) == 0:
+            lib().orc_roulette(self.h, int(sp), float(pkeep))
+        else:
+            E, v = (np.ascontiguousarray(np.asarray(a, dtype=float)) for a in pkeep)
+            lib().orc_roulette_fn(self.h, int(sp), len(E), _p(E), _p(v))
 
     def split(self, sp, p):
-        lib().orc_split(self.h, int(sp), float(p))
+        """p: a number, or a table (energies in J, mean numbers of copies)."""
+        if np.ndim(p) == 0:
+            lib().orc_split(self.h, int(sp), float(p))
+        else:
+            E, v = (np.ascontiguousarray(np.asarray(a, dtype=float)) for a in p)
+            lib().orc_split_fn(self.h, int(sp), len(E), _p(E), _p(v))
 
     def set_wall(self, sp, coord0, v, drop=True):
         lib().orc_set_wall(self.h, int(sp), int(coord0), float(v), 1 if drop else 0)

@@ -180,6 +180,10 @@ struct World {
     // {z1, z2, v[3]}, 2 step {z, v1[3], v2[3]}, 3 confined double layer {sx, sy, sz, ez0}
     int field_kind = 0;
     double fp[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    // species bits (1 << species): pushed at all (RestrictedPusher /
+    // NullPusher, pusher.jl:67-76), feeling the EM field, feeling the
+    // continuum loss (RestrictedForcing, pusher.jl:28-34)
+    int push_mask = 7, field_mask = 7, loss_mask = 7;
     // wall crossings: {species, sid, x[3], p[3], w, t}
     struct WallRec { int species; uint64_t sid; double x[3], p[3], w, t; };
     mutable std::vector<WallRec> wall;   // appended by walkers (which see a const World)
@@ -365,7 +369,7 @@ static void force(Walker& Wk, int species, const double* p, double* f, const dou
     const World& W = *Wk.W;
     double v[3];
     velocity(species, p, v);
-    double q = (species == ELECTRON ? -1.0 : 1.0) * e;
+    double q = ((W.field_mask >> species) & 1) ? (species == ELECTRON ? -1.0 : 1.0) * e : 0.0;
     double Eloc[3];
     efield(Wk, W, r, Eloc);
     const double* Ef = Eloc;
@@ -373,7 +377,7 @@ static void force(Walker& Wk, int species, const double* p, double* f, const dou
     f[0] = q * (Ef[0] + (v[1] * W.B[2] - v[2] * W.B[1]));
     f[1] = q * (Ef[1] + (v[2] * W.B[0] - v[0] * W.B[2]));
     f[2] = q * (Ef[2] + (v[0] * W.B[1] - v[1] * W.B[0]));
-    if (W.cl_order > 0) {
+    if (W.cl_order > 0 && ((W.loss_mask >> species) & 1)) {
         double x = kinenergy(species, p);
         const std::vector<double>& a = (species == ELECTRON) ? W.ec : W.pc;
         double t[4];
@@ -393,6 +397,10 @@ static void force(Walker& Wk, int species, const double* p, double* f, const dou
 // advance_particle(RK2Pusher, y, dt) (pusher.jl:41-63)
 static void advance_particle(Walker& Wk, int species, double dt) {
     Part& y = *Wk.P;
+    if (!((Wk.W->push_mask >> species) & 1)) {  // not pushed: the clock only (pusher.jl:73, 76)
+        y.t = y.t + dt;
+        return;
+    }
     double v1[3], f1[3], v2[3], f2[3], p2[3];
     double x2[3];
     velocity(species, y.p, v1);
@@ -1221,6 +1229,65 @@ int orc_split(void* w, int species, double p) {
     return 0;
 }
 
+// f(E) of a table (energies in J, ascending), linear in E between nodes and
+// constant beyond the ends, as the device evaluates it: v_i + (E - E_i) s_i
+// with the interval's slope s_i (population.jl:291-305 and 316-331 take f as
+// a function; the library takes it tabulated).
+static double table_fn(const double* tE, const double* tV, int n, double e) {
+    if (!(e > tE[0])) return tV[0];
+    if (!(e < tE[n - 1])) return tV[n - 1];
+    const int lo = int(std::upper_bound(tE, tE + n, e) - tE) - 1;
+    const double s = (tV[lo + 1] - tV[lo]) / (tE[lo + 1] - tE[lo]);
+    return std::fma(e - tE[lo], s, tV[lo]);
+}
+
+// roulette!(f, popl) (population.jl:291-305) with f(kinenergy) from a table;
+// the keep probability rounded to FP32 as the device holds it
+int orc_roulette_fn(void* w, int species, int n, const double* tE, const double* tV) {
+    World* W = static_cast<World*>(w);
+    for (Part& P : W->sp[species].parts) {
+        if (!P.active) continue;
+        const double q = double(float(table_fn(tE, tV, n, kinenergy(species, P.p))));
+        const uint32_t v = stream_word(*W, P.ctr, P.sid);
+        const double u = double(((v >> 9) << 1) | 1u) * 5.9604644775390625e-8;
+        P.ctr += 1;
+        if (u < q) P.w /= q;
+        else P.active = false;
+    }
+    auto& v = W->sp[species].parts;
+    v.erase(std::remove_if(v.begin(), v.end(), [](const Part& q) { return !q.active; }), v.end());
+    return 0;
+}
+
+// split!(f, popl) (population.jl:316-331) with the mean number of copies
+// f(kinenergy) from a table, rounded to FP32 as the device holds it
+int orc_split_fn(void* w, int species, int n, const double* tE, const double* tV) {
+    World* W = static_cast<World*>(w);
+    auto& v = W->sp[species].parts;
+    const size_t n0 = v.size();
+    for (size_t i = 0; i < n0; ++i) {
+        if (!v[i].active) continue;
+        const float pf = float(table_fn(tE, tV, n, kinenergy(species, v[i].p)));
+        v[i].w /= (1.0 + double(pf));
+        const uint32_t word = stream_word(*W, v[i].ctr, v[i].sid);
+        const uint32_t ctr0 = v[i].ctr;
+        v[i].ctr += 1;
+        const float u = float(double(((word >> 9) << 1) | 1u) * 5.9604644775390625e-8);
+        const int k = poisson_inv(pf, u);
+        for (int j = 0; j < k; ++j) {
+            uint32_t a = ctr0, b = uint32_t(v[i].sid), c2 = uint32_t(v[i].sid >> 32), d = 2u + uint32_t(j >> 1);
+            philox(a, b, c2, d, W->k0, W->k1);
+            Part q = v[i];
+            q.sid = (j & 1) ? (uint64_t(c2) | (uint64_t(d) << 32)) : (uint64_t(a) | (uint64_t(b) << 32));
+            if (W->nswarm > 0)
+                q.sid = (q.sid & 0x00FFFFFFFFFFFFFFull) | (v[i].sid & 0xFF00000000000000ull);
+            q.ctr = 0;
+            v.push_back(q);
+        }
+    }
+    return 0;
+}
+
 int orc_set_wall(void* w, int species, int coord, double v, int drop) {
     World* W = static_cast<World*>(w);
     W->sp[species].wall_coord = coord;
@@ -1249,6 +1316,12 @@ int orc_set_field(void* w, int kind, const double* params, int n) {
     World* W = static_cast<World*>(w);
     W->field_kind = kind;
     for (int i = 0; i < 8; ++i) W->fp[i] = (i < n) ? params[i] : 0.0;
+    return 0;
+}
+
+int orc_set_push_mask(void* w, int push, int field, int loss) {
+    World* W = static_cast<World*>(w);
+    W->push_mask = push; W->field_mask = field; W->loss_mask = loss;
     return 0;
 }
 

@@ -16,10 +16,11 @@ from .tables import (Electron, Photon, Positron, BinaryIntervals, ChebyshevColli
                      momentum_norm_from_kin, precheb, CollisionTable, lxcat_table, ratebound_split, load_lxcat,
                      lxcat_collision_table, LXCatSet)
 from .forcing import (HomogeneousField, DoubleLayerField, StepField, ConfinedDoubleLayerField, ElectromagneticField,
-                      NullForcing, CombinedForcing, RK2Pusher)
+                      NullForcing, CombinedForcing, RK2Pusher, RestrictedForcing, RestrictedPusher, NullPusher)
 from .population import (ElectronState, PhotonState, PositronState, ParticleArrays, Population, MultiPopulation,
                          init, advance, run, nparticles, nactives, weight, meanenergy, maxenergy, spread, posvar,
-                         spectrum, repack, droplow, kinenergy, AbstractCallback, VoidCallback, CombinedCallback,
+                         spectrum, repack, droplow, roulette, split, energy_table, ENERGY_TABLE_NODES,
+                         kinenergy, AbstractCallback, VoidCallback, CombinedCallback,
                          CollisionCounter, PopulationTargetCallback, ParticleCountCallback, WallCallback,
                          RouletteCallback, SplitCallback)
 from . import workloads, learned

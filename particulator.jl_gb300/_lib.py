@@ -109,8 +109,11 @@ _SIGS = {
                                        _P(Process)]),
     "pcl_set_forcing": (C.c_int, [C.c_void_p, _P(_d), _P(_d), C.c_int, C.c_int, _d, _P(_d), _P(_d)]),
     "pcl_set_field": (C.c_int, [C.c_void_p, C.c_int, _P(_d), C.c_int]),
+    "pcl_set_push_mask": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "pcl_roulette": (C.c_int, [C.c_void_p, C.c_int, _d]),
     "pcl_split": (C.c_int, [C.c_void_p, C.c_int, _d]),
+    "pcl_roulette_fn": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_d), _P(_d)]),
+    "pcl_split_fn": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_d), _P(_d)]),
     "pcl_roulette_swarms": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_d)]),
     "pcl_set_wall": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _d, C.c_int, _i64]),
     "pcl_get_wall": (C.c_int, [C.c_void_p, _P(_i64), _P(_i32), _P(_u64), _P(_d), _P(_d), _P(_d), _P(_d)]),

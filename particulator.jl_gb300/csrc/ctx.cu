@@ -120,7 +120,8 @@ PCL_INTERNAL int build_blob(Ctx* c) {
         h.tally_only = (S.flags & PCL_SPECIES_TALLY_ONLY) ? 1 : 0;
         h.xscale = float(1.0 / (S.xmax / mc2));
         h.cut = S.set ? float(S.cut / mc2) : INFINITY;
-        h.charge = charge[s];
+        h.charge = ((c->field_mask >> s) & 1) ? charge[s] : 0.0f;   // RestrictedForcing of the field
+        h.frozen = ((c->push_mask >> s) & 1) ? 0 : 1;
         h.table_kind = S.table_kind;
         h.wall_coord = (S.wall_coord >= 0 && c->wall_cap > 0) ? S.wall_coord : -1;
         h.wall_v = float(S.wall_v);
@@ -146,7 +147,7 @@ PCL_INTERNAL int build_blob(Ctx* c) {
                     data.push_back(S.rb.empty() ? 0.0f : float(rate_to_dev(S.rb[k + S.order * i])));
         }
         h.cl_off = -1;
-        if (c->cl_order > 0 && s != PCL_PHOTON) {
+        if (c->cl_order > 0 && s != PCL_PHOTON && ((c->loss_mask >> s) & 1)) {
             const std::vector<double>& cf = (s == PCL_ELECTRON) ? c->cl_ec : c->cl_pc;
             h.cl_off = off();
             h.cl_k = c->cl_k;
@@ -284,8 +285,10 @@ PCL_INTERNAL StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, i
     A.wall_n = c->d_wall_n; A.wall_cap = c->wall_cap;
     A.general = (c->field_kind != 0) ? 1 : 0;
     A.learn = c->learn_on ? 1 : 0;
-    for (int s = 0; s < 3; ++s)
+    for (int s = 0; s < 3; ++s) {
         if (c->sp[s].wall_coord >= 0 && c->wall_cap > 0) A.general = 1;
+        if (c->sp[s].set && !((c->push_mask >> s) & 1)) A.general = 1;   // a species that is not pushed
+    }
     A.event = (c->cfg.classic_step == 0) ? 1 : 0;
     A.stash = c->cfg.stash_entries > 0 ? c->cfg.stash_entries : PCL_STASH_MAX;
     if (c->learn_on) {  // suspended collisions go to queue 0 unless set_lq says otherwise
@@ -921,6 +924,18 @@ int pcl_set_field(void* ctx, int kind, const double* params, int nparams) {
         return fail(c, PCL_ERR_INVALID, "confined double layer widths must be > 0");
     c->field_kind = kind;
     for (int i = 0; i < 8; ++i) c->field_p[i] = (i < need[kind]) ? params[i] : 0.0;
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
+int pcl_set_push_mask(void* ctx, int pushed, int field, int loss) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    if (pushed < 0 || pushed > 7 || field < 0 || field > 7 || loss < 0 || loss > 7)
+        return fail(c, PCL_ERR_INVALID, "species masks are 3-bit");
+    c->push_mask = pushed;
+    c->field_mask = field;
+    c->loss_mask = loss;
     c->blob_dirty = true;
     return PCL_OK;
 }

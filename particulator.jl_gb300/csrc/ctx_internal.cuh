@@ -30,6 +30,11 @@ __global__ void k_roulette(float4* xw, uint4* meta, long long n, float pkeep, ui
                            unsigned long long* dead);
 __global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, double e,
                         int nswarm, uint32_t k0, uint32_t k1, unsigned long long* nslots, unsigned long long* lost);
+__global__ void k_roulette_fn(float4* xw, const float4* ps, uint4* meta, long long n, int species, const double* tab,
+                              int nt, uint32_t k0, uint32_t k1, unsigned long long* dead);
+__global__ void k_split_fn(float4* xw, float4* ps, uint4* meta, long long n, long long cap, int species,
+                           const double* tab, int nt, int nswarm, uint32_t k0, uint32_t k1,
+                           unsigned long long* nslots, unsigned long long* lost);
 __global__ void k_roulette_swarms(float4* xw, uint4* meta, long long n, const float* pkeep, int nswarm, uint32_t k0,
                                   uint32_t k1, unsigned long long* dead);
 __global__ void k_swarm_count(const uint4* meta, const unsigned long long* nslots, long long cap, int nswarm,
@@ -129,6 +134,9 @@ struct Ctx {
     // forcing
     double E[3] = {0, 0, 0}, B[3] = {0, 0, 0};
     int field_kind = 0;
+    // species bits: pushed at all, feeling the EM field, feeling the continuum
+    // loss (RestrictedPusher / NullPusher / RestrictedForcing)
+    int push_mask = 7, field_mask = 7, loss_mask = 7;
     double field_p[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // SI
     int cl_order = 0, cl_k = 0;
     double cl_xmax = 0;

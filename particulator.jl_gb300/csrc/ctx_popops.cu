@@ -92,6 +92,90 @@ int pcl_split(void* ctx, int species, double p) {
     return PCL_OK;
 }
 
+// A table of f(E) for pcl_roulette_fn / pcl_split_fn: 1 to 4096 nodes, the
+// energies (J) finite, >= 0 and strictly increasing, the values finite and
+// within [vmin, vmax]; copied to the context's scratch (after its first 256 B)
+// as the device evaluates it (table_fn): the energies in units of m_e c^2,
+// the values, the slopes of the intervals, the energies rounded to FP32.
+static int stage_table(Ctx* c, int n, const double* energy, const double* value, double vmin, double vmax,
+                       const double** dtab) {
+    if (n < 1 || n > 4096 || !energy || !value) return fail(c, PCL_ERR_INVALID, "table of 1 to 4096 nodes");
+    const size_t nd = 3 * size_t(n) + (size_t(n) + 1) / 2;
+    std::vector<double> h(nd, 0.0);
+    for (int i = 0; i < n; ++i) {
+        if (!std::isfinite(energy[i]) || energy[i] < 0.0 || (i > 0 && !(energy[i] > energy[i - 1])))
+            return fail(c, PCL_ERR_INVALID, "table energies must be finite, >= 0 and strictly increasing");
+        if (!std::isfinite(value[i]) || value[i] < vmin || value[i] > vmax)
+            return fail(c, PCL_ERR_INVALID, "table value out of range");
+        h[i] = energy[i] / si::mc2;
+        h[n + i] = value[i];
+    }
+    for (int i = 0; i + 1 < n; ++i) {
+        h[2 * n + i] = (h[n + i + 1] - h[n + i]) / (h[i + 1] - h[i]);
+        if (!std::isfinite(h[2 * n + i])) return fail(c, PCL_ERR_INVALID, "table nodes too close");
+    }
+    float* f = reinterpret_cast<float*>(h.data() + 3 * size_t(n));
+    for (int i = 0; i < n; ++i) f[i] = float(h[i]);
+    int rc = ensure_scratch(c, 256 + sizeof(double) * nd);
+    if (rc) return rc;
+    double* d = reinterpret_cast<double*>(static_cast<char*>(c->d_scr) + 256);
+    CK(cudaMemcpyAsync(d, h.data(), sizeof(double) * nd, cudaMemcpyHostToDevice, c->stream));
+    *dtab = d;
+    return PCL_OK;
+}
+
+int pcl_roulette_fn(void* ctx, int species, int n, const double* energy, const double* pkeep) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    CK(cudaSetDevice(c->device));
+    SpeciesState& S = c->sp[species];
+    long long np = 0;
+    if (S.cap <= 0 || (rc = get_n(c, species, np)) || np == 0) return rc;
+    const double* dtab = nullptr;
+    if ((rc = stage_table(c, n, energy, pkeep, -1e300, 1e300, &dtab))) return rc;
+    unsigned long long* killed = static_cast<unsigned long long*>(c->d_scr);
+    CK(cudaMemsetAsync(killed, 0, sizeof(unsigned long long), c->stream));
+    const int grid = int(std::min<long long>((np + 255) / 256, 8ll * c->sm_count));
+    k_roulette_fn<<<grid, 256, 0, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], np, species, dtab, n,
+                                               uint32_t(c->cfg.seed), uint32_t(c->cfg.seed >> 32), killed);
+    CK(cudaGetLastError());
+    unsigned long long hk = 0;
+    CK(cudaMemcpyAsync(&hk, killed, sizeof(hk), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->live[species] = std::max<long long>(0, c->live[species] - (long long)hk);
+    return PCL_OK;
+}
+
+int pcl_split_fn(void* ctx, int species, int n, const double* energy, const double* mean) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    int rc = check_species(c, species);
+    if (rc) return rc;
+    CK(cudaSetDevice(c->device));
+    SpeciesState& S = c->sp[species];
+    long long np = 0;
+    if (S.cap <= 0 || (rc = get_n(c, species, np)) || np == 0) return rc;
+    const double* dtab = nullptr;
+    if ((rc = stage_table(c, n, energy, mean, 0.0, 64.0, &dtab))) return rc;
+    unsigned long long* lost = static_cast<unsigned long long*>(c->d_scr);
+    CK(cudaMemsetAsync(lost, 0, sizeof(unsigned long long), c->stream));
+    const int grid = int(std::min<long long>((np + 255) / 256, 8ll * c->sm_count));
+    k_split_fn<<<grid, 256, 0, c->stream>>>(S.xw[S.cur], S.ps[S.cur], S.meta[S.cur], np, S.cap, species, dtab, n,
+                                            c->nswarm, uint32_t(c->cfg.seed), uint32_t(c->cfg.seed >> 32),
+                                            &c->d_ctl->n[species], lost);
+    CK(cudaGetLastError());
+    unsigned long long hl = 0;
+    CK(cudaMemcpyAsync(&hl, lost, sizeof(hl), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    long long nn = 0;
+    if ((rc = get_n(c, species, nn))) return rc;
+    c->live[species] += nn - np;
+    if (hl) return fail(c, PCL_ERR_CAPACITY, "split copies beyond the population capacity were lost");
+    return PCL_OK;
+}
+
 int pcl_set_wall(void* ctx, int species, int coord, double v, int drop, int64_t capacity) {
     Ctx* c = static_cast<Ctx*>(ctx);
     if (!c) return PCL_ERR_INVALID;

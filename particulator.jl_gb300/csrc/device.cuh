@@ -58,7 +58,7 @@ struct SpeciesHdr {
     int32_t wall_coord;   // WallCallback (callback.jl:146-184): axis 0-2, -1 = none
     float   wall_v;       // wall position (m)
     int32_t wall_drop;    // drop the particle once recorded
-    int32_t pad_w;
+    int32_t frozen;       // not pushed (RestrictedPusher / NullPusher): the clock only
     DevProc proc[16];
 };
 

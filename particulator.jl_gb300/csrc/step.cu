@@ -383,6 +383,7 @@ __device__ __forceinline__ void push(Lane& L, const SpeciesHdr& S, const KCtx& K
 // the wall is set to.  The sub-step starts (k + 1) dt - th in ns since the
 // launch start (dt_hi: dt in ns).
 __device__ __forceinline__ void push_general(Lane& L, const SpeciesHdr& S, const KCtx& K, float h, float dt_hi) {
+    if (S.frozen) return;   // RestrictedPusher / NullPusher (pusher.jl:73, 76): the clock only
     const float ox = L.x, oy = L.y, oz = L.z, opx = L.px, opy = L.py, opz = L.pz;
     const float t_in = __fmaf_rn(float(L.k + 1), dt_hi, -dd_val(L.th, L.tlo));
     push<true>(L, S, K, h);
@@ -1528,7 +1529,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                         L.nsub = 0;
                         dd_add(L.th, L.tlo, dt_hi, dt_lo);  // remainder below eps carries over (mixed_population.jl:65)
                         L.r = setr(S, K, E, L.sw);  // advance_init! of the next step
-                        if (MULTI && L.species == PCL_PHOTON && (!GENERAL || S.wall_coord < 0)) {
+                        if (MULTI && L.species == PCL_PHOTON && (!GENERAL || (S.wall_coord < 0 && !S.frozen))) {
                             // A photon's collision-free whole steps in this
                             // iteration, each exactly as its own iteration would
                             // run it (the same clock decision, decrement, push and
@@ -1537,7 +1538,8 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
                             // not change in flight, whatever the field.  The step
                             // that collides, the launch's last step, and every
                             // step of photons with a wall (whose crossings are
-                            // recorded per sub-step) are left to the loop.
+                            // recorded per sub-step) or not pushed at all are
+                            // left to the loop.
                             const int k0 = L.k;
                             while (L.k + 1 < nsteps && dd_val(L.th, L.tlo) > kEpsT) {
                                 const float tn = L.s / L.r;
@@ -2147,6 +2149,54 @@ __global__ void k_roulette(float4* xw, uint4* meta, long long n, float pkeep, ui
     }
 }
 
+// f(E) of a table of nt nodes (tab: energies E_i ascending, values v_i,
+// slopes (v_{i+1} - v_i) / (E_{i+1} - E_i) in FP64, then the energies
+// rounded to FP32), linear in E between nodes and constant beyond the ends.
+// The interval is found by bisection over the FP32 energies (at most 12
+// halvings for 4096 nodes) and corrected with FP64 comparisons, so it is the
+// FP64 interval; then one FP64 multiply-add: GB300's FP64 rate is a small
+// fraction of its FP32 rate, and the division it saves dominated the cost.
+__device__ __forceinline__ double table_fn(const double* tab, int nt, double e) {
+    const double* tE = tab;
+    const double* tV = tab + nt;
+    const double* tS = tab + 2 * nt;
+    const float* tF = reinterpret_cast<const float*>(tab + 3 * nt);
+    if (!(e > tE[0])) return tV[0];
+    if (!(e < tE[nt - 1])) return tV[nt - 1];
+    const float ef = float(e);
+    int lo = 0, hi = nt - 1;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (tF[mid] <= ef) lo = mid; else hi = mid;
+    }
+    while (lo > 0 && e < tE[lo]) --lo;
+    while (lo < nt - 2 && !(e < tE[lo + 1])) ++lo;
+    return __fma_rn(__dsub_rn(e, tE[lo]), tS[lo], tV[lo]);
+}
+
+// roulette!(f, popl) (population.jl:291-305) with f of the kinetic energy
+// given as a table (energies in units of m_e c^2): keep with probability
+// q = f(E) (one draw), dividing the weight by q, else remove; q <= 0
+// removes, q >= 1 keeps.  E from the FP32 momentum with IEEE operations.
+__global__ void k_roulette_fn(float4* xw, const float4* ps, uint4* meta, long long n, int species, const double* tab,
+                              int nt, uint32_t k0, uint32_t k1, unsigned long long* dead) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        uint4 m = meta[i];
+        if (m.z == PCL_DEAD_CTR) continue;
+        const float4 q4 = ps[i];
+        const float q = float(table_fn(tab, nt, double(kin_energy_exact(species, q4.x, q4.y, q4.z))));
+        const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
+        if (u < q) {
+            xw[i].w = xw[i].w / q;
+            meta[i].z = m.z + 1u;
+        } else {
+            meta[i].z = PCL_DEAD_CTR;
+            atomicAdd(dead, 1ull);
+        }
+    }
+}
+
 // roulette! with a keep probability per swarm (batched swarms: the swarm is
 // the top 8 bits of the stream id); pkeep >= 1 leaves a swarm untouched and
 // takes no draw.
@@ -2248,42 +2298,66 @@ __global__ void k_roulette_cap(float4* xw, uint4* meta, const unsigned long long
 // (ctr, sid, 2 + j/2) of its parent and a fresh counter; in swarm mode
 // (nswarm > 0) its top 8 bits stay the parent's swarm, as for any secondary.
 // x, p, w, s and the step clock are copied.
+// One particle of split!: weight / (1 + p), Poisson(p) copies (above).
+__device__ __forceinline__ void split_one(float4* xw, float4* ps, uint4* meta, long long i, uint4 m, long long cap,
+                                          float p, double e, int nswarm, uint32_t k0, uint32_t k1,
+                                          unsigned long long* nslots, unsigned long long* lost) {
+    const double pd = double(p);
+    float4 a = xw[i];
+    a.w = a.w / (1.0f + p);
+    xw[i] = a;
+    const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
+    const uint32_t ctr0 = m.z;
+    meta[i].z = m.z + 1u;
+    int k = 0;
+    double P = e, F = e;
+    const double ud = double(u);
+    while (ud > F && k < 1024) {
+        ++k;
+        P = __dmul_rn(P, __ddiv_rn(pd, double(k)));
+        F = __dadd_rn(F, P);
+    }
+    if (k == 0) return;
+    const float4 b = ps[i];
+    for (int j = 0; j < k; ++j) {
+        uint32_t c0 = ctr0, c1 = m.x, c2 = m.y, c3 = 2u + uint32_t(j >> 1);
+        philox4x32_10(c0, c1, c2, c3, k0, k1);
+        uint32_t lo = (j & 1) ? c2 : c0, hi = (j & 1) ? c3 : c1;
+        if (nswarm > 0) hi = (hi & 0x00FFFFFFu) | (m.y & 0xFF000000u);
+        const unsigned long long q = atomicAdd(nslots, 1ull);
+        if ((long long)q < cap) {
+            xw[q] = a;
+            ps[q] = b;
+            meta[q] = make_uint4(lo, hi, 0u, m.w);
+        } else {
+            atomicAdd(lost, 1ull);
+        }
+    }
+}
+
 __global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long long cap, float p, double e,
                         int nswarm, uint32_t k0, uint32_t k1, unsigned long long* nslots, unsigned long long* lost) {
-    const double pd = double(p);
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
-        uint4 m = meta[i];
+        const uint4 m = meta[i];
         if (m.z == PCL_DEAD_CTR) continue;
-        float4 a = xw[i];
-        a.w = a.w / (1.0f + p);
-        xw[i] = a;
-        const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
-        const uint32_t ctr0 = m.z;
-        meta[i].z = m.z + 1u;
-        int k = 0;
-        double P = e, F = e;
-        const double ud = double(u);
-        while (ud > F && k < 1024) {
-            ++k;
-            P = __dmul_rn(P, __ddiv_rn(pd, double(k)));
-            F = __dadd_rn(F, P);
-        }
-        const float4 b = ps[i];
-        for (int j = 0; j < k; ++j) {
-            uint32_t c0 = ctr0, c1 = m.x, c2 = m.y, c3 = 2u + uint32_t(j >> 1);
-            philox4x32_10(c0, c1, c2, c3, k0, k1);
-            uint32_t lo = (j & 1) ? c2 : c0, hi = (j & 1) ? c3 : c1;
-            if (nswarm > 0) hi = (hi & 0x00FFFFFFu) | (m.y & 0xFF000000u);
-            const unsigned long long q = atomicAdd(nslots, 1ull);
-            if ((long long)q < cap) {
-                xw[q] = a;
-                ps[q] = b;
-                meta[q] = make_uint4(lo, hi, 0u, m.w);
-            } else {
-                atomicAdd(lost, 1ull);
-            }
-        }
+        split_one(xw, ps, meta, i, m, cap, p, e, nswarm, k0, k1, nslots, lost);
+    }
+}
+
+// split!(f, popl) (population.jl:316-331) with the mean number of copies a
+// function of the kinetic energy, given as a table as for k_roulette_fn
+// (values in [0, 64]); exp(-p) is the device's.
+__global__ void k_split_fn(float4* xw, float4* ps, uint4* meta, long long n, long long cap, int species,
+                           const double* tab, int nt, int nswarm, uint32_t k0, uint32_t k1,
+                           unsigned long long* nslots, unsigned long long* lost) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const uint4 m = meta[i];
+        if (m.z == PCL_DEAD_CTR) continue;
+        const float4 q4 = ps[i];
+        const float p = float(table_fn(tab, nt, double(kin_energy_exact(species, q4.x, q4.y, q4.z))));
+        split_one(xw, ps, meta, i, m, cap, p, exp(-double(p)), nswarm, k0, k1, nslots, lost);
     }
 }
 

@@ -76,15 +76,58 @@ class CombinedForcing:
         self.tpl = tpl
 
 
+_SPECIES = {"electron": 0, "photon": 1, "positron": 2}
+
+
+def _species_bit(particle) -> int:
+    return 1 << (_SPECIES[particle.lower()] if isinstance(particle, str) else int(particle))
+
+
+class RestrictedForcing:
+    """RestrictedForcing{T}(f) (pusher.jl:28-34): f acts on species T only
+    (the field or the continuum loss of one species, e.g. losses for
+    positrons alone)."""
+
+    def __init__(self, particle, forcing):
+        self.bit = _species_bit(particle)
+        self.forcing = forcing
+
+
+def _leaves(forcing, mask=7):
+    """(forcing, species mask) of every leaf of a combined / restricted
+    forcing."""
+    if isinstance(forcing, CombinedForcing):
+        for f in forcing.tpl:
+            yield from _leaves(f, mask)
+    elif isinstance(forcing, RestrictedForcing):
+        yield from _leaves(forcing.forcing, mask & forcing.bit)
+    else:
+        yield forcing, mask
+
+
 class RK2Pusher:
     """RK2Pusher(forcing) (pusher.jl:37-63), Ralston's 2/3 two-stage scheme."""
 
     def __init__(self, forcing):
         self.forcing = forcing
 
+    def device_masks(self):
+        """(pushed, field, loss): the species bits pushed at all, feeling the
+        EM field, feeling the continuum loss (pcl_set_push_mask).  Every EM
+        field acts on the same species, and there is one loss term at most."""
+        field, loss = None, 7
+        for f, m in _leaves(self.forcing):
+            if isinstance(f, ElectromagneticField):
+                if field is not None and field != m:
+                    raise NotImplementedError("EM fields restricted to different species")
+                field = m
+            elif isinstance(f, ChebContinuumLoss):
+                loss = m
+        return 7, (7 if field is None else field), loss
+
     def device_forcing(self):
         """(E, B, ChebContinuumLoss | None) the device integrates."""
-        items = self.forcing.tpl if isinstance(self.forcing, CombinedForcing) else (self.forcing,)
+        items = [f for f, _ in _leaves(self.forcing)]
         E = np.zeros(3)
         B = np.zeros(3)
         cl = None
@@ -110,10 +153,43 @@ class RK2Pusher:
     def device_efield(self):
         """(kind, params) of the position-dependent E (pcl_set_field); kind 0
         when E is homogeneous."""
-        items = self.forcing.tpl if isinstance(self.forcing, CombinedForcing) else (self.forcing,)
+        items = [f for f, _ in _leaves(self.forcing)]
         found = [f.e for f in items if isinstance(f, ElectromagneticField) and hasattr(f.e, "device")]
         if not found:
             return 0, []
         if len(found) > 1 or np.any(self.device_forcing()[0] != 0):
             raise NotImplementedError("one position-dependent E and no homogeneous E beside it")
         return found[0].device()
+
+
+class RestrictedPusher:
+    """RestrictedPusher{T}(p) (pusher.jl:67-73): p advances species T; the
+    other species only advance their clocks (no motion, photons included)."""
+
+    def __init__(self, particle, pusher):
+        self.bit = _species_bit(particle)
+        self.pusher = pusher
+
+    def device_masks(self):
+        push, field, loss = self.pusher.device_masks()
+        return push & self.bit, field, loss
+
+    def device_forcing(self):
+        return self.pusher.device_forcing()
+
+    def device_efield(self):
+        return self.pusher.device_efield()
+
+
+class NullPusher:
+    """NullPusher (pusher.jl:75-76): no particle moves; clocks advance, and
+    collisions happen as the null-collision clock says."""
+
+    def device_masks(self):
+        return 0, 7, 7
+
+    def device_forcing(self):
+        return np.zeros(3), np.zeros(3), None
+
+    def device_efield(self):
+        return 0, []

@@ -211,6 +211,32 @@ class PinnedHost:
             pass
 
 
+# Nodes at which roulette!/split! functions of the kinetic energy are
+# tabulated for the device: 4096 log-spaced energies from 1 meV to 10 GeV
+# (0.73 % apart; f is linear between them, constant beyond).
+ENERGY_TABLE_NODES = np.geomspace(1e-3, 1e10, 4096) * co.eV
+
+
+def energy_table(f):
+    """(energies in J, values) of a roulette!/split! function of the kinetic
+    energy for pcl_roulette_fn / pcl_split_fn: a pair of arrays as given, or a
+    callable evaluated at ENERGY_TABLE_NODES (on the array if it takes one,
+    else node by node)."""
+    if not callable(f):
+        E, v = (np.ascontiguousarray(np.asarray(a, dtype=float)) for a in f)
+        if E.ndim != 1 or E.shape != v.shape:
+            raise ValueError("a table is two 1-D arrays of the same length")
+        return E, v
+    E = ENERGY_TABLE_NODES.copy()
+    try:
+        v = np.asarray(f(E), dtype=float)
+        if v.shape != E.shape:
+            raise ValueError
+    except Exception:
+        v = np.array([float(f(e)) for e in E])
+    return E, np.ascontiguousarray(v)
+
+
 class MultiPopulation:
     """MultiPopulation(:electron => ..., :photon => ..., :positron => ...)
     (mixed_population.jl:4-12).  Owns one device context; configuration
@@ -295,10 +321,12 @@ class MultiPopulation:
     def pairs(self):
         return [(PARTICLE_NAMES[k], v) for k, v in sorted(self.index.items())]
 
-    def set_pusher(self, pusher: RK2Pusher):
+    def set_pusher(self, pusher):
+        """RK2Pusher, RestrictedPusher or NullPusher (pusher.jl:37-76)."""
         E, B, cl = pusher.device_forcing()
         kind, fparams = pusher.device_efield()
-        key = (tuple(E), tuple(B), id(cl), kind, tuple(fparams))
+        masks = tuple(int(m) for m in pusher.device_masks())
+        key = (tuple(E), tuple(B), id(cl), kind, tuple(fparams), masks)
         if key == self._pusher_key:
             return
         L = _lib.lib()
@@ -312,6 +340,7 @@ class MultiPopulation:
         _lib.check(rc, self.ctx, "pcl_set_forcing")
         fp = np.ascontiguousarray(np.asarray(fparams, dtype=float)) if fparams else None
         _lib.check(L.pcl_set_field(self.ctx, int(kind), _lib.dptr(fp), len(fparams)), self.ctx, "pcl_set_field")
+        _lib.check(L.pcl_set_push_mask(self.ctx, *masks), self.ctx, "pcl_set_push_mask")
         self._pusher_key = key
 
     def set_swarms(self, E, Fdt, safety: float = 1.15):
@@ -333,10 +362,18 @@ class MultiPopulation:
         _lib.check(_lib.lib().pcl_swarm_moments(self.ctx, key, ns, _lib.dptr(out)), self.ctx, "pcl_swarm_moments")
         return out.reshape(ns, 6)
 
-    def roulette(self, particle, pkeep: float):
-        """roulette!(pkeep, popl) (population.jl:291-311) on the device."""
+    def roulette(self, particle, pkeep):
+        """roulette!(pkeep, popl) (population.jl:291-311) on the device.
+        pkeep: a number; a function of the kinetic energy (J), as roulette!(f,
+        popl) takes it, tabulated by `energy_table`; or such a table
+        (energies, keep probabilities), linear between nodes."""
         key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
-        _lib.check(_lib.lib().pcl_roulette(self.ctx, key, float(pkeep)), self.ctx, "pcl_roulette")
+        if np.ndim(pkeep) == 0 and not callable(pkeep):
+            _lib.check(_lib.lib().pcl_roulette(self.ctx, key, float(pkeep)), self.ctx, "pcl_roulette")
+            return
+        E, v = energy_table(pkeep)
+        _lib.check(_lib.lib().pcl_roulette_fn(self.ctx, key, len(E), _lib.dptr(E), _lib.dptr(v)), self.ctx,
+                   "pcl_roulette_fn")
 
     def roulette_swarms(self, particle, pkeep):
         """Per-swarm roulette! (pcl_roulette_swarms): keep probability pkeep[s]
@@ -384,10 +421,20 @@ class MultiPopulation:
             _lib.check(_lib.lib().pcl_compact(self.ctx), self.ctx, "pcl_compact")
         return out
 
-    def split(self, particle, p: float):
-        """split!(p, popl) (population.jl:318-335) on the device."""
+    def split(self, particle, p):
+        """split!(p, popl) (population.jl:316-335) on the device.  p: a
+        number; a function of the kinetic energy (J) giving the mean number of
+        copies, tabulated by `energy_table` (the reference's docstring says f
+        receives the energy, its code passes the particle state,
+        population.jl:320: the device form covers f of the energy); or such a
+        table (energies, means in [0, 64])."""
         key = SPECIES_BY_NAME[particle] if isinstance(particle, str) else int(particle)
-        _lib.check(_lib.lib().pcl_split(self.ctx, key, float(p)), self.ctx, "pcl_split")
+        if np.ndim(p) == 0 and not callable(p):
+            _lib.check(_lib.lib().pcl_split(self.ctx, key, float(p)), self.ctx, "pcl_split")
+            return
+        E, v = energy_table(p)
+        _lib.check(_lib.lib().pcl_split_fn(self.ctx, key, len(E), _lib.dptr(E), _lib.dptr(v)), self.ctx,
+                   "pcl_split_fn")
 
     def packed_buffers(self, pinned: bool = False):
         """Host buffers in the packed device layout for every species, sized to
@@ -797,6 +844,24 @@ def posvar(pop: Population) -> np.ndarray:
 def repack(pop: Population):
     """repack! (population.jl:229-259): compact dead slots (all species)."""
     _lib.check(_lib.lib().pcl_compact(pop.ctx), pop.ctx, "pcl_compact")
+
+
+def roulette(f, pop: Population):
+    """roulette!(f, popl) (population.jl:291-309): f a keep probability, a
+    function of the kinetic energy (J) or a table of it (MultiPopulation.
+    roulette); on the device, over the population's species."""
+    if pop._mp is None:
+        raise RuntimeError("population is not attached to a MultiPopulation")
+    pop._mp.roulette(pop.particle, f)
+
+
+def split(f, pop: Population):
+    """split!(f, popl) (population.jl:316-335): f a mean number of copies, a
+    function of the kinetic energy (J) or a table of it (MultiPopulation.
+    split); on the device, over the population's species."""
+    if pop._mp is None:
+        raise RuntimeError("population is not attached to a MultiPopulation")
+    pop._mp.split(pop.particle, f)
 
 
 def droplow(pop: Population):

@@ -402,6 +402,108 @@ def test_roulette_split_parity(pcl, oracle, gpu, air):
     mp.close()
 
 
+def test_roulette_split_tables(pcl, oracle, gpu, air):
+    """roulette!(f, popl) and split!(f, popl) with f of the kinetic energy
+    (population.jl:291-305, 316-331) on the device (pcl_roulette_fn,
+    pcl_split_fn): a constant table gives the constant roulette's particles
+    bit for bit; energy-dependent tables match the oracle (survivors, copies,
+    weights, and the copies' evolution afterwards); a callable gives the same
+    particles as its own tabulation."""
+    eV = pcl.co.eV
+    out = []
+    for f in (0.375, (np.array([1.0, 1e8]) * eV, np.array([0.375, 0.375]))):
+        mp = _mixed(pcl, air, n=(4096, 1024, 512), seed=62)
+        mp.roulette(pcl.Electron, f)
+        pcl.repack(mp.get(pcl.Electron))
+        out.append(mp.get(0).particles())
+        mp.close()
+    a, b = out
+    assert 0.3 * 4096 < len(a.w) < 0.45 * 4096
+    oa, ob = np.argsort(a.sid), np.argsort(b.sid)
+    for fld in ("sid", "ctr", "p", "x", "w"):
+        np.testing.assert_array_equal(getattr(b, fld)[ob], getattr(a, fld)[oa])
+    keep = (np.array([1e4, 3e7]) * eV, np.array([0.1, 0.9]))
+    copies = (np.array([1e4, 3e7]) * eV, np.array([0.0, 2.0]))
+    mp = _mixed(pcl, air, n=(4096, 1024, 1024), seed=63)
+    pusher = _pusher(pcl, air, E=1e6)
+    W = _oracle_from(oracle, pcl, mp, air, pusher)
+    mp.roulette(pcl.Electron, keep)
+    W.roulette(pcl.Electron, keep)
+    mp.split(pcl.Positron, copies)
+    W.split(pcl.Positron, copies)
+    pcl.repack(mp.get(pcl.Electron))
+    # log-uniform energies over 10 keV - 30 MeV: a value linear in E averages
+    # 1/8 of the way along its range (keep ~0.2, ~0.25 copies)
+    for k, lo, hi in ((pcl.Electron, 0.15 * 4096, 0.3 * 4096), (pcl.Positron, 1.15 * 1024, 1.4 * 1024)):
+        g, o = mp.get(k).particles(), W.download(k)
+        assert lo < len(g.w) < hi, (k, len(g.w))
+        rep = oracle.compare_populations(g, o, k, rtol=3 * RTOL, max_unmatched_frac=0.002)
+        assert rep["ok"], str(rep)
+    for k in range(3):
+        pcl.advance(mp, pusher, (k + 1) * 5e-12)
+        W.advance((k + 1) * 5e-12, 4)
+    _check(pcl, oracle, mp, W, rtol=3 * RTOL, stol=2e-4)
+    mp.close()
+    out = []
+    for f in (lambda E: np.clip(0.1 + 0.8 * np.log(E / (1e4 * eV)) / np.log(3e3), 0.1, 0.9),
+              pcl.energy_table(lambda E: np.clip(0.1 + 0.8 * np.log(E / (1e4 * eV)) / np.log(3e3), 0.1, 0.9))):
+        mp = _mixed(pcl, air, n=(4096, 1024, 512), seed=64)
+        pcl.roulette(f, mp.get(pcl.Electron))
+        pcl.split(f, mp.get(pcl.Photon))
+        out.append([mp.get(q).particles() for q in (0, 1)])
+        mp.close()
+    for a, b in zip(*out):
+        oa, ob = np.argsort(a.sid), np.argsort(b.sid)
+        for fld in ("sid", "ctr", "p", "w"):
+            np.testing.assert_array_equal(getattr(b, fld)[ob], getattr(a, fld)[oa])
+
+
+@pytest.mark.parametrize("spl", [1, 8])
+def test_restricted_pushers(pcl, oracle, gpu, air, spl):
+    """RestrictedForcing{T}, RestrictedPusher{T} and NullPusher (pusher.jl:
+    28-34, 67-76) on the device against the oracle (pcl_set_push_mask; a
+    species that is not pushed runs on the general kernel, the others on the
+    homogeneous one), with one and eight steps per launch; and the restricted
+    forcing's starting electrons (field, no loss) equal those of a run with the
+    field alone bit for bit (the same kernel: a forcing restricted away from a
+    species is a zero charge or no loss table in its header)."""
+    zero = pcl.HomogeneousField((0.0, 0.0, 0.0))
+    em = pcl.ElectromagneticField(pcl.HomogeneousField((0.0, 0.0, -2e6)), zero)
+    full = pcl.RK2Pusher(pcl.CombinedForcing(em, air["cl"]))
+    pushers = {"restricted_forcing": pcl.RK2Pusher(pcl.CombinedForcing(pcl.RestrictedForcing("electron", em),
+                                                                      pcl.RestrictedForcing("positron", air["cl"]))),
+               "restricted_pusher": pcl.RestrictedPusher("electron", full),
+               "null": pcl.NullPusher()}
+    finals = {}
+    for name, pusher in pushers.items():
+        mp = _mixed(pcl, air, n=(2048, 1024, 1024), seed=70, steps_per_launch=spl)
+        W = _oracle_from(oracle, pcl, mp, air, pusher)
+        x0 = {k: mp.get(k).particles() for k in (0, 1, 2)}
+        pcl.run(mp, pusher, 8e-12, 1e-12)
+        for k in range(8):
+            W.advance((k + 1) * 1e-12, 4)
+        _check(pcl, oracle, mp, W, rtol=3 * RTOL, stol=2e-4)
+        if name == "null":
+            start = np.concatenate([x0[k].x for k in x0]).astype(np.float32)
+            for k in (0, 1, 2):
+                x = mp.get(k).particles().x.astype(np.float32)
+                assert np.all((x[:, None, :] == start[None, :, :]).all(axis=2).any(axis=1)), k
+        finals[name] = mp.get(pcl.Electron).particles()
+        mp.close()
+    # the restricted forcing's electrons feel the field and no loss
+    mp = _mixed(pcl, air, n=(2048, 1024, 1024), seed=70, steps_per_launch=spl)
+    sids = mp.get(pcl.Electron).particles().sid
+    pcl.run(mp, pcl.RK2Pusher(pcl.CombinedForcing(em)), 8e-12, 1e-12)
+    ref = mp.get(pcl.Electron).particles()
+    mp.close()
+    a, b = ref, finals["restricted_forcing"]
+    ia, ib = np.isin(a.sid, sids), np.isin(b.sid, sids)
+    assert ia.sum() == ib.sum() > 1000
+    oa, ob = np.argsort(a.sid[ia]), np.argsort(b.sid[ib])
+    for fld in ("sid", "ctr", "p", "x", "s", "w"):
+        np.testing.assert_array_equal(getattr(b, fld)[ib][ob], getattr(a, fld)[ia][oa])
+
+
 def test_roulette_callback_keeps_weight(pcl, gpu, air):
     """RouletteCallback(m): populations stay near m while the total weight is
     kept in expectation."""

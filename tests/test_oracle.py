@@ -427,6 +427,147 @@ def test_oracle_split(pcl, oracle, air):
     assert np.all(np.isin(np.round(cn / pn.max(), 12), np.round(pn / pn.max(), 12)))
 
 
+def test_oracle_roulette_split_tables(pcl, oracle, air):
+    """roulette!(f, popl) and split!(f, popl) (population.jl:291-305,
+    316-331) with f of the kinetic energy given as a table: a constant table
+    gives the constant forms' particles bit for bit; an energy-dependent one
+    keeps (or copies) each energy band at f's rate, and keeps the expected
+    total weight."""
+    n = 40000
+    eV = pcl.co.eV
+    flat = (np.array([1.0, 1e7]) * eV, np.array([0.375, 0.375]))
+    for op, const, tab in (("roulette", 0.375, flat), ("split", 0.75, (flat[0], np.array([0.75, 0.75])))):
+        out = []
+        for f in (const, tab):
+            W = _world(pcl, oracle, air)
+            W.upload(pcl.Electron, _electrons(pcl, oracle, n))
+            getattr(W, op)(pcl.Electron, f)
+            out.append(W.download(pcl.Electron))
+        a, b = out
+        oa, ob = np.argsort(a.sid), np.argsort(b.sid)
+        for fld in ("sid", "ctr", "p", "x", "w"):
+            np.testing.assert_array_equal(getattr(b, fld)[ob], getattr(a, fld)[oa])
+    # keep probability rising linearly in E from 0.1 at 20 keV to 0.9 at 10 MeV
+    E0, E1 = 2e4 * eV, 1e7 * eV
+    tab = (np.array([E0, E1]), np.array([0.1, 0.9]))
+    arr = _electrons(pcl, oracle, n)
+    W = _world(pcl, oracle, air)
+    W.upload(pcl.Electron, arr)
+    W.roulette(pcl.Electron, tab)
+    d = W.download(pcl.Electron)
+    Ein = pcl.kinenergy(pcl.Electron, arr.p)
+    q = np.interp(Ein, *tab)
+    kept = np.isin(arr.sid, d.sid)
+    assert abs(kept.sum() - q.sum()) < 5 * np.sqrt(np.sum(q * (1 - q)))
+    for lo, hi in ((2e4, 2e5), (2e5, 2e6), (2e6, 1e7)):
+        band = (Ein >= lo * eV) & (Ein < hi * eV)
+        assert abs(kept[band].sum() - q[band].sum()) < 5 * np.sqrt(np.sum(q[band] * (1 - q[band]))) + 1
+    qd = np.interp(pcl.kinenergy(pcl.Electron, d.p), *tab)
+    # w / q in Float64, q held in FP32 as on the device
+    np.testing.assert_allclose(d.w, 1.0 / qd.astype(np.float32).astype(np.float64), rtol=2e-7)
+    assert abs(d.w.sum() - n) < 6 * np.sqrt(np.sum((1 - q) / q))
+    # mean copies rising from 0 to 2 over the same range
+    tab2 = (np.array([E0, E1]), np.array([0.0, 2.0]))
+    W = _world(pcl, oracle, air)
+    W.upload(pcl.Electron, arr)
+    W.split(pcl.Electron, tab2)
+    d = W.download(pcl.Electron)
+    mu = np.interp(Ein, *tab2)
+    parent = np.isin(d.sid, arr.sid)
+    assert parent.sum() == n
+    assert abs((~parent).sum() - mu.sum()) < 5 * np.sqrt(mu.sum())
+    assert abs(d.w.sum() - n) < 5 * np.sqrt(np.sum(mu / (1 + mu) ** 2))
+
+
+def _species_arrays(pcl, oracle, sp, n, sid0, seed):
+    rng = np.random.default_rng(seed)
+    E = np.exp(rng.uniform(np.log(3e4), np.log(1e7), n)) * pcl.co.eV
+    p = pcl.workloads.isotropic(n, 1.0, rng, sp)
+    p *= (pcl.momentum_norm_from_kin(sp, E) / np.linalg.norm(p, axis=1))[:, None]
+    x = rng.normal(scale=1e-3, size=(n, 3))
+    return oracle.Arrays(x, p, np.ones(n), np.zeros(n), -np.log(rng.random(n)),
+                         np.arange(sid0, sid0 + n, dtype=np.uint64), np.zeros(n, np.uint32))
+
+
+def _run_world(pcl, oracle, air, pusher, steps=5, dt=1e-12):
+    W = oracle.OracleWorld(11, air["tabs"], air["cuts"], pusher)
+    init = {}
+    for sp, sid0 in ((pcl.Electron, 0), (pcl.Photon, 1 << 20), (pcl.Positron, 2 << 20)):
+        init[sp] = _species_arrays(pcl, oracle, sp, 3000, sid0, 7 + sp)
+        W.upload(sp, init[sp])
+    for k in range(steps):
+        W.advance((k + 1) * dt, 4)
+    return {sp: W.download(sp) for sp in init}, init
+
+
+def _same(a, b, sids):
+    """The particles of a and b with the given (starting) stream ids are equal
+    bit for bit."""
+    a_in, b_in = np.isin(a.sid, sids), np.isin(b.sid, sids)
+    assert a_in.sum() == b_in.sum() > 100
+    oa, ob = np.argsort(a.sid[a_in]), np.argsort(b.sid[b_in])
+    for fld in ("sid", "ctr", "p", "x", "w", "s"):
+        np.testing.assert_array_equal(getattr(b, fld)[b_in][ob], getattr(a, fld)[a_in][oa])
+
+
+def test_oracle_restricted_pushers(pcl, oracle, air):
+    """RestrictedForcing{T}, RestrictedPusher{T} and NullPusher (pusher.jl:
+    28-34, 67-76) in the oracle.  A field and a continuum loss restricted to
+    the electrons give the starting electrons of the unrestricted run and the
+    starting positrons of a run with neither, bit for bit (no particle's
+    evolution depends on another's; secondaries can descend from either
+    species, so only the starting particles are compared).  Under NullPusher no particle moves: every particle,
+    secondaries included, sits where a particle started.  Under
+    RestrictedPusher{Electron} the starting photons and positrons keep their
+    positions, and the electrons are those of the unrestricted run."""
+    zero = pcl.HomogeneousField((0.0, 0.0, 0.0))
+    em = pcl.ElectromagneticField(pcl.HomogeneousField((0.0, 0.0, -2e6)), zero)
+    full = pcl.RK2Pusher(pcl.CombinedForcing(em, air["cl"]))
+    bare = pcl.RK2Pusher(pcl.CombinedForcing(pcl.ElectromagneticField(zero, zero)))
+    restr = pcl.RK2Pusher(pcl.CombinedForcing(pcl.RestrictedForcing("electron", em),
+                                              pcl.RestrictedForcing(pcl.Electron, air["cl"])))
+    assert restr.device_masks() == (7, 1, 1)
+    rf, init = _run_world(pcl, oracle, air, full)
+    rb, _ = _run_world(pcl, oracle, air, bare)
+    rr, _ = _run_world(pcl, oracle, air, restr)
+    _same(rf[pcl.Electron], rr[pcl.Electron], init[pcl.Electron].sid)
+    _same(rb[pcl.Positron], rr[pcl.Positron], init[pcl.Positron].sid)
+    assert not np.array_equal(np.sort(rf[pcl.Positron].p[:, 2]), np.sort(rr[pcl.Positron].p[:, 2]))
+    start = np.concatenate([init[sp].x for sp in init])
+    rn, _ = _run_world(pcl, oracle, air, pcl.NullPusher())
+    assert pcl.NullPusher().device_masks() == (0, 7, 7)
+    for sp in rn:
+        d = rn[sp]
+        assert len(d.w) > 0
+        assert np.all((d.x[:, None, :] == start[None, :, :]).all(axis=2).any(axis=1)), sp
+    rp, _ = _run_world(pcl, oracle, air, pcl.RestrictedPusher("electron", full))
+    assert pcl.RestrictedPusher("electron", full).device_masks() == (1, 7, 7)
+    _same(rf[pcl.Electron], rp[pcl.Electron], init[pcl.Electron].sid)
+    for sp in (pcl.Photon, pcl.Positron):
+        d = rp[sp]
+        first = np.isin(d.sid, init[sp].sid)
+        assert first.sum() > 100
+        m = {int(q): i for i, q in enumerate(init[sp].sid)}
+        idx = np.array([m[int(q)] for q in d.sid[first]])
+        np.testing.assert_array_equal(d.x[first], init[sp].x[idx])
+
+
+def test_energy_table(pcl):
+    """The tabulation of a roulette!/split! function of the energy: a
+    vectorised callable and a scalar-only one give the same nodes and values;
+    tables pass through; malformed tables are refused."""
+    E, v = pcl.energy_table(lambda e: np.minimum(1.0, e / (1e6 * pcl.co.eV)))
+    E2, v2 = pcl.energy_table(lambda e: min(1.0, e / (1e6 * pcl.co.eV)))
+    np.testing.assert_array_equal(E, pcl.ENERGY_TABLE_NODES)
+    np.testing.assert_array_equal(E2, E)
+    np.testing.assert_array_equal(v2, v)
+    assert len(E) == 4096 and np.all(np.diff(E) > 0) and v[-1] == 1.0
+    t = pcl.energy_table(([1.0, 2.0], [0.5, 0.25]))
+    np.testing.assert_array_equal(t[1], [0.5, 0.25])
+    with pytest.raises(ValueError):
+        pcl.energy_table(([1.0, 2.0], [0.5]))
+
+
 def test_split_poisson_inversion_is_bounded(oracle):
     """The Poisson inversion of split! (the device's arithmetic, restated in the
     oracle) sums the pmf in Float64, so even the largest uniform the streams
