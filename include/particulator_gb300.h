@@ -263,6 +263,11 @@ int pcl_set_forcing(void* ctx, const double E[3], const double B[3], int cl_orde
  * on; `loss`, those the continuum loss acts on.  7 = every species (the
  * default). */
 int pcl_set_push_mask(void* ctx, int pushed, int field, int loss);
+/* A position-dependent B (ElectromagneticField(e, b) with b a field functor,
+ * field.jl:54-70): the kinds and parameters of pcl_set_field, fields in T;
+ * kind 0 = the homogeneous B of pcl_set_forcing.  Runs on the general step
+ * kernel. */
+int pcl_set_bfield(void* ctx, int kind, const double* params, int nparams);
 int pcl_set_field(void* ctx, int kind, const double* params, int nparams);
 /* WallCallback{P}(coord, v, drop) (callback.jl:146-184): while advancing,
  * a particle of `species` crossing the plane x[coord] = v (coord 0-2; -1

@@ -37,6 +37,7 @@ def lib():
         L.orc_set_swarms.argtypes = [C.c_void_p, C.c_int, _P(_d), _P(_d), _P(_d)]
         L.orc_set_field.argtypes = [C.c_void_p, C.c_int, _P(_d), C.c_int]
         L.orc_set_push_mask.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.orc_set_bfield.argtypes = [C.c_void_p, C.c_int, _P(_d), C.c_int]
         L.orc_set_wall.argtypes = [C.c_void_p, C.c_int, C.c_int, _d, C.c_int]
         L.orc_roulette.argtypes = [C.c_void_p, C.c_int, _d]
         L.orc_split.argtypes = [C.c_void_p, C.c_int, _d]
@@ -144,6 +145,10 @@ class OracleWorld:
         self._keep.append(fp)
         L.orc_set_field(self.h, int(kind), _p(fp), len(fparams))
         L.orc_set_push_mask(self.h, *(int(m) for m in pusher.device_masks()))
+        bkind, bparams = pusher.device_bfield()
+        bp = np.ascontiguousarray(np.asarray(bparams, dtype=float)) if bparams else np.zeros(1)
+        self._keep.append(bp)
+        L.orc_set_bfield(self.h, int(bkind), _p(bp), len(bparams))
 
     def set_swarms(self, tabs, E, Fdt, safety=1.15):
         """Swarm mode: per-swarm field E [n,3] (V/m) and the rate bound of the

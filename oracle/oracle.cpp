@@ -184,6 +184,10 @@ struct World {
     // NullPusher, pusher.jl:67-76), feeling the EM field, feeling the
     // continuum loss (RestrictedForcing, pusher.jl:28-34)
     int push_mask = 7, field_mask = 7, loss_mask = 7;
+    // position-dependent B (field.jl:54-70 with a field functor as b): the
+    // kinds and layout of the E field's, in T
+    int bfield_kind = 0;
+    double bp[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     // wall crossings: {species, sid, x[3], p[3], w, t}
     struct WallRec { int species; uint64_t sid; double x[3], p[3], w, t; };
     mutable std::vector<WallRec> wall;   // appended by walkers (which see a const World)
@@ -330,11 +334,11 @@ static inline void velocity(int species, const double* p, double* v) {
 
 // force(CombinedForcing(ElectromagneticField, ChebContinuumLoss), s)
 // (pusher.jl:14-23, field.jl:54-70, continuum.jl:45-57)
-// E at position r (field.jl:4-52).  The double-layer and step fields jump at
-// their planes: a stage position within the tie tolerance of one is a tie.
-static void efield(Walker& Wk, const World& W, const double* r, double* Eo) {
-    const double* fp = W.fp;
-    switch (W.field_kind) {
+// A field of field.jl:4-52 at position r: kind 0 the homogeneous value h.
+// The double-layer and step fields jump at their planes: a stage position
+// within the tie tolerance of one is a tie.
+static void field_at(Walker& Wk, int kind, const double* fp, const double* h, const double* r, double* Eo) {
+    switch (kind) {
         case 1: {  // DoubleLayerField: v between z1 and z2, else 0
             const double sc = std::max(std::fabs(fp[1] - fp[0]), 1e-9);
             Wk.near(r[2], fp[0], sc);
@@ -359,8 +363,12 @@ static void efield(Walker& Wk, const World& W, const double* r, double* Eo) {
             break;
         }
         default:
-            for (int a = 0; a < 3; ++a) Eo[a] = W.E[a];
+            for (int a = 0; a < 3; ++a) Eo[a] = h[a];
     }
+}
+
+static void efield(Walker& Wk, const World& W, const double* r, double* Eo) {
+    field_at(Wk, W.field_kind, W.fp, W.E, r, Eo);
 }
 
 static void force(Walker& Wk, int species, const double* p, double* f, const double* r) {
@@ -374,9 +382,11 @@ static void force(Walker& Wk, int species, const double* p, double* f, const dou
     efield(Wk, W, r, Eloc);
     const double* Ef = Eloc;
     if (W.nswarm > 0) Ef = W.swarm_E.data() + 3 * size_t(std::min(int(Wk.P->sid >> 56), W.nswarm - 1));
-    f[0] = q * (Ef[0] + (v[1] * W.B[2] - v[2] * W.B[1]));
-    f[1] = q * (Ef[1] + (v[2] * W.B[0] - v[0] * W.B[2]));
-    f[2] = q * (Ef[2] + (v[0] * W.B[1] - v[1] * W.B[0]));
+    double Bl[3];
+    field_at(Wk, W.bfield_kind, W.bp, W.B, r, Bl);
+    f[0] = q * (Ef[0] + (v[1] * Bl[2] - v[2] * Bl[1]));
+    f[1] = q * (Ef[1] + (v[2] * Bl[0] - v[0] * Bl[2]));
+    f[2] = q * (Ef[2] + (v[0] * Bl[1] - v[1] * Bl[0]));
     if (W.cl_order > 0 && ((W.loss_mask >> species) & 1)) {
         double x = kinenergy(species, p);
         const std::vector<double>& a = (species == ELECTRON) ? W.ec : W.pc;
@@ -1316,6 +1326,13 @@ int orc_set_field(void* w, int kind, const double* params, int n) {
     World* W = static_cast<World*>(w);
     W->field_kind = kind;
     for (int i = 0; i < 8; ++i) W->fp[i] = (i < n) ? params[i] : 0.0;
+    return 0;
+}
+
+int orc_set_bfield(void* w, int kind, const double* params, int n) {
+    World* W = static_cast<World*>(w);
+    W->bfield_kind = kind;
+    for (int i = 0; i < 8; ++i) W->bp[i] = (i < n) ? params[i] : 0.0;
     return 0;
 }
 

@@ -110,6 +110,7 @@ _SIGS = {
     "pcl_set_forcing": (C.c_int, [C.c_void_p, _P(_d), _P(_d), C.c_int, C.c_int, _d, _P(_d), _P(_d)]),
     "pcl_set_field": (C.c_int, [C.c_void_p, C.c_int, _P(_d), C.c_int]),
     "pcl_set_push_mask": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "pcl_set_bfield": (C.c_int, [C.c_void_p, C.c_int, _P(_d), C.c_int]),
     "pcl_roulette": (C.c_int, [C.c_void_p, C.c_int, _d]),
     "pcl_split": (C.c_int, [C.c_void_p, C.c_int, _d]),
     "pcl_roulette_fn": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _P(_d), _P(_d)]),

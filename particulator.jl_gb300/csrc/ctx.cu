@@ -217,6 +217,23 @@ PCL_INTERNAL int build_blob(Ctx* c) {
             default: break;
         }
     }
+    H.bfield_kind = c->bfield_kind;
+    {
+        const double* q = c->bfield_p;
+        auto fb = [&](double v) { return float(e * v / m_e * NS); };
+        switch (c->bfield_kind) {
+            case 1: H.bp[0] = float(q[0]); H.bp[1] = float(q[1]);
+                    for (int a = 0; a < 3; ++a) H.bp[2 + a] = fb(q[2 + a]);
+                    break;
+            case 2: H.bp[0] = float(q[0]);
+                    for (int a = 0; a < 6; ++a) H.bp[1 + a] = fb(q[1 + a]);
+                    break;
+            case 3: for (int a = 0; a < 3; ++a) H.bp[a] = float(q[a]);
+                    H.bp[3] = fb(q[3]);
+                    break;
+            default: break;
+        }
+    }
     H.nswarm = c->nswarm;
     H.swarm_off = off();
     if (c->nswarm > 0) {
@@ -283,7 +300,7 @@ PCL_INTERNAL StepArgs make_args(Ctx* c, double dt, int nsteps, int spill_mode, i
     A.blob_bytes = int(c->blob.size());
     A.wall_xw = c->d_wall_xw; A.wall_pt = c->d_wall_pt; A.wall_meta = c->d_wall_meta;
     A.wall_n = c->d_wall_n; A.wall_cap = c->wall_cap;
-    A.general = (c->field_kind != 0) ? 1 : 0;
+    A.general = (c->field_kind != 0 || c->bfield_kind != 0) ? 1 : 0;
     A.learn = c->learn_on ? 1 : 0;
     for (int s = 0; s < 3; ++s) {
         if (c->sp[s].wall_coord >= 0 && c->wall_cap > 0) A.general = 1;
@@ -924,6 +941,20 @@ int pcl_set_field(void* ctx, int kind, const double* params, int nparams) {
         return fail(c, PCL_ERR_INVALID, "confined double layer widths must be > 0");
     c->field_kind = kind;
     for (int i = 0; i < 8; ++i) c->field_p[i] = (i < need[kind]) ? params[i] : 0.0;
+    c->blob_dirty = true;
+    return PCL_OK;
+}
+
+int pcl_set_bfield(void* ctx, int kind, const double* params, int nparams) {
+    Ctx* c = static_cast<Ctx*>(ctx);
+    if (!c) return PCL_ERR_INVALID;
+    static const int need[4] = {0, 5, 7, 4};
+    if (kind < 0 || kind > 3 || nparams < need[kind] || (need[kind] > 0 && !params))
+        return fail(c, PCL_ERR_INVALID, "field kind or parameters");
+    if (kind == 3 && !(params[0] > 0 && params[1] > 0 && params[2] > 0))
+        return fail(c, PCL_ERR_INVALID, "confined double layer widths must be > 0");
+    c->bfield_kind = kind;
+    for (int i = 0; i < 8; ++i) c->bfield_p[i] = (i < need[kind]) ? params[i] : 0.0;
     c->blob_dirty = true;
     return PCL_OK;
 }

@@ -137,6 +137,8 @@ struct Ctx {
     // species bits: pushed at all, feeling the EM field, feeling the continuum
     // loss (RestrictedPusher / NullPusher / RestrictedForcing)
     int push_mask = 7, field_mask = 7, loss_mask = 7;
+    int bfield_kind = 0;
+    double bfield_p[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // SI (m, T)
     double field_p[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // SI
     int cl_order = 0, cl_k = 0;
     double cl_xmax = 0;

@@ -85,6 +85,11 @@ struct BlobHdr {
     int32_t field_kind;
     int32_t pad_f;
     float   fp[8];
+    // position-dependent B (ElectromagneticField with a field functor as b,
+    // field.jl:54-70): the same kinds and layout, fields in the units of B
+    int32_t bfield_kind;
+    int32_t pad_b[3];
+    float   bp[8];
 };
 
 // Device-side counters of one context (global memory, zeroed per launch

@@ -269,17 +269,11 @@ __device__ __forceinline__ float cl_mag(const SpeciesHdr& S, const KCtx& K, floa
     return cheb_dot(K.blob + S.cl_off + i * S.cl_order, t, S.cl_order);
 }
 
-// E at position (x, y, z) (field.jl:4-52); a batched swarm's own field wins.
-__device__ __forceinline__ void efield(const KCtx& K, int sw, float x, float y, float z, float& ex, float& ey,
-                                       float& ez) {
-    const BlobHdr* H = K.H;
-    if (H->nswarm > 0) {
-        const float* E = K.blob + H->swarm_off + 4 * sw;
-        ex = E[0]; ey = E[1]; ez = E[2];
-        return;
-    }
-    const float* f = H->fp;
-    switch (H->field_kind) {
+// A field of field.jl:4-52 at position (x, y, z): kind 0 the homogeneous
+// value h, 1 double layer, 2 step, 3 confined double layer (parameters f).
+__device__ __forceinline__ void field_at(int kind, const float* f, const float* h, float x, float y, float z,
+                                         float& ex, float& ey, float& ez) {
+    switch (kind) {
         case 1: {  // DoubleLayerField
             const bool in = f[0] < z && z < f[1];
             ex = in ? f[2] : 0.0f; ey = in ? f[3] : 0.0f; ez = in ? f[4] : 0.0f;
@@ -300,8 +294,20 @@ __device__ __forceinline__ void efield(const KCtx& K, int sw, float x, float y, 
             break;
         }
         default:
-            ex = H->E[0]; ey = H->E[1]; ez = H->E[2];
+            ex = h[0]; ey = h[1]; ez = h[2];
     }
+}
+
+// E at position (x, y, z); a batched swarm's own field wins.
+__device__ __forceinline__ void efield(const KCtx& K, int sw, float x, float y, float z, float& ex, float& ey,
+                                       float& ez) {
+    const BlobHdr* H = K.H;
+    if (H->nswarm > 0) {
+        const float* E = K.blob + H->swarm_off + 4 * sw;
+        ex = E[0]; ey = E[1]; ez = E[2];
+        return;
+    }
+    field_at(H->field_kind, H->fp, H->E, x, y, z, ex, ey, ez);
 }
 
 // force(CombinedForcing(ElectromagneticField, ChebContinuumLoss), lepton)
@@ -331,7 +337,9 @@ __device__ __forceinline__ void lepton_force(const SpeciesHdr& S, const KCtx& K,
         }
     }
     if (K.hasB) {
-        const float* B = K.H->B;
+        float B[3];
+        if (GENERAL) field_at(K.H->bfield_kind, K.H->bp, K.H->B, x, y, z, B[0], B[1], B[2]);
+        else { B[0] = K.H->B[0]; B[1] = K.H->B[1]; B[2] = K.H->B[2]; }
         fx = __fmul_rn(q, __fadd_rn(ex, __fmaf_rn(by, B[2], -__fmul_rn(bz, B[1]))));
         fy = __fmul_rn(q, __fadd_rn(ey, __fmaf_rn(bz, B[0], -__fmul_rn(bx, B[2]))));
         fz = __fmul_rn(q, __fadd_rn(ez, __fmaf_rn(bx, B[1], -__fmul_rn(by, B[0]))));
@@ -1254,7 +1262,7 @@ __global__ void __launch_bounds__(256, MINB) k_step(StepArgs A) {
     K.A = &A;
     K.cap = nullptr;
     K.ncap = nullptr;
-    K.hasB = H->B[0] != 0.0f || H->B[1] != 0.0f || H->B[2] != 0.0f;
+    K.hasB = H->B[0] != 0.0f || H->B[1] != 0.0f || H->B[2] != 0.0f || H->bfield_kind != 0;
     // the multi-step instance without the learned samplers keeps a homogeneous
     // E field in registers (measured 5 % faster there; the one-step instance
     // ran slower with it, and the learned instance spilled)

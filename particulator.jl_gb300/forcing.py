@@ -133,13 +133,13 @@ class RK2Pusher:
         cl = None
         for f in items:
             if isinstance(f, ElectromagneticField):
-                if not isinstance(f.b, HomogeneousField):
-                    raise NotImplementedError("only a homogeneous B runs on the device")
+                for g in (f.e, f.b):
+                    if not isinstance(g, HomogeneousField) and not hasattr(g, "device"):
+                        raise NotImplementedError(f"field {type(g).__name__} has no device implementation")
                 if isinstance(f.e, HomogeneousField):
                     E += np.array(f.e.v)
-                elif not hasattr(f.e, "device"):
-                    raise NotImplementedError(f"field {type(f.e).__name__} has no device implementation")
-                B += np.array(f.b.v)
+                if isinstance(f.b, HomogeneousField):
+                    B += np.array(f.b.v)
             elif isinstance(f, ChebContinuumLoss):
                 if cl is not None:
                     raise NotImplementedError("one continuum-loss term at most")
@@ -161,6 +161,17 @@ class RK2Pusher:
             raise NotImplementedError("one position-dependent E and no homogeneous E beside it")
         return found[0].device()
 
+    def device_bfield(self):
+        """(kind, params) of the position-dependent B (pcl_set_bfield), in T;
+        kind 0 when B is homogeneous."""
+        items = [f for f, _ in _leaves(self.forcing)]
+        found = [f.b for f in items if isinstance(f, ElectromagneticField) and hasattr(f.b, "device")]
+        if not found:
+            return 0, []
+        if len(found) > 1 or np.any(self.device_forcing()[1] != 0):
+            raise NotImplementedError("one position-dependent B and no homogeneous B beside it")
+        return found[0].device()
+
 
 class RestrictedPusher:
     """RestrictedPusher{T}(p) (pusher.jl:67-73): p advances species T; the
@@ -180,6 +191,9 @@ class RestrictedPusher:
     def device_efield(self):
         return self.pusher.device_efield()
 
+    def device_bfield(self):
+        return self.pusher.device_bfield()
+
 
 class NullPusher:
     """NullPusher (pusher.jl:75-76): no particle moves; clocks advance, and
@@ -192,4 +206,7 @@ class NullPusher:
         return np.zeros(3), np.zeros(3), None
 
     def device_efield(self):
+        return 0, []
+
+    def device_bfield(self):
         return 0, []

@@ -325,8 +325,9 @@ class MultiPopulation:
         """RK2Pusher, RestrictedPusher or NullPusher (pusher.jl:37-76)."""
         E, B, cl = pusher.device_forcing()
         kind, fparams = pusher.device_efield()
+        bkind, bparams = pusher.device_bfield()
         masks = tuple(int(m) for m in pusher.device_masks())
-        key = (tuple(E), tuple(B), id(cl), kind, tuple(fparams), masks)
+        key = (tuple(E), tuple(B), id(cl), kind, tuple(fparams), bkind, tuple(bparams), masks)
         if key == self._pusher_key:
             return
         L = _lib.lib()
@@ -340,6 +341,8 @@ class MultiPopulation:
         _lib.check(rc, self.ctx, "pcl_set_forcing")
         fp = np.ascontiguousarray(np.asarray(fparams, dtype=float)) if fparams else None
         _lib.check(L.pcl_set_field(self.ctx, int(kind), _lib.dptr(fp), len(fparams)), self.ctx, "pcl_set_field")
+        bp = np.ascontiguousarray(np.asarray(bparams, dtype=float)) if bparams else None
+        _lib.check(L.pcl_set_bfield(self.ctx, int(bkind), _lib.dptr(bp), len(bparams)), self.ctx, "pcl_set_bfield")
         _lib.check(L.pcl_set_push_mask(self.ctx, *masks), self.ctx, "pcl_set_push_mask")
         self._pusher_key = key
 

@@ -279,7 +279,12 @@ def load_lxcat(fnames, densities: dict, energy, photon_weight: float = 1.0,
         if "weight_scale" in item:
             cs0 = cs0 * item["weight_scale"]
         if item["kind"] == "PHOTOEMISSION":
-            raise NotImplementedError("PHOTOEMISSION has no device implementation")
+            # the reference draws a photon count for it (slow-electron.jl:141-144)
+            # into a MultiplePhotonOutcome that no apply! method takes
+            # (collisions.jl:79-130), so a PHOTOEMISSION collision cannot
+            # complete there: there is no behaviour to reproduce
+            raise NotImplementedError("PHOTOEMISSION: the reference has no apply! for its MultiplePhotonOutcome "
+                                      "(collisions.jl:79-130); not reproduced")
         it = dict(item)
         it["nu"] = dens * v * np.interp(energy, e0, cs0)
         targets.setdefault(item["target"], []).append(it)

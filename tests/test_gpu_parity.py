@@ -504,6 +504,31 @@ def test_restricted_pushers(pcl, oracle, gpu, air, spl):
         np.testing.assert_array_equal(getattr(b, fld)[ib][ob], getattr(a, fld)[ia][oa])
 
 
+@pytest.mark.parametrize("spl", [1, 8])
+def test_position_dependent_b(pcl, oracle, gpu, air, spl):
+    """A position-dependent B (ElectromagneticField(e, b) with b a field
+    functor, field.jl:54-70; pcl_set_bfield): a 0.1 T slab across the middle
+    of the population, with the field and the continuum loss, on the general
+    kernel with one and eight steps per launch, against the oracle."""
+    B = pcl.DoubleLayerField(-0.001, 0.001, (0.1, 0.0, 0.05))
+    pusher = pcl.RK2Pusher(pcl.CombinedForcing(
+        pcl.ElectromagneticField(pcl.HomogeneousField((0.0, 0.0, -2e6)), B), air["cl"]))
+    rng = np.random.default_rng(71)
+    pops = {pcl.Electron: random_population(pcl, pcl.Electron, 4096, 1e4, 3e7, rng, spread_x=0.003),
+            pcl.Photon: random_population(pcl, pcl.Photon, 1024, 5e3, 3e7, rng, spread_x=0.003),
+            pcl.Positron: random_population(pcl, pcl.Positron, 1024, 1e4, 3e7, rng, spread_x=0.003)}
+    mp = pcl.MultiPopulation(*[(k, pcl.Population(1 << 16, pops[k], air["tabs"][k], air["cuts"][k], particle=k))
+                               for k in pops], seed=71, steps_per_launch=spl)
+    W = _oracle_from(oracle, pcl, mp, air, pusher)
+    pcl.run(mp, pusher, 8 * 5e-12, 5e-12)
+    for k in range(8):
+        W.advance((k + 1) * 5e-12, 4)
+    # s carries the FP32 rate-bound error once per collision: 5-ps steps, the
+    # bound of the E-field shapes' test
+    _check(pcl, oracle, mp, W, rtol=3 * RTOL, stol=4e-4)
+    mp.close()
+
+
 def test_roulette_callback_keeps_weight(pcl, gpu, air):
     """RouletteCallback(m): populations stay near m while the total weight is
     kept in expectation."""

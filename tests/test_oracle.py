@@ -552,6 +552,32 @@ def test_oracle_restricted_pushers(pcl, oracle, air):
         np.testing.assert_array_equal(d.x[first], init[sp].x[idx])
 
 
+def test_oracle_position_dependent_b(pcl, oracle, air):
+    """ElectromagneticField(e, b) with b a field functor (field.jl:54-70):
+    a StepField B whose step lies below every particle gives the particles of
+    the homogeneous B above the step bit for bit, and one whose step lies above
+    them those of the B below it; a DoubleLayerField B covering nothing gives
+    the field-free run."""
+    zero = pcl.HomogeneousField((0.0, 0.0, 0.0))
+    E = pcl.HomogeneousField((0.0, 0.0, -2e6))
+    Bv = (0.05, 0.0, 0.02)
+
+    def run(b):
+        return _run_world(pcl, oracle, air, pcl.RK2Pusher(pcl.CombinedForcing(pcl.ElectromagneticField(E, b),
+                                                                               air["cl"])))[0]
+    hom, _ = run(pcl.HomogeneousField(Bv)), None
+    above = run(pcl.StepField(-1.0, (0.0, 0.0, 0.0), Bv))
+    below = run(pcl.StepField(1.0, Bv, (0.0, 0.0, 0.0)))
+    none = run(zero)
+    empty = run(pcl.DoubleLayerField(5.0, 6.0, Bv))
+    for sp in hom:
+        for other in (above, below):
+            _same(hom[sp], other[sp], hom[sp].sid)
+        _same(none[sp], empty[sp], none[sp].sid)
+    assert not np.array_equal(np.sort(hom[pcl.Electron].p[:, 0]), np.sort(none[pcl.Electron].p[:, 0]))
+    assert pcl.RK2Pusher(pcl.ElectromagneticField(E, pcl.StepField(1.0, Bv, Bv))).device_bfield()[0] == 2
+
+
 def test_energy_table(pcl):
     """The tabulation of a roulette!/split! function of the energy: a
     vectorised callable and a scalar-only one give the same nodes and values;
