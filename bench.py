@@ -17,8 +17,10 @@ Metric: particle-steps/s (live particles at step start x steps / time).
 stream); `e2e` times the same steps through the C ABI with the population
 copied in from and out to pinned host buffers every step.  The same line
 carries the batched form (256 swarms in one context against 256 sequential
-plain contexts) and the learned form (network samplers against the plain
-form on the same state).  Inputs (16 M x 48 B = 805 MB) are far larger than
+plain contexts), the learned form (network samplers against the plain form
+on the same state) and the fields form (the general step kernel with
+position-dependent fields and a wall record, against the homogeneous field on
+the same state and launch shape).  Inputs (16 M x 48 B = 805 MB) are far larger than
 L2 (129 MB).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
@@ -835,6 +837,7 @@ def run_fields(args, pcl):
             pcl.run(mp, pusher, args.warmup * dt, dt, cb)
             tal0 = mp.tallies()
             L.pcl_sync(mp.ctx)
+            L.pcl_kernel_stats(mp.ctx, None, None, None, None, 1)
             L.pcl_timer_start(mp.ctx)
             pcl.run(mp, pusher, (args.warmup + args.steps) * dt, dt, cb)
             ms = C.c_double()
@@ -845,7 +848,8 @@ def run_fields(args, pcl):
             L.pcl_kernel_stats(mp.ctx, None, None, C.byref(nl), None, 1)
             row = {"arm": name, "general_kernel": field is not None or wall is not None,
                    "value": ps / (ms.value / 1e3), "ms_per_step": ms.value / args.steps,
-                   "particle_steps": int(ps), "live_at_end": [int(v) for v in tal1.live]}
+                   "particle_steps": int(ps), "live_at_end": [int(v) for v in tal1.live],
+                   "gpu_launches": int(nl.value)}
             if cb is not None:
                 row["wall_records"] = int(len(cb.states().w))
             rows.append(row)
@@ -860,9 +864,9 @@ def run_fields(args, pcl):
             "config": {"workload": WORKLOAD + " (field shapes of field.jl)", "particles": args.n,
                        "steps_per_launch": 64, "compaction_period": 8,
                        "l2": "inputs larger than L2 (population > 800 MB)"},
-            "value_is": "the slowest general-kernel arm", "arms": rows, "clocks": clk.summary()}
-    print(json.dumps(line))
-    return 0
+            "value_is": "the slowest general-kernel arm", "arms": rows, "clocks": clk.summary(),
+            "gpu_launches": sum(r["gpu_launches"] for r in rows)}
+    return line
 
 
 def _printing(fn):
@@ -877,7 +881,8 @@ def _form_summary(line: dict, plain_value: float) -> dict:
     keep = ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "dtype", "config", "roofline",
             "gpu_launches", "clocks")
     out = {k: line[k] for k in keep if k in line}
-    for k in ("sequential_plain", "batched_over_sequential", "plain", "learned_over_plain", "learned"):
+    for k in ("sequential_plain", "batched_over_sequential", "plain", "learned_over_plain", "learned", "value_is",
+              "arms"):
         if k in line:
             out[k] = line[k]
     out["over_plain_16M_line"] = line["value"] / plain_value if plain_value else None
@@ -929,7 +934,7 @@ def main():
         graft.build()
         fn = {"swarms": _printing(run_swarms), "learned": _printing(run_learned), "plain": run_plain,
               "reid": run_reid, "mlp": run_mlp, "kernels": run_kernels,
-              "fields": run_fields}[args.workload]
+              "fields": _printing(run_fields)}[args.workload]
         return fn(args, graft.load_package())
     ws, rank = _dist()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -1047,7 +1052,7 @@ def main():
                          f"oracle"}
     forms = {}
     if rank == 0 and ws == 1 and not args.no_forms:
-        for name, fn in (("batched", run_swarms), ("learned", run_learned)):
+        for name, fn in (("batched", run_swarms), ("learned", run_learned), ("fields", run_fields)):
             try:
                 forms[name] = _form_summary(fn(args, pcl), value)
             except Exception as ex:  # pragma: no cover
