@@ -126,21 +126,22 @@ def _peaks():
 
 # DRAM bytes (read + write) per slot of one k_step launch, from one ncu
 # capture (dram__bytes_read.sum + dram__bytes_write.sum) of the event kernel on
-# a 4 M-particle draw of the same mixed state at the commit named below;
+# a 4 M-particle draw of the same mixed state at the commit named below (the
+# same 84.9 B as at b3cc758);
 # scaled to a launch by the slots
 # it processes: the reads grow in proportion, the writes are bounded by 48 B
 # per slot.
 K_STEP_DRAM_BYTES_PER_SLOT = 84.9
 K_STEP_DRAM_CAPTURE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the 4th k_step launch of "
                        "'bench.py --n 4194304 --steps 3 --warmup 3 --steps-per-launch 1 --no-cpu --no-e2e --no-forms' at commit "
-                       "b3cc758: 201.8 MB read + 154.3 MB written over 4.19 M slots")
+                       "34299a7: 201.8 MB read + 154.3 MB written over 4.19 M slots")
 
 # Warp instructions per particle-step of the event step kernel on a 4 M draw
 # of the same state, by steps per launch (ncu smsp__inst_executed.sum of one
-# launch over its particle-steps, commit b3cc758: the one-step instance, and
+# launch over its particle-steps, commit 34299a7: the one-step instance, and
 # the multi-step instance at 64 steps per launch), for the issue ceiling:
 # 152 SMs x 4 schedulers x 2.07 GHz warp instructions per second.
-K_STEP_WARP_INST_PER_PSTEP = {1: 46.8, 64: 41.3}
+K_STEP_WARP_INST_PER_PSTEP = {1: 46.7, 64: 40.9}
 ISSUE_RATE = 152 * 4 * 2.07e9
 
 WORKLOAD = "rrea-air-0.5MVm-mixed-16M"
