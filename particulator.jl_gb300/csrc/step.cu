@@ -2306,15 +2306,15 @@ __global__ void k_roulette_cap(float4* xw, uint4* meta, const unsigned long long
 // (ctr, sid, 2 + j/2) of its parent and a fresh counter; in swarm mode
 // (nswarm > 0) its top 8 bits stay the parent's swarm, as for any secondary.
 // x, p, w, s and the step clock are copied.
-// One particle of split!: weight / (1 + p), Poisson(p) copies (above).
+// One particle of split!: weight / (1 + p), Poisson(p) copies (above), u the
+// particle's draw and e = exp(-p).
 __device__ __forceinline__ void split_one(float4* xw, float4* ps, uint4* meta, long long i, uint4 m, long long cap,
-                                          float p, double e, int nswarm, uint32_t k0, uint32_t k1,
+                                          float p, float u, double e, int nswarm, uint32_t k0, uint32_t k1,
                                           unsigned long long* nslots, unsigned long long* lost) {
     const double pd = double(p);
     float4 a = xw[i];
     a.w = a.w / (1.0f + p);
     xw[i] = a;
-    const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
     const uint32_t ctr0 = m.z;
     meta[i].z = m.z + 1u;
     int k = 0;
@@ -2349,13 +2349,18 @@ __global__ void k_split(float4* xw, float4* ps, uint4* meta, long long n, long l
          i += (long long)gridDim.x * blockDim.x) {
         const uint4 m = meta[i];
         if (m.z == PCL_DEAD_CTR) continue;
-        split_one(xw, ps, meta, i, m, cap, p, e, nswarm, k0, k1, nslots, lost);
+        const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
+        split_one(xw, ps, meta, i, m, cap, p, u, e, nswarm, k0, k1, nslots, lost);
     }
 }
 
 // split!(f, popl) (population.jl:316-331) with the mean number of copies a
 // function of the kinetic energy, given as a table as for k_roulette_fn
-// (values in [0, 64]); exp(-p) is the device's.
+// (values in [0, 64]); exp(-p) is the device's FP64 exp.  A particle draws no
+// copy when u <= exp(-p), i.e. -ln u >= p: where the FP32 logarithm (within a
+// few ulp) clears p by a relative 1e-5, that outcome is certain and the FP64
+// exponential is skipped (e = 1 gives the same k = 0), so the copies are
+// those of the exact test.
 __global__ void k_split_fn(float4* xw, float4* ps, uint4* meta, long long n, long long cap, int species,
                            const double* tab, int nt, int nswarm, uint32_t k0, uint32_t k1,
                            unsigned long long* nslots, unsigned long long* lost) {
@@ -2365,7 +2370,9 @@ __global__ void k_split_fn(float4* xw, float4* ps, uint4* meta, long long n, lon
         if (m.z == PCL_DEAD_CTR) continue;
         const float4 q4 = ps[i];
         const float p = float(table_fn(tab, nt, double(kin_energy_exact(species, q4.x, q4.y, q4.z))));
-        split_one(xw, ps, meta, i, m, cap, p, exp(-double(p)), nswarm, k0, k1, nslots, lost);
+        const float u = bits_to_u(stream_word(m.z, m.x, m.y, k0, k1));
+        const bool none = -logf(u) > p * 1.00001f + 1e-6f;
+        split_one(xw, ps, meta, i, m, cap, p, u, none ? 1.0 : exp(-double(p)), nswarm, k0, k1, nslots, lost);
     }
 }
 
