@@ -15,7 +15,11 @@
 //   setr!/apply!/do_one_collision! ...... src/collisions.jl:63-199
 //   precheb/chebval/rate/ratebound ...... src/cheby.jl:57-143, src/collision_table.jl:82-106
 //   RK2Pusher/CombinedForcing ........... src/pusher.jl:14-63
-//   ElectromagneticField(Homogeneous) ... src/field.jl:4-8, 54-70
+//   RestrictedForcing/RestrictedPusher/
+//   NullPusher (species masks) .......... src/pusher.jl:28-34, 67-76
+//   ElectromagneticField (E and B as any
+//   field of field.jl) .................. src/field.jl:4-70
+//   roulette!/split! (constant, f(E)) ... src/population.jl:291-335
 //   ChebContinuumLoss.force ............. src/continuum.jl:45-57
 //   kinenergy/velocity/gamma ............ src/electron.jl:47-56, positron.jl:34-43, photon.jl:46-52
 //   turn, nextcoll, modified Tsai ....... src/util.jl:17, 40-57, 143-159

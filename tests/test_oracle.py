@@ -369,6 +369,33 @@ def test_field_shapes(pcl):
     assert pusher.device_efield()[0] == 2 and np.all(pusher.device_forcing()[0] == 0)
 
 
+def test_pusher_descriptions(pcl, air):
+    """What the device is told about a pusher (pusher.jl:14-76, field.jl:54-70):
+    species masks of restricted forcings and pushers, nested restrictions
+    intersecting, a position-dependent B beside a homogeneous E, and the
+    combinations the device cannot run refused."""
+    zero = pcl.HomogeneousField((0.0, 0.0, 0.0))
+    em = pcl.ElectromagneticField(pcl.HomogeneousField((0.0, 0.0, 1e5)), zero)
+    R = pcl.RestrictedForcing
+    assert pcl.RK2Pusher(pcl.CombinedForcing(em, air["cl"])).device_masks() == (7, 7, 7)
+    assert pcl.RK2Pusher(pcl.CombinedForcing(R("positron", em), air["cl"])).device_masks() == (7, 4, 7)
+    assert pcl.RK2Pusher(R("electron", R("electron", pcl.CombinedForcing(em, air["cl"])))).device_masks() == (7, 1, 1)
+    assert pcl.RK2Pusher(R("electron", R("positron", em))).device_masks() == (7, 0, 7)
+    assert pcl.RestrictedPusher(pcl.Photon, pcl.RK2Pusher(em)).device_masks() == (2, 7, 7)
+    assert pcl.NullPusher().device_forcing()[2] is None
+    with pytest.raises(NotImplementedError):   # EM fields on different species
+        pcl.RK2Pusher(pcl.CombinedForcing(R("electron", em), R("positron", em))).device_masks()
+    bl = pcl.DoubleLayerField(0.0, 1.0, (0.1, 0.0, 0.0))
+    p = pcl.RK2Pusher(pcl.ElectromagneticField(pcl.HomogeneousField((0.0, 0.0, 1e5)), bl))
+    E, B, _ = p.device_forcing()
+    assert np.all(E == [0, 0, 1e5]) and np.all(B == 0)
+    assert p.device_bfield() == (1, [0.0, 1.0, 0.1, 0.0, 0.0]) and p.device_efield() == (0, [])
+    with pytest.raises(NotImplementedError):   # a position-dependent B beside a homogeneous one
+        pcl.RK2Pusher(pcl.CombinedForcing(pcl.ElectromagneticField(zero, bl),
+                                          pcl.ElectromagneticField(zero, pcl.HomogeneousField((0, 0, 1.0))))
+                      ).device_bfield()
+
+
 def _electrons(pcl, oracle, n, seed=3):
     rng = np.random.default_rng(seed)
     E = np.exp(rng.uniform(np.log(2e4), np.log(1e7), n)) * pcl.co.eV
