@@ -211,7 +211,10 @@ PCL_INTERNAL int build_blob(Ctx* c) {
             case 2: H.fp[0] = float(q[0]);
                     for (int a = 0; a < 6; ++a) H.fp[1 + a] = fe(q[1 + a]);
                     break;
-            case 3: for (int a = 0; a < 3; ++a) H.fp[a] = float(q[a]);
+            case 3: for (int a = 0; a < 3; ++a) {   // the widths as the reciprocals the device multiplies by
+                        H.fp[a] = float(0.5 / (q[a] * q[a]));
+                        H.fp[4 + a] = float(1.0 / (q[a] * q[a]));
+                    }
                     H.fp[3] = fe(q[3]);
                     break;
             default: break;
@@ -228,7 +231,10 @@ PCL_INTERNAL int build_blob(Ctx* c) {
             case 2: H.bp[0] = float(q[0]);
                     for (int a = 0; a < 6; ++a) H.bp[1 + a] = fb(q[1 + a]);
                     break;
-            case 3: for (int a = 0; a < 3; ++a) H.bp[a] = float(q[a]);
+            case 3: for (int a = 0; a < 3; ++a) {
+                        H.bp[a] = float(0.5 / (q[a] * q[a]));
+                        H.bp[4 + a] = float(1.0 / (q[a] * q[a]));
+                    }
                     H.bp[3] = fb(q[3]);
                     break;
             default: break;

@@ -81,7 +81,7 @@ struct BlobHdr {
     int32_t swarm_off; // float offset of [nswarm][4] = {E field (device units), Fdt (N s)}
     // position-dependent E (field.jl:10-52), lengths in m, fields in the units of E:
     // 0 homogeneous (E), 1 double layer {z1, z2, v[3]}, 2 step {z, v1[3], v2[3]},
-    // 3 confined double layer {sx, sy, sz, ez0}
+    // 3 confined double layer {1/(2 sx^2), 1/(2 sy^2), 1/(2 sz^2), ez0, 1/sx^2, 1/sy^2, 1/sz^2}
     int32_t field_kind;
     int32_t pad_f;
     float   fp[8];

@@ -284,13 +284,11 @@ __device__ __forceinline__ void field_at(int kind, const float* f, const float* 
             ex = below ? f[1] : f[4]; ey = below ? f[2] : f[5]; ez = below ? f[3] : f[6];
             break;
         }
-        case 3: {  // ConfinedDoubleLayerField
-            const float sx = f[0], sy = f[1], sz = f[2];
-            const float g = f[3] * expf(-(x * x / (2.0f * sx * sx) + y * y / (2.0f * sy * sy) +
-                                          z * z / (2.0f * sz * sz)));
-            ex = -(g * x * z) / (sx * sx);
-            ey = -(g * y * z) / (sy * sy);
-            ez = g - (g * z * z) / (sz * sz);
+        case 3: {  // ConfinedDoubleLayerField: f = {1/(2 sx^2), 1/(2 sy^2), 1/(2 sz^2), ez0, 1/sx^2, 1/sy^2, 1/sz^2}
+            const float g = f[3] * expf(-(x * x * f[0] + y * y * f[1] + z * z * f[2]));
+            ex = -(g * x * z) * f[4];
+            ey = -(g * y * z) * f[5];
+            ez = g - (g * z * z) * f[6];
             break;
         }
         default:
