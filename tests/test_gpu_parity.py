@@ -529,6 +529,41 @@ def test_position_dependent_b(pcl, oracle, gpu, air, spl):
     mp.close()
 
 
+def test_new_entry_points_refuse_bad_arguments(pcl, gpu, air):
+    """pcl_roulette_fn / pcl_split_fn / pcl_set_push_mask / pcl_set_bfield
+    refuse malformed input with PCL_ERR_INVALID and a message, and leave the
+    context usable: tables that are empty, too long, not increasing, or with a
+    split mean outside [0, 64]; masks beyond 3 bits; unknown field kinds or a
+    confined layer without widths."""
+    eV = pcl.co.eV
+    mp = _mixed(pcl, air, n=(512, 256, 128), seed=72)
+    bad_tables = [(np.array([]), np.array([])),
+                  (np.geomspace(1.0, 1e9, 4097) * eV, np.full(4097, 0.5)),
+                  (np.array([2.0, 1.0]) * eV, np.array([0.5, 0.5])),
+                  (np.array([1.0, 1.0]) * eV, np.array([0.5, 0.5])),
+                  (np.array([1.0, np.nan]) * eV, np.array([0.5, 0.5]))]
+    for E, v in bad_tables:
+        with pytest.raises(pcl.PCLError):
+            mp.roulette(pcl.Electron, (E, v))
+        with pytest.raises(pcl.PCLError):
+            mp.split(pcl.Electron, (E, v))
+    with pytest.raises(pcl.PCLError):
+        mp.split(pcl.Electron, (np.array([1.0, 2.0]) * eV, np.array([0.5, 65.0])))
+    L = pcl.lib()
+    for masks in ((8, 7, 7), (7, -1, 7), (7, 7, 9)):
+        with pytest.raises(pcl.PCLError):
+            pcl._lib.check(L.pcl_set_push_mask(mp.ctx, *masks), mp.ctx, "pcl_set_push_mask")
+    for kind, params in ((4, [0.0] * 8), (1, [0.0, 1.0]), (3, [0.0, 1.0, 1.0, 1.0])):
+        p = np.ascontiguousarray(np.asarray(params, dtype=float))
+        with pytest.raises(pcl.PCLError):
+            pcl._lib.check(L.pcl_set_bfield(mp.ctx, kind, pcl._lib.dptr(p), len(params)), mp.ctx, "pcl_set_bfield")
+    n0 = len(mp.get(pcl.Electron).particles().w)
+    mp.roulette(pcl.Electron, (np.array([1.0, 1e9]) * eV, np.array([1.0, 1.0])))
+    pcl.advance(mp, _pusher(pcl, air), 1e-12)
+    assert len(mp.get(pcl.Electron).particles().w) > 0.9 * n0
+    mp.close()
+
+
 def test_roulette_callback_keeps_weight(pcl, gpu, air):
     """RouletteCallback(m): populations stay near m while the total weight is
     kept in expectation."""
