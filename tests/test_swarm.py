@@ -239,10 +239,12 @@ def test_batched_multistep_launches(pcl, oracle, gpu):
 
 
 @pytest.mark.gpu
-def test_split_keeps_swarm(pcl, oracle, gpu):
-    """split! in swarm mode: every copy stays in its parent's swarm (top 8
-    bits of the stream id), so each swarm's count grows by its own copies; the
-    copies and weights equal the oracle's, and the next steps still match."""
+@pytest.mark.parametrize("form", ["constant", "table"])
+def test_split_keeps_swarm(pcl, oracle, gpu, form):
+    """split! in swarm mode, with a constant mean or a table of f(E)
+    (pcl_split_fn): every copy stays in its parent's swarm (top 8 bits of the
+    stream id), so each swarm's count grows by its own copies; the copies and
+    weights equal the oracle's, and the next steps still match."""
     b = _batch(pcl)
     et, gt, pt = b.tables
     tabs = {pcl.Electron: et, pcl.Photon: gt, pcl.Positron: pt}
@@ -258,8 +260,9 @@ def test_split_keeps_swarm(pcl, oracle, gpu):
     nsw = len(b.E)
     n0 = b.mpopl.swarm_counts(pcl.Electron)
     mu = 0.6
-    b.mpopl.split(pcl.Electron, mu)
-    W.split(pcl.Electron, mu)
+    f = mu if form == "constant" else (np.array([1.0, 1e9]) * EV, np.array([mu, mu]))
+    b.mpopl.split(pcl.Electron, f)
+    W.split(pcl.Electron, f)
     n1 = b.mpopl.swarm_counts(pcl.Electron)
     g = b.mpopl.get(pcl.Electron).particles()
     assert np.all((g.sid >> np.uint64(56)) < nsw)
