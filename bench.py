@@ -816,6 +816,7 @@ def run_fields(args, pcl):
     CUDA events on the context's stream; the wall arm's records are read back
     inside the timed region, as run! does after every launch."""
     L = pcl.lib()
+    peak, peak_kind = _peaks()
     E0 = (0.0, 0.0, -5e5)
     zc = 191.0   # mean z of the grown state's electrons (m); spread 8.7 m
     arms = (("homogeneous E (the headline kernel)", None, None),
@@ -845,12 +846,16 @@ def run_fields(args, pcl):
             L.pcl_timer_stop(mp.ctx, C.byref(ms))
             tal1 = mp.tallies()
             ps = tal1.particle_steps - tal0.particle_steps
-            nl = C.c_int64()
-            L.pcl_kernel_stats(mp.ctx, None, None, C.byref(nl), None, 1)
+            kms = C.c_double(); kl = C.c_int64(); nl = C.c_int64(); kb = C.c_double()
+            L.pcl_kernel_stats(mp.ctx, C.byref(kms), C.byref(kl), C.byref(nl), C.byref(kb), 1)
+            # 96 B per particle-step over the step kernel's time, as for the plain line
+            ach = 96.0 * ps / (kms.value / 1e3) / 1e9 if kms.value > 0 else None
             row = {"arm": name, "general_kernel": field is not None or wall is not None,
                    "value": ps / (ms.value / 1e3), "ms_per_step": ms.value / args.steps,
                    "particle_steps": int(ps), "live_at_end": [int(v) for v in tal1.live],
-                   "gpu_launches": int(nl.value)}
+                   "gpu_launches": int(nl.value), "step_kernel_ms": kms.value,
+                   "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                                "frac": ach / peak if ach else None, "peak_kind": peak_kind}}
             if cb is not None:
                 row["wall_records"] = int(len(cb.states().w))
             rows.append(row)
@@ -866,6 +871,8 @@ def run_fields(args, pcl):
                        "steps_per_launch": 64, "compaction_period": 8,
                        "l2": "inputs larger than L2 (population > 800 MB)"},
             "value_is": "the slowest general-kernel arm", "arms": rows, "clocks": clk.summary(),
+            "roofline": min((r["roofline"] for r in rows[1:] if r["roofline"]["frac"]), key=lambda q: q["frac"],
+                            default=None),
             "gpu_launches": sum(r["gpu_launches"] for r in rows)}
     return line
 
